@@ -1,0 +1,73 @@
+// Shared device/host definitions for the helmgpu CUDA library.
+//
+// Complex numbers are stored interleaved (re, im) as double2 / float2 so a
+// complex FP64 value is one 128-bit load and two complex FP32 values are one
+// 128-bit load.  Node arrays are column-major with axis 1 fastest; a block of
+// right-hand sides is stored column by column with leading dimension ld >= N.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hz {
+
+template <typename T> struct cvec;
+template <> struct cvec<double> { using type = double2; };
+template <> struct cvec<float> { using type = float2; };
+template <typename T> using cplx = typename cvec<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T re, T im) {
+  cplx<T> z;
+  z.x = re;
+  z.y = im;
+  return z;
+}
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) {
+  return mk<T>(a.x + b.x, a.y + b.y);
+}
+template <typename T> __host__ __device__ __forceinline__ cplx<T> csub(cplx<T> a, cplx<T> b) {
+  return mk<T>(a.x - b.x, a.y - b.y);
+}
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// acc + a*b
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cfma(cplx<T> a, cplx<T> b, cplx<T> acc) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+  return acc;
+}
+// acc + conj(a)*b
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cfma_conj(cplx<T> a, cplx<T> b, cplx<T> acc) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+  return acc;
+}
+// acc - a*b
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cfms(cplx<T> a, cplx<T> b, cplx<T> acc) {
+  acc.x = fma(-a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(-a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+  return acc;
+}
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cscale(T s, cplx<T> a) {
+  return mk<T>(s * a.x, s * a.y);
+}
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cconj(cplx<T> a) { return mk<T>(a.x, -a.y); }
+
+template <typename To, typename From> __host__ __device__ __forceinline__ cplx<To> ccast(cplx<From> a) {
+  return mk<To>((To)a.x, (To)a.y);
+}
+
+// Node grid of one multigrid level.  2D grids have nz == 1.
+struct Grid {
+  int nx, ny, nz;
+  long long N;
+};
+
+}  // namespace hz

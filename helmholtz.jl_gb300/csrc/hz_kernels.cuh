@@ -1,0 +1,139 @@
+// Launch wrappers for the helmgpu kernels (implemented in hz_stencil.cu and
+// hz_krylov.cu).  Every wrapper launches on ctx.stream, counts the launch and,
+// when profiling is on, brackets it with CUDA events.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "hz_common.cuh"
+
+namespace hz {
+
+// Per-handle launch context: stream, launch counter and the optional
+// per-kernel event timer.
+struct Ctx {
+  cudaStream_t stream = nullptr;
+  long long launches = 0;
+  bool profile = false;
+  std::vector<std::string> names;  // kernel name table
+  std::vector<long long> counts;
+  std::vector<double> total_ms;
+  struct Pending {
+    int id;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  int name_id(const char* name);
+  void before(int id, cudaEvent_t* a);
+  void after(int id, cudaEvent_t a);
+  void resolve();  // after a stream sync: fold pending event pairs into the table
+  void release();
+};
+
+// Jacobi / residual modes of the stencil kernels.
+enum StencilMode { MODE_APPLY = 0, MODE_RESID = 1, MODE_JACOBI = 2 };
+
+// Fine-level operator: constant-coefficient nodal Laplacian with the
+// reference's ghost-reflection boundary rows plus a per-node complex diagonal.
+struct FineOp {
+  Grid g;
+  double o[3];  // 1/h_d^2: interior off-diagonal magnitude per axis
+  double b[3];  // BC/h_d^2: boundary-row off-diagonal magnitude per axis
+  int adj;      // 1: apply the adjoint (transposed boundary rows, conjugated diagonal)
+};
+
+// y = op(x) on nodes of a fine level, for the columns cols[0..ncols) of the
+// RHS block (column c starts at c*ld), computed in precision T.  b may be
+// FP64 while x/y are FP32, and x may be FP32 while y is FP64.
+template <typename T, typename TX, typename TB>
+void launch_fine(Ctx& ctx, int mode, const FineOp& op, const cplx<T>* diag, const cplx<T>* dinv, const cplx<TX>* x,
+                 const cplx<TB>* b, cplx<T>* y, long long ld, const int* cols, int ncols, double w);
+
+// Galerkin level: 3^d stored complex coefficients per node, coef[k*cld + p]
+// is the entry A(p, p + offset_k), offset_k = (k%3-1, k/3%3-1, k/9-1).
+template <typename T, typename TB>
+void launch_rap(Ctx& ctx, int mode, const Grid& g, const cplx<T>* coef, long long cld, const cplx<T>* dinv,
+                const cplx<T>* x, const cplx<TB>* b, cplx<T>* y, long long ld, const int* cols, int ncols, double w);
+
+// y = w * dinv .* b  (first Jacobi sweep from a zero guess); adj conjugates dinv.
+template <typename T, typename TB>
+void launch_jacobi0(Ctx& ctx, const Grid& g, const cplx<T>* dinv, int adj, const cplx<TB>* b, cplx<T>* y, long long ld,
+                    const int* cols, int ncols, double w);
+
+// Full-weighting restriction rc = P^T rf / 2^d (fine grid gf, coarse grid gc).
+template <typename T>
+void launch_restrict(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* rf, long long ldf, cplx<T>* rc,
+                     long long ldc, const int* cols, int ncols);
+
+// xout = xin + P ec (bi/trilinear nodal prolongation); xin may be null (xout = P ec).
+template <typename T>
+void launch_prolong(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* ec, long long ldc, const cplx<T>* xin,
+                    cplx<T>* xout, long long ldf, const int* cols, int ncols);
+
+// Banded LU solve with partial pivoting (factors from the host factorisation,
+// LAPACK gbtrf layout, ldab = 2kl+ku+1), one CTA per column, FP64 arithmetic.
+// The column lives in shared memory when N*16 bytes fit, else in gwork
+// (N values per active column).
+template <typename T>
+void launch_band_solve(Ctx& ctx, long long N, int kl, int ku, const double2* ab, const int* ipiv, const cplx<T>* b,
+                       cplx<T>* x, long long ld, const int* cols, int ncols, double2* gwork);
+
+// ---- setup kernels ---------------------------------------------------------
+void launch_probe_init(Ctx& ctx, const Grid& gc, int dim, double2* out, long long ld);
+void launch_probe_scatter(Ctx& ctx, const Grid& gc, int dim, const double2* y, long long ld, double2* coef,
+                          long long cld);
+void launch_coef_transpose(Ctx& ctx, const Grid& g, int dim, const double2* coef, double2* coefT, long long cld);
+template <typename T>
+void launch_center_inverse(Ctx& ctx, const Grid& g, int dim, const double2* coef, long long cld, cplx<T>* dinv);
+template <typename To, typename From>
+void launch_cast(Ctx& ctx, const cplx<From>* in, cplx<To>* out, long long n);
+// Column-wise cast between RHS blocks (active columns only).
+template <typename To, typename From>
+void launch_cast_cols(Ctx& ctx, long long N, const cplx<From>* in, long long ldi, cplx<To>* out, long long ldo,
+                      const int* cols, int ncols);
+template <typename T>
+void launch_zero_cols(Ctx& ctx, long long N, cplx<T>* x, long long ld, const int* cols, int ncols);
+
+// ---- Krylov kernels (FP64) -------------------------------------------------
+// Conventions: per-column device arrays are indexed by the column number c
+// (not by the position in the active list); V_i column c lives at
+// V + (i*vstride + c)*ld.  Partial sums go to part[(pos*K1 + slot)*nblk + blk]
+// and are folded in a fixed order by launch_reduce (deterministic results).
+int krylov_nblk(long long N, int ncols);
+// slots i < K: conj(V_{i0+i}) . w ; slot K (want_norm): ||w||^2
+void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
+                 const double2* w, long long wld, const int* cols, int ncols, int nblk, int want_norm, double2* part);
+// w -= sum_{i<K} h[c*hstride + i0 + i] V_{i0+i}; then (want_dots) slots i < K:
+// conj(V_{i0+i}) . w_new and (want_norm) the next slot: ||w_new||^2.
+void launch_update(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
+                   const double2* h, int hstride, double2* w, long long wld, const int* cols, int ncols, int nblk,
+                   int want_dots, int want_norm, double2* part);
+// out[c*ostride + slot] = sum over blocks of part (slot < K1); accum adds to out.
+void launch_reduce(Ctx& ctx, const double2* part, const int* cols, int ncols, int K1, int nblk, double2* out,
+                   int ostride, int accum);
+// y[:, c] = s[c] * x[:, c]
+void launch_scale_cols(Ctx& ctx, long long N, const double2* x, long long xld, double2* y, long long yld,
+                       const double* s, const int* cols, int ncols);
+// x[:, c] += sum_{i < kcol[c]} y[c*ystride + i] Z_i[:, c], Z in precision TZ.
+template <typename TZ>
+void launch_update_x(Ctx& ctx, long long N, const cplx<TZ>* Z, long long zstride, long long ld, const int* kcol,
+                     const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols);
+// nrm[c] = sqrt(Re red[c*stride + slot]), inv[c] = 1/nrm[c] (0 for a zero norm).
+void launch_norms(Ctx& ctx, const double2* red, int stride, int slot, const int* cols, int ncols, double* nrm,
+                  double* inv);
+// g[c*(m+1) + 0] = beta[c], the other entries of g zero.
+void launch_cycle_init(Ctx& ctx, int m, const int* cols, int ncols, const double* beta, double2* g);
+// Arnoldi step j of column c: h = hA + hB (hB may be null), h_{j+1,j} =
+// sqrt(Re nrm[c*hstride]); apply rotations 0..j-1, form rotation j, update g,
+// est[c] = |g_{j+1}|, inv_hn[c] = 1/h_{j+1,j}.  Hh[c*(m+1)*m + jj*(m+1) + i],
+// cs/sn[c*m + i], g[c*(m+1) + i].
+void launch_arnoldi_step(Ctx& ctx, int j, int m, const int* cols, int ncols, const double2* hA, const double2* hB,
+                         const double2* nrm, int hstride, double2* Hh, double2* cs, double2* sn, double2* g,
+                         double* est, double* inv_hn);
+// Back substitution R y = g for the first kcol[c] entries: y[c*m + i].
+void launch_lsq(Ctx& ctx, int m, const int* cols, int ncols, const int* kcol, const double2* Hh, const double2* g,
+                double2* y);
+
+}  // namespace hz

@@ -1,0 +1,514 @@
+// FP64 FGMRES kernels (Arnoldi with classical Gram-Schmidt, Givens rotations,
+// least squares, solution update) batched over the active right-hand-side
+// columns, plus the multigrid setup kernels (Galerkin probing, coefficient
+// transpose, casts).
+//
+// Replaces solveGMRES_MG of Multigrid.jl / KrylovMethods.jl called at
+// src/ShiftedLaplacianMultigridSolver.jl:89 and the RAP products of MGsetup
+// (src/ShiftedLaplacianMultigridSolver.jl:64-65).
+#include <algorithm>
+
+#include "hz_launch.cuh"
+
+namespace hz {
+
+static constexpr int KG = 16;  // dot products carried per pass in registers
+static constexpr int RT = 256; // threads per reduction CTA
+
+int krylov_nblk(long long N, int ncols) {
+  long long target = 4LL * kSMs * 2;  // ~8 CTAs of 256 threads per SM in total
+  long long nb = (target + ncols - 1) / std::max(ncols, 1);
+  long long maxb = (N + RT - 1) / RT;
+  nb = std::max(1LL, std::min(nb, maxb));
+  return (int)nb;
+}
+
+// Block-wide sum of NV complex values per thread, result written by thread 0
+// into part[slot*nblk] (stride nblk between slots).
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double2 (&v)[NV], int nv, double2* part, int nblk) {
+  __shared__ double2 red[RT / 32][NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < NV; ++s) {
+    if (s < nv) {
+      double a = v[s].x, b = v[s].y;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+      }
+      if (lane == 0) red[warp][s] = mk<double>(a, b);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double a = 0, b = 0;
+    for (int w = 0; w < RT / 32; ++w) {
+      a += red[w][threadIdx.x].x;
+      b += red[w][threadIdx.x].y;
+    }
+    part[(long long)threadIdx.x * nblk + blockIdx.x] = mk<double>(a, b);
+  }
+}
+
+__global__ void __launch_bounds__(RT) k_dots(long long N, const double2* __restrict__ V, long long vstride,
+                                             long long ld, int i0, int K, const double2* __restrict__ w, long long wld,
+                                             const int* __restrict__ cols, int nblk, int want_norm,
+                                             double2* __restrict__ part) {
+  const int pos = blockIdx.y;
+  const int c = cols[pos];
+  const int K1 = K + want_norm;
+  const double2* wc = w + (long long)c * wld;
+  double2 acc[KG + 1];
+#pragma unroll
+  for (int s = 0; s <= KG; ++s) acc[s] = mk<double>(0, 0);
+  double nrm = 0.0;
+  const long long stride = (long long)nblk * RT;
+  for (long long p = (long long)blockIdx.x * RT + threadIdx.x; p < N; p += stride) {
+    const double2 wv = wc[p];
+#pragma unroll
+    for (int s = 0; s < KG; ++s) {
+      if (s < K) {
+        const double2 vv = V[((long long)(i0 + s) * vstride + c) * ld + p];
+        acc[s] = cfma_conj<double>(vv, wv, acc[s]);
+      }
+    }
+    if (want_norm) nrm = fma(wv.x, wv.x, fma(wv.y, wv.y, nrm));
+  }
+  // slot K carries the norm; every index below is a compile-time constant
+#pragma unroll
+  for (int s = KG; s >= 0; --s) {
+    if (s == K) acc[s] = mk<double>(nrm, 0.0);
+  }
+  block_reduce_store<KG + 1>(acc, K1, part + (long long)pos * K1 * nblk, nblk);
+}
+
+void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
+                 const double2* w, long long wld, const int* cols, int ncols, int nblk, int want_norm, double2* part) {
+  if (ncols <= 0) return;
+  if (K > KG) throw std::runtime_error("launch_dots: too many vectors in one pass");
+  dim3 grid(nblk, ncols);
+  HZ_LAUNCH(ctx, "krylov_dots", k_dots, grid, RT, 0, N, V, vstride, ld, i0, K, w, wld, cols, nblk, want_norm, part);
+}
+
+__global__ void __launch_bounds__(RT) k_update(long long N, const double2* __restrict__ V, long long vstride,
+                                               long long ld, int i0, int K, const double2* __restrict__ h, int hstride,
+                                               double2* __restrict__ w, long long wld, const int* __restrict__ cols,
+                                               int nblk, int want_dots, int want_norm, double2* __restrict__ part) {
+  const int pos = blockIdx.y;
+  const int c = cols[pos];
+  double2 hv[KG];
+#pragma unroll
+  for (int s = 0; s < KG; ++s) hv[s] = (s < K) ? h[(long long)c * hstride + i0 + s] : mk<double>(0, 0);
+  double2 acc[KG + 1];
+#pragma unroll
+  for (int s = 0; s <= KG; ++s) acc[s] = mk<double>(0, 0);
+  const int nd = want_dots ? K : 0;
+  double nrm = 0.0;
+  double2* wc = w + (long long)c * wld;
+  const long long stride = (long long)nblk * RT;
+  for (long long p = (long long)blockIdx.x * RT + threadIdx.x; p < N; p += stride) {
+    double2 vv[KG];
+    double2 wv = wc[p];
+#pragma unroll
+    for (int s = 0; s < KG; ++s) {
+      if (s < K) {
+        vv[s] = V[((long long)(i0 + s) * vstride + c) * ld + p];
+        wv = cfms<double>(hv[s], vv[s], wv);
+      }
+    }
+    wc[p] = wv;
+    if (want_dots) {
+#pragma unroll
+      for (int s = 0; s < KG; ++s)
+        if (s < K) acc[s] = cfma_conj<double>(vv[s], wv, acc[s]);
+    }
+    if (want_norm) nrm = fma(wv.x, wv.x, fma(wv.y, wv.y, nrm));
+  }
+#pragma unroll
+  for (int s = KG; s >= 0; --s) {
+    if (s == nd) acc[s] = mk<double>(nrm, 0.0);
+  }
+  const int K1 = nd + want_norm;
+  if (K1 > 0) block_reduce_store<KG + 1>(acc, K1, part + (long long)pos * K1 * nblk, nblk);
+}
+
+void launch_update(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
+                   const double2* h, int hstride, double2* w, long long wld, const int* cols, int ncols, int nblk,
+                   int want_dots, int want_norm, double2* part) {
+  if (ncols <= 0) return;
+  if (K > KG) throw std::runtime_error("launch_update: too many vectors in one pass");
+  dim3 grid(nblk, ncols);
+  HZ_LAUNCH(ctx, "krylov_update", k_update, grid, RT, 0, N, V, vstride, ld, i0, K, h, hstride, w, wld, cols, nblk,
+            want_dots, want_norm, part);
+}
+
+// One warp per (column, slot): fixed-order sum over the nblk partials.
+__global__ void k_reduce(const double2* __restrict__ part, const int* __restrict__ cols, int ncols, int K1, int nblk,
+                         double2* __restrict__ out, int ostride, int accum) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= ncols * K1) return;
+  const int pos = gw / K1, slot = gw % K1;
+  const double2* pp = part + ((long long)pos * K1 + slot) * nblk;
+  double a = 0, b = 0;
+  for (int i = lane; i < nblk; i += 32) {
+    a += pp[i].x;
+    b += pp[i].y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    double2* dst = out + (long long)cols[pos] * ostride + slot;
+    if (accum) {
+      a += dst->x;
+      b += dst->y;
+    }
+    *dst = mk<double>(a, b);
+  }
+}
+
+void launch_reduce(Ctx& ctx, const double2* part, const int* cols, int ncols, int K1, int nblk, double2* out,
+                   int ostride, int accum) {
+  if (ncols <= 0 || K1 <= 0) return;
+  long long warps = (long long)ncols * K1;
+  int blocks = (int)((warps * 32 + 255) / 256);
+  HZ_LAUNCH(ctx, "krylov_reduce", k_reduce, blocks, 256, 0, part, cols, ncols, K1, nblk, out, ostride, accum);
+}
+
+__global__ void __launch_bounds__(256) k_scale_cols(long long N, const double2* __restrict__ x, long long xld,
+                                                    double2* __restrict__ y, long long yld,
+                                                    const double* __restrict__ s, const int* __restrict__ cols) {
+  const int c = cols[blockIdx.y];
+  const double sc = s[c];
+  const double2* xc = x + (long long)c * xld;
+  double2* yc = y + (long long)c * yld;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
+    const double2 v = xc[p];
+    yc[p] = mk<double>(sc * v.x, sc * v.y);
+  }
+}
+
+void launch_scale_cols(Ctx& ctx, long long N, const double2* x, long long xld, double2* y, long long yld,
+                       const double* s, const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  int nb = krylov_nblk(N, ncols);
+  dim3 grid(nb, ncols);
+  HZ_LAUNCH(ctx, "scale_cols", k_scale_cols, grid, 256, 0, N, x, xld, y, yld, s, cols);
+}
+
+template <typename TZ>
+__global__ void __launch_bounds__(256) k_update_x(long long N, const cplx<TZ>* __restrict__ Z, long long zstride,
+                                                  long long ld, const int* __restrict__ kcol,
+                                                  const double2* __restrict__ y, int ystride, double2* __restrict__ x,
+                                                  long long xld, const int* __restrict__ cols) {
+  const int c = cols[blockIdx.y];
+  const int k = kcol[c];
+  double2 yv[KG];
+#pragma unroll
+  for (int s = 0; s < KG; ++s) yv[s] = (s < k) ? y[(long long)c * ystride + s] : mk<double>(0, 0);
+  double2* xc = x + (long long)c * xld;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
+    double2 acc = xc[p];
+#pragma unroll
+    for (int s = 0; s < KG; ++s) {
+      if (s < k) {
+        const cplx<TZ> z = Z[((long long)s * zstride + c) * ld + p];
+        acc = cfma<double>(yv[s], mk<double>((double)z.x, (double)z.y), acc);
+      }
+    }
+    for (int s = KG; s < k; ++s) {  // restart lengths above KG
+      const cplx<TZ> z = Z[((long long)s * zstride + c) * ld + p];
+      acc = cfma<double>(y[(long long)c * ystride + s], mk<double>((double)z.x, (double)z.y), acc);
+    }
+    xc[p] = acc;
+  }
+}
+
+template <typename TZ>
+void launch_update_x(Ctx& ctx, long long N, const cplx<TZ>* Z, long long zstride, long long ld, const int* kcol,
+                     const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  int nb = krylov_nblk(N, ncols);
+  dim3 grid(nb, ncols);
+  HZ_LAUNCH(ctx, "update_x", k_update_x<TZ>, grid, 256, 0, N, Z, zstride, ld, kcol, y, ystride, x, xld, cols);
+}
+
+__global__ void k_norms(const double2* __restrict__ red, int stride, int slot, const int* __restrict__ cols, int ncols,
+                        double* __restrict__ nrm, double* __restrict__ inv) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  const double v = sqrt(fmax(red[(long long)c * stride + slot].x, 0.0));
+  nrm[c] = v;
+  if (inv) inv[c] = (v > 0) ? 1.0 / v : 0.0;
+}
+
+void launch_norms(Ctx& ctx, const double2* red, int stride, int slot, const int* cols, int ncols, double* nrm,
+                  double* inv) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "krylov_norms", k_norms, (ncols + 127) / 128, 128, 0, red, stride, slot, cols, ncols, nrm, inv);
+}
+
+__global__ void k_cycle_init(int m, const int* __restrict__ cols, int ncols, const double* __restrict__ beta,
+                             double2* __restrict__ g) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  for (int i = 0; i <= m; ++i) g[(long long)c * (m + 1) + i] = mk<double>(i == 0 ? beta[c] : 0.0, 0.0);
+}
+
+void launch_cycle_init(Ctx& ctx, int m, const int* cols, int ncols, const double* beta, double2* g) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "cycle_init", k_cycle_init, (ncols + 127) / 128, 128, 0, m, cols, ncols, beta, g);
+}
+
+// Complex Givens rotation convention: (u, v) -> (conj(c) u + conj(s) v, -s u + c v).
+__global__ void k_arnoldi_step(int j, int m, const int* __restrict__ cols, int ncols, const double2* __restrict__ hA,
+                               const double2* __restrict__ hB, const double2* __restrict__ nrm, int hstride,
+                               double2* __restrict__ Hh, double2* __restrict__ cs, double2* __restrict__ sn,
+                               double2* __restrict__ g, double* __restrict__ est, double* __restrict__ inv_hn) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  double2* H = Hh + (long long)c * (m + 1) * m + (long long)j * (m + 1);
+  const double2* csc = cs + (long long)c * m;
+  const double2* snc = sn + (long long)c * m;
+  for (int i = 0; i <= j; ++i) {
+    double2 v = hA[(long long)c * hstride + i];
+    if (hB) v = cadd<double>(v, hB[(long long)c * hstride + i]);
+    H[i] = v;
+  }
+  const double hn = sqrt(fmax(nrm[(long long)c * hstride].x, 0.0));
+  H[j + 1] = mk<double>(hn, 0.0);
+  for (int i = 0; i < j; ++i) {
+    const double2 u = H[i], v = H[i + 1];
+    const double2 ci = csc[i], si = snc[i];
+    H[i] = cadd<double>(cmul<double>(cconj<double>(ci), u), cmul<double>(cconj<double>(si), v));
+    H[i + 1] = csub<double>(cmul<double>(ci, v), cmul<double>(si, u));
+  }
+  const double2 a = H[j], b = H[j + 1];
+  double den = sqrt(a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y);
+  double2 cj, sj;
+  if (den > 0) {
+    cj = mk<double>(a.x / den, a.y / den);
+    sj = mk<double>(b.x / den, b.y / den);
+  } else {
+    cj = mk<double>(1.0, 0.0);
+    sj = mk<double>(0.0, 0.0);
+    den = 0.0;
+  }
+  cs[(long long)c * m + j] = cj;
+  sn[(long long)c * m + j] = sj;
+  H[j] = mk<double>(den, 0.0);
+  H[j + 1] = mk<double>(0.0, 0.0);
+  double2* gc = g + (long long)c * (m + 1);
+  const double2 gj = gc[j];
+  gc[j] = cmul<double>(cconj<double>(cj), gj);
+  const double2 gn = cmul<double>(sj, gj);
+  gc[j + 1] = mk<double>(-gn.x, -gn.y);
+  est[c] = sqrt(gn.x * gn.x + gn.y * gn.y);
+  inv_hn[c] = (hn > 0) ? 1.0 / hn : 0.0;
+}
+
+void launch_arnoldi_step(Ctx& ctx, int j, int m, const int* cols, int ncols, const double2* hA, const double2* hB,
+                         const double2* nrm, int hstride, double2* Hh, double2* cs, double2* sn, double2* g,
+                         double* est, double* inv_hn) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "arnoldi_step", k_arnoldi_step, (ncols + 63) / 64, 64, 0, j, m, cols, ncols, hA, hB, nrm, hstride, Hh,
+            cs, sn, g, est, inv_hn);
+}
+
+__global__ void k_lsq(int m, const int* __restrict__ cols, int ncols, const int* __restrict__ kcol,
+                      const double2* __restrict__ Hh, const double2* __restrict__ g, double2* __restrict__ y) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  const int k = kcol[c];
+  const double2* H = Hh + (long long)c * (m + 1) * m;
+  const double2* gc = g + (long long)c * (m + 1);
+  double2* yc = y + (long long)c * m;
+  for (int i = k - 1; i >= 0; --i) {
+    double2 s = gc[i];
+    for (int l = i + 1; l < k; ++l) s = cfms<double>(H[(long long)l * (m + 1) + i], yc[l], s);
+    const double2 d = H[(long long)i * (m + 1) + i];
+    const double den = d.x * d.x + d.y * d.y;
+    yc[i] = (den > 0) ? mk<double>((s.x * d.x + s.y * d.y) / den, (s.y * d.x - s.x * d.y) / den) : mk<double>(0, 0);
+  }
+}
+
+void launch_lsq(Ctx& ctx, int m, const int* cols, int ncols, const int* kcol, const double2* Hh, const double2* g,
+                double2* y) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "lsq", k_lsq, (ncols + 63) / 64, 64, 0, m, cols, ncols, kcol, Hh, g, y);
+}
+
+// ---------------------------------------------------------------------------
+// Setup kernels
+// ---------------------------------------------------------------------------
+// Galerkin probing: column k of the probe block is the indicator of the
+// coarse nodes whose subscripts are congruent to pattern(k) modulo 3.  Within
+// a 3^d neighbourhood exactly one node of each class exists, so R A P applied
+// to probe k yields, at node I, the entry A_c(I, J) for that unique J.
+__global__ void k_probe_init(Grid g, int dim, double2* out, long long ld) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.N) return;
+  const int i = (int)(p % g.nx);
+  const long long t = p / g.nx;
+  const int j = (int)(t % g.ny);
+  const int k = (int)(t / g.ny);
+  const int cls = (i % 3) + 3 * (j % 3) + (dim == 3 ? 9 * (k % 3) : 0);
+  const int ns = dim == 3 ? 27 : 9;
+  for (int s = 0; s < ns; ++s) out[(long long)s * ld + p] = mk<double>(s == cls ? 1.0 : 0.0, 0.0);
+}
+
+void launch_probe_init(Ctx& ctx, const Grid& gc, int dim, double2* out, long long ld) {
+  long long nb = (gc.N + 255) / 256;
+  HZ_LAUNCH(ctx, "probe_init", k_probe_init, (unsigned)nb, 256, 0, gc, dim, out, ld);
+}
+
+__device__ __forceinline__ int off3(int cls_d, int I) {
+  // offset o in {-1,0,1} with (I + o) = cls_d (mod 3)
+  int o = ((cls_d - I) % 3 + 3) % 3;
+  return o == 2 ? -1 : o;
+}
+
+__global__ void k_probe_scatter(Grid g, int dim, const double2* __restrict__ y, long long ld, double2* coef,
+                                long long cld) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.N) return;
+  const int i = (int)(p % g.nx);
+  const long long t = p / g.nx;
+  const int j = (int)(t % g.ny);
+  const int k = (int)(t / g.ny);
+  const int ns = dim == 3 ? 27 : 9;
+  for (int s = 0; s < ns; ++s) {
+    const int ox = off3(s % 3, i), oy = off3((s / 3) % 3, j), oz = dim == 3 ? off3(s / 9, k) : 0;
+    const int slot = (ox + 1) + 3 * (oy + 1) + (dim == 3 ? 9 * (oz + 1) : 0);
+    coef[(long long)slot * cld + p] = y[(long long)s * ld + p];
+  }
+}
+
+void launch_probe_scatter(Ctx& ctx, const Grid& gc, int dim, const double2* y, long long ld, double2* coef,
+                          long long cld) {
+  long long nb = (gc.N + 255) / 256;
+  HZ_LAUNCH(ctx, "probe_scatter", k_probe_scatter, (unsigned)nb, 256, 0, gc, dim, y, ld, coef, cld);
+}
+
+// coefT[o][I] = conj(coef[-o][I + o]) (zero where I + o is outside the grid).
+__global__ void k_coef_transpose(Grid g, int dim, const double2* __restrict__ coef, double2* __restrict__ coefT,
+                                 long long cld) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.N) return;
+  const int i = (int)(p % g.nx);
+  const long long t = p / g.nx;
+  const int j = (int)(t % g.ny);
+  const int k = (int)(t / g.ny);
+  const int ns = dim == 3 ? 27 : 9;
+  for (int s = 0; s < ns; ++s) {
+    const int ox = s % 3 - 1, oy = (s / 3) % 3 - 1, oz = dim == 3 ? s / 9 - 1 : 0;
+    const int ii = i + ox, jj = j + oy, kk = k + oz;
+    double2 v = mk<double>(0, 0);
+    if (ii >= 0 && ii < g.nx && jj >= 0 && jj < g.ny && kk >= 0 && kk < g.nz) {
+      const long long q = ii + (long long)g.nx * (jj + (long long)g.ny * kk);
+      const int ms = (1 - ox) + 3 * (1 - oy) + (dim == 3 ? 9 * (1 - oz) : 0);
+      v = coef[(long long)ms * cld + q];
+      v.y = -v.y;
+    }
+    coefT[(long long)s * cld + p] = v;
+  }
+}
+
+void launch_coef_transpose(Ctx& ctx, const Grid& g, int dim, const double2* coef, double2* coefT, long long cld) {
+  long long nb = (g.N + 255) / 256;
+  HZ_LAUNCH(ctx, "coef_transpose", k_coef_transpose, (unsigned)nb, 256, 0, g, dim, coef, coefT, cld);
+}
+
+template <typename T>
+__global__ void k_center_inverse(long long N, int center, const double2* __restrict__ coef, long long cld,
+                                 cplx<T>* __restrict__ dinv) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  const double2 d = coef[(long long)center * cld + p];
+  const double den = d.x * d.x + d.y * d.y;
+  dinv[p] = mk<T>((T)(d.x / den), (T)(-d.y / den));
+}
+
+template <typename T>
+void launch_center_inverse(Ctx& ctx, const Grid& g, int dim, const double2* coef, long long cld, cplx<T>* dinv) {
+  long long nb = (g.N + 255) / 256;
+  HZ_LAUNCH(ctx, "center_inverse", k_center_inverse<T>, (unsigned)nb, 256, 0, g.N, dim == 3 ? 13 : 4, coef, cld,
+            dinv);
+}
+
+template <typename To, typename From>
+__global__ void k_cast(const cplx<From>* __restrict__ in, cplx<To>* __restrict__ out, long long n) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+    out[p] = mk<To>((To)in[p].x, (To)in[p].y);
+}
+
+template <typename To, typename From>
+void launch_cast(Ctx& ctx, const cplx<From>* in, cplx<To>* out, long long n) {
+  if (n <= 0) return;
+  long long nb = std::min<long long>((n + 255) / 256, 16LL * kSMs);
+  HZ_LAUNCH(ctx, "cast", (k_cast<To, From>), (unsigned)nb, 256, 0, in, out, n);
+}
+
+template <typename To, typename From>
+__global__ void k_cast_cols(long long N, const cplx<From>* __restrict__ in, long long ldi, cplx<To>* __restrict__ out,
+                            long long ldo, const int* __restrict__ cols) {
+  const int c = cols[blockIdx.y];
+  const cplx<From>* ic = in + (long long)c * ldi;
+  cplx<To>* oc = out + (long long)c * ldo;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x)
+    oc[p] = mk<To>((To)ic[p].x, (To)ic[p].y);
+}
+
+template <typename To, typename From>
+void launch_cast_cols(Ctx& ctx, long long N, const cplx<From>* in, long long ldi, cplx<To>* out, long long ldo,
+                      const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  int nb = krylov_nblk(N, ncols);
+  dim3 grid(nb, ncols);
+  HZ_LAUNCH(ctx, "cast_cols", (k_cast_cols<To, From>), grid, 256, 0, N, in, ldi, out, ldo, cols);
+}
+
+template <typename T>
+__global__ void k_zero_cols(long long N, cplx<T>* __restrict__ x, long long ld, const int* __restrict__ cols) {
+  const int c = cols[blockIdx.y];
+  cplx<T>* xc = x + (long long)c * ld;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x)
+    xc[p] = mk<T>(0, 0);
+}
+
+template <typename T>
+void launch_zero_cols(Ctx& ctx, long long N, cplx<T>* x, long long ld, const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  int nb = krylov_nblk(N, ncols);
+  dim3 grid(nb, ncols);
+  HZ_LAUNCH(ctx, "zero_cols", k_zero_cols<T>, grid, 256, 0, N, x, ld, cols);
+}
+
+// explicit instantiations
+template void launch_update_x<double>(Ctx&, long long, const double2*, long long, long long, const int*,
+                                      const double2*, int, double2*, long long, const int*, int);
+template void launch_update_x<float>(Ctx&, long long, const float2*, long long, long long, const int*, const double2*,
+                                     int, double2*, long long, const int*, int);
+template void launch_center_inverse<double>(Ctx&, const Grid&, int, const double2*, long long, double2*);
+template void launch_center_inverse<float>(Ctx&, const Grid&, int, const double2*, long long, float2*);
+template void launch_cast<float, double>(Ctx&, const double2*, float2*, long long);
+template void launch_cast<double, float>(Ctx&, const float2*, double2*, long long);
+template void launch_cast_cols<float, double>(Ctx&, long long, const double2*, long long, float2*, long long,
+                                              const int*, int);
+template void launch_cast_cols<double, float>(Ctx&, long long, const float2*, long long, double2*, long long,
+                                              const int*, int);
+template void launch_cast_cols<double, double>(Ctx&, long long, const double2*, long long, double2*, long long,
+                                               const int*, int);
+template void launch_zero_cols<double>(Ctx&, long long, double2*, long long, const int*, int);
+template void launch_zero_cols<float>(Ctx&, long long, float2*, long long, const int*, int);
+
+}  // namespace hz

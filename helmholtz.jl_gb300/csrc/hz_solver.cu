@@ -1,0 +1,970 @@
+// helmgpu solver runtime and C ABI.
+//
+// One handle = one Helmholtz problem on one GPU: the matrix-free fine-level
+// operator, a lazily built Galerkin multigrid hierarchy per orientation
+// (H and its adjoint), the coarsest banded LU factors, the FGMRES workspace
+// sized for the largest right-hand-side block seen so far, and the CUDA
+// stream every kernel runs on.
+//
+// Reference path replaced: src/ShiftedLaplacianMultigridSolver.jl:33-102
+// (solveLinearSystem: lazy MGsetup, shift operator, FGMRES on H
+// preconditioned by one cycle on SH), src/GetHelmholtz.jl:33-50,81-95
+// (operator assembly, shift, getHelmholtzFun).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/helmgpu.h"
+#include "hz_host.h"
+#include "hz_kernels.cuh"
+
+namespace {
+
+using namespace hz;
+
+struct HzError {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  throw HzError{code, buf};
+}
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(e == cudaErrorMemoryAllocation ? HZ_ERR_ALLOC : HZ_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+}
+
+// Owning device buffer.
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t b) {
+    if (b <= bytes && p) return;
+    reset();
+    if (b == 0) return;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      fail(HZ_ERR_ALLOC, "cudaMalloc of %.3f GB failed: %s", b / 1e9, cudaGetErrorString(e));
+    }
+    bytes = b;
+  }
+  template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+thread_local std::string g_thread_error;
+
+struct Level {
+  Grid g;
+  long long ld = 0;  // leading dimension of the RHS blocks of this level
+  // Galerkin coefficients (levels >= 1): FP64 master and FP32 copy
+  DBuf coef64, coef32, dinv64, dinv32;
+  // work buffers (precision of the cycle): x/t ping-pong, r residual, b right-hand side
+  DBuf x, t, r, b;
+};
+
+struct Hierarchy {
+  bool built = false;
+  int adj = 0;
+  std::vector<std::unique_ptr<Level>> lv;
+  // coarsest LU (band, FP64)
+  long long nc = 0;
+  int kl = 0, ku = 0;
+  DBuf ab, ipiv, bandwork;
+};
+
+}  // namespace
+
+struct hz_handle {
+  hz_problem prob{};
+  std::vector<double> m, gamma;
+  hz_options opt{};
+  int dev = 0;
+  Ctx ctx;
+  Grid g0{};
+  FineOp fop{};
+  // fine-level diagonals: H, SH (FP64), 1/diag(SH) (FP64), FP32 copies of SH
+  DBuf diagH, diagSH, dinvSH, diagSH32, dinvSH32;
+  Hierarchy hier[2];
+  // FGMRES workspace
+  int rcap = 0;
+  int mcap = 0;
+  DBuf Bd, Xd, V, Z, part, hA, hB, nr, Hh, cs, sn, gv, yv, est, invhn, bnorm, bnorm_inv, beta, beta_inv, cols, kcol;
+  DBuf tmpA, tmpB;  // hz_apply staging
+  double* h_est = nullptr;  // pinned
+  double* h_nrm = nullptr;  // pinned
+  std::string err;
+  double setup_time = 0, solve_time = 0;
+  long long nprec = 0;
+  std::vector<double> col_relres;
+  std::vector<int> col_iters;
+  long long h2d = 0, d2h = 0;
+};
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+double secs(clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+template <typename T> struct PrecT;
+template <> struct PrecT<double> { static constexpr bool fp64 = true; };
+template <> struct PrecT<float> { static constexpr bool fp64 = false; };
+
+long long num_nodes(const hz_problem& p) {
+  long long N = 1;
+  for (int d = 0; d < p.dim; ++d) N *= (p.n[d] + 1);
+  return N;
+}
+
+Grid make_grid(const hz_problem& p) {
+  Grid g;
+  g.nx = (int)(p.n[0] + 1);
+  g.ny = (int)(p.n[1] + 1);
+  g.nz = p.dim == 3 ? (int)(p.n[2] + 1) : 1;
+  g.N = (long long)g.nx * g.ny * g.nz;
+  return g;
+}
+
+Grid coarsen(const Grid& f, int dim) {
+  if ((f.nx - 1) % 2 || (f.ny - 1) % 2 || (dim == 3 && (f.nz - 1) % 2))
+    fail(HZ_ERR_ARG, "cannot coarsen a %dx%dx%d node grid: cell counts must be even on every level", f.nx, f.ny, f.nz);
+  Grid c;
+  c.nx = (f.nx - 1) / 2 + 1;
+  c.ny = (f.ny - 1) / 2 + 1;
+  c.nz = dim == 3 ? (f.nz - 1) / 2 + 1 : 1;
+  if (c.nx < 2 || c.ny < 2 || (dim == 3 && c.nz < 2)) fail(HZ_ERR_ARG, "too many multigrid levels for this grid");
+  c.N = (long long)c.nx * c.ny * c.nz;
+  return c;
+}
+
+void set_device(hz_handle* h) { ck(cudaSetDevice(h->dev), "cudaSetDevice"); }
+
+void sync(hz_handle* h) {
+  ck(cudaStreamSynchronize(h->ctx.stream), "stream sync");
+  h->ctx.resolve();
+}
+
+// ---- hierarchy setup -------------------------------------------------------
+
+// Stencil offsets per level are all within one node; the banded storage uses
+// kl = ku = nx*ny + nx + 1 (3D) or nx + 1 (2D).
+void factor_coarsest(hz_handle* h, Hierarchy& H) {
+  Level& L = *H.lv.back();
+  const Grid g = L.g;
+  const int dim = h->prob.dim;
+  const long long N = g.N;
+  const int bw = dim == 3 ? g.nx * g.ny + g.nx + 1 : g.nx + 1;
+  const int kl = bw, ku = bw;
+  const long long ldab = 2LL * kl + ku + 1;
+  const int ns = dim == 3 ? 27 : 9;
+  // gather the stencil coefficients of the coarsest level on the host
+  std::vector<std::complex<double>> coef((size_t)ns * N, 0.0);
+  if (H.lv.size() == 1) {
+    // single-level hierarchy: the fine operator itself (5/7-point)
+    std::vector<std::complex<double>> d((size_t)N);
+    ck(cudaMemcpy(d.data(), h->diagSH.p, N * 16, cudaMemcpyDeviceToHost), "copy diag");
+    const double BC = h->prob.order_neumann_bc == 1 ? 1.0 : 2.0;
+    for (long long p = 0; p < N; ++p) {
+      const int i = (int)(p % g.nx), j = (int)((p / g.nx) % g.ny), k = (int)(p / ((long long)g.nx * g.ny));
+      const int center = dim == 3 ? 13 : 4;
+      coef[(size_t)center * N + p] = H.adj ? std::conj(d[(size_t)p]) : d[(size_t)p];
+      const int pos[3] = {i, j, k};
+      const int nn[3] = {g.nx, g.ny, g.nz};
+      for (int ax = 0; ax < dim; ++ax) {
+        const double o = 1.0 / (h->prob.h[ax] * h->prob.h[ax]), b = BC * o;
+        const int q = pos[ax], n = nn[ax];
+        double cl, cr;
+        if (!H.adj) {
+          cl = (q > 0) ? ((q == n - 1) ? b : o) : 0.0;
+          cr = (q < n - 1) ? ((q == 0) ? b : o) : 0.0;
+        } else {
+          cl = (q > 0) ? ((q - 1 == 0) ? b : o) : 0.0;
+          cr = (q < n - 1) ? ((q + 1 == n - 1) ? b : o) : 0.0;
+        }
+        const int stride = ax == 0 ? 1 : (ax == 1 ? 3 : 9);
+        coef[(size_t)(center - stride) * N + p] = -cl;
+        coef[(size_t)(center + stride) * N + p] = -cr;
+      }
+    }
+  } else {
+    ck(cudaMemcpy(coef.data(), L.coef64.p, (size_t)ns * N * 16, cudaMemcpyDeviceToHost), "copy coarse coef");
+  }
+  std::vector<std::complex<double>> ab((size_t)(ldab * N), 0.0);
+  const int kv = kl + ku;
+  for (long long p = 0; p < N; ++p) {
+    const int i = (int)(p % g.nx), j = (int)((p / g.nx) % g.ny), k = (int)(p / ((long long)g.nx * g.ny));
+    for (int s = 0; s < ns; ++s) {
+      const std::complex<double> v = coef[(size_t)s * N + p];
+      if (v == 0.0) continue;
+      const int ox = s % 3 - 1, oy = (s / 3) % 3 - 1, oz = dim == 3 ? s / 9 - 1 : 0;
+      const int ii = i + ox, jj = j + oy, kk = k + oz;
+      if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || kk < 0 || kk >= g.nz) continue;
+      const long long q = ii + (long long)g.nx * (jj + (long long)g.ny * kk);
+      ab[(size_t)(q * ldab + kv + p - q)] = v;  // A(p, q)
+    }
+  }
+  std::vector<int> ipiv((size_t)N);
+  int info = band_lu_factor(N, kl, ku, ab.data(), ipiv.data());
+  if (info != 0) fail(HZ_ERR_NUMERIC, "coarsest-level LU: zero pivot in column %d", info);
+  H.nc = N;
+  H.kl = kl;
+  H.ku = ku;
+  H.ab.alloc(ab.size() * 16);
+  H.ipiv.alloc(ipiv.size() * sizeof(int));
+  ck(cudaMemcpy(H.ab.p, ab.data(), ab.size() * 16, cudaMemcpyHostToDevice), "upload band LU");
+  ck(cudaMemcpy(H.ipiv.p, ipiv.data(), ipiv.size() * sizeof(int), cudaMemcpyHostToDevice), "upload pivots");
+}
+
+void build_hierarchy(hz_handle* h, int adj) {
+  Hierarchy& H = h->hier[adj];
+  const int dim = h->prob.dim;
+  const int L = std::max(1, h->opt.levels);
+  const bool mixed = h->opt.precision == HZ_PREC_MIXED;
+  const int ns = dim == 3 ? 27 : 9;
+  H.lv.clear();
+  H.adj = adj;
+  auto l0 = std::make_unique<Level>();
+  l0->g = h->g0;
+  l0->ld = h->g0.N;
+  H.lv.push_back(std::move(l0));
+  FineOp fop = h->fop;
+  fop.adj = adj;
+  DBuf pin, pf, pg;
+  DBuf dcols;
+  std::vector<int> seq(ns);
+  for (int s = 0; s < ns; ++s) seq[s] = s;
+  dcols.alloc(ns * sizeof(int));
+  ck(cudaMemcpy(dcols.p, seq.data(), ns * sizeof(int), cudaMemcpyHostToDevice), "upload probe cols");
+  const int* pc = dcols.as<int>();
+  for (int l = 0; l + 1 < L; ++l) {
+    Level& F = *H.lv[l];
+    auto C = std::make_unique<Level>();
+    C->g = coarsen(F.g, dim);
+    C->ld = C->g.N;
+    const long long Nf = F.g.N, Nc = C->g.N;
+    pin.alloc((size_t)ns * Nc * 16);
+    pf.alloc((size_t)ns * Nf * 16);
+    pg.alloc((size_t)ns * Nf * 16);
+    launch_probe_init(h->ctx, C->g, dim, pin.as<double2>(), Nc);
+    launch_prolong<double>(h->ctx, F.g, C->g, pin.as<double2>(), Nc, nullptr, pf.as<double2>(), Nf, pc, ns);
+    if (l == 0)
+      launch_fine<double, double, double>(h->ctx, MODE_APPLY, fop, h->diagSH.as<double2>(), nullptr,
+                                          pf.as<double2>(), (const double2*)nullptr, pg.as<double2>(), Nf, pc, ns,
+                                          0.0);
+    else
+      launch_rap<double, double>(h->ctx, MODE_APPLY, F.g, F.coef64.as<double2>(), Nf, nullptr, pf.as<double2>(),
+                                 (const double2*)nullptr, pg.as<double2>(), Nf, pc, ns, 0.0);
+    launch_restrict<double>(h->ctx, F.g, C->g, pg.as<double2>(), Nf, pin.as<double2>(), Nc, pc, ns);
+    C->coef64.alloc((size_t)ns * Nc * 16);
+    launch_probe_scatter(h->ctx, C->g, dim, pin.as<double2>(), Nc, C->coef64.as<double2>(), Nc);
+    C->dinv64.alloc((size_t)Nc * 16);
+    launch_center_inverse<double>(h->ctx, C->g, dim, C->coef64.as<double2>(), Nc, C->dinv64.as<double2>());
+    if (mixed) {
+      C->coef32.alloc((size_t)ns * Nc * 8);
+      launch_cast<float, double>(h->ctx, C->coef64.as<double2>(), C->coef32.as<float2>(), (long long)ns * Nc);
+      C->dinv32.alloc((size_t)Nc * 8);
+      launch_center_inverse<float>(h->ctx, C->g, dim, C->coef64.as<double2>(), Nc, C->dinv32.as<float2>());
+    }
+    H.lv.push_back(std::move(C));
+  }
+  sync(h);
+  factor_coarsest(h, H);
+  H.built = true;
+}
+
+// ---- workspace ---------------------------------------------------------------
+
+void ensure_workspace(hz_handle* h, int nrhs) {
+  const int m = std::max(1, h->opt.inner);
+  if (nrhs <= h->rcap && m <= h->mcap) return;
+  const int R = std::max(nrhs, h->rcap);
+  const long long N = h->g0.N;
+  const bool mixed = h->opt.precision == HZ_PREC_MIXED;
+  const size_t zb = mixed ? 8 : 16;
+  h->Bd.alloc((size_t)R * N * 16);
+  h->Xd.alloc((size_t)R * N * 16);
+  h->V.alloc((size_t)(m + 1) * R * N * 16);
+  h->Z.alloc((size_t)m * R * N * zb);
+  const int nblk = krylov_nblk(N, 1);
+  h->part.alloc((size_t)R * 18 * nblk * 16);
+  const int HS = m + 2;
+  h->hA.alloc((size_t)R * HS * 16);
+  h->hB.alloc((size_t)R * HS * 16);
+  h->nr.alloc((size_t)R * HS * 16);
+  h->Hh.alloc((size_t)R * (m + 1) * m * 16);
+  h->cs.alloc((size_t)R * m * 16);
+  h->sn.alloc((size_t)R * m * 16);
+  h->gv.alloc((size_t)R * (m + 1) * 16);
+  h->yv.alloc((size_t)R * m * 16);
+  h->est.alloc((size_t)R * 8);
+  h->invhn.alloc((size_t)R * 8);
+  h->bnorm.alloc((size_t)R * 8);
+  h->bnorm_inv.alloc((size_t)R * 8);
+  h->beta.alloc((size_t)R * 8);
+  h->beta_inv.alloc((size_t)R * 8);
+  h->cols.alloc((size_t)R * sizeof(int));
+  h->kcol.alloc((size_t)R * sizeof(int));
+  if (h->h_est) cudaFreeHost(h->h_est);
+  if (h->h_nrm) cudaFreeHost(h->h_nrm);
+  h->h_est = nullptr;
+  h->h_nrm = nullptr;
+  ck(cudaMallocHost(&h->h_est, (size_t)R * 8), "pinned est");
+  ck(cudaMallocHost(&h->h_nrm, (size_t)R * 8), "pinned nrm");
+  // multigrid work buffers per level and orientation (allocated on demand in the cycle)
+  h->rcap = R;
+  h->mcap = m;
+}
+
+template <typename T>
+void ensure_level_buffers(hz_handle* h, Hierarchy& H, int R) {
+  const size_t es = sizeof(cplx<T>);
+  for (size_t l = 0; l < H.lv.size(); ++l) {
+    Level& L = *H.lv[l];
+    const size_t bytes = (size_t)R * L.ld * es;
+    if (l > 0) {
+      L.b.alloc(bytes);
+      L.x.alloc(bytes);
+    }
+    if (l + 1 < H.lv.size()) {
+      L.t.alloc(bytes);
+      L.r.alloc(bytes);
+    }
+  }
+  if (H.lv.size() > 0 && H.nc * 16 > 200LL * 1024) H.bandwork.alloc((size_t)R * H.nc * 16);
+}
+
+// ---- multigrid cycle -----------------------------------------------------------
+
+template <typename T> const cplx<T>* fine_diag(hz_handle* h);
+template <> const double2* fine_diag<double>(hz_handle* h) { return h->diagSH.as<double2>(); }
+template <> const float2* fine_diag<float>(hz_handle* h) { return h->diagSH32.as<float2>(); }
+template <typename T> const cplx<T>* fine_dinv(hz_handle* h);
+template <> const double2* fine_dinv<double>(hz_handle* h) { return h->dinvSH.as<double2>(); }
+template <> const float2* fine_dinv<float>(hz_handle* h) { return h->dinvSH32.as<float2>(); }
+template <typename T> const cplx<T>* lev_coef(Level& L);
+template <> const double2* lev_coef<double>(Level& L) { return L.coef64.as<double2>(); }
+template <> const float2* lev_coef<float>(Level& L) { return L.coef32.as<float2>(); }
+template <typename T> const cplx<T>* lev_dinv(Level& L);
+template <> const double2* lev_dinv<double>(Level& L) { return L.dinv64.as<double2>(); }
+template <> const float2* lev_dinv<float>(Level& L) { return L.dinv32.as<float2>(); }
+
+// One level operation in precision T with right-hand side of precision TB.
+template <typename T, typename TB>
+void lev_op(hz_handle* h, Hierarchy& H, int l, int mode, const cplx<T>* x, const cplx<TB>* b, cplx<T>* y,
+            const int* cols, int nc) {
+  Level& L = *H.lv[l];
+  const double w = h->opt.relax_param;
+  if (l == 0) {
+    FineOp fop = h->fop;
+    fop.adj = H.adj;
+    launch_fine<T, T, TB>(h->ctx, mode, fop, fine_diag<T>(h), fine_dinv<T>(h), x, b, y, L.ld, cols, nc, w);
+  } else {
+    launch_rap<T, TB>(h->ctx, mode, L.g, lev_coef<T>(L), L.g.N, lev_dinv<T>(L), x, b, y, L.ld, cols, nc, w);
+  }
+}
+
+template <typename T, typename TB>
+void lev_jacobi0(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* y, const int* cols, int nc) {
+  Level& L = *H.lv[l];
+  const cplx<T>* dinv = (l == 0) ? fine_dinv<T>(h) : lev_dinv<T>(L);
+  launch_jacobi0<T, TB>(h->ctx, L.g, dinv, l == 0 ? H.adj : 0, b, y, L.ld, cols, nc, h->opt.relax_param);
+}
+
+// x_out = cycle(b) on level l with zero initial guess.
+template <typename T, typename TB>
+void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out, const int* cols, int nc) {
+  Level& L = *H.lv[l];
+  const int last = (int)H.lv.size() - 1;
+  if (l == last) {
+    if (!std::is_same<T, TB>::value) fail(HZ_ERR_STATE, "single-level mixed hierarchy is not supported");
+    launch_band_solve<T>(h->ctx, H.nc, H.kl, H.ku, H.ab.as<double2>(), H.ipiv.as<int>(), (const cplx<T>*)b, out,
+                         L.ld, cols, nc, H.bandwork.as<double2>());
+    return;
+  }
+  Level& C = *H.lv[l + 1];
+  const int pre = std::max(0, h->opt.relax_pre), post = std::max(0, h->opt.relax_post);
+  cplx<T>* tb = L.t.as<cplx<T>>();
+  cplx<T>* rb = L.r.as<cplx<T>>();
+  // choose the first buffer so that the last Jacobi sweep lands in `out`
+  const int writes = (pre > 0 ? pre : 0) + post;
+  cplx<T>* cur;
+  cplx<T>* oth;
+  if (pre > 0) {
+    cur = (writes % 2 == 1) ? out : tb;
+    oth = (cur == out) ? tb : out;
+  } else {
+    cur = (post % 2 == 0) ? out : tb;
+    oth = (cur == out) ? tb : out;
+  }
+  const int ncalls = (h->opt.cycle == 'W' && l + 1 < last) ? 2 : 1;
+  bool zero_guess = true;
+  if (pre > 0) {
+    lev_jacobi0<T, TB>(h, H, l, b, cur, cols, nc);
+    for (int s = 1; s < pre; ++s) {
+      lev_op<T, TB>(h, H, l, MODE_JACOBI, cur, b, oth, cols, nc);
+      std::swap(cur, oth);
+    }
+    zero_guess = false;
+  }
+  for (int call = 0; call < ncalls; ++call) {
+    if (zero_guess) {
+      // residual = b: restrict b directly
+      if (std::is_same<T, TB>::value) {
+        launch_restrict<T>(h->ctx, L.g, C.g, (const cplx<T>*)b, L.ld, C.b.as<cplx<T>>(), C.ld, cols, nc);
+      } else {
+        launch_cast_cols<T, TB>(h->ctx, L.g.N, b, L.ld, rb, L.ld, cols, nc);
+        launch_restrict<T>(h->ctx, L.g, C.g, rb, L.ld, C.b.as<cplx<T>>(), C.ld, cols, nc);
+      }
+    } else {
+      lev_op<T, TB>(h, H, l, MODE_RESID, cur, b, rb, cols, nc);
+      launch_restrict<T>(h->ctx, L.g, C.g, rb, L.ld, C.b.as<cplx<T>>(), C.ld, cols, nc);
+    }
+    mg_cycle<T, T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+    launch_prolong<T>(h->ctx, L.g, C.g, C.x.as<cplx<T>>(), C.ld, zero_guess ? nullptr : cur, cur, L.ld, cols, nc);
+    zero_guess = false;
+  }
+  for (int s = 0; s < post; ++s) {
+    lev_op<T, TB>(h, H, l, MODE_JACOBI, cur, b, oth, cols, nc);
+    std::swap(cur, oth);
+  }
+  if (cur != out) fail(HZ_ERR_STATE, "internal: cycle result not in output buffer");
+}
+
+// Z_j = M^{-1} V_j for the active columns.
+void precondition(hz_handle* h, Hierarchy& H, const double2* vj, void* zj, const int* cols, int nc) {
+  if (h->opt.precision == HZ_PREC_MIXED) {
+    if (H.lv.size() == 1) {
+      // single level: FP64 band solve then cast
+      fail(HZ_ERR_ARG, "mixed precision needs at least 2 multigrid levels");
+    }
+    mg_cycle<float, double>(h, H, 0, vj, (float2*)zj, cols, nc);
+  } else {
+    mg_cycle<double, double>(h, H, 0, vj, (double2*)zj, cols, nc);
+  }
+}
+
+// y = H x (outer operator, FP64 arithmetic) for the active columns.
+template <typename TX>
+void apply_H(hz_handle* h, int adj, int mode, const cplx<TX>* x, const double2* b, double2* y, const int* cols,
+             int nc) {
+  FineOp fop = h->fop;
+  fop.adj = adj;
+  launch_fine<double, TX, double>(h->ctx, mode, fop, h->diagH.as<double2>(), nullptr, x, b, y, h->g0.N, cols, nc,
+                                  0.0);
+}
+
+void upload_cols(hz_handle* h, const std::vector<int>& c) {
+  ck(cudaMemcpyAsync(h->cols.p, c.data(), c.size() * sizeof(int), cudaMemcpyHostToDevice, h->ctx.stream),
+     "upload cols");
+  // the host vector must stay valid until the copy is done
+  ck(cudaStreamSynchronize(h->ctx.stream), "sync cols");
+}
+
+// Column 2-norms of a block into host memory.
+void col_norms(hz_handle* h, const double2* x, const std::vector<int>& cols, double* dev_nrm, double* dev_inv,
+               double* host_out) {
+  const long long N = h->g0.N;
+  const int nc = (int)cols.size();
+  const int nblk = krylov_nblk(N, nc);
+  const int* dc = h->cols.as<int>();
+  const int HS = h->mcap + 2;
+  launch_dots(h->ctx, N, x, 0, N, 0, 0, x, N, dc, nc, nblk, 1, h->part.as<double2>());
+  launch_reduce(h->ctx, h->part.as<double2>(), dc, nc, 1, nblk, h->nr.as<double2>(), HS, 0);
+  launch_norms(h->ctx, h->nr.as<double2>(), HS, 0, dc, nc, dev_nrm, dev_inv);
+  if (host_out) {
+    ck(cudaMemcpyAsync(h->h_nrm, dev_nrm, (size_t)h->rcap * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "norms d2h");
+    sync(h);
+    for (int c : cols) host_out[c] = h->h_nrm[c];
+  }
+}
+
+// FGMRES(m) on H (or H^H) right-preconditioned by one multigrid cycle.
+int fgmres(hz_handle* h, int adj, int nrhs) {
+  Hierarchy& H = h->hier[adj];
+  const long long N = h->g0.N;
+  const int m = h->mcap;
+  const int HS = m + 2;
+  const bool mixed = h->opt.precision == HZ_PREC_MIXED;
+  const size_t zb = mixed ? 8 : 16;
+  double2* B = h->Bd.as<double2>();
+  double2* X = h->Xd.as<double2>();
+  double2* V = h->V.as<double2>();
+  const long long vstride = h->rcap;
+  auto Vj = [&](int j) { return V + (long long)j * vstride * N; };
+  auto Zj = [&](int j) { return (char*)h->Z.p + (size_t)j * vstride * N * zb; };
+  double2* part = h->part.as<double2>();
+  int* dc = h->cols.as<int>();
+
+  std::vector<int> all(nrhs);
+  for (int c = 0; c < nrhs; ++c) all[c] = c;
+  upload_cols(h, all);
+  std::vector<double> bn(nrhs, 0.0), rn(nrhs, 0.0);
+  col_norms(h, B, all, h->bnorm.as<double>(), h->bnorm_inv.as<double>(), bn.data());
+  launch_zero_cols<double>(h->ctx, N, X, N, dc, nrhs);
+  h->col_relres.assign(nrhs, 0.0);
+  h->col_iters.assign(nrhs, 0);
+  std::vector<int> act;
+  for (int c = 0; c < nrhs; ++c) {
+    if (!std::isfinite(bn[c])) fail(HZ_ERR_NUMERIC, "right-hand side column %d holds NaN or Inf", c);
+    if (bn[c] > 0) act.push_back(c);
+  }
+  if (act.empty()) return 0;
+  if (mixed)
+    ensure_level_buffers<float>(h, H, h->rcap);
+  else
+    ensure_level_buffers<double>(h, H, h->rcap);
+  const double tol = h->opt.rel_tol;
+  // r0 = b (x0 = 0): V_0 = b / ||b||
+  upload_cols(h, act);
+  launch_scale_cols(h->ctx, N, B, N, Vj(0), N, h->bnorm_inv.as<double>(), dc, (int)act.size());
+  launch_cycle_init(h->ctx, m, dc, (int)act.size(), h->bnorm.as<double>(), h->gv.as<double2>());
+  std::vector<int> kcol(h->rcap, 0);
+  int outer = 0;
+  for (outer = 1; outer <= std::max(1, h->opt.max_outer); ++outer) {
+    std::vector<int> live = act;
+    std::fill(kcol.begin(), kcol.end(), 0);
+    for (int j = 0; j < m && !live.empty(); ++j) {
+      upload_cols(h, live);
+      const int nl = (int)live.size();
+      precondition(h, H, Vj(j), Zj(j), dc, nl);
+      double2* w = Vj(j + 1);
+      if (mixed)
+        apply_H<float>(h, adj, MODE_APPLY, (const float2*)Zj(j), nullptr, w, dc, nl);
+      else
+        apply_H<double>(h, adj, MODE_APPLY, (const double2*)Zj(j), nullptr, w, dc, nl);
+      // classical Gram-Schmidt, two passes
+      const int K = j + 1;
+      const int nblk = krylov_nblk(N, nl);
+      double2* hA = h->hA.as<double2>();
+      double2* hB = h->hB.as<double2>();
+      for (int i0 = 0; i0 < K; i0 += 16) {
+        const int k = std::min(16, K - i0);
+        launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, 0, part);
+        launch_reduce(h->ctx, part, dc, nl, k, nblk, hA + i0, HS, 0);
+      }
+      if (K <= 16) {
+        launch_update(h->ctx, N, V, vstride, N, 0, K, hA, HS, w, N, dc, nl, nblk, 1, 0, part);
+        launch_reduce(h->ctx, part, dc, nl, K, nblk, hB, HS, 0);
+      } else {
+        for (int i0 = 0; i0 < K; i0 += 16)
+          launch_update(h->ctx, N, V, vstride, N, i0, std::min(16, K - i0), hA, HS, w, N, dc, nl, nblk, 0, 0, part);
+        for (int i0 = 0; i0 < K; i0 += 16) {
+          const int k = std::min(16, K - i0);
+          launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, 0, part);
+          launch_reduce(h->ctx, part, dc, nl, k, nblk, hB + i0, HS, 0);
+        }
+      }
+      for (int i0 = 0; i0 < K; i0 += 16) {
+        const int k = std::min(16, K - i0);
+        const bool lastg = i0 + 16 >= K;
+        launch_update(h->ctx, N, V, vstride, N, i0, k, hB, HS, w, N, dc, nl, nblk, 0, lastg ? 1 : 0, part);
+        if (lastg) launch_reduce(h->ctx, part, dc, nl, 1, nblk, h->nr.as<double2>(), HS, 0);
+      }
+      launch_arnoldi_step(h->ctx, j, m, dc, nl, hA, hB, h->nr.as<double2>(), HS, h->Hh.as<double2>(),
+                          h->cs.as<double2>(), h->sn.as<double2>(), h->gv.as<double2>(), h->est.as<double>(),
+                          h->invhn.as<double>());
+      launch_scale_cols(h->ctx, N, w, N, w, N, h->invhn.as<double>(), dc, nl);
+      ck(cudaMemcpyAsync(h->h_est, h->est.p, (size_t)h->rcap * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "est");
+      sync(h);
+      std::vector<int> still;
+      for (int c : live) {
+        kcol[c] = j + 1;
+        h->col_iters[c] += 1;
+        h->nprec += 1;
+        const double e = h->h_est[c];
+        if (!std::isfinite(e)) fail(HZ_ERR_NUMERIC, "FGMRES breakdown (NaN/Inf) in column %d", c);
+        if (!(e / bn[c] <= tol)) still.push_back(c);
+      }
+      live.swap(still);
+    }
+    // x += Z y
+    upload_cols(h, act);
+    ck(cudaMemcpyAsync(h->kcol.p, kcol.data(), (size_t)h->rcap * sizeof(int), cudaMemcpyHostToDevice,
+                       h->ctx.stream),
+       "kcol");
+    launch_lsq(h->ctx, m, dc, (int)act.size(), h->kcol.as<int>(), h->Hh.as<double2>(), h->gv.as<double2>(),
+               h->yv.as<double2>());
+    if (mixed)
+      launch_update_x<float>(h->ctx, N, (const float2*)h->Z.p, vstride, N, h->kcol.as<int>(), h->yv.as<double2>(), m,
+                             X, N, dc, (int)act.size());
+    else
+      launch_update_x<double>(h->ctx, N, (const double2*)h->Z.p, vstride, N, h->kcol.as<int>(), h->yv.as<double2>(),
+                              m, X, N, dc, (int)act.size());
+    // true residual r = b - H x into V_0, its norm, convergence test
+    apply_H<double>(h, adj, MODE_RESID, X, B, Vj(0), dc, (int)act.size());
+    col_norms(h, Vj(0), act, h->beta.as<double>(), h->beta_inv.as<double>(), rn.data());
+    std::vector<int> next;
+    for (int c : act) {
+      h->col_relres[c] = rn[c] / bn[c];
+      if (!std::isfinite(rn[c])) fail(HZ_ERR_NUMERIC, "residual of column %d is NaN or Inf", c);
+      if (!(h->col_relres[c] <= tol)) next.push_back(c);
+    }
+    act.swap(next);
+    if (act.empty()) break;
+    if (outer == std::max(1, h->opt.max_outer)) break;
+    upload_cols(h, act);
+    launch_scale_cols(h->ctx, N, Vj(0), N, Vj(0), N, h->beta_inv.as<double>(), dc, (int)act.size());
+    launch_cycle_init(h->ctx, m, dc, (int)act.size(), h->beta.as<double>(), h->gv.as<double2>());
+  }
+  return std::min(outer, std::max(1, h->opt.max_outer));
+}
+
+void init_fine(hz_handle* h) {
+  const hz_problem& p = h->prob;
+  const long long N = num_nodes(p);
+  h->g0 = make_grid(p);
+  FineOp f{};
+  f.g = h->g0;
+  const double BC = p.order_neumann_bc == 1 ? 1.0 : 2.0;
+  for (int d = 0; d < 3; ++d) {
+    const double hd = d < p.dim ? p.h[d] : 1.0;
+    f.o[d] = 1.0 / (hd * hd);
+    f.b[d] = BC / (hd * hd);
+  }
+  f.adj = 0;
+  h->fop = f;
+  // diagonals on the host in FP64
+  std::vector<std::complex<double>> mass((size_t)N), dH((size_t)N), dSH((size_t)N), iSH((size_t)N);
+  int st = hz_helmholtz_mass(&h->prob, reinterpret_cast<double*>(mass.data()));
+  if (st != HZ_OK) fail(st, "invalid problem (mass term)");
+  const Grid g = h->g0;
+  const double s = h->opt.shift;
+  const double w2 = p.omega_re * p.omega_re;  // shift uses real omega (GetHelmholtzShiftOP)
+  for (long long q = 0; q < N; ++q) {
+    const int i = (int)(q % g.nx), j = (int)((q / g.nx) % g.ny), k = (int)(q / ((long long)g.nx * g.ny));
+    const int pos[3] = {i, j, k};
+    const int nn[3] = {g.nx, g.ny, g.nz};
+    double lap = 0.0;
+    for (int d = 0; d < p.dim; ++d) {
+      const bool bnd = pos[d] == 0 || pos[d] == nn[d] - 1;
+      lap += (bnd ? BC : 2.0) / (p.h[d] * p.h[d]);
+    }
+    dH[(size_t)q] = lap + mass[(size_t)q];
+    dSH[(size_t)q] = dH[(size_t)q] + std::complex<double>(0.0, s * w2 * p.m[q]);
+    iSH[(size_t)q] = 1.0 / dSH[(size_t)q];
+  }
+  h->diagH.alloc((size_t)N * 16);
+  h->diagSH.alloc((size_t)N * 16);
+  h->dinvSH.alloc((size_t)N * 16);
+  ck(cudaMemcpy(h->diagH.p, dH.data(), N * 16, cudaMemcpyHostToDevice), "upload diagH");
+  ck(cudaMemcpy(h->diagSH.p, dSH.data(), N * 16, cudaMemcpyHostToDevice), "upload diagSH");
+  ck(cudaMemcpy(h->dinvSH.p, iSH.data(), N * 16, cudaMemcpyHostToDevice), "upload dinvSH");
+  if (h->opt.precision == HZ_PREC_MIXED) {
+    h->diagSH32.alloc((size_t)N * 8);
+    h->dinvSH32.alloc((size_t)N * 8);
+    launch_cast<float, double>(h->ctx, h->diagSH.as<double2>(), h->diagSH32.as<float2>(), N);
+    launch_cast<float, double>(h->ctx, h->dinvSH.as<double2>(), h->dinvSH32.as<float2>(), N);
+    sync(h);
+  }
+}
+
+void validate(const hz_problem* p, const hz_options* o) {
+  if (!p || !o) fail(HZ_ERR_ARG, "null problem or options");
+  if (p->dim != 2 && p->dim != 3) fail(HZ_ERR_ARG, "dim must be 2 or 3 (got %d)", p->dim);
+  for (int d = 0; d < p->dim; ++d) {
+    if (p->n[d] < 1) fail(HZ_ERR_ARG, "n[%d] must be >= 1", d);
+    if (!(p->h[d] > 0)) fail(HZ_ERR_ARG, "h[%d] must be > 0", d);
+  }
+  if (!p->m || !p->gamma) fail(HZ_ERR_ARG, "m and gamma must be given");
+  if (!(p->omega_re != 0.0)) fail(HZ_ERR_ARG, "omega must have a nonzero real part");
+  if (o->levels < 1 || o->levels > 16) fail(HZ_ERR_ARG, "levels must be in [1, 16]");
+  if (o->inner < 1 || o->inner > 64) fail(HZ_ERR_ARG, "inner (restart length) must be in [1, 64]");
+  if (o->krylov != HZ_KRYLOV_FGMRES) fail(HZ_ERR_ARG, "only the FGMRES Krylov method is built");
+  if (o->cycle != 'V' && o->cycle != 'W') fail(HZ_ERR_ARG, "cycle must be 'V' or 'W'");
+  if (o->coarse_op != HZ_COARSE_GALERKIN) fail(HZ_ERR_ARG, "only Galerkin coarse operators are built");
+  if (o->precision != HZ_PREC_FP64 && o->precision != HZ_PREC_MIXED) fail(HZ_ERR_ARG, "unknown precision");
+  if (o->precision == HZ_PREC_MIXED && o->levels < 2) fail(HZ_ERR_ARG, "mixed precision needs at least 2 levels");
+  if (!(o->rel_tol > 0)) fail(HZ_ERR_ARG, "rel_tol must be > 0");
+}
+
+void copy_in(hz_handle* h, const double* src, double2* dst, long long N, int nrhs, int mem) {
+  const size_t bytes = (size_t)N * nrhs * 16;
+  if (mem == HZ_MEM_HOST) {
+    ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->ctx.stream), "copy B to device");
+    h->h2d += (long long)bytes;
+  } else {
+    ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, h->ctx.stream), "copy B on device");
+  }
+}
+
+void copy_out(hz_handle* h, const double2* src, double* dst, long long N, int nrhs, int mem) {
+  const size_t bytes = (size_t)N * nrhs * 16;
+  if (mem == HZ_MEM_HOST) {
+    ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->ctx.stream), "copy X to host");
+    h->d2h += (long long)bytes;
+  } else {
+    ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, h->ctx.stream), "copy X on device");
+  }
+}
+
+template <typename F>
+int guarded(hz_handle* h, F&& f) {
+  try {
+    f();
+    return HZ_OK;
+  } catch (const HzError& e) {
+    if (h) h->err = e.msg;
+    g_thread_error = e.msg;
+    return e.code;
+  } catch (const std::exception& e) {
+    if (h) h->err = e.what();
+    g_thread_error = e.what();
+    return HZ_ERR_CUDA;
+  }
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int32_t hz_version(void) { return HZ_ABI_VERSION; }
+
+const char* hz_last_error(const hz_handle* h) { return h ? h->err.c_str() : g_thread_error.c_str(); }
+
+void hz_default_options(hz_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->levels = 3;
+  o->max_outer = 50;
+  o->rel_tol = 1e-8;
+  o->relax_pre = 1;
+  o->relax_post = 1;
+  o->relax_param = 0.8;
+  o->cycle = 'V';
+  o->krylov = HZ_KRYLOV_FGMRES;
+  o->inner = 10;
+  o->shift = 0.5;
+  o->precision = HZ_PREC_FP64;
+  o->coarse_op = HZ_COARSE_GALERKIN;
+}
+
+int hz_create(const hz_problem* prob, const hz_options* opt, hz_handle** out) {
+  if (!out) return HZ_ERR_ARG;
+  *out = nullptr;
+  auto h = std::make_unique<hz_handle>();
+  int st = guarded(nullptr, [&] {
+    validate(prob, opt);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      fail(HZ_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (opt->device < 0 || opt->device >= ndev) fail(HZ_ERR_ARG, "device %d out of range", opt->device);
+    h->prob = *prob;
+    h->opt = *opt;
+    if (h->prob.order_neumann_bc != 1) h->prob.order_neumann_bc = 2;
+    const long long N = num_nodes(*prob);
+    h->m.assign(prob->m, prob->m + N);
+    h->gamma.assign(prob->gamma, prob->gamma + N);
+    h->prob.m = h->m.data();
+    h->prob.gamma = h->gamma.data();
+    h->dev = opt->device;
+    set_device(h.get());
+    ck(cudaStreamCreateWithFlags(&h->ctx.stream, cudaStreamNonBlocking), "stream");
+    h->ctx.profile = opt->profile != 0;
+    auto t0 = clk::now();
+    init_fine(h.get());
+    h->setup_time += secs(t0, clk::now());
+  });
+  if (st != HZ_OK) {
+    if (h->ctx.stream) cudaStreamDestroy(h->ctx.stream);
+    return st;
+  }
+  *out = h.release();
+  return HZ_OK;
+}
+
+int hz_destroy(hz_handle* h) {
+  if (!h) return HZ_OK;
+  cudaSetDevice(h->dev);
+  if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
+  h->ctx.release();
+  if (h->h_est) cudaFreeHost(h->h_est);
+  if (h->h_nrm) cudaFreeHost(h->h_nrm);
+  if (h->ctx.stream) cudaStreamDestroy(h->ctx.stream);
+  delete h;
+  return HZ_OK;
+}
+
+int hz_solve(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, int32_t transpose, int32_t mem,
+             hz_stats* stats) {
+  if (!h) return HZ_ERR_ARG;
+  int conv_status = HZ_OK;
+  int st = guarded(h, [&] {
+    if (!B || !X) fail(HZ_ERR_ARG, "null B or X");
+    if (n != h->g0.N) fail(HZ_ERR_ARG, "B has %lld rows, the grid has %lld nodes", (long long)n, h->g0.N);
+    if (nrhs < 1) fail(HZ_ERR_ARG, "nrhs must be >= 1");
+    if (transpose != 0 && transpose != 1) fail(HZ_ERR_ARG, "transpose must be 0 or 1");
+    if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "mem must be HZ_MEM_HOST or HZ_MEM_DEVICE");
+    if (h->prob.omega_im != 0.0) fail(HZ_ERR_ARG, "the solver needs a real omega (GetHelmholtzShiftOP takes Float64)");
+    set_device(h);
+    const long long l0 = h->ctx.launches;
+    h->h2d = h->d2h = 0;
+    auto t0 = clk::now();
+    if (!h->hier[transpose].built) build_hierarchy(h, transpose);
+    ensure_workspace(h, nrhs);
+    auto t1 = clk::now();
+    h->setup_time += secs(t0, t1);
+    copy_in(h, B, h->Bd.as<double2>(), n, nrhs, mem);
+    const long long np0 = h->nprec;
+    int outer = fgmres(h, transpose, nrhs);
+    copy_out(h, h->Xd.as<double2>(), X, n, nrhs, mem);
+    sync(h);
+    auto t2 = clk::now();
+    h->solve_time += secs(t1, t2);
+    int nconv = 0, maxit = 0;
+    double maxrr = 0.0;
+    for (int c = 0; c < nrhs; ++c) {
+      if (h->col_relres[c] <= h->opt.rel_tol) ++nconv;
+      maxrr = std::max(maxrr, h->col_relres[c]);
+      maxit = std::max(maxit, h->col_iters[c]);
+    }
+    if (nconv < nrhs) conv_status = HZ_NOT_CONVERGED;
+    if (stats) {
+      stats->outer = outer;
+      stats->n_prec = (int32_t)(h->nprec - np0);
+      stats->max_col_iters = maxit;
+      stats->converged_cols = nconv;
+      stats->max_relres = maxrr;
+      stats->setup_time = h->setup_time;
+      stats->solve_time = h->solve_time;
+      stats->kernel_launches = h->ctx.launches - l0;
+      stats->h2d_bytes = h->h2d;
+      stats->d2h_bytes = h->d2h;
+    }
+    if (h->opt.verbose)
+      fprintf(stderr, "helmgpu: %d columns, %d outer cycles, max rel. residual %.3e, solve %.3f s\n", nrhs, outer,
+              maxrr, secs(t1, t2));
+  });
+  if (st != HZ_OK) return st;
+  if (conv_status != HZ_OK) h->err = "not converged within max_outer restart cycles";
+  return conv_status;
+}
+
+int hz_column_stats(const hz_handle* h, double* relres, int32_t* iters, int32_t nrhs) {
+  if (!h) return HZ_ERR_ARG;
+  if (nrhs > (int)h->col_relres.size()) return HZ_ERR_ARG;
+  for (int c = 0; c < nrhs; ++c) {
+    if (relres) relres[c] = h->col_relres[c];
+    if (iters) iters[c] = h->col_iters[c];
+  }
+  return HZ_OK;
+}
+
+int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, double* Y, int64_t n, int32_t nrhs,
+             int32_t mem) {
+  if (!h) return HZ_ERR_ARG;
+  return guarded(h, [&] {
+    if (!X || !Y) fail(HZ_ERR_ARG, "null X or Y");
+    if (n != h->g0.N) fail(HZ_ERR_ARG, "X has %lld rows, the grid has %lld nodes", (long long)n, h->g0.N);
+    if (nrhs < 1) fail(HZ_ERR_ARG, "nrhs must be >= 1");
+    if (op != HZ_OP_H && op != HZ_OP_SH) fail(HZ_ERR_ARG, "op must be HZ_OP_H or HZ_OP_SH");
+    if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "bad mem");
+    set_device(h);
+    const long long l0 = h->ctx.launches;
+    h->h2d = h->d2h = 0;
+    const double2* xd;
+    double2* yd;
+    const size_t bytes = (size_t)n * nrhs * 16;
+    if (mem == HZ_MEM_HOST) {
+      h->tmpA.alloc(bytes);
+      h->tmpB.alloc(bytes);
+      copy_in(h, X, h->tmpA.as<double2>(), n, nrhs, HZ_MEM_HOST);
+      xd = h->tmpA.as<double2>();
+      yd = h->tmpB.as<double2>();
+    } else {
+      xd = reinterpret_cast<const double2*>(X);
+      yd = reinterpret_cast<double2*>(Y);
+    }
+    std::vector<int> all(nrhs);
+    for (int c = 0; c < nrhs; ++c) all[c] = c;
+    DBuf dc;
+    dc.alloc(all.size() * sizeof(int));
+    ck(cudaMemcpyAsync(dc.p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, h->ctx.stream), "cols");
+    FineOp fop = h->fop;
+    fop.adj = transpose ? 1 : 0;
+    const double2* diag = (op == HZ_OP_H) ? h->diagH.as<double2>() : h->diagSH.as<double2>();
+    launch_fine<double, double, double>(h->ctx, MODE_APPLY, fop, diag, nullptr, xd, (const double2*)nullptr, yd, n,
+                                        dc.as<int>(), nrhs, 0.0);
+    if (mem == HZ_MEM_HOST) copy_out(h, yd, Y, n, nrhs, HZ_MEM_HOST);
+    sync(h);
+    (void)l0;
+  });
+}
+
+int hz_clear(hz_handle* h) {
+  if (!h) return HZ_ERR_ARG;
+  return guarded(h, [&] {
+    set_device(h);
+    sync(h);
+    for (auto& H : h->hier) {
+      H.lv.clear();
+      H.ab.reset();
+      H.ipiv.reset();
+      H.bandwork.reset();
+      H.built = false;
+    }
+  });
+}
+
+int hz_copy(const hz_handle* h, hz_handle** out) {
+  if (!h || !out) return HZ_ERR_ARG;
+  hz_problem p = h->prob;
+  return hz_create(&p, &h->opt, out);
+}
+
+void* hz_stream(hz_handle* h) { return h ? (void*)h->ctx.stream : nullptr; }
+
+int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches, double* total_ms) {
+  if (!h) return HZ_ERR_ARG;
+  h->ctx.resolve();
+  const int n = (int)h->ctx.names.size();
+  if (idx < 0 || idx >= n) return n;
+  if (name && name_len > 0) {
+    std::strncpy(name, h->ctx.names[idx].c_str(), (size_t)name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (launches) *launches = h->ctx.counts[idx];
+  if (total_ms) *total_ms = h->ctx.total_ms[idx];
+  return n;
+}
+
+int hz_reset_kernel_times(hz_handle* h) {
+  if (!h) return HZ_ERR_ARG;
+  h->ctx.resolve();
+  std::fill(h->ctx.counts.begin(), h->ctx.counts.end(), 0);
+  std::fill(h->ctx.total_ms.begin(), h->ctx.total_ms.end(), 0.0);
+  return HZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,538 @@
+// Multigrid kernels: matrix-free fine-level Helmholtz stencil, Galerkin
+// coarse-level stencils, damped Jacobi, full-weighting restriction,
+// bi/trilinear prolongation, the banded coarsest solve and the setup kernels.
+//
+// Replaces the sparse assembly + ParSpMatVec SpMV of the reference
+// (src/GetHelmholtz.jl:33-50, 85-95; src/PlainNodalLaplacian.jl:18-46) and
+// the Multigrid.jl relaxation / transfer / coarse-solve steps called from
+// src/ShiftedLaplacianMultigridSolver.jl:89.
+#include <algorithm>
+#include <cstdio>
+#include <stdexcept>
+
+#include "hz_launch.cuh"
+
+namespace hz {
+
+// ---------------------------------------------------------------------------
+// Launch bookkeeping
+// ---------------------------------------------------------------------------
+int Ctx::name_id(const char* name) {
+  for (size_t i = 0; i < names.size(); ++i)
+    if (names[i] == name) return (int)i;
+  names.emplace_back(name);
+  counts.push_back(0);
+  total_ms.push_back(0.0);
+  return (int)names.size() - 1;
+}
+
+void Ctx::before(int id, cudaEvent_t* a) {
+  (void)id;
+  if (!profile) return;
+  if (pool.empty()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    pool.push_back(e);
+  }
+  *a = pool.back();
+  pool.pop_back();
+  cudaEventRecord(*a, stream);
+}
+
+void Ctx::after(int id, cudaEvent_t a) {
+  ++launches;
+  if (!profile) return;
+  cudaEvent_t b;
+  if (pool.empty()) {
+    cudaEventCreate(&b);
+  } else {
+    b = pool.back();
+    pool.pop_back();
+  }
+  cudaEventRecord(b, stream);
+  pending.push_back({id, a, b});
+}
+
+void Ctx::resolve() {
+  for (auto& p : pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      counts[p.id] += 1;
+      total_ms[p.id] += ms;
+    }
+    pool.push_back(p.a);
+    pool.push_back(p.b);
+  }
+  pending.clear();
+}
+
+void Ctx::release() {
+  resolve();
+  for (auto e : pool) cudaEventDestroy(e);
+  pool.clear();
+}
+
+
+// ---------------------------------------------------------------------------
+// Fine-level stencil
+// ---------------------------------------------------------------------------
+template <typename T> struct FineOpT {
+  int nx, ny, nz;
+  long long N;
+  T o[3], b[3];
+  int adj;
+};
+
+// Off-diagonal magnitudes of the two neighbours of node i on an axis of n
+// nodes.  Row i of the 1D operator is (2u_i - u_{i-1} - u_{i+1})/h^2 inside and
+// (BC u_0 - BC u_1)/h^2, (BC u_{n-1} - BC u_{n-2})/h^2 on the boundary rows
+// (src/PlainNodalLaplacian.jl:18-30).  The adjoint takes entry (j, i).
+template <typename T>
+__device__ __forceinline__ void axis_coef(int i, int n, T o, T bb, int adj, T& cl, T& cr) {
+  if (!adj) {
+    cl = (i > 0) ? ((i == n - 1) ? bb : o) : T(0);
+    cr = (i < n - 1) ? ((i == 0) ? bb : o) : T(0);
+  } else {
+    cl = (i > 0) ? ((i - 1 == 0) ? bb : o) : T(0);
+    cr = (i < n - 1) ? ((i + 1 == n - 1) ? bb : o) : T(0);
+  }
+}
+
+template <typename T, typename TX, typename TB, int MODE, bool IS3D>
+__global__ void __launch_bounds__(256) k_fine(FineOpT<T> op, const cplx<T>* __restrict__ diag,
+                                              const cplx<T>* __restrict__ dinv, const cplx<TX>* __restrict__ x,
+                                              const cplx<TB>* __restrict__ b, cplx<T>* __restrict__ y, long long ld,
+                                              const int* __restrict__ cols, int ncols, int cpb, T w) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= op.N) return;
+  const int nx = op.nx, ny = op.ny;
+  const int i = (int)(p % nx);
+  const long long t = p / nx;
+  const int j = (int)(t % ny);
+  const int k = (int)(t / ny);
+  T cxl, cxr, cyl, cyr, czl = 0, czr = 0;
+  axis_coef<T>(i, nx, op.o[0], op.b[0], op.adj, cxl, cxr);
+  axis_coef<T>(j, ny, op.o[1], op.b[1], op.adj, cyl, cyr);
+  if (IS3D) axis_coef<T>(k, op.nz, op.o[2], op.b[2], op.adj, czl, czr);
+  // clamped neighbour offsets: a missing neighbour has a zero coefficient
+  const long long sx = 1, sy = nx, sz = (long long)nx * ny;
+  const long long oxl = (i > 0) ? -sx : 0, oxr = (i < nx - 1) ? sx : 0;
+  const long long oyl = (j > 0) ? -sy : 0, oyr = (j < ny - 1) ? sy : 0;
+  long long ozl = 0, ozr = 0;
+  if (IS3D) {
+    ozl = (k > 0) ? -sz : 0;
+    ozr = (k < op.nz - 1) ? sz : 0;
+  }
+  cplx<T> d = diag[p];
+  if (op.adj) d.y = -d.y;
+  cplx<T> di = mk<T>(0, 0);
+  if (MODE == MODE_JACOBI) {
+    di = dinv[p];
+    if (op.adj) di.y = -di.y;
+  }
+  const int c0 = blockIdx.y * cpb;
+  const int c1 = min(ncols, c0 + cpb);
+  for (int ci = c0; ci < c1; ++ci) {
+    const long long off = (long long)cols[ci] * ld;
+    const cplx<TX>* xc = x + off + p;
+    const cplx<T> xp = ccast<T, TX>(xc[0]);
+    const cplx<T> a = ccast<T, TX>(xc[oxl]), bq = ccast<T, TX>(xc[oxr]);
+    const cplx<T> c = ccast<T, TX>(xc[oyl]), e = ccast<T, TX>(xc[oyr]);
+    T sr = cxl * a.x + cxr * bq.x + cyl * c.x + cyr * e.x;
+    T si = cxl * a.y + cxr * bq.y + cyl * c.y + cyr * e.y;
+    if (IS3D) {
+      const cplx<T> f = ccast<T, TX>(xc[ozl]), g = ccast<T, TX>(xc[ozr]);
+      sr += czl * f.x + czr * g.x;
+      si += czl * f.y + czr * g.y;
+    }
+    cplx<T> ax = mk<T>(-sr, -si);
+    ax = cfma<T>(d, xp, ax);
+    if (MODE == MODE_APPLY) {
+      y[off + p] = ax;
+    } else {
+      const cplx<TB> bb = b[off + p];
+      const cplx<T> r = mk<T>((T)bb.x - ax.x, (T)bb.y - ax.y);
+      if (MODE == MODE_RESID) {
+        y[off + p] = r;
+      } else {
+        const cplx<T> dr = cmul<T>(di, r);
+        y[off + p] = mk<T>(xp.x + w * dr.x, xp.y + w * dr.y);
+      }
+    }
+  }
+}
+
+template <typename T, typename TX, typename TB>
+void launch_fine(Ctx& ctx, int mode, const FineOp& op, const cplx<T>* diag, const cplx<T>* dinv, const cplx<TX>* x,
+                 const cplx<TB>* b, cplx<T>* y, long long ld, const int* cols, int ncols, double w) {
+  if (ncols <= 0) return;
+  FineOpT<T> o;
+  o.nx = op.g.nx;
+  o.ny = op.g.ny;
+  o.nz = op.g.nz;
+  o.N = op.g.N;
+  for (int d = 0; d < 3; ++d) {
+    o.o[d] = (T)op.o[d];
+    o.b[d] = (T)op.b[d];
+  }
+  o.adj = op.adj;
+  const int TPB = 256;
+  long long nbx = (op.g.N + TPB - 1) / TPB;
+  int ch = chunks_for(nbx, ncols);
+  int cpb = (ncols + ch - 1) / ch;
+  dim3 grid((unsigned)nbx, (unsigned)ch);
+  const bool is3d = op.g.nz > 1;
+#define HZ_FINE_CASE(M, D, NAME) \
+  HZ_LAUNCH(ctx, NAME, (k_fine<T, TX, TB, M, D>), grid, TPB, 0, o, diag, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
+  if (mode == MODE_APPLY) {
+    if (is3d) HZ_FINE_CASE(MODE_APPLY, true, "fine_apply");
+    else HZ_FINE_CASE(MODE_APPLY, false, "fine_apply");
+  } else if (mode == MODE_RESID) {
+    if (is3d) HZ_FINE_CASE(MODE_RESID, true, "fine_resid");
+    else HZ_FINE_CASE(MODE_RESID, false, "fine_resid");
+  } else {
+    if (is3d) HZ_FINE_CASE(MODE_JACOBI, true, "fine_jacobi");
+    else HZ_FINE_CASE(MODE_JACOBI, false, "fine_jacobi");
+  }
+#undef HZ_FINE_CASE
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin (stored-coefficient) stencil
+// ---------------------------------------------------------------------------
+template <typename T, typename TB, int MODE, bool IS3D>
+__global__ void __launch_bounds__(128) k_rap(Grid g, const cplx<T>* __restrict__ coef, long long cld,
+                                             const cplx<T>* __restrict__ dinv, const cplx<T>* __restrict__ x,
+                                             const cplx<TB>* __restrict__ b, cplx<T>* __restrict__ y, long long ld,
+                                             const int* __restrict__ cols, int ncols, int cpb, T w) {
+  constexpr int NS = IS3D ? 27 : 9;
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.N) return;
+  const int nx = g.nx, ny = g.ny;
+  const int i = (int)(p % nx);
+  const long long t = p / nx;
+  const int j = (int)(t % ny);
+  const int k = (int)(t / ny);
+  const long long sy = nx, sz = (long long)nx * ny;
+  const long long dxo[3] = {(i > 0) ? -1LL : 0LL, 0LL, (i < nx - 1) ? 1LL : 0LL};
+  const long long dyo[3] = {(j > 0) ? -sy : 0LL, 0LL, (j < ny - 1) ? sy : 0LL};
+  long long dzo[3] = {0, 0, 0};
+  if (IS3D) {
+    dzo[0] = (k > 0) ? -sz : 0;
+    dzo[2] = (k < g.nz - 1) ? sz : 0;
+  }
+  cplx<T> c[NS];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    c[s] = coef[s * cld + p];
+  }
+  cplx<T> di = mk<T>(0, 0);
+  if (MODE == MODE_JACOBI) di = dinv[p];
+  const int c0 = blockIdx.y * cpb;
+  const int c1 = min(ncols, c0 + cpb);
+  for (int ci = c0; ci < c1; ++ci) {
+    const long long off = (long long)cols[ci] * ld;
+    const cplx<T>* xc = x + off + p;
+    cplx<T> ax = mk<T>(0, 0);
+    cplx<T> xp = mk<T>(0, 0);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const long long o = dxo[s % 3] + dyo[(s / 3) % 3] + (IS3D ? dzo[s / 9] : 0LL);
+      const cplx<T> v = xc[o];
+      if (s == NS / 2) xp = v;
+      ax = cfma<T>(c[s], v, ax);
+    }
+    if (MODE == MODE_APPLY) {
+      y[off + p] = ax;
+    } else {
+      const cplx<TB> bb = b[off + p];
+      const cplx<T> r = mk<T>((T)bb.x - ax.x, (T)bb.y - ax.y);
+      if (MODE == MODE_RESID) {
+        y[off + p] = r;
+      } else {
+        const cplx<T> dr = cmul<T>(di, r);
+        y[off + p] = mk<T>(xp.x + w * dr.x, xp.y + w * dr.y);
+      }
+    }
+  }
+}
+
+template <typename T, typename TB>
+void launch_rap(Ctx& ctx, int mode, const Grid& g, const cplx<T>* coef, long long cld, const cplx<T>* dinv,
+                const cplx<T>* x, const cplx<TB>* b, cplx<T>* y, long long ld, const int* cols, int ncols, double w) {
+  if (ncols <= 0) return;
+  const int TPB = 128;
+  long long nbx = (g.N + TPB - 1) / TPB;
+  int ch = chunks_for(nbx, ncols);
+  int cpb = (ncols + ch - 1) / ch;
+  dim3 grid((unsigned)nbx, (unsigned)ch);
+  const bool is3d = g.nz > 1;
+#define HZ_RAP_CASE(M, D, NAME) \
+  HZ_LAUNCH(ctx, NAME, (k_rap<T, TB, M, D>), grid, TPB, 0, g, coef, cld, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
+  if (mode == MODE_APPLY) {
+    if (is3d) HZ_RAP_CASE(MODE_APPLY, true, "rap_apply");
+    else HZ_RAP_CASE(MODE_APPLY, false, "rap_apply");
+  } else if (mode == MODE_RESID) {
+    if (is3d) HZ_RAP_CASE(MODE_RESID, true, "rap_resid");
+    else HZ_RAP_CASE(MODE_RESID, false, "rap_resid");
+  } else {
+    if (is3d) HZ_RAP_CASE(MODE_JACOBI, true, "rap_jacobi");
+    else HZ_RAP_CASE(MODE_JACOBI, false, "rap_jacobi");
+  }
+#undef HZ_RAP_CASE
+}
+
+// ---------------------------------------------------------------------------
+// First Jacobi sweep from a zero guess: y = w dinv b
+// ---------------------------------------------------------------------------
+template <typename T, typename TB>
+__global__ void __launch_bounds__(256) k_jacobi0(long long N, const cplx<T>* __restrict__ dinv, int adj,
+                                                 const cplx<TB>* __restrict__ b, cplx<T>* __restrict__ y, long long ld,
+                                                 const int* __restrict__ cols, int ncols, int cpb, T w) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  cplx<T> di = dinv[p];
+  if (adj) di.y = -di.y;
+  di.x *= w;
+  di.y *= w;
+  const int c0 = blockIdx.y * cpb;
+  const int c1 = min(ncols, c0 + cpb);
+  for (int ci = c0; ci < c1; ++ci) {
+    const long long off = (long long)cols[ci] * ld;
+    const cplx<TB> bb = b[off + p];
+    y[off + p] = cmul<T>(di, mk<T>((T)bb.x, (T)bb.y));
+  }
+}
+
+template <typename T, typename TB>
+void launch_jacobi0(Ctx& ctx, const Grid& g, const cplx<T>* dinv, int adj, const cplx<TB>* b, cplx<T>* y, long long ld,
+                    const int* cols, int ncols, double w) {
+  if (ncols <= 0) return;
+  const int TPB = 256;
+  long long nbx = (g.N + TPB - 1) / TPB;
+  int ch = chunks_for(nbx, ncols);
+  int cpb = (ncols + ch - 1) / ch;
+  dim3 grid((unsigned)nbx, (unsigned)ch);
+  HZ_LAUNCH(ctx, "jacobi0", (k_jacobi0<T, TB>), grid, TPB, 0, g.N, dinv, adj, b, y, ld, cols, ncols, cpb, (T)w);
+}
+
+// ---------------------------------------------------------------------------
+// Transfers
+// ---------------------------------------------------------------------------
+template <typename T, bool IS3D>
+__global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const cplx<T>* __restrict__ rf, long long ldf,
+                                                  cplx<T>* __restrict__ rc, long long ldc, const int* __restrict__ cols,
+                                                  int ncols, int cpb) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= gc.N) return;
+  const int I = (int)(q % gc.nx);
+  const long long t = q / gc.nx;
+  const int J = (int)(t % gc.ny);
+  const int K = (int)(t / gc.ny);
+  const int fi = 2 * I, fj = 2 * J, fk = 2 * K;
+  const long long sy = gf.nx, sz = (long long)gf.nx * gf.ny;
+  const long long pc = fi + fj * sy + (IS3D ? fk * sz : 0);
+  // weights of the three fine nodes per axis; a missing node has weight 0
+  const T wx[3] = {(fi > 0) ? T(0.5) : T(0), T(1), (fi < gf.nx - 1) ? T(0.5) : T(0)};
+  const T wy[3] = {(fj > 0) ? T(0.5) : T(0), T(1), (fj < gf.ny - 1) ? T(0.5) : T(0)};
+  T wz[3] = {T(0), T(1), T(0)};
+  if (IS3D) {
+    wz[0] = (fk > 0) ? T(0.5) : T(0);
+    wz[2] = (fk < gf.nz - 1) ? T(0.5) : T(0);
+  }
+  const long long ox[3] = {(fi > 0) ? -1LL : 0LL, 0LL, (fi < gf.nx - 1) ? 1LL : 0LL};
+  const long long oy[3] = {(fj > 0) ? -sy : 0LL, 0LL, (fj < gf.ny - 1) ? sy : 0LL};
+  long long oz[3] = {0, 0, 0};
+  if (IS3D) {
+    oz[0] = (fk > 0) ? -sz : 0;
+    oz[2] = (fk < gf.nz - 1) ? sz : 0;
+  }
+  const T scale = IS3D ? T(0.125) : T(0.25);
+  const int c0 = blockIdx.y * cpb;
+  const int c1 = min(ncols, c0 + cpb);
+  for (int ci = c0; ci < c1; ++ci) {
+    const int col = cols[ci];
+    const cplx<T>* r = rf + (long long)col * ldf + pc;
+    T ar = 0, ai = 0;
+#pragma unroll
+    for (int c = 0; c < (IS3D ? 3 : 1); ++c) {
+#pragma unroll
+      for (int bq = 0; bq < 3; ++bq) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const T wgt = wx[a] * wy[bq] * (IS3D ? wz[c] : T(1));
+          const cplx<T> v = r[ox[a] + oy[bq] + (IS3D ? oz[c] : 0LL)];
+          ar += wgt * v.x;
+          ai += wgt * v.y;
+        }
+      }
+    }
+    rc[(long long)col * ldc + q] = mk<T>(scale * ar, scale * ai);
+  }
+}
+
+template <typename T>
+void launch_restrict(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* rf, long long ldf, cplx<T>* rc,
+                     long long ldc, const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  const int TPB = 256;
+  long long nbx = (gc.N + TPB - 1) / TPB;
+  int ch = chunks_for(nbx, ncols);
+  int cpb = (ncols + ch - 1) / ch;
+  dim3 grid((unsigned)nbx, (unsigned)ch);
+  if (gf.nz > 1)
+    HZ_LAUNCH(ctx, "restrict", (k_restrict<T, true>), grid, TPB, 0, gf, gc, rf, ldf, rc, ldc, cols, ncols, cpb);
+  else
+    HZ_LAUNCH(ctx, "restrict", (k_restrict<T, false>), grid, TPB, 0, gf, gc, rf, ldf, rc, ldc, cols, ncols, cpb);
+}
+
+template <typename T, bool IS3D>
+__global__ void __launch_bounds__(256) k_prolong(Grid gf, Grid gc, const cplx<T>* __restrict__ ec, long long ldc,
+                                                 const cplx<T>* xin, cplx<T>* xout, long long ldf,
+                                                 const int* __restrict__ cols, int ncols, int cpb) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= gf.N) return;
+  const int i = (int)(p % gf.nx);
+  const long long t = p / gf.nx;
+  const int j = (int)(t % gf.ny);
+  const int k = (int)(t / gf.ny);
+  // Parent pair per axis: (i>>1, (i+1)>>1).  An even fine index has both
+  // entries equal to its single parent, an odd one has its two neighbours, so
+  // a uniform weight of 1/2 per axis is exact linear interpolation.
+  const long long sy = gc.nx, sz = (long long)gc.nx * gc.ny;
+  const long long a0 = i >> 1, a1 = (i + 1) >> 1;
+  const long long b0 = (long long)(j >> 1) * sy, b1 = (long long)((j + 1) >> 1) * sy;
+  const long long z0 = IS3D ? (long long)(k >> 1) * sz : 0, z1 = IS3D ? (long long)((k + 1) >> 1) * sz : 0;
+  const T wgt = IS3D ? T(0.125) : T(0.25);
+  const int c0 = blockIdx.y * cpb;
+  const int c1 = min(ncols, c0 + cpb);
+  for (int ci = c0; ci < c1; ++ci) {
+    const int col = cols[ci];
+    const cplx<T>* e = ec + (long long)col * ldc;
+    cplx<T> v0 = e[z0 + b0 + a0], v1 = e[z0 + b0 + a1], v2 = e[z0 + b1 + a0], v3 = e[z0 + b1 + a1];
+    T ar = (v0.x + v1.x) + (v2.x + v3.x);
+    T ai = (v0.y + v1.y) + (v2.y + v3.y);
+    if (IS3D) {
+      cplx<T> u0 = e[z1 + b0 + a0], u1 = e[z1 + b0 + a1], u2 = e[z1 + b1 + a0], u3 = e[z1 + b1 + a1];
+      ar += (u0.x + u1.x) + (u2.x + u3.x);
+      ai += (u0.y + u1.y) + (u2.y + u3.y);
+    }
+    const long long o = (long long)col * ldf + p;
+    const cplx<T> base = xin ? xin[o] : mk<T>(0, 0);
+    xout[o] = mk<T>(base.x + wgt * ar, base.y + wgt * ai);
+  }
+}
+
+template <typename T>
+void launch_prolong(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* ec, long long ldc, const cplx<T>* xin,
+                    cplx<T>* xout, long long ldf, const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  const int TPB = 256;
+  long long nbx = (gf.N + TPB - 1) / TPB;
+  int ch = chunks_for(nbx, ncols);
+  int cpb = (ncols + ch - 1) / ch;
+  dim3 grid((unsigned)nbx, (unsigned)ch);
+  if (gf.nz > 1)
+    HZ_LAUNCH(ctx, "prolong", (k_prolong<T, true>), grid, TPB, 0, gf, gc, ec, ldc, xin, xout, ldf, cols, ncols, cpb);
+  else
+    HZ_LAUNCH(ctx, "prolong", (k_prolong<T, false>), grid, TPB, 0, gf, gc, ec, ldc, xin, xout, ldf, cols, ncols, cpb);
+}
+
+// ---------------------------------------------------------------------------
+// Coarsest level: banded LU solve (LAPACK gbtrs order), FP64 arithmetic.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_band_solve(long long N, int kl, int ku, const double2* __restrict__ ab,
+                                                    const int* __restrict__ ipiv, const cplx<T>* __restrict__ b,
+                                                    cplx<T>* __restrict__ x, long long ld, const int* __restrict__ cols,
+                                                    double2* gwork) {
+  extern __shared__ double2 smem[];
+  const int col = cols[blockIdx.x];
+  double2* v = gwork ? gwork + (long long)blockIdx.x * N : smem;
+  const cplx<T>* bc = b + (long long)col * ld;
+  cplx<T>* xc = x + (long long)col * ld;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (long long p = tid; p < N; p += nt) v[p] = mk<double>((double)bc[p].x, (double)bc[p].y);
+  __syncthreads();
+  const int kv = kl + ku;
+  const long long ldab = 2LL * kl + ku + 1;
+  // forward: L with the row interchanges applied step by step
+  for (long long jj = 0; jj < N - 1; ++jj) {
+    const int lm = (int)min((long long)kl, N - 1 - jj);
+    const long long l = ipiv[jj];
+    const double2 bj = v[jj];
+    const double2 bl = v[l];
+    __syncthreads();
+    const double2 piv = (l != jj) ? bl : bj;
+    const double2* Lc = ab + jj * ldab + kv;
+    for (int r = tid + 1; r <= lm; r += nt) {
+      const double2 val = (jj + r == l) ? bj : v[jj + r];
+      v[jj + r] = cfms<double>(Lc[r], piv, val);
+    }
+    if (tid == 0) v[jj] = piv;
+    __syncthreads();
+  }
+  // backward: U has kl + ku superdiagonals
+  for (long long jj = N - 1; jj >= 0; --jj) {
+    const double2* Uc = ab + jj * ldab + kv;  // Uc[i - jj] = U(i, jj), i <= jj
+    const double2 u = Uc[0];
+    const double2 bj = v[jj];
+    const double den = u.x * u.x + u.y * u.y;
+    const double2 xj = mk<double>((bj.x * u.x + bj.y * u.y) / den, (bj.y * u.x - bj.x * u.y) / den);
+    const long long lo = max(0LL, jj - kv);
+    for (long long i = lo + tid; i < jj; i += nt) v[i] = cfms<double>(Uc[i - jj], xj, v[i]);
+    if (tid == 0) xc[jj] = mk<T>((T)xj.x, (T)xj.y);
+    __syncthreads();
+  }
+}
+
+static constexpr long long kBandSmemMax = 200LL * 1024;
+
+template <typename T>
+void launch_band_solve(Ctx& ctx, long long N, int kl, int ku, const double2* ab, const int* ipiv, const cplx<T>* b,
+                       cplx<T>* x, long long ld, const int* cols, int ncols, double2* gwork) {
+  if (ncols <= 0) return;
+  const long long bytes = N * (long long)sizeof(double2);
+  if (bytes <= kBandSmemMax) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_band_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBandSmemMax);
+      attr_set = true;
+    }
+    HZ_LAUNCH(ctx, "band_solve", k_band_solve<T>, ncols, 256, (size_t)bytes, N, kl, ku, ab, ipiv, b, x, ld, cols,
+              (double2*)nullptr);
+  } else {
+    if (!gwork) throw std::runtime_error("band_solve: coarsest level too large for shared memory and no workspace");
+    HZ_LAUNCH(ctx, "band_solve", k_band_solve<T>, ncols, 256, 0, N, kl, ku, ab, ipiv, b, x, ld, cols, gwork);
+  }
+}
+
+// explicit instantiations
+#define HZ_INST_T_TB(T, TB)                                                                                        \
+  template void launch_fine<T, T, TB>(Ctx&, int, const FineOp&, const cplx<T>*, const cplx<T>*, const cplx<T>*,     \
+                                      const cplx<TB>*, cplx<T>*, long long, const int*, int, double);               \
+  template void launch_rap<T, TB>(Ctx&, int, const Grid&, const cplx<T>*, long long, const cplx<T>*,                \
+                                  const cplx<T>*, const cplx<TB>*, cplx<T>*, long long, const int*, int, double);   \
+  template void launch_jacobi0<T, TB>(Ctx&, const Grid&, const cplx<T>*, int, const cplx<TB>*, cplx<T>*, long long, \
+                                      const int*, int, double);
+HZ_INST_T_TB(double, double)
+HZ_INST_T_TB(float, float)
+HZ_INST_T_TB(float, double)
+template void launch_fine<double, float, double>(Ctx&, int, const FineOp&, const double2*, const double2*,
+                                                 const float2*, const double2*, double2*, long long, const int*, int,
+                                                 double);
+#undef HZ_INST_T_TB
+template void launch_restrict<double>(Ctx&, const Grid&, const Grid&, const double2*, long long, double2*, long long,
+                                      const int*, int);
+template void launch_restrict<float>(Ctx&, const Grid&, const Grid&, const float2*, long long, float2*, long long,
+                                     const int*, int);
+template void launch_prolong<double>(Ctx&, const Grid&, const Grid&, const double2*, long long, const double2*,
+                                     double2*, long long, const int*, int);
+template void launch_prolong<float>(Ctx&, const Grid&, const Grid&, const float2*, long long, const float2*, float2*,
+                                    long long, const int*, int);
+template void launch_band_solve<double>(Ctx&, long long, int, int, const double2*, const int*, const double2*,
+                                        double2*, long long, const int*, int, double2*);
+template void launch_band_solve<float>(Ctx&, long long, int, int, const double2*, const int*, const float2*, float2*,
+                                       long long, const int*, int, double2*);
+
+}  // namespace hz

@@ -1,0 +1,189 @@
+/*
+ * helmgpu -- GB300-native shifted-Laplacian multigrid Helmholtz solver (C ABI).
+ *
+ * Drop-in boundary for the acoustic path of JuliaInv/Helmholtz.jl.  Every
+ * entry point takes plain pointers and sizes; no C++ or PyTorch types cross
+ * this interface.  Complex values are interleaved (re, im) pairs of double
+ * (Julia ComplexF64 / C99 double _Complex layout).  Node arrays are
+ * column-major with axis 1 fastest, exactly the vec() ordering of the
+ * reference (src/PlainNodalLaplacian.jl:32-46, src/getPointSource.jl:82-100).
+ *
+ * Status convention: 0 = ok, > 0 = finished but not converged (X is still
+ * valid, the reference prints a warning: src/ShiftedLaplacianMultigridSolver.jl:97-99),
+ * < 0 = error (the message is available from hz_last_error).  No exception
+ * or C++ object crosses the ABI.  A handle is single-thread affine; it owns
+ * its CUDA stream, device memory, multigrid hierarchy and coarsest LU factors.
+ */
+#ifndef HELMGPU_H
+#define HELMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HZ_ABI_VERSION 1
+
+/* status codes */
+#define HZ_OK 0
+#define HZ_NOT_CONVERGED 1
+#define HZ_ERR_ARG (-1)
+#define HZ_ERR_CUDA (-2)
+#define HZ_ERR_ALLOC (-3)
+#define HZ_ERR_NUMERIC (-4)
+#define HZ_ERR_STATE (-5)
+#define HZ_ERR_NO_DEVICE (-6)
+
+/* where B / X / Y live */
+#define HZ_MEM_HOST 0
+#define HZ_MEM_DEVICE 1
+
+/* precision of the multigrid preconditioner (the outer FGMRES is always FP64) */
+#define HZ_PREC_FP64 0
+#define HZ_PREC_MIXED 1 /* complex-FP32 V-cycle, FP64 coarsest LU */
+
+#define HZ_KRYLOV_FGMRES 0
+#define HZ_KRYLOV_BICGSTAB 1
+
+#define HZ_COARSE_GALERKIN 0     /* A_{l+1} = R A_l P (reference default RAP path) */
+#define HZ_COARSE_REDISCRETIZE 1 /* re-assembled 5/7-point operator from restricted m, gamma */
+
+#define HZ_OP_H 0  /* Helmholtz operator H */
+#define HZ_OP_SH 1 /* shifted operator SH = H + i*shift*w^2*diag(m) */
+
+/* The Helmholtz problem: the fields of HelmholtzParam (src/Helmholtz.jl:13-20)
+ * plus the mesh (jInv RegularMesh: n cells per axis, h).  m and gamma are
+ * copied at hz_create; the caller keeps ownership. */
+typedef struct hz_problem {
+  int32_t dim;             /* 2 or 3 */
+  int64_t n[3];            /* cells per axis; nodes per axis = n + 1 */
+  double h[3];             /* cell size per axis */
+  double omega_re;         /* angular frequency (complex allowed for hz_apply only) */
+  double omega_im;
+  const double* m;         /* slowness squared at the nodes, prod(n+1) values */
+  const double* gamma;     /* total attenuation at the nodes (absorbing layer included) */
+  int32_t neumann_on_top;  /* HelmholtzParam.NeumannOnTop */
+  int32_t sommerfeld;      /* HelmholtzParam.Sommerfeld */
+  int32_t order_neumann_bc;/* 1 or 2 (reference default 2, src/PlainNodalLaplacian.jl:4-15) */
+} hz_problem;
+
+/* Solver options: the in-scope subset of Multigrid.jl getMGparam
+ * (test/ShiftedLaplacianTest.jl:63-64) plus the solver constructor
+ * arguments of getShiftedLaplacianMultigridSolver
+ * (src/ShiftedLaplacianMultigridSolver.jl:24-30). */
+typedef struct hz_options {
+  int32_t levels;        /* multigrid levels (>= 1) */
+  int32_t max_outer;     /* MGparam.maxOuterIter: FGMRES restart cycles */
+  double rel_tol;        /* relative residual ||b - H x|| / ||b|| per column */
+  int32_t relax_pre;     /* Jacobi sweeps before the coarse correction */
+  int32_t relax_post;    /* Jacobi sweeps after the coarse correction */
+  double relax_param;    /* Jacobi damping w */
+  int32_t cycle;         /* 'V' or 'W' */
+  int32_t krylov;        /* HZ_KRYLOV_* */
+  int32_t inner;         /* FGMRES restart length */
+  double shift;          /* s in SH = H + i s w^2 diag(m) */
+  int32_t precision;     /* HZ_PREC_* */
+  int32_t coarse_op;     /* HZ_COARSE_* */
+  int32_t verbose;
+  int32_t profile;       /* 1: time every kernel launch with CUDA events */
+  int32_t device;        /* CUDA device ordinal */
+  int32_t reserved[7];
+} hz_options;
+
+typedef struct hz_stats {
+  int32_t outer;           /* restart cycles performed */
+  int32_t n_prec;          /* preconditioner applications (sum over columns) */
+  int32_t max_col_iters;   /* most inner iterations taken by one column */
+  int32_t converged_cols;  /* columns that reached rel_tol */
+  double max_relres;       /* largest true relative residual over the columns */
+  double setup_time;       /* seconds, accumulated like ShiftedLaplacianMultigridSolver.setupTime */
+  double solve_time;       /* seconds, accumulated like .solveTime */
+  int64_t kernel_launches; /* kernels launched by the last call */
+  int64_t h2d_bytes;       /* host->device bytes copied by the last call */
+  int64_t d2h_bytes;       /* device->host bytes copied by the last call */
+} hz_stats;
+
+typedef struct hz_handle hz_handle;
+
+/* Library version (HZ_ABI_VERSION). */
+int32_t hz_version(void);
+
+/* Last error message of this handle, or of the calling thread when h is NULL. */
+const char* hz_last_error(const hz_handle* h);
+
+/* Fill options with the defaults of the reference's SLMG usage:
+ * 3 levels, V(1,1) Jacobi w=0.8, FGMRES(10), shift 0.5, tol 1e-8. */
+void hz_default_options(hz_options* opt);
+
+/* Build a solver handle: replaces getShiftedLaplacianMultigridSolver
+ * (src/ShiftedLaplacianMultigridSolver.jl:24-30) together with the operator
+ * assembly of GetHelmholtzOperator (src/GetHelmholtz.jl:33-50) and
+ * GetHelmholtzShiftOP (src/GetHelmholtz.jl:81-83), which the library keeps
+ * matrix-free on the device.  The multigrid hierarchy is built lazily by the
+ * first hz_solve, as MGsetup is (src/ShiftedLaplacianMultigridSolver.jl:50-66). */
+int hz_create(const hz_problem* prob, const hz_options* opt, hz_handle** out);
+
+/* Release everything the handle owns. */
+int hz_destroy(hz_handle* h);
+
+/* Solve H X = B (transpose = 0) or H^H X = B (transpose = 1) for nrhs columns:
+ * replaces solveLinearSystem(ShiftedHT, B, param, doTranspose)
+ * (src/ShiftedLaplacianMultigridSolver.jl:33-102).  B and X are n x nrhs
+ * column-major complex, on the host or the device (mem).  Zero columns give
+ * zero solutions; stats may be NULL. */
+int hz_solve(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, int32_t transpose,
+             int32_t mem, hz_stats* stats);
+
+/* Per-column results of the last hz_solve: true relative residual and inner
+ * iterations taken.  Either pointer may be NULL. */
+int hz_column_stats(const hz_handle* h, double* relres, int32_t* iters, int32_t nrhs);
+
+/* Y = op X with op = H or SH (transpose = 1: the adjoint): the matrix-free
+ * replacement of getHelmholtzFun's closure (src/GetHelmholtz.jl:85-95) and of
+ * the sparse products H*x the reference tests take. */
+int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, double* Y, int64_t n, int32_t nrhs,
+             int32_t mem);
+
+/* Drop the multigrid hierarchy (clear!, src/ShiftedLaplacianMultigridSolver.jl:105-109). */
+int hz_clear(hz_handle* h);
+
+/* Independent copy of a handle's problem and options (copySolver,
+ * src/ShiftedLaplacianMultigridSolver.jl:18-22); the hierarchy is rebuilt lazily. */
+int hz_copy(const hz_handle* h, hz_handle** out);
+
+/* The CUDA stream (cudaStream_t) every kernel of this handle runs on. */
+void* hz_stream(hz_handle* h);
+
+/* Kernel timing table (options.profile = 1): entry idx -> name, launches,
+ * total milliseconds.  Returns the number of entries, or < 0 on error. */
+int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches, double* total_ms);
+int hz_reset_kernel_times(hz_handle* h);
+
+/* ---- host-side discretisation helpers (no GPU needed) ---------------------- */
+
+/* getMaximalFrequency (src/GetHelmholtz.jl:75-79): 0.2*pi / (max(h) sqrt(max(m))). */
+double hz_max_frequency(const double* m, int64_t count, const double* h, int32_t dim);
+
+/* getABL (src/GetHelmholtz.jl:97-220): absorbing-layer gamma on the node grid
+ * nodes[dim]; pad[dim] layer widths; writes prod(nodes) values. */
+int hz_abl(int32_t dim, const int64_t* nodes, int32_t neumann_at_first_dim, const int64_t* pad, double amp,
+           double* gamma_out);
+
+/* getSommerfeldBC (src/GetHelmholtz.jl:222-247): complex boundary term on the
+ * node grid (interleaved complex, prod(n+1) values). */
+int hz_sommerfeld(int32_t dim, const int64_t* n, const double* h, const double* m, double omega,
+                  int32_t neumann_on_top, int32_t order_neumann_bc, double* somm_out);
+
+/* Diagonal of H (src/GetHelmholtz.jl:41-47): -w^2 m (1 - i gamma / Re w) - Somm. */
+int hz_helmholtz_mass(const hz_problem* prob, double* mass_out);
+
+/* getAcousticPointSource with getTopPointSrc / loc2cs (src/getPointSource.jl:63-111):
+ * 1-based node subscript src[dim]; writes a complex column of prod(n+1) values. */
+int hz_point_source(int32_t dim, const int64_t* n, const double* h, const int64_t* src, double* q_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HELMGPU_H */

@@ -1,0 +1,160 @@
+"""GPU parity of the full shifted-Laplacian multigrid FGMRES solve
+(src/ShiftedLaplacianMultigridSolver.jl:33-102) against the oracle:
+the plain FP64 form to relative error <= 1e-6 at residual 1e-8, the mixed
+form to <= 1e-4 at residual 1e-6 (bounds of the solver's specification);
+iteration counts of the FP64 form equal the C oracle's."""
+import numpy as np
+import pytest
+
+import problems as PB
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(hz, P, levels, tol, precision="fp64", cycle="V", inner=10, max_outer=60, pre=1, post=1):
+    MG = hz.getMGparam(complex, int, levels, 1, max_outer, tol, "Jac", 0.8, pre, post, cycle, "Julia", 0.5, 0.0,
+                       precision=precision)
+    return hz.getShiftedLaplacianMultigridSolver(PB.hz_param(hz, P), MG, 0.5, "GMRES", inner)
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_config1_point_source_fp64(hz, O):
+    """129x129 gradient+ellipse model, source at (0.5, 2h), 3 levels V(1,1), FGMRES(10), tol 1e-8."""
+    P = PB.gradient_2d((128, 128), pad=16)
+    M = PB.hz_param(hz, P).Mesh
+    q, src = hz.getAcousticPointSource(M, np.complex128, [65, 3])
+    q = q.ravel(order="F")
+    S = _solver(hz, P, 3, 1e-8)
+    X, S = hz.solveLinearSystem(None, q, S)
+    assert X.shape == q.shape
+    Xref = O.direct_solve(P["H"], q)
+    assert _rel(X, Xref) <= 1e-6
+    assert np.linalg.norm(P["H"] @ X - q) / np.linalg.norm(q) <= 1e-8
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, q, levels=3, tol=1e-8, max_outer=60)
+    assert int(S.last_iters[0]) == int(sol.result.iters[0])
+    assert S.setupTime > 0 and S.solveTime > 0 and S.nPrec >= 1
+
+
+@pytest.mark.parametrize("precision,tol,bound", [("fp64", 1e-8, 1e-6), ("mixed", 1e-6, 1e-4)])
+def test_multi_rhs_2d(hz, O, cpu_slmg, precision, tol, bound):
+    P = PB.layered((128, 64), seed=3, pad=8, lengths=[2.0, 1.0])
+    n = P["m"].size
+    B = PB.rhs(n, 6, seed=2)
+    B[:, 4] = 0.0  # zero column -> zero solution
+    S = _solver(hz, P, 4, tol, precision)
+    X, S = hz.solveLinearSystem(None, B, S)
+    Xref = O.direct_solve(P["H"], B)
+    for c in range(6):
+        if c == 4:
+            assert not np.any(X[:, 4])
+            continue
+        assert _rel(X[:, c], Xref[:, c]) <= bound, c
+        assert np.linalg.norm(P["H"] @ X[:, c] - B[:, c]) / np.linalg.norm(B[:, c]) <= tol * 1.0001
+    if precision == "fp64":
+        SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+        r = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 4).solve(B, tol=tol, max_outer=60)
+        np.testing.assert_array_equal(S.last_iters, r.iters)
+
+
+@pytest.mark.parametrize("precision,tol,bound", [("fp64", 1e-8, 1e-6), ("mixed", 1e-6, 1e-4)])
+def test_3d_layered_ellipsoid(hz, O, precision, tol, bound):
+    P = PB.layered((32, 32, 32), seed=6, pad=4, ellipsoid=True)
+    n = P["m"].size
+    B = PB.rhs(n, 3, seed=4)
+    S = _solver(hz, P, 3, tol, precision)
+    X, S = hz.solveLinearSystem(None, B, S)
+    Xref = O.direct_solve(P["H"], B)
+    assert _rel(X, Xref) <= bound
+    assert np.max(S.last_relres) <= tol
+
+
+def test_transpose_solve(hz, O):
+    P = PB.gradient_2d((64, 64), pad=8)
+    n = P["m"].size
+    B = PB.rhs(n, 2, seed=8)
+    S = _solver(hz, P, 3, 1e-8)
+    X, S = hz.solveLinearSystem(None, B, S, 1)
+    Xref = O.direct_solve(P["H"].conj().T.tocsr(), B)
+    assert _rel(X, Xref) <= 1e-6
+    X0, S = hz.solveLinearSystem(None, B, S, 0)  # and back: both hierarchies kept
+    assert _rel(X0, O.direct_solve(P["H"], B)) <= 1e-6
+
+
+def test_w_cycle_and_more_sweeps(hz, O, cpu_slmg):
+    P = PB.gradient_2d((64, 64), pad=8)
+    n = P["m"].size
+    B = PB.rhs(n, 2, seed=12)
+    S = _solver(hz, P, 3, 1e-8, cycle="W", pre=2, post=2)
+    X, S = hz.solveLinearSystem(None, B, S)
+    assert _rel(X, O.direct_solve(P["H"], B)) <= 1e-6
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    r = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 3).solve(B, tol=1e-8, max_outer=60, cycle="W", pre=2, post=2)
+    np.testing.assert_array_equal(S.last_iters, r.iters)
+
+
+def test_device_arrays_and_inplace(hz, O):
+    import torch
+    P = PB.gradient_2d((64, 32), pad=6)
+    n = P["m"].size
+    B = PB.rhs(n, 3, seed=21)
+    S = _solver(hz, P, 3, 1e-8)
+    Xh, S = hz.solveLinearSystem(None, B, S)
+    Xd, S = hz.solveLinearSystem(None, torch.from_numpy(B).to("cuda"), S)
+    np.testing.assert_allclose(Xd.cpu().numpy(), Xh, rtol=0, atol=1e-14 * np.abs(Xh).max())
+    Xi = np.zeros_like(B)
+    hz.solveLinearSystemInPlace(None, B, Xi, S)
+    np.testing.assert_array_equal(Xi, Xh)
+
+
+def test_single_level_and_restart_lengths(hz, O):
+    P = PB.gradient_2d((32, 32), pad=4)
+    n = P["m"].size
+    B = PB.rhs(n, 2, seed=5)
+    Xref = O.direct_solve(P["H"], B)
+    for levels, inner in ((1, 5), (2, 20), (3, 17)):
+        S = _solver(hz, P, levels, 1e-9, inner=inner)
+        X, S = hz.solveLinearSystem(None, B, S)
+        assert _rel(X, Xref) <= 1e-6, (levels, inner)
+
+
+def test_not_converged_is_a_warning(hz, O, capsys):
+    P = PB.gradient_2d((64, 64), pad=8)
+    n = P["m"].size
+    B = PB.rhs(n, 1, seed=3)
+    S = _solver(hz, P, 3, 1e-12, max_outer=1, inner=3)
+    X, S = hz.solveLinearSystem(None, B, S)
+    assert "WARNING" in capsys.readouterr().out
+    assert np.all(np.isfinite(X))
+    assert S.last_relres[0] > 1e-12
+
+
+def test_nan_rhs_is_an_error(hz):
+    P = PB.gradient_2d((32, 32), pad=4)
+    n = P["m"].size
+    B = PB.rhs(n, 2, seed=5)
+    B[3, 1] = np.nan
+    S = _solver(hz, P, 2, 1e-8)
+    with pytest.raises(hz._lib.HelmgpuError) as ei:
+        hz.solveLinearSystem(None, B, S)
+    assert ei.value.code == hz._lib.HZ_ERR_NUMERIC
+    # the handle stays usable
+    B[3, 1] = 0.0
+    X, S = hz.solveLinearSystem(None, B, S)
+    assert np.all(np.isfinite(X))
+
+
+def test_clear_and_copy(hz, O):
+    P = PB.gradient_2d((32, 32), pad=4)
+    n = P["m"].size
+    B = PB.rhs(n, 1, seed=5)[:, 0]
+    S = _solver(hz, P, 3, 1e-8)
+    X1, S = hz.solveLinearSystem(None, B, S)
+    hz.clear_(S)
+    X2, S = hz.solveLinearSystem(None, B, S)
+    np.testing.assert_array_equal(X1, X2)
+    S2 = hz.copySolver(S)
+    X3, S2 = hz.solveLinearSystem(None, B, S2)
+    np.testing.assert_array_equal(X1, X3)

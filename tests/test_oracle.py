@@ -1,0 +1,131 @@
+"""CPU tests of the oracle: pinned by the reference's own known-answer test,
+checked against the committed golden vectors, and cross-checked between the
+NumPy and the C restatements."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import problems as PB
+
+GOLD = Path(__file__).resolve().parent / "golden" / "golden.npz"
+
+
+def _fictitious_source(O, u, mfun, w, rhs, refinements=4):
+    """test/testFictitiousSource2D.jl:10-70 restated: manufactured solution on
+    [-1,1]^2 starting from 32x48 cells, absorbing layer getABL(n+1, true, 5, 0.1),
+    no Sommerfeld; energy error |V (u_h - u)^H A (u_h - u)| per refinement."""
+    n = np.array([32, 48])
+    errs = []
+    for _ in range(refinements):
+        n = n * 2
+        M = O.getRegularMesh([-1.0, 1.0, -1.0, 1.0], n)
+        xn = O.getNodalGrid(M)
+        gamma = O.getABL(M.n + 1, True, [5, 5], 0.1).ravel(order="F")
+        uk = u(xn[:, 0], xn[:, 1])
+        mk = mfun(xn[:, 0], xn[:, 1])
+        rk = rhs(xn[:, 0], xn[:, 1]) + 1j * w**2 * gamma * mk * uk
+        A = O.GetHelmholtzOperator(M, mk, w, gamma, True, False)
+        ut = O.direct_solve(A, -rk)
+        e = ut - uk
+        errs.append(abs(M.h[0] * M.h[1] * np.vdot(e, A @ e)))
+    return np.array(errs)
+
+
+@pytest.mark.parametrize("model", ["constant", "gaussian"])
+def test_oracle_manufactured_solution_second_order(O, model):
+    w = 2 * np.pi
+    u = lambda x, y: np.cos(np.pi * x) * np.cos(np.pi * y)  # noqa: E731
+    if model == "constant":
+        mfun = lambda x, y: np.ones_like(x)  # noqa: E731
+    else:
+        mfun = lambda x, y: np.exp(-2.0 * (x**2 + y**2))  # noqa: E731
+    rhs = lambda x, y: -2 * np.pi**2 * u(x, y) + mfun(x, y) * u(x, y) * w**2  # noqa: E731
+    errs = _fictitious_source(O, u, mfun, w, rhs)
+    factors = errs[:-1] / errs[1:]
+    assert np.all(factors > 1.5), factors
+    # energy error converges at second order: factor -> 4 per halving of h
+    assert factors[-1] > 3.4, factors
+
+
+def test_oracle_matches_golden(O):
+    g = np.load(GOLD)
+    M = O.getRegularMesh([0.0, 2.0, 0.0, 1.0], [16, 8])
+    nn = M.n + 1
+    m, w = g["m2"], float(g["w2"])
+    for neu in (0, 1):
+        np.testing.assert_array_equal(O.getABL(nn, bool(neu), [3, 2], 0.9 * w).ravel(order="F"), g[f"abl2_neu{neu}"])
+        np.testing.assert_array_equal(O.getSommerfeldBC(M, m, w, bool(neu)).ravel(order="F"), g[f"somm2_neu{neu}"])
+    H, gam = O.GetHelmholtzOperatorABL(M, m, w, 0.01 * w * np.ones(m.size), True, [3, 2], 0.9 * w, True)
+    np.testing.assert_array_equal(np.ravel(gam, order="F"), g["gamma2"])
+    np.testing.assert_allclose(H @ g["X2"], g["HX2"], rtol=0, atol=1e-12 * np.abs(g["HX2"]).max())
+    M3 = O.getRegularMesh([0.0, 1.5, 0.0, 1.0, 0.0, 2.0], [6, 4, 8])
+    for neu in (0, 1):
+        np.testing.assert_array_equal(O.getABL(M3.n + 1, bool(neu), [2, 2, 3], 0.9 * float(g["w3"])).ravel(order="F"),
+                                      g[f"abl3_neu{neu}"])
+
+
+def test_laplacian_rows_follow_reference_boundary_rule(O):
+    """(2u_0 - 2u_1)/h^2 boundary rows (orderNeumannBC = 2), interior [-1 2 -1]/h^2."""
+    D = O.dxxMat(5, 0.5).toarray()
+    h2 = 0.25
+    np.testing.assert_allclose(D[0, :2] * h2, [2, -2])
+    np.testing.assert_allclose(D[-1, -2:] * h2, [-2, 2])
+    np.testing.assert_allclose(D[2, 1:4] * h2, [-1, 2, -1])
+    D1 = O.dxxMat(5, 0.5, 1).toarray()
+    np.testing.assert_allclose(D1[0, :2] * h2, [1, -1])
+
+
+def test_abl_corner_rule_2d(O):
+    """2D absorbing layer corners combine as a + b - ab (src/GetHelmholtz.jl:141-163)."""
+    g = O.getABL([20, 12], False, [4, 3], 1.0)
+    a = (4.0**2) / 16  # b_bwd1[0]
+    b = (3.0**2) / 9   # b_bwd2[0]
+    assert g[0, 0] == pytest.approx(a + b - a * b)
+    assert g[10, 6] == 0.0
+    gn = O.getABL([20, 12], True, [4, 3], 1.0)
+    assert gn[10, 0] == 0.0  # no layer on top with NeumannAtFirstDim
+
+
+def test_oracle_slmg_matches_direct_solve(O):
+    P = PB.gradient_2d((64, 64))
+    B = PB.rhs(P["H"].shape[0], 3, seed=3)
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=3, tol=1e-10, max_outer=60)
+    X = O.direct_solve(P["H"], B)
+    assert np.all(sol.result.converged)
+    assert np.linalg.norm(sol.X - X) / np.linalg.norm(X) < 1e-7
+
+
+def test_oracle_transpose_solve(O):
+    P = PB.gradient_2d((32, 32))
+    B = PB.rhs(P["H"].shape[0], 2, seed=5)
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=2, tol=1e-10, max_outer=60,
+                       transpose=True)
+    X = O.direct_solve(P["H"].conj().T.tocsr(), B)
+    assert np.linalg.norm(sol.X - X) / np.linalg.norm(X) < 1e-7
+
+
+def test_c_oracle_matches_numpy_oracle(O, cpu_slmg):
+    P = PB.gradient_2d((64, 64))
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    B = PB.rhs(P["H"].shape[0], 3, seed=7)
+    B[:, 1] = 0.0  # a zero column stays zero
+    cpu = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 3)
+    r = cpu.solve(B, tol=1e-8, max_outer=60)
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=3, tol=1e-8, max_outer=60)
+    np.testing.assert_array_equal(r.iters, sol.result.iters)
+    assert np.linalg.norm(r.X - sol.X) <= 1e-12 * np.linalg.norm(sol.X)
+    assert np.all(r.X[:, 1] == 0)
+
+
+def test_c_oracle_w_cycle_3d(O, cpu_slmg):
+    P = PB.layered((16, 16, 16), seed=2, pad=3, ellipsoid=True)
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    B = PB.rhs(P["H"].shape[0], 2, seed=9)
+    cpu = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 3)
+    r = cpu.solve(B, tol=1e-8, max_outer=60, cycle="W")
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=3, tol=1e-8, max_outer=60,
+                       cycle="W")
+    np.testing.assert_array_equal(r.iters, sol.result.iters)
+    X = O.direct_solve(P["H"], B)
+    assert np.linalg.norm(r.X - X) / np.linalg.norm(X) < 1e-6
