@@ -1,0 +1,440 @@
+"""Throughput benchmark: right-hand sides solved per second to relative
+residual 1e-6 by the shifted-Laplacian multigrid FGMRES solve on one GB300.
+
+One step = one hz_solve of the whole right-hand-side block of the workload
+(every column to rel. residual <= tol).  The headline arm runs the
+complex-FP32 V-cycle inside the FP64 FGMRES ("mixed"); the plain FP64 form of
+the same solver is timed in the same process for the ratio the metric names.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c3|c5]
+  python bench.py --impl reference ...   # CPU reference path (C oracle, all host threads)
+
+Under torchrun each rank solves its own seeded block of right-hand sides
+(no data-path collective; weak scaling), timing is max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RHS solved/s to rel. residual 1e-6 on 1 GB300: learned+mixed vs plain FP64 SLMG"
+
+# Synthetic seeded workloads (shapes, sizes and value distributions of the
+# measured configurations; no external dataset is needed).
+WORKLOADS = {
+    # 2D 1025 x 513 nodes, h = 10 m, 12 seeded layers in [1.5, 4.5] km/s,
+    # absorbing layer 32 cells, 64 sources along the surface row, 5 levels
+    "c2": dict(name="2D 1025x513 layered, 64 surface sources, 5 levels, FGMRES(10) tol 1e-6",
+               cells=(1024, 512), h=0.010, nrhs=64, levels=5, pad=32, ellipsoid=False, tol=1e-6),
+    # 3D 129^3 nodes layered + ellipsoid, absorbing layer 12, 4x4 surface sources, 4 levels
+    "c3": dict(name="3D 129^3 layered+ellipsoid, 16 surface sources, 4 levels, FGMRES(10) tol 1e-6",
+               cells=(128, 128, 128), h=0.010, nrhs=16, levels=4, pad=12, ellipsoid=True, tol=1e-6),
+    # 3D 257^3 nodes (16,974,593 unknowns per RHS), absorbing layer 16, 32 surface sources
+    "c5": dict(name="3D 257^3 layered+ellipsoid, 32 surface sources, 5 levels, FGMRES(10) tol 1e-6",
+               cells=(256, 256, 256), h=0.010, nrhs=32, levels=5, pad=16, ellipsoid=True, tol=1e-6),
+}
+
+
+def make_problem(wl: dict, seed: int):
+    """Seeded layered (+ ellipsoid) velocity model, 10 points per wavelength,
+    attenuation 0.01 w plus a quadratic absorbing layer of amplitude 0.95 w."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    cells = wl["cells"]
+    dim = len(cells)
+    nodes = [c + 1 for c in cells]
+    rng = np.random.default_rng(seed)
+    # layered model with depth along the last axis
+    nl = 12
+    wts = rng.uniform(0.5, 1.5, size=nl)
+    bounds = np.concatenate([[0], np.cumsum(wts) / np.sum(wts) * nodes[-1]]).astype(np.int64)
+    bounds[-1] = nodes[-1]
+    vel = np.sort(rng.uniform(1.5, 4.5, size=nl))
+    vz = np.empty(nodes[-1])
+    for k in range(nl):
+        vz[bounds[k]:bounds[k + 1]] = vel[k]
+    v = np.broadcast_to(vz.reshape((1,) * (dim - 1) + (nodes[-1],)), nodes).copy()
+    if wl["ellipsoid"]:
+        c = rng.uniform(0.3, 0.7, size=dim)
+        ax = rng.uniform(0.08, 0.2, size=dim)
+        grids = np.ogrid[tuple(slice(0, n) for n in nodes)]
+        r = sum(((g / (n - 1) - ci) / ai) ** 2 for g, n, ci, ai in zip(grids, nodes, c, ax))
+        v[r <= 1.0] = 4.5
+    m = (1.0 / v**2).ravel(order="F")
+    h = np.full(dim, wl["h"])
+    w = (0.1 * 2 * np.pi) / (h.max() * np.sqrt(m.max()))
+    return dict(dim=dim, cells=cells, nodes=nodes, h=h, m=m, w=w)
+
+
+def sources(P: dict, nrhs: int, seed: int) -> np.ndarray:
+    """Delta sources q = 1/||h||^2 on the surface (depth index 1): evenly spaced
+    along the surface row in 2D, on a square grid of the surface in 3D."""
+    nodes = P["nodes"]
+    N = int(np.prod(nodes))
+    B = np.zeros((N, nrhs), dtype=np.complex128, order="F")
+    amp = 1.0 / float(np.linalg.norm(P["h"])) ** 2
+    if P["dim"] == 2:
+        xs = np.linspace(nodes[0] * 0.05, nodes[0] * 0.95, nrhs).astype(np.int64)
+        for c in range(nrhs):
+            B[int(xs[c]) + nodes[0] * 1, c] = amp
+    else:
+        k = int(np.ceil(np.sqrt(nrhs)))
+        g0 = np.linspace(nodes[0] * 0.2, nodes[0] * 0.8, k).astype(np.int64)
+        g1 = np.linspace(nodes[1] * 0.2, nodes[1] * 0.8, k).astype(np.int64)
+        shift = seed % 3
+        for c in range(nrhs):
+            i, j = int(g0[c % k]) + shift, int(g1[c // k])
+            B[i + nodes[0] * (j + nodes[1] * 1), c] = amp
+    return B
+
+
+def gamma_of(P: dict, pad: int, lib, hz) -> np.ndarray:
+    abl = hz.getABL(P["nodes"], True, [pad] * P["dim"], 0.95 * P["w"]).ravel(order="F")
+    return abl + 0.01 * P["w"]
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, device: int = 0):
+        self.samples = []
+        self.proc = None
+        self.device = device
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def kernel_table(lib, h):
+    n = lib.hz_kernel_times(h, -1, None, 0, None, None, None, None)
+    rows = []
+    for i in range(n):
+        name = C.create_string_buffer(64)
+        la = C.c_int64()
+        lt = C.c_int64()
+        ms = C.c_double()
+        by = C.c_double()
+        lib.hz_kernel_times(h, i, name, 64, C.byref(la), C.byref(lt), C.byref(ms), C.byref(by))
+        rows.append(dict(name=name.value.decode(), launches=la.value, timed=lt.value, ms=ms.value,
+                         bytes=by.value))
+    return rows
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(workload, {}).get(kernel)
+    except (ValueError, OSError):
+        return None
+
+
+def run_ours(args, rank, ws, dist):
+    import torch
+    import __graft_entry__ as ge
+    ge._load_build_module().build()
+    hz = ge.load_package()
+    L = hz._lib
+    lib = L.load()
+    wl = WORKLOADS[args.workload]
+    P = make_problem(wl, seed=1234)
+    gam = gamma_of(P, wl["pad"], lib, hz)
+    nrhs = wl["nrhs"]
+    B = sources(P, nrhs, seed=rank)
+    n = B.shape[0]
+
+    def make_handle(precision):
+        prob = L.hz_problem()
+        prob.dim = P["dim"]
+        for d in range(P["dim"]):
+            prob.n[d] = P["cells"][d]
+            prob.h[d] = P["h"][d]
+        prob.omega_re, prob.omega_im = P["w"], 0.0
+        keep = (np.ascontiguousarray(P["m"]), np.ascontiguousarray(gam))
+        prob.m = keep[0].ctypes.data_as(C.POINTER(C.c_double))
+        prob.gamma = keep[1].ctypes.data_as(C.POINTER(C.c_double))
+        prob.neumann_on_top, prob.sommerfeld, prob.order_neumann_bc = 1, 1, 2
+        o = L.hz_options()
+        lib.hz_default_options(C.byref(o))
+        o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, 200
+        o.precision = precision
+        o.device = torch.cuda.current_device()
+        hh = C.c_void_p()
+        L.check(lib.hz_create(C.byref(prob), C.byref(o), C.byref(hh)))
+        return hh
+
+    Bd = torch.from_numpy(np.ascontiguousarray(B.T)).to("cuda")  # (nrhs, n) row-major = column-major n x nrhs
+    Xd = torch.empty_like(Bd)
+
+    def solve_device(hh):
+        st = L.hz_stats()
+        code = lib.hz_solve(hh, Bd.data_ptr(), Xd.data_ptr(), n, nrhs, 0, L.HZ_MEM_DEVICE, C.byref(st))
+        L.check(code, hh)
+        return st, code
+
+    def timed(hh, steps, fn):
+        stream = torch.cuda.ExternalStream(lib.hz_stream(hh))
+        barrier(dist)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        last = None
+        for _ in range(steps):
+            last = fn(hh)
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        barrier(dist)
+        return e0.elapsed_time(e1) / 1000.0, last
+
+    results = {}
+    order = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
+    for prec in order:
+        hh = make_handle(L.HZ_PREC_MIXED if prec == "mixed" else L.HZ_PREC_FP64)
+        t_setup0 = time.perf_counter()
+        for _ in range(args.warmup):
+            solve_device(hh)
+        setup_and_warm = time.perf_counter() - t_setup0
+        steps = args.steps if prec == order[0] else max(1, args.plain_steps)
+        lib.hz_reset_kernel_times(hh)
+        lib.hz_set_profile(hh, 1 if prec == order[0] else 0)
+        launches0 = None
+        with ClockSampler(torch.cuda.current_device()) as clocks:
+            t, (st, code) = timed(hh, steps, solve_device)
+        t = max_over_ranks(dist, t)
+        rr = np.zeros(nrhs)
+        it = np.zeros(nrhs, dtype=np.int32)
+        lib.hz_column_stats(hh, rr.ctypes.data_as(C.POINTER(C.c_double)), it.ctypes.data_as(C.POINTER(C.c_int32)),
+                            nrhs)
+        kt = kernel_table(lib, hh)
+        res = dict(seconds=t, steps=steps, rhs_per_s=nrhs * ws * steps / t, ms_per_step=1000.0 * t / steps,
+                   max_relres=float(rr.max()), mean_iters=float(it.mean()), max_iters=int(it.max()),
+                   outer=int(st.outer), launches_per_step=int(st.kernel_launches), kernels=kt,
+                   clocks=clocks.summary(), setup_warm_s=setup_and_warm, code=int(code))
+        if prec == order[0]:
+            # end to end through the public call with host buffers (pinned), copies inside the timed region
+            Bh = torch.from_numpy(np.ascontiguousarray(B.T)).pin_memory()
+            Xh = torch.empty_like(Bh).pin_memory()
+
+            def solve_host(hh_):
+                st_ = L.hz_stats()
+                L.check(lib.hz_solve(hh_, Bh.data_ptr(), Xh.data_ptr(), n, nrhs, 0, L.HZ_MEM_HOST, C.byref(st_)),
+                        hh_)
+                return st_
+
+            lib.hz_set_profile(hh, 0)
+            solve_host(hh)
+            t0 = time.perf_counter()
+            barrier(dist)
+            for _ in range(steps):
+                st_h = solve_host(hh)
+            barrier(dist)
+            te = max_over_ranks(dist, time.perf_counter() - t0)
+            res["e2e"] = dict(value=nrhs * ws * steps / te, unit="RHS/s", h2d_bytes_per_step=int(st_h.h2d_bytes),
+                              d2h_bytes_per_step=int(st_h.d2h_bytes))
+            # accuracy check of the last device solve against the FP64 operator
+            Y = torch.empty_like(Xd)
+            L.check(lib.hz_apply(hh, L.HZ_OP_H, 0, Xd.data_ptr(), Y.data_ptr(), n, nrhs, L.HZ_MEM_DEVICE), hh)
+            rel = torch.linalg.vector_norm(Y - Bd, dim=1) / torch.linalg.vector_norm(Bd, dim=1)
+            res["check_relres_max"] = float(rel.max())
+        lib.hz_destroy(hh)
+        results[prec] = res
+        torch.cuda.empty_cache()
+    return results, wl, P
+
+
+def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4):
+    """C oracle (threaded CSR SLMG, plain FP64) on a bounded sample of the
+    workload: the full grid and operator, a few of its right-hand sides."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import helmholtz_oracle as O
+    import slmg_cpu
+    M = O.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
+    gam = gam_fn()
+    H = O.GetHelmholtzOperator(M, P["m"], P["w"], gam, True, True)
+    SH = (H + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"])
+    B = sources(P, wl["nrhs"], seed=0)
+    ncols = 1
+    r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200)
+    t1 = r.solve_s
+    ncols = int(max(1, min(ncols_max, budget_s // max(t1, 1e-3))))
+    if ncols > 1:
+        r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200)
+    return dict(value=ncols / r.solve_s, unit="RHS/s", cores=r.threads, kind="port",
+                sample=f"{ncols} of the {wl['nrhs']} right-hand sides of the same workload (full grid, "
+                       f"same operator, plain FP64 SLMG in threaded C, {int(r.iters.mean())} iterations per RHS)",
+                seconds=r.solve_s, setup_s=r.setup_s, max_relres=float(r.relres.max()))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("HZ_BENCH_WORKLOAD", "c2"), choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"])
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    peak, peak_kind = load_peaks()
+
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        if rank != 0:
+            return
+        wl = WORKLOADS[args.workload]
+        P = make_problem(wl, seed=1234)
+        import __graft_entry__ as ge
+        hz = ge.load_package()
+        gam = gamma_of(P, wl["pad"], None, hz)
+        vals = []
+        cs = None
+        for i in range(args.warmup + args.steps):
+            cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps))
+            if i >= args.warmup:
+                vals.append(cs["value"])
+        v = float(np.mean(vals))
+        line = dict(metric=METRIC, value=v, unit="RHS/s", impl="reference", n_gpus=args.gpus, steps=args.steps,
+                    warmup=args.warmup, higher_is_better=True, dtype="c128",
+                    config=dict(workload=wl["name"], nrhs=wl["nrhs"]),
+                    cpu_baseline=dict(value=v, unit="RHS/s", cores=cs["cores"], kind="port", sample=cs["sample"]),
+                    e2e=dict(value=v, unit="RHS/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                    note="reference path = the C oracle port of the Julia SLMG (Julia and Multigrid.jl are absent)")
+        print(json.dumps(line))
+        return
+
+    rank, ws, dist = dist_setup()
+    results, wl, P = run_ours(args, rank, ws, dist)
+    if rank != 0:
+        return
+    head = results[args.precision if args.precision != "both" else "mixed"]
+    # dominant kernel of the timed region (event-timed per launch on the handle's stream)
+    kt = [k for k in head["kernels"] if k["timed"] > 0]
+    dom = max(kt, key=lambda k: k["ms"]) if kt else None
+    roofline = None
+    if dom:
+        achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
+        tr = traffic_from_profiles(dom["name"], args.workload)
+        roofline = dict(bound="hbm", kernel=dom["name"], achieved=achieved, peak=peak, unit="GB/s",
+                        frac=achieved / peak, peak_source=f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                        traffic=tr, avg_launch_ms=dom["ms"] / dom["timed"],
+                        share=dom["ms"] / sum(k["ms"] for k in kt))
+    cpu = None
+    if not args.no_cpu:
+        import __graft_entry__ as ge
+        hz = ge.load_package()
+        gam = gamma_of(P, wl["pad"], None, hz)
+        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget)
+    plain = results.get("fp64")
+    line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
+                warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
+                vs_baseline=None, dtype="c64 V-cycle / c128 FGMRES", data="synthetic (seeded layered model)",
+                config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
+                            precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
+                            l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9)),
+                e2e=head.get("e2e"), gpu_launches=head["launches_per_step"] * args.steps,
+                clocks=head["clocks"], roofline=roofline,
+                cpu_baseline=cpu,
+                max_relres=head["max_relres"], check_relres_max=head.get("check_relres_max"),
+                mean_iters=head["mean_iters"],
+                plain_fp64=None if plain is None else dict(rhs_per_s=plain["rhs_per_s"],
+                                                           ms_per_step=plain["ms_per_step"],
+                                                           mean_iters=plain["mean_iters"],
+                                                           max_relres=plain["max_relres"]),
+                mixed_over_plain=None if plain is None else head["rhs_per_s"] / plain["rhs_per_s"],
+                kernels=[dict(name=k["name"], launches=k["launches"], ms=round(k["ms"], 3),
+                              gbs=(k["bytes"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None)
+                         for k in sorted(kt, key=lambda k: -k["ms"])[:12]])
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -102,8 +102,9 @@ SIGNATURES = {
     "hz_clear": (C.c_int, [_vp]),
     "hz_copy": (C.c_int, [_vp, C.POINTER(_vp)]),
     "hz_stream": (_vp, [_vp]),
-    "hz_kernel_times": (C.c_int, [_vp, C.c_int32, C.c_char_p, C.c_int32, _i64p, _dp]),
+    "hz_kernel_times": (C.c_int, [_vp, C.c_int32, C.c_char_p, C.c_int32, _i64p, _i64p, _dp, _dp]),
     "hz_reset_kernel_times": (C.c_int, [_vp]),
+    "hz_set_profile": (C.c_int, [_vp, C.c_int32]),
     "hz_max_frequency": (C.c_double, [_dp, C.c_int64, _dp, C.c_int32]),
     "hz_abl": (C.c_int, [C.c_int32, _i64p, C.c_int32, _i64p, C.c_double, _dp]),
     "hz_sommerfeld": (C.c_int, [C.c_int32, _i64p, _dp, _dp, C.c_double, C.c_int32, C.c_int32, _dp]),

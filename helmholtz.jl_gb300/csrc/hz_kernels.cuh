@@ -17,8 +17,10 @@ struct Ctx {
   long long launches = 0;
   bool profile = false;
   std::vector<std::string> names;  // kernel name table
-  std::vector<long long> counts;
-  std::vector<double> total_ms;
+  std::vector<long long> counts;   // launches per kernel
+  std::vector<long long> timed;    // launches with an event pair (profiling on)
+  std::vector<double> total_ms;    // event-timed milliseconds per kernel
+  std::vector<double> alg_bytes;   // algorithmic bytes per kernel (all launches)
   struct Pending {
     int id;
     cudaEvent_t a, b;
@@ -27,7 +29,7 @@ struct Ctx {
   std::vector<cudaEvent_t> pool;
   int name_id(const char* name);
   void before(int id, cudaEvent_t* a);
-  void after(int id, cudaEvent_t a);
+  void after(int id, cudaEvent_t a, double bytes);
   void resolve();  // after a stream sync: fold pending event pairs into the table
   void release();
 };
@@ -116,10 +118,12 @@ void launch_reduce(Ctx& ctx, const double2* part, const int* cols, int ncols, in
 // y[:, c] = s[c] * x[:, c]
 void launch_scale_cols(Ctx& ctx, long long N, const double2* x, long long xld, double2* y, long long yld,
                        const double* s, const int* cols, int ncols);
-// x[:, c] += sum_{i < kcol[c]} y[c*ystride + i] Z_i[:, c], Z in precision TZ.
+// x[:, c] += sum_{i < kcol[c]} y[c*ystride + i] Z_i[:, c], Z in precision TZ;
+// zcols = sum of kcol over the active columns (for the byte count).
 template <typename TZ>
 void launch_update_x(Ctx& ctx, long long N, const cplx<TZ>* Z, long long zstride, long long ld, const int* kcol,
-                     const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols);
+                     const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols,
+                     long long zcols);
 // nrm[c] = sqrt(Re red[c*stride + slot]), inv[c] = 1/nrm[c] (0 for a zero norm).
 void launch_norms(Ctx& ctx, const double2* red, int stride, int slot, const int* cols, int ncols, double* nrm,
                   double* inv);

@@ -13,6 +13,10 @@
 namespace hz {
 
 static constexpr int KG = 16;  // dot products carried per pass in registers
+
+// sqrt of a reduced sum of squares: rounding can leave it a hair below zero;
+// NaN and Inf pass through so the host sees a corrupted column.
+__device__ __forceinline__ double safe_sqrt(double v) { return (v > 0.0 || v != v) ? sqrt(v) : 0.0; }
 static constexpr int RT = 256; // threads per reduction CTA
 
 int krylov_nblk(long long N, int ncols) {
@@ -89,7 +93,8 @@ void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, lon
   if (ncols <= 0) return;
   if (K > KG) throw std::runtime_error("launch_dots: too many vectors in one pass");
   dim3 grid(nblk, ncols);
-  HZ_LAUNCH(ctx, "krylov_dots", k_dots, grid, RT, 0, N, V, vstride, ld, i0, K, w, wld, cols, nblk, want_norm, part);
+  const double bytes = (double)N * ncols * (K + 1) * sizeof(double2);
+  HZ_LAUNCH(ctx, "krylov_dots", bytes, k_dots, grid, RT, 0, N, V, vstride, ld, i0, K, w, wld, cols, nblk, want_norm, part);
 }
 
 __global__ void __launch_bounds__(RT) k_update(long long N, const double2* __restrict__ V, long long vstride,
@@ -140,7 +145,8 @@ void launch_update(Ctx& ctx, long long N, const double2* V, long long vstride, l
   if (ncols <= 0) return;
   if (K > KG) throw std::runtime_error("launch_update: too many vectors in one pass");
   dim3 grid(nblk, ncols);
-  HZ_LAUNCH(ctx, "krylov_update", k_update, grid, RT, 0, N, V, vstride, ld, i0, K, h, hstride, w, wld, cols, nblk,
+  const double bytes = (double)N * ncols * (K + 2) * sizeof(double2);
+  HZ_LAUNCH(ctx, "krylov_update", bytes, k_update, grid, RT, 0, N, V, vstride, ld, i0, K, h, hstride, w, wld, cols, nblk,
             want_dots, want_norm, part);
 }
 
@@ -177,7 +183,7 @@ void launch_reduce(Ctx& ctx, const double2* part, const int* cols, int ncols, in
   if (ncols <= 0 || K1 <= 0) return;
   long long warps = (long long)ncols * K1;
   int blocks = (int)((warps * 32 + 255) / 256);
-  HZ_LAUNCH(ctx, "krylov_reduce", k_reduce, blocks, 256, 0, part, cols, ncols, K1, nblk, out, ostride, accum);
+  HZ_LAUNCH(ctx, "krylov_reduce", (double)ncols * K1 * (nblk + 1) * sizeof(double2), k_reduce, blocks, 256, 0, part, cols, ncols, K1, nblk, out, ostride, accum);
 }
 
 __global__ void __launch_bounds__(256) k_scale_cols(long long N, const double2* __restrict__ x, long long xld,
@@ -198,7 +204,7 @@ void launch_scale_cols(Ctx& ctx, long long N, const double2* x, long long xld, d
   if (ncols <= 0) return;
   int nb = krylov_nblk(N, ncols);
   dim3 grid(nb, ncols);
-  HZ_LAUNCH(ctx, "scale_cols", k_scale_cols, grid, 256, 0, N, x, xld, y, yld, s, cols);
+  HZ_LAUNCH(ctx, "scale_cols", (double)N * ncols * 2 * sizeof(double2), k_scale_cols, grid, 256, 0, N, x, xld, y, yld, s, cols);
 }
 
 template <typename TZ>
@@ -231,11 +237,13 @@ __global__ void __launch_bounds__(256) k_update_x(long long N, const cplx<TZ>* _
 
 template <typename TZ>
 void launch_update_x(Ctx& ctx, long long N, const cplx<TZ>* Z, long long zstride, long long ld, const int* kcol,
-                     const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols) {
+                     const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols,
+                     long long zcols) {
   if (ncols <= 0) return;
   int nb = krylov_nblk(N, ncols);
   dim3 grid(nb, ncols);
-  HZ_LAUNCH(ctx, "update_x", k_update_x<TZ>, grid, 256, 0, N, Z, zstride, ld, kcol, y, ystride, x, xld, cols);
+  const double bytes = (double)N * (ncols * 2.0 * sizeof(double2) + zcols * sizeof(cplx<TZ>));
+  HZ_LAUNCH(ctx, "update_x", bytes, k_update_x<TZ>, grid, 256, 0, N, Z, zstride, ld, kcol, y, ystride, x, xld, cols);
 }
 
 __global__ void k_norms(const double2* __restrict__ red, int stride, int slot, const int* __restrict__ cols, int ncols,
@@ -243,7 +251,7 @@ __global__ void k_norms(const double2* __restrict__ red, int stride, int slot, c
   const int pos = blockIdx.x * blockDim.x + threadIdx.x;
   if (pos >= ncols) return;
   const int c = cols[pos];
-  const double v = sqrt(fmax(red[(long long)c * stride + slot].x, 0.0));
+  const double v = safe_sqrt(red[(long long)c * stride + slot].x);
   nrm[c] = v;
   if (inv) inv[c] = (v > 0) ? 1.0 / v : 0.0;
 }
@@ -251,7 +259,7 @@ __global__ void k_norms(const double2* __restrict__ red, int stride, int slot, c
 void launch_norms(Ctx& ctx, const double2* red, int stride, int slot, const int* cols, int ncols, double* nrm,
                   double* inv) {
   if (ncols <= 0) return;
-  HZ_LAUNCH(ctx, "krylov_norms", k_norms, (ncols + 127) / 128, 128, 0, red, stride, slot, cols, ncols, nrm, inv);
+  HZ_LAUNCH(ctx, "krylov_norms", 0.0, k_norms, (ncols + 127) / 128, 128, 0, red, stride, slot, cols, ncols, nrm, inv);
 }
 
 __global__ void k_cycle_init(int m, const int* __restrict__ cols, int ncols, const double* __restrict__ beta,
@@ -264,7 +272,7 @@ __global__ void k_cycle_init(int m, const int* __restrict__ cols, int ncols, con
 
 void launch_cycle_init(Ctx& ctx, int m, const int* cols, int ncols, const double* beta, double2* g) {
   if (ncols <= 0) return;
-  HZ_LAUNCH(ctx, "cycle_init", k_cycle_init, (ncols + 127) / 128, 128, 0, m, cols, ncols, beta, g);
+  HZ_LAUNCH(ctx, "cycle_init", 0.0, k_cycle_init, (ncols + 127) / 128, 128, 0, m, cols, ncols, beta, g);
 }
 
 // Complex Givens rotation convention: (u, v) -> (conj(c) u + conj(s) v, -s u + c v).
@@ -283,7 +291,7 @@ __global__ void k_arnoldi_step(int j, int m, const int* __restrict__ cols, int n
     if (hB) v = cadd<double>(v, hB[(long long)c * hstride + i]);
     H[i] = v;
   }
-  const double hn = sqrt(fmax(nrm[(long long)c * hstride].x, 0.0));
+  const double hn = safe_sqrt(nrm[(long long)c * hstride].x);
   H[j + 1] = mk<double>(hn, 0.0);
   for (int i = 0; i < j; ++i) {
     const double2 u = H[i], v = H[i + 1];
@@ -319,7 +327,7 @@ void launch_arnoldi_step(Ctx& ctx, int j, int m, const int* cols, int ncols, con
                          const double2* nrm, int hstride, double2* Hh, double2* cs, double2* sn, double2* g,
                          double* est, double* inv_hn) {
   if (ncols <= 0) return;
-  HZ_LAUNCH(ctx, "arnoldi_step", k_arnoldi_step, (ncols + 63) / 64, 64, 0, j, m, cols, ncols, hA, hB, nrm, hstride, Hh,
+  HZ_LAUNCH(ctx, "arnoldi_step", 0.0, k_arnoldi_step, (ncols + 63) / 64, 64, 0, j, m, cols, ncols, hA, hB, nrm, hstride, Hh,
             cs, sn, g, est, inv_hn);
 }
 
@@ -344,7 +352,7 @@ __global__ void k_lsq(int m, const int* __restrict__ cols, int ncols, const int*
 void launch_lsq(Ctx& ctx, int m, const int* cols, int ncols, const int* kcol, const double2* Hh, const double2* g,
                 double2* y) {
   if (ncols <= 0) return;
-  HZ_LAUNCH(ctx, "lsq", k_lsq, (ncols + 63) / 64, 64, 0, m, cols, ncols, kcol, Hh, g, y);
+  HZ_LAUNCH(ctx, "lsq", 0.0, k_lsq, (ncols + 63) / 64, 64, 0, m, cols, ncols, kcol, Hh, g, y);
 }
 
 // ---------------------------------------------------------------------------
@@ -368,7 +376,7 @@ __global__ void k_probe_init(Grid g, int dim, double2* out, long long ld) {
 
 void launch_probe_init(Ctx& ctx, const Grid& gc, int dim, double2* out, long long ld) {
   long long nb = (gc.N + 255) / 256;
-  HZ_LAUNCH(ctx, "probe_init", k_probe_init, (unsigned)nb, 256, 0, gc, dim, out, ld);
+  HZ_LAUNCH(ctx, "probe_init", (double)gc.N * (dim == 3 ? 27 : 9) * sizeof(double2), k_probe_init, (unsigned)nb, 256, 0, gc, dim, out, ld);
 }
 
 __device__ __forceinline__ int off3(int cls_d, int I) {
@@ -396,7 +404,7 @@ __global__ void k_probe_scatter(Grid g, int dim, const double2* __restrict__ y, 
 void launch_probe_scatter(Ctx& ctx, const Grid& gc, int dim, const double2* y, long long ld, double2* coef,
                           long long cld) {
   long long nb = (gc.N + 255) / 256;
-  HZ_LAUNCH(ctx, "probe_scatter", k_probe_scatter, (unsigned)nb, 256, 0, gc, dim, y, ld, coef, cld);
+  HZ_LAUNCH(ctx, "probe_scatter", 2.0 * gc.N * (dim == 3 ? 27 : 9) * sizeof(double2), k_probe_scatter, (unsigned)nb, 256, 0, gc, dim, y, ld, coef, cld);
 }
 
 // coefT[o][I] = conj(coef[-o][I + o]) (zero where I + o is outside the grid).
@@ -425,7 +433,7 @@ __global__ void k_coef_transpose(Grid g, int dim, const double2* __restrict__ co
 
 void launch_coef_transpose(Ctx& ctx, const Grid& g, int dim, const double2* coef, double2* coefT, long long cld) {
   long long nb = (g.N + 255) / 256;
-  HZ_LAUNCH(ctx, "coef_transpose", k_coef_transpose, (unsigned)nb, 256, 0, g, dim, coef, coefT, cld);
+  HZ_LAUNCH(ctx, "coef_transpose", 2.0 * g.N * (dim == 3 ? 27 : 9) * sizeof(double2), k_coef_transpose, (unsigned)nb, 256, 0, g, dim, coef, coefT, cld);
 }
 
 template <typename T>
@@ -441,7 +449,7 @@ __global__ void k_center_inverse(long long N, int center, const double2* __restr
 template <typename T>
 void launch_center_inverse(Ctx& ctx, const Grid& g, int dim, const double2* coef, long long cld, cplx<T>* dinv) {
   long long nb = (g.N + 255) / 256;
-  HZ_LAUNCH(ctx, "center_inverse", k_center_inverse<T>, (unsigned)nb, 256, 0, g.N, dim == 3 ? 13 : 4, coef, cld,
+  HZ_LAUNCH(ctx, "center_inverse", (double)g.N * (sizeof(double2) + sizeof(cplx<T>)), k_center_inverse<T>, (unsigned)nb, 256, 0, g.N, dim == 3 ? 13 : 4, coef, cld,
             dinv);
 }
 
@@ -455,7 +463,7 @@ template <typename To, typename From>
 void launch_cast(Ctx& ctx, const cplx<From>* in, cplx<To>* out, long long n) {
   if (n <= 0) return;
   long long nb = std::min<long long>((n + 255) / 256, 16LL * kSMs);
-  HZ_LAUNCH(ctx, "cast", (k_cast<To, From>), (unsigned)nb, 256, 0, in, out, n);
+  HZ_LAUNCH(ctx, "cast", (double)n * (sizeof(cplx<To>) + sizeof(cplx<From>)), (k_cast<To, From>), (unsigned)nb, 256, 0, in, out, n);
 }
 
 template <typename To, typename From>
@@ -474,7 +482,7 @@ void launch_cast_cols(Ctx& ctx, long long N, const cplx<From>* in, long long ldi
   if (ncols <= 0) return;
   int nb = krylov_nblk(N, ncols);
   dim3 grid(nb, ncols);
-  HZ_LAUNCH(ctx, "cast_cols", (k_cast_cols<To, From>), grid, 256, 0, N, in, ldi, out, ldo, cols);
+  HZ_LAUNCH(ctx, "cast_cols", (double)N * ncols * (sizeof(cplx<To>) + sizeof(cplx<From>)), (k_cast_cols<To, From>), grid, 256, 0, N, in, ldi, out, ldo, cols);
 }
 
 template <typename T>
@@ -490,14 +498,14 @@ void launch_zero_cols(Ctx& ctx, long long N, cplx<T>* x, long long ld, const int
   if (ncols <= 0) return;
   int nb = krylov_nblk(N, ncols);
   dim3 grid(nb, ncols);
-  HZ_LAUNCH(ctx, "zero_cols", k_zero_cols<T>, grid, 256, 0, N, x, ld, cols);
+  HZ_LAUNCH(ctx, "zero_cols", (double)N * ncols * sizeof(cplx<T>), k_zero_cols<T>, grid, 256, 0, N, x, ld, cols);
 }
 
 // explicit instantiations
 template void launch_update_x<double>(Ctx&, long long, const double2*, long long, long long, const int*,
-                                      const double2*, int, double2*, long long, const int*, int);
+                                      const double2*, int, double2*, long long, const int*, int, long long);
 template void launch_update_x<float>(Ctx&, long long, const float2*, long long, long long, const int*, const double2*,
-                                     int, double2*, long long, const int*, int);
+                                     int, double2*, long long, const int*, int, long long);
 template void launch_center_inverse<double>(Ctx&, const Grid&, int, const double2*, long long, double2*);
 template void launch_center_inverse<float>(Ctx&, const Grid&, int, const double2*, long long, float2*);
 template void launch_cast<float, double>(Ctx&, const double2*, float2*, long long);

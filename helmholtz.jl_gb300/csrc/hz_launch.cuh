@@ -17,7 +17,9 @@ static inline void check_launch(const char* name) {
   }
 }
 
-#define HZ_LAUNCH(ctx, name, kern, grid, block, smem, ...)      \
+// bytes: the launch's algorithmic DRAM bytes (each input read once, each
+// output written once), the numerator of its roofline fraction.
+#define HZ_LAUNCH(ctx, name, bytes, kern, grid, block, smem, ...) \
   do {                                                          \
     static thread_local int _id = -1;                           \
     if (_id < 0 || (size_t)_id >= (ctx).names.size() ||         \
@@ -27,7 +29,7 @@ static inline void check_launch(const char* name) {
     (ctx).before(_id, &_a);                                     \
     kern<<<grid, block, smem, (ctx).stream>>>(__VA_ARGS__);     \
     check_launch(name);                                         \
-    (ctx).after(_id, _a);                                       \
+    (ctx).after(_id, _a, (double)(bytes));                      \
   } while (0)
 
 static constexpr int kSMs = 152;

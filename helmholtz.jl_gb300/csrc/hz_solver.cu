@@ -611,12 +611,14 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
        "kcol");
     launch_lsq(h->ctx, m, dc, (int)act.size(), h->kcol.as<int>(), h->Hh.as<double2>(), h->gv.as<double2>(),
                h->yv.as<double2>());
+    long long zcols = 0;
+    for (int c : act) zcols += kcol[c];
     if (mixed)
       launch_update_x<float>(h->ctx, N, (const float2*)h->Z.p, vstride, N, h->kcol.as<int>(), h->yv.as<double2>(), m,
-                             X, N, dc, (int)act.size());
+                             X, N, dc, (int)act.size(), zcols);
     else
       launch_update_x<double>(h->ctx, N, (const double2*)h->Z.p, vstride, N, h->kcol.as<int>(), h->yv.as<double2>(),
-                              m, X, N, dc, (int)act.size());
+                              m, X, N, dc, (int)act.size(), zcols);
     // true residual r = b - H x into V_0, its norm, convergence test
     apply_H<double>(h, adj, MODE_RESID, X, B, Vj(0), dc, (int)act.size());
     col_norms(h, Vj(0), act, h->beta.as<double>(), h->beta_inv.as<double>(), rn.data());
@@ -945,8 +947,11 @@ int hz_copy(const hz_handle* h, hz_handle** out) {
 
 void* hz_stream(hz_handle* h) { return h ? (void*)h->ctx.stream : nullptr; }
 
-int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches, double* total_ms) {
+int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches,
+                    int64_t* timed_launches, double* total_ms, double* alg_bytes) {
   if (!h) return HZ_ERR_ARG;
+  cudaSetDevice(h->dev);
+  if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
   h->ctx.resolve();
   const int n = (int)h->ctx.names.size();
   if (idx < 0 || idx >= n) return n;
@@ -955,15 +960,30 @@ int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int
     name[name_len - 1] = 0;
   }
   if (launches) *launches = h->ctx.counts[idx];
+  if (timed_launches) *timed_launches = h->ctx.timed[idx];
   if (total_ms) *total_ms = h->ctx.total_ms[idx];
+  if (alg_bytes) *alg_bytes = h->ctx.alg_bytes[idx];
   return n;
 }
 
 int hz_reset_kernel_times(hz_handle* h) {
   if (!h) return HZ_ERR_ARG;
+  cudaSetDevice(h->dev);
+  if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
   h->ctx.resolve();
   std::fill(h->ctx.counts.begin(), h->ctx.counts.end(), 0);
+  std::fill(h->ctx.timed.begin(), h->ctx.timed.end(), 0);
   std::fill(h->ctx.total_ms.begin(), h->ctx.total_ms.end(), 0.0);
+  std::fill(h->ctx.alg_bytes.begin(), h->ctx.alg_bytes.end(), 0.0);
+  return HZ_OK;
+}
+
+int hz_set_profile(hz_handle* h, int32_t on) {
+  if (!h) return HZ_ERR_ARG;
+  cudaSetDevice(h->dev);
+  if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
+  h->ctx.resolve();
+  h->ctx.profile = on != 0;
   return HZ_OK;
 }
 

@@ -22,7 +22,9 @@ int Ctx::name_id(const char* name) {
     if (names[i] == name) return (int)i;
   names.emplace_back(name);
   counts.push_back(0);
+  timed.push_back(0);
   total_ms.push_back(0.0);
+  alg_bytes.push_back(0.0);
   return (int)names.size() - 1;
 }
 
@@ -39,8 +41,10 @@ void Ctx::before(int id, cudaEvent_t* a) {
   cudaEventRecord(*a, stream);
 }
 
-void Ctx::after(int id, cudaEvent_t a) {
+void Ctx::after(int id, cudaEvent_t a, double bytes) {
   ++launches;
+  counts[id] += 1;
+  alg_bytes[id] += bytes;
   if (!profile) return;
   cudaEvent_t b;
   if (pool.empty()) {
@@ -57,7 +61,7 @@ void Ctx::resolve() {
   for (auto& p : pending) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
-      counts[p.id] += 1;
+      timed[p.id] += 1;
       total_ms[p.id] += ms;
     }
     pool.push_back(p.a);
@@ -182,8 +186,13 @@ void launch_fine(Ctx& ctx, int mode, const FineOp& op, const cplx<T>* diag, cons
   int cpb = (ncols + ch - 1) / ch;
   dim3 grid((unsigned)nbx, (unsigned)ch);
   const bool is3d = op.g.nz > 1;
+  // x (and b) read and y written once per active column, the diagonal (and
+  // its inverse) once per node
+  double fbytes = (double)op.g.N * ncols * (sizeof(cplx<TX>) + sizeof(cplx<T>)) + (double)op.g.N * sizeof(cplx<T>);
+  if (mode != MODE_APPLY) fbytes += (double)op.g.N * ncols * sizeof(cplx<TB>);
+  if (mode == MODE_JACOBI) fbytes += (double)op.g.N * sizeof(cplx<T>);
 #define HZ_FINE_CASE(M, D, NAME) \
-  HZ_LAUNCH(ctx, NAME, (k_fine<T, TX, TB, M, D>), grid, TPB, 0, o, diag, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
+  HZ_LAUNCH(ctx, NAME, fbytes, (k_fine<T, TX, TB, M, D>), grid, TPB, 0, o, diag, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
   if (mode == MODE_APPLY) {
     if (is3d) HZ_FINE_CASE(MODE_APPLY, true, "fine_apply");
     else HZ_FINE_CASE(MODE_APPLY, false, "fine_apply");
@@ -267,8 +276,12 @@ void launch_rap(Ctx& ctx, int mode, const Grid& g, const cplx<T>* coef, long lon
   int cpb = (ncols + ch - 1) / ch;
   dim3 grid((unsigned)nbx, (unsigned)ch);
   const bool is3d = g.nz > 1;
+  const int ns = is3d ? 27 : 9;
+  double rbytes = (double)g.N * ncols * 2 * sizeof(cplx<T>) + (double)g.N * ns * sizeof(cplx<T>);
+  if (mode != MODE_APPLY) rbytes += (double)g.N * ncols * sizeof(cplx<TB>);
+  if (mode == MODE_JACOBI) rbytes += (double)g.N * sizeof(cplx<T>);
 #define HZ_RAP_CASE(M, D, NAME) \
-  HZ_LAUNCH(ctx, NAME, (k_rap<T, TB, M, D>), grid, TPB, 0, g, coef, cld, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
+  HZ_LAUNCH(ctx, NAME, rbytes, (k_rap<T, TB, M, D>), grid, TPB, 0, g, coef, cld, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
   if (mode == MODE_APPLY) {
     if (is3d) HZ_RAP_CASE(MODE_APPLY, true, "rap_apply");
     else HZ_RAP_CASE(MODE_APPLY, false, "rap_apply");
@@ -313,7 +326,8 @@ void launch_jacobi0(Ctx& ctx, const Grid& g, const cplx<T>* dinv, int adj, const
   int ch = chunks_for(nbx, ncols);
   int cpb = (ncols + ch - 1) / ch;
   dim3 grid((unsigned)nbx, (unsigned)ch);
-  HZ_LAUNCH(ctx, "jacobi0", (k_jacobi0<T, TB>), grid, TPB, 0, g.N, dinv, adj, b, y, ld, cols, ncols, cpb, (T)w);
+  const double jbytes = (double)g.N * ncols * (sizeof(cplx<TB>) + sizeof(cplx<T>)) + (double)g.N * sizeof(cplx<T>);
+  HZ_LAUNCH(ctx, "jacobi0", jbytes, (k_jacobi0<T, TB>), grid, TPB, 0, g.N, dinv, adj, b, y, ld, cols, ncols, cpb, (T)w);
 }
 
 // ---------------------------------------------------------------------------
@@ -380,10 +394,11 @@ void launch_restrict(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* rf
   int ch = chunks_for(nbx, ncols);
   int cpb = (ncols + ch - 1) / ch;
   dim3 grid((unsigned)nbx, (unsigned)ch);
+  const double tbytes = (double)ncols * (gf.N + gc.N) * sizeof(cplx<T>);
   if (gf.nz > 1)
-    HZ_LAUNCH(ctx, "restrict", (k_restrict<T, true>), grid, TPB, 0, gf, gc, rf, ldf, rc, ldc, cols, ncols, cpb);
+    HZ_LAUNCH(ctx, "restrict", tbytes, (k_restrict<T, true>), grid, TPB, 0, gf, gc, rf, ldf, rc, ldc, cols, ncols, cpb);
   else
-    HZ_LAUNCH(ctx, "restrict", (k_restrict<T, false>), grid, TPB, 0, gf, gc, rf, ldf, rc, ldc, cols, ncols, cpb);
+    HZ_LAUNCH(ctx, "restrict", tbytes, (k_restrict<T, false>), grid, TPB, 0, gf, gc, rf, ldf, rc, ldc, cols, ncols, cpb);
 }
 
 template <typename T, bool IS3D>
@@ -432,10 +447,11 @@ void launch_prolong(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* ec,
   int ch = chunks_for(nbx, ncols);
   int cpb = (ncols + ch - 1) / ch;
   dim3 grid((unsigned)nbx, (unsigned)ch);
+  const double pbytes = (double)ncols * (gc.N + (xin ? 2 : 1) * gf.N) * sizeof(cplx<T>);
   if (gf.nz > 1)
-    HZ_LAUNCH(ctx, "prolong", (k_prolong<T, true>), grid, TPB, 0, gf, gc, ec, ldc, xin, xout, ldf, cols, ncols, cpb);
+    HZ_LAUNCH(ctx, "prolong", pbytes, (k_prolong<T, true>), grid, TPB, 0, gf, gc, ec, ldc, xin, xout, ldf, cols, ncols, cpb);
   else
-    HZ_LAUNCH(ctx, "prolong", (k_prolong<T, false>), grid, TPB, 0, gf, gc, ec, ldc, xin, xout, ldf, cols, ncols, cpb);
+    HZ_LAUNCH(ctx, "prolong", pbytes, (k_prolong<T, false>), grid, TPB, 0, gf, gc, ec, ldc, xin, xout, ldf, cols, ncols, cpb);
 }
 
 // ---------------------------------------------------------------------------
@@ -493,17 +509,19 @@ void launch_band_solve(Ctx& ctx, long long N, int kl, int ku, const double2* ab,
                        cplx<T>* x, long long ld, const int* cols, int ncols, double2* gwork) {
   if (ncols <= 0) return;
   const long long bytes = N * (long long)sizeof(double2);
+  // the band factors once (shared through L2) plus each column in and out
+  const double bbytes = (double)N * (2.0 * kl + ku + 1) * sizeof(double2) + (double)ncols * N * 2 * sizeof(cplx<T>);
   if (bytes <= kBandSmemMax) {
     static bool attr_set = false;
     if (!attr_set) {
       cudaFuncSetAttribute(k_band_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBandSmemMax);
       attr_set = true;
     }
-    HZ_LAUNCH(ctx, "band_solve", k_band_solve<T>, ncols, 256, (size_t)bytes, N, kl, ku, ab, ipiv, b, x, ld, cols,
+    HZ_LAUNCH(ctx, "band_solve", bbytes, k_band_solve<T>, ncols, 256, (size_t)bytes, N, kl, ku, ab, ipiv, b, x, ld, cols,
               (double2*)nullptr);
   } else {
     if (!gwork) throw std::runtime_error("band_solve: coarsest level too large for shared memory and no workspace");
-    HZ_LAUNCH(ctx, "band_solve", k_band_solve<T>, ncols, 256, 0, N, kl, ku, ab, ipiv, b, x, ld, cols, gwork);
+    HZ_LAUNCH(ctx, "band_solve", bbytes, k_band_solve<T>, ncols, 256, 0, N, kl, ku, ab, ipiv, b, x, ld, cols, gwork);
   }
 }
 

@@ -155,10 +155,16 @@ int hz_copy(const hz_handle* h, hz_handle** out);
 /* The CUDA stream (cudaStream_t) every kernel of this handle runs on. */
 void* hz_stream(hz_handle* h);
 
-/* Kernel timing table (options.profile = 1): entry idx -> name, launches,
- * total milliseconds.  Returns the number of entries, or < 0 on error. */
-int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches, double* total_ms);
+/* Per-kernel launch table of the handle: entry idx -> kernel name, launches,
+ * launches timed with CUDA events (while profiling is on), their total
+ * milliseconds, and the algorithmic bytes of all launches (each input read
+ * once, each output written once).  Returns the number of entries (call with
+ * idx = -1 to get it), or < 0 on error.  Output pointers may be NULL. */
+int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches,
+                    int64_t* timed_launches, double* total_ms, double* alg_bytes);
 int hz_reset_kernel_times(hz_handle* h);
+/* Turn per-launch CUDA-event timing on (1) or off (0) (options.profile at create time). */
+int hz_set_profile(hz_handle* h, int32_t on);
 
 /* ---- host-side discretisation helpers (no GPU needed) ---------------------- */
 
