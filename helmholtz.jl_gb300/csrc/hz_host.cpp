@@ -210,3 +210,87 @@ int band_lu_factor(long long N, int kl, int ku, std::complex<double>* ab, int* i
 }
 
 }  // namespace hz
+
+namespace hz {
+
+// Block operators of the banded solve.  For block I (rows s..e, nb rows):
+//  forward:  the elimination steps s..e of gbtrs (row interchange, then
+//            rows j+1..j+kl -= L(.,j) v_j) touch only rows s .. e+kl, so their
+//            composition is one dense W x W matrix T_I (W = min(nb+kl, N-s))
+//            applied to that window;
+//  backward: x_I = U_II^{-1} (y_I - U_{I,right} x_right), stored as
+//            G_I = [U_II^{-1} | -U_II^{-1} U_{I,right}] (nb x Wb, Wb = min(nb+kv, N-s)).
+// Both are row-major.  ab must hold the factors with the true U diagonal.
+void band_block_operators(long long N, int kl, int ku, const std::complex<double>* ab, const int* ipiv, int nb,
+                          std::vector<BandBlock>& blocks, std::vector<std::complex<double>>& T,
+                          std::vector<std::complex<double>>& G) {
+  const long long ldab = 2LL * kl + ku + 1;
+  const int kv = kl + ku;
+  auto A = [&](long long i, long long j) -> cd { return ab[j * ldab + kv + i - j]; };
+  const long long nbk = (N + nb - 1) / nb;
+  blocks.resize((size_t)nbk);
+  long long toff = 0, goff = 0;
+  for (long long I = 0; I < nbk; ++I) {
+    BandBlock& B = blocks[(size_t)I];
+    B.s = I * nb;
+    B.nb = (int)std::min<long long>(nb, N - B.s);
+    B.W = (int)std::min<long long>((long long)nb + kl, N - B.s);
+    B.Wb = (int)std::min<long long>((long long)B.nb + kv, N - B.s);
+    B.toff = toff;
+    B.goff = goff;
+    toff += (long long)B.W * B.W;
+    goff += (long long)B.nb * B.Wb;
+  }
+  T.assign((size_t)toff, cd(0.0));
+  G.assign((size_t)goff, cd(0.0));
+#pragma omp parallel for schedule(dynamic)
+  for (long long I = 0; I < nbk; ++I) {
+    const BandBlock& B = blocks[(size_t)I];
+    const int W = B.W;
+    cd* t = T.data() + B.toff;
+    for (int i = 0; i < W; ++i) t[(size_t)i * W + i] = 1.0;
+    const long long jend = std::min<long long>(B.s + B.nb - 1, N - 2);
+    for (long long j = B.s; j <= jend; ++j) {
+      const int lm = (int)std::min<long long>(kl, N - 1 - j);
+      const int rj = (int)(j - B.s);
+      const int rl = (int)(ipiv[j] - B.s);
+      if (rl != rj)
+        for (int c = 0; c < W; ++c) std::swap(t[(size_t)rj * W + c], t[(size_t)rl * W + c]);
+      for (int r = 1; r <= lm; ++r) {
+        const cd l = A(j + r, j);
+        if (l == 0.0) continue;
+        cd* dst = t + (size_t)(rj + r) * W;
+        const cd* src = t + (size_t)rj * W;
+        for (int c = 0; c < W; ++c) dst[c] -= l * src[c];
+      }
+    }
+    // backward operator
+    const int n = B.nb, Wb = B.Wb;
+    std::vector<cd> inv((size_t)n * n, 0.0);  // U_II^{-1}, row-major upper triangular
+    for (int col = n - 1; col >= 0; --col) {
+      // solve U_II z = e_col by back substitution (z has entries 0..col)
+      inv[(size_t)col * n + col] = 1.0 / A(B.s + col, B.s + col);
+      for (int i = col - 1; i >= 0; --i) {
+        cd acc = 0.0;
+        const int kmax = std::min(col, i + kv);
+        for (int k = i + 1; k <= kmax; ++k) acc += A(B.s + i, B.s + k) * inv[(size_t)k * n + col];
+        inv[(size_t)i * n + col] = -acc / A(B.s + i, B.s + i);
+      }
+    }
+    cd* g = G.data() + B.goff;
+    for (int i = 0; i < n; ++i)
+      for (int k = i; k < n; ++k) g[(size_t)i * Wb + k] = inv[(size_t)i * n + k];
+    // -U_II^{-1} U_right, U_right(k, c) = U(s+k, s+n+c) for c < Wb - n
+    for (int i = 0; i < n; ++i) {
+      for (int c = 0; c < Wb - n; ++c) {
+        const long long gc = B.s + n + c;
+        cd acc = 0.0;
+        const int kmin = (int)std::max<long long>(i, gc - kv - B.s);  // U(s+k, gc) = 0 for gc-(s+k) > kv
+        for (int k = kmin; k < n; ++k) acc += inv[(size_t)i * n + k] * A(B.s + k, gc);
+        g[(size_t)i * Wb + n + c] = -acc;
+      }
+    }
+  }
+}
+
+}  // namespace hz

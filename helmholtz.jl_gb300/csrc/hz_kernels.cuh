@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "hz_common.cuh"
+#include "hz_host.h"
 
 namespace hz {
 
@@ -74,13 +75,18 @@ template <typename T>
 void launch_prolong(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* ec, long long ldc, const cplx<T>* xin,
                     cplx<T>* xout, long long ldf, const int* cols, int ncols);
 
-// Banded LU solve with partial pivoting (factors from the host factorisation,
-// LAPACK gbtrf layout, ldab = 2kl+ku+1), one CTA per column, FP64 arithmetic.
-// The column lives in shared memory when N*16 bytes fit, else in gwork
-// (N values per active column).
+// Coarsest-level direct solve: blocked banded LU (see band_block_operators);
+// T / G are the device copies of the forward / backward block operators.
+// work holds 3 * ncols * N FP64 complex values.
+struct BandSolveOps {
+  long long N = 0;
+  std::vector<BandBlock> blocks;
+  const double2* T = nullptr;
+  const double2* G = nullptr;
+};
 template <typename T>
-void launch_band_solve(Ctx& ctx, long long N, int kl, int ku, const double2* ab, const int* ipiv, const cplx<T>* b,
-                       cplx<T>* x, long long ld, const int* cols, int ncols, double2* gwork);
+void launch_band_solve(Ctx& ctx, const BandSolveOps& op, const cplx<T>* b, cplx<T>* x, long long ld, const int* cols,
+                       int ncols, double2* work);
 
 // ---- setup kernels ---------------------------------------------------------
 void launch_probe_init(Ctx& ctx, const Grid& gc, int dim, double2* out, long long ld);
@@ -104,14 +110,20 @@ void launch_zero_cols(Ctx& ctx, long long N, cplx<T>* x, long long ld, const int
 // V + (i*vstride + c)*ld.  Partial sums go to part[(pos*K1 + slot)*nblk + blk]
 // and are folded in a fixed order by launch_reduce (deterministic results).
 int krylov_nblk(long long N, int ncols);
-// slots i < K: conj(V_{i0+i}) . w ; slot K (want_norm): ||w||^2
+// slots i < K: conj(V_{i0+i}) . w ; slot K (want_norm): ||w||^2.  Columns with
+// mask[c] == 0 (mask may be null) yield zeros.
 void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
-                 const double2* w, long long wld, const int* cols, int ncols, int nblk, int want_norm, double2* part);
-// w -= sum_{i<K} h[c*hstride + i0 + i] V_{i0+i}; then (want_dots) slots i < K:
-// conj(V_{i0+i}) . w_new and (want_norm) the next slot: ||w_new||^2.
+                 const double2* w, long long wld, const int* cols, int ncols, int nblk, int want_norm, double2* part,
+                 const int* mask = nullptr);
+// w -= sum_{i<K} h[c*hstride + i0 + i] V_{i0+i}; with want_norm, slot 0 of the
+// partials holds ||w_new||^2.  Columns with mask[c] == 0 are left untouched.
 void launch_update(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
                    const double2* h, int hstride, double2* w, long long wld, const int* cols, int ncols, int nblk,
-                   int want_dots, int want_norm, double2* part);
+                   int want_norm, double2* part, const int* mask = nullptr);
+// flag[c] = (after[c*astride] < before[c*bstride + bslot] / 2): DGKS test for a
+// second Gram-Schmidt pass.
+void launch_dgks(Ctx& ctx, const int* cols, int ncols, const double2* before, int bstride, int bslot,
+                 const double2* after, int astride, int* flag);
 // out[c*ostride + slot] = sum over blocks of part (slot < K1); accum adds to out.
 void launch_reduce(Ctx& ctx, const double2* part, const int* cols, int ncols, int K1, int nblk, double2* out,
                    int ostride, int accum);
@@ -130,12 +142,13 @@ void launch_norms(Ctx& ctx, const double2* red, int stride, int slot, const int*
 // g[c*(m+1) + 0] = beta[c], the other entries of g zero.
 void launch_cycle_init(Ctx& ctx, int m, const int* cols, int ncols, const double* beta, double2* g);
 // Arnoldi step j of column c: h = hA + hB (hB may be null), h_{j+1,j} =
-// sqrt(Re nrm[c*hstride]); apply rotations 0..j-1, form rotation j, update g,
-// est[c] = |g_{j+1}|, inv_hn[c] = 1/h_{j+1,j}.  Hh[c*(m+1)*m + jj*(m+1) + i],
-// cs/sn[c*m + i], g[c*(m+1) + i].
+// sqrt(Re nrm[c*hstride]) or, where flag[c] is set (second pass taken),
+// sqrt(Re nrm2[c*hstride]); apply rotations 0..j-1, form rotation j, update
+// g, est[c] = |g_{j+1}|, inv_hn[c] = 1/h_{j+1,j}.
+// Hh[c*(m+1)*m + jj*(m+1) + i], cs/sn[c*m + i], g[c*(m+1) + i].
 void launch_arnoldi_step(Ctx& ctx, int j, int m, const int* cols, int ncols, const double2* hA, const double2* hB,
-                         const double2* nrm, int hstride, double2* Hh, double2* cs, double2* sn, double2* g,
-                         double* est, double* inv_hn);
+                         const double2* nrm, const double2* nrm2, const int* flag, int hstride, double2* Hh,
+                         double2* cs, double2* sn, double2* g, double* est, double* inv_hn);
 // Back substitution R y = g for the first kcol[c] entries: y[c*m + i].
 void launch_lsq(Ctx& ctx, int m, const int* cols, int ncols, const int* kcol, const double2* Hh, const double2* g,
                 double2* y);

@@ -27,11 +27,13 @@ int krylov_nblk(long long N, int ncols) {
   return (int)nb;
 }
 
-// Block-wide sum of NV complex values per thread, result written by thread 0
-// into part[slot*nblk] (stride nblk between slots).
+// Block-wide sums of nv complex values (v[0..nv)) and, when want_norm, one
+// real value; thread s writes slot s of this block's partials:
+// part[s*nblk + blockIdx.x] (the norm goes to slot nv).
 template <int NV>
-__device__ __forceinline__ void block_reduce_store(double2 (&v)[NV], int nv, double2* part, int nblk) {
-  __shared__ double2 red[RT / 32][NV];
+__device__ __forceinline__ void block_reduce_store(const double2 (&v)[NV], int nv, double nrm, int want_norm,
+                                                   double2* part, int nblk) {
+  __shared__ double2 red[RT / 32][NV + 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int s = 0; s < NV; ++s) {
@@ -45,109 +47,152 @@ __device__ __forceinline__ void block_reduce_store(double2 (&v)[NV], int nv, dou
       if (lane == 0) red[warp][s] = mk<double>(a, b);
     }
   }
+  if (want_norm) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+    if (lane == 0) red[warp][NV] = mk<double>(nrm, 0.0);
+  }
   __syncthreads();
-  if (threadIdx.x < nv) {
+  const int tot = nv + want_norm;
+  if (threadIdx.x < tot) {
+    const int src = (threadIdx.x < nv) ? threadIdx.x : NV;
     double a = 0, b = 0;
     for (int w = 0; w < RT / 32; ++w) {
-      a += red[w][threadIdx.x].x;
-      b += red[w][threadIdx.x].y;
+      a += red[w][src].x;
+      b += red[w][src].y;
     }
     part[(long long)threadIdx.x * nblk + blockIdx.x] = mk<double>(a, b);
   }
 }
 
-__global__ void __launch_bounds__(RT) k_dots(long long N, const double2* __restrict__ V, long long vstride,
-                                             long long ld, int i0, int K, const double2* __restrict__ w, long long wld,
-                                             const int* __restrict__ cols, int nblk, int want_norm,
-                                             double2* __restrict__ part) {
+// Zero partials of a masked-off column (the reduce then yields zeros).
+__device__ __forceinline__ void store_zero_partials(int K1, double2* part, int nblk) {
+  if (threadIdx.x < K1) part[(long long)threadIdx.x * nblk + blockIdx.x] = mk<double>(0, 0);
+}
+
+template <int KT>
+__global__ void __launch_bounds__(RT, 2) k_dots(long long N, const double2* __restrict__ V, long long vstride,
+                                                long long ld, int i0, const double2* __restrict__ w, long long wld,
+                                                const int* __restrict__ cols, const int* __restrict__ mask, int nblk,
+                                                int want_norm, double2* __restrict__ part) {
   const int pos = blockIdx.y;
   const int c = cols[pos];
-  const int K1 = K + want_norm;
+  const int K1 = KT + want_norm;
+  double2* pp = part + (long long)pos * K1 * nblk;
+  if (mask && !mask[c]) {
+    store_zero_partials(K1, pp, nblk);
+    return;
+  }
   const double2* wc = w + (long long)c * wld;
-  double2 acc[KG + 1];
+  const double2* vb = V + ((long long)i0 * vstride + c) * ld;
+  const long long vs = vstride * ld;  // distance between consecutive basis vectors
+  constexpr int KA = KT > 0 ? KT : 1;  // KT = 0: the norm alone
+  double2 acc[KA];
 #pragma unroll
-  for (int s = 0; s <= KG; ++s) acc[s] = mk<double>(0, 0);
+  for (int s = 0; s < KA; ++s) acc[s] = mk<double>(0, 0);
   double nrm = 0.0;
   const long long stride = (long long)nblk * RT;
   for (long long p = (long long)blockIdx.x * RT + threadIdx.x; p < N; p += stride) {
     const double2 wv = wc[p];
 #pragma unroll
-    for (int s = 0; s < KG; ++s) {
-      if (s < K) {
-        const double2 vv = V[((long long)(i0 + s) * vstride + c) * ld + p];
-        acc[s] = cfma_conj<double>(vv, wv, acc[s]);
-      }
-    }
+    for (int s = 0; s < KT; ++s) acc[s] = cfma_conj<double>(vb[s * vs + p], wv, acc[s]);
     if (want_norm) nrm = fma(wv.x, wv.x, fma(wv.y, wv.y, nrm));
   }
-  // slot K carries the norm; every index below is a compile-time constant
-#pragma unroll
-  for (int s = KG; s >= 0; --s) {
-    if (s == K) acc[s] = mk<double>(nrm, 0.0);
-  }
-  block_reduce_store<KG + 1>(acc, K1, part + (long long)pos * K1 * nblk, nblk);
+  block_reduce_store<KA>(acc, KT, nrm, want_norm, pp, nblk);
 }
 
-void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
-                 const double2* w, long long wld, const int* cols, int ncols, int nblk, int want_norm, double2* part) {
-  if (ncols <= 0) return;
-  if (K > KG) throw std::runtime_error("launch_dots: too many vectors in one pass");
-  dim3 grid(nblk, ncols);
-  const double bytes = (double)N * ncols * (K + 1) * sizeof(double2);
-  HZ_LAUNCH(ctx, "krylov_dots", bytes, k_dots, grid, RT, 0, N, V, vstride, ld, i0, K, w, wld, cols, nblk, want_norm, part);
-}
-
-__global__ void __launch_bounds__(RT) k_update(long long N, const double2* __restrict__ V, long long vstride,
-                                               long long ld, int i0, int K, const double2* __restrict__ h, int hstride,
-                                               double2* __restrict__ w, long long wld, const int* __restrict__ cols,
-                                               int nblk, int want_dots, int want_norm, double2* __restrict__ part) {
+template <int KT>
+__global__ void __launch_bounds__(RT, 2) k_update(long long N, const double2* __restrict__ V, long long vstride,
+                                                  long long ld, int i0, const double2* __restrict__ h, int hstride,
+                                                  double2* __restrict__ w, long long wld,
+                                                  const int* __restrict__ cols, const int* __restrict__ mask,
+                                                  int nblk, int want_norm, double2* __restrict__ part) {
   const int pos = blockIdx.y;
   const int c = cols[pos];
-  double2 hv[KG];
+  double2* pp = part + (long long)pos * want_norm * nblk;
+  if (mask && !mask[c]) {
+    store_zero_partials(want_norm, pp, nblk);
+    return;
+  }
+  double2 hv[KT];
 #pragma unroll
-  for (int s = 0; s < KG; ++s) hv[s] = (s < K) ? h[(long long)c * hstride + i0 + s] : mk<double>(0, 0);
-  double2 acc[KG + 1];
-#pragma unroll
-  for (int s = 0; s <= KG; ++s) acc[s] = mk<double>(0, 0);
-  const int nd = want_dots ? K : 0;
+  for (int s = 0; s < KT; ++s) hv[s] = h[(long long)c * hstride + i0 + s];
+  const double2* vb = V + ((long long)i0 * vstride + c) * ld;
+  const long long vs = vstride * ld;
   double nrm = 0.0;
   double2* wc = w + (long long)c * wld;
   const long long stride = (long long)nblk * RT;
   for (long long p = (long long)blockIdx.x * RT + threadIdx.x; p < N; p += stride) {
-    double2 vv[KG];
     double2 wv = wc[p];
 #pragma unroll
-    for (int s = 0; s < KG; ++s) {
-      if (s < K) {
-        vv[s] = V[((long long)(i0 + s) * vstride + c) * ld + p];
-        wv = cfms<double>(hv[s], vv[s], wv);
-      }
-    }
+    for (int s = 0; s < KT; ++s) wv = cfms<double>(hv[s], vb[s * vs + p], wv);
     wc[p] = wv;
-    if (want_dots) {
-#pragma unroll
-      for (int s = 0; s < KG; ++s)
-        if (s < K) acc[s] = cfma_conj<double>(vv[s], wv, acc[s]);
-    }
     if (want_norm) nrm = fma(wv.x, wv.x, fma(wv.y, wv.y, nrm));
   }
-#pragma unroll
-  for (int s = KG; s >= 0; --s) {
-    if (s == nd) acc[s] = mk<double>(nrm, 0.0);
+  if (want_norm) {
+    const double2 none[1] = {mk<double>(0, 0)};
+    block_reduce_store<1>(none, 0, nrm, 1, pp, nblk);
   }
-  const int K1 = nd + want_norm;
-  if (K1 > 0) block_reduce_store<KG + 1>(acc, K1, part + (long long)pos * K1 * nblk, nblk);
+}
+
+#define HZ_K_CASES(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16)
+
+void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
+                 const double2* w, long long wld, const int* cols, int ncols, int nblk, int want_norm, double2* part,
+                 const int* mask) {
+  if (ncols <= 0) return;
+  dim3 grid(nblk, ncols);
+  const double bytes = (double)N * ncols * (K + 1) * sizeof(double2);
+  switch (K) {
+#define HZ_DOTS_CASE(k)                                                                                     \
+  case k:                                                                                                   \
+    HZ_LAUNCH(ctx, "krylov_dots", bytes, k_dots<k>, grid, RT, 0, N, V, vstride, ld, i0, w, wld, cols, mask, \
+              nblk, want_norm, part);                                                                       \
+    break;
+    HZ_DOTS_CASE(0)
+    HZ_K_CASES(HZ_DOTS_CASE)
+#undef HZ_DOTS_CASE
+    default:
+      throw std::runtime_error("launch_dots: 1..16 vectors per pass");
+  }
 }
 
 void launch_update(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
                    const double2* h, int hstride, double2* w, long long wld, const int* cols, int ncols, int nblk,
-                   int want_dots, int want_norm, double2* part) {
+                   int want_norm, double2* part, const int* mask) {
   if (ncols <= 0) return;
-  if (K > KG) throw std::runtime_error("launch_update: too many vectors in one pass");
   dim3 grid(nblk, ncols);
   const double bytes = (double)N * ncols * (K + 2) * sizeof(double2);
-  HZ_LAUNCH(ctx, "krylov_update", bytes, k_update, grid, RT, 0, N, V, vstride, ld, i0, K, h, hstride, w, wld, cols, nblk,
-            want_dots, want_norm, part);
+  switch (K) {
+#define HZ_UPD_CASE(k)                                                                                           \
+  case k:                                                                                                        \
+    HZ_LAUNCH(ctx, "krylov_update", bytes, k_update<k>, grid, RT, 0, N, V, vstride, ld, i0, h, hstride, w, wld, \
+              cols, mask, nblk, want_norm, part);                                                                \
+    break;
+    HZ_K_CASES(HZ_UPD_CASE)
+#undef HZ_UPD_CASE
+    default:
+      throw std::runtime_error("launch_update: 1..16 vectors per pass");
+  }
+}
+
+// DGKS test per column: a second Gram-Schmidt pass is needed when the first
+// one removed more than half of the squared norm (||w'||^2 < ||w||^2 / 2).
+__global__ void k_dgks(const int* __restrict__ cols, int ncols, const double2* __restrict__ before, int bstride,
+                       int bslot, const double2* __restrict__ after, int astride, int* __restrict__ flag) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  const double b = before[(long long)c * bstride + bslot].x;
+  const double a = after[(long long)c * astride].x;
+  flag[c] = (a < 0.5 * b) ? 1 : 0;
+}
+
+void launch_dgks(Ctx& ctx, const int* cols, int ncols, const double2* before, int bstride, int bslot,
+                 const double2* after, int astride, int* flag) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "dgks", 0.0, k_dgks, (ncols + 127) / 128, 128, 0, cols, ncols, before, bstride, bslot, after, astride,
+            flag);
 }
 
 // One warp per (column, slot): fixed-order sum over the nblk partials.
@@ -277,7 +322,8 @@ void launch_cycle_init(Ctx& ctx, int m, const int* cols, int ncols, const double
 
 // Complex Givens rotation convention: (u, v) -> (conj(c) u + conj(s) v, -s u + c v).
 __global__ void k_arnoldi_step(int j, int m, const int* __restrict__ cols, int ncols, const double2* __restrict__ hA,
-                               const double2* __restrict__ hB, const double2* __restrict__ nrm, int hstride,
+                               const double2* __restrict__ hB, const double2* __restrict__ nrm,
+                               const double2* __restrict__ nrm2, const int* __restrict__ flag, int hstride,
                                double2* __restrict__ Hh, double2* __restrict__ cs, double2* __restrict__ sn,
                                double2* __restrict__ g, double* __restrict__ est, double* __restrict__ inv_hn) {
   const int pos = blockIdx.x * blockDim.x + threadIdx.x;
@@ -291,7 +337,8 @@ __global__ void k_arnoldi_step(int j, int m, const int* __restrict__ cols, int n
     if (hB) v = cadd<double>(v, hB[(long long)c * hstride + i]);
     H[i] = v;
   }
-  const double hn = safe_sqrt(nrm[(long long)c * hstride].x);
+  const bool second = flag && flag[c];
+  const double hn = safe_sqrt((second ? nrm2 : nrm)[(long long)c * hstride].x);
   H[j + 1] = mk<double>(hn, 0.0);
   for (int i = 0; i < j; ++i) {
     const double2 u = H[i], v = H[i + 1];
@@ -324,11 +371,11 @@ __global__ void k_arnoldi_step(int j, int m, const int* __restrict__ cols, int n
 }
 
 void launch_arnoldi_step(Ctx& ctx, int j, int m, const int* cols, int ncols, const double2* hA, const double2* hB,
-                         const double2* nrm, int hstride, double2* Hh, double2* cs, double2* sn, double2* g,
-                         double* est, double* inv_hn) {
+                         const double2* nrm, const double2* nrm2, const int* flag, int hstride, double2* Hh,
+                         double2* cs, double2* sn, double2* g, double* est, double* inv_hn) {
   if (ncols <= 0) return;
-  HZ_LAUNCH(ctx, "arnoldi_step", 0.0, k_arnoldi_step, (ncols + 63) / 64, 64, 0, j, m, cols, ncols, hA, hB, nrm, hstride, Hh,
-            cs, sn, g, est, inv_hn);
+  HZ_LAUNCH(ctx, "arnoldi_step", 0.0, k_arnoldi_step, (ncols + 63) / 64, 64, 0, j, m, cols, ncols, hA, hB, nrm, nrm2,
+            flag, hstride, Hh, cs, sn, g, est, inv_hn);
 }
 
 __global__ void k_lsq(int m, const int* __restrict__ cols, int ncols, const int* __restrict__ kcol,

@@ -94,10 +94,11 @@ struct Hierarchy {
   bool built = false;
   int adj = 0;
   std::vector<std::unique_ptr<Level>> lv;
-  // coarsest LU (band, FP64)
+  // coarsest LU (band, FP64) as blocked operators
   long long nc = 0;
   int kl = 0, ku = 0;
-  DBuf ab, ipiv, bandwork;
+  DBuf bandT, bandG, bandwork;
+  BandSolveOps band;
 };
 
 }  // namespace
@@ -116,7 +117,8 @@ struct hz_handle {
   // FGMRES workspace
   int rcap = 0;
   int mcap = 0;
-  DBuf Bd, Xd, V, Z, part, hA, hB, nr, Hh, cs, sn, gv, yv, est, invhn, bnorm, bnorm_inv, beta, beta_inv, cols, kcol;
+  DBuf Bd, Xd, V, Z, part, hA, hB, nr, nr2, flag, Hh, cs, sn, gv, yv, est, invhn, bnorm, bnorm_inv, beta, beta_inv,
+      cols, kcol;
   DBuf tmpA, tmpB;  // hz_apply staging
   double* h_est = nullptr;  // pinned
   double* h_nrm = nullptr;  // pinned
@@ -233,13 +235,20 @@ void factor_coarsest(hz_handle* h, Hierarchy& H) {
   std::vector<int> ipiv((size_t)N);
   int info = band_lu_factor(N, kl, ku, ab.data(), ipiv.data());
   if (info != 0) fail(HZ_ERR_NUMERIC, "coarsest-level LU: zero pivot in column %d", info);
+  // dense block operators of the blocked banded solve, block size kl
+  std::vector<std::complex<double>> T, G;
+  H.band.blocks.clear();
+  band_block_operators(N, kl, ku, ab.data(), ipiv.data(), std::max(kl, 1), H.band.blocks, T, G);
   H.nc = N;
   H.kl = kl;
   H.ku = ku;
-  H.ab.alloc(ab.size() * 16);
-  H.ipiv.alloc(ipiv.size() * sizeof(int));
-  ck(cudaMemcpy(H.ab.p, ab.data(), ab.size() * 16, cudaMemcpyHostToDevice), "upload band LU");
-  ck(cudaMemcpy(H.ipiv.p, ipiv.data(), ipiv.size() * sizeof(int), cudaMemcpyHostToDevice), "upload pivots");
+  H.bandT.alloc(T.size() * 16);
+  H.bandG.alloc(G.size() * 16);
+  ck(cudaMemcpy(H.bandT.p, T.data(), T.size() * 16, cudaMemcpyHostToDevice), "upload band forward operators");
+  ck(cudaMemcpy(H.bandG.p, G.data(), G.size() * 16, cudaMemcpyHostToDevice), "upload band backward operators");
+  H.band.N = N;
+  H.band.T = H.bandT.as<double2>();
+  H.band.G = H.bandG.as<double2>();
 }
 
 void build_hierarchy(hz_handle* h, int adj) {
@@ -318,6 +327,8 @@ void ensure_workspace(hz_handle* h, int nrhs) {
   h->hA.alloc((size_t)R * HS * 16);
   h->hB.alloc((size_t)R * HS * 16);
   h->nr.alloc((size_t)R * HS * 16);
+  h->nr2.alloc((size_t)R * HS * 16);
+  h->flag.alloc((size_t)R * sizeof(int));
   h->Hh.alloc((size_t)R * (m + 1) * m * 16);
   h->cs.alloc((size_t)R * m * 16);
   h->sn.alloc((size_t)R * m * 16);
@@ -357,7 +368,7 @@ void ensure_level_buffers(hz_handle* h, Hierarchy& H, int R) {
       L.r.alloc(bytes);
     }
   }
-  if (H.lv.size() > 0 && H.nc * 16 > 200LL * 1024) H.bandwork.alloc((size_t)R * H.nc * 16);
+  H.bandwork.alloc((size_t)3 * R * H.nc * 16);
 }
 
 // ---- multigrid cycle -----------------------------------------------------------
@@ -404,8 +415,7 @@ void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out
   const int last = (int)H.lv.size() - 1;
   if (l == last) {
     if (!std::is_same<T, TB>::value) fail(HZ_ERR_STATE, "single-level mixed hierarchy is not supported");
-    launch_band_solve<T>(h->ctx, H.nc, H.kl, H.ku, H.ab.as<double2>(), H.ipiv.as<int>(), (const cplx<T>*)b, out,
-                         L.ld, cols, nc, H.bandwork.as<double2>());
+    launch_band_solve<T>(h->ctx, H.band, (const cplx<T>*)b, out, L.ld, cols, nc, H.bandwork.as<double2>());
     return;
   }
   Level& C = *H.lv[l + 1];
@@ -559,37 +569,35 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
         apply_H<float>(h, adj, MODE_APPLY, (const float2*)Zj(j), nullptr, w, dc, nl);
       else
         apply_H<double>(h, adj, MODE_APPLY, (const double2*)Zj(j), nullptr, w, dc, nl);
-      // classical Gram-Schmidt, two passes
+      // classical Gram-Schmidt with the DGKS test: pass 1 (dots + ||w||^2,
+      // update + ||w'||^2) for every column, pass 2 only for the columns whose
+      // norm dropped below 1/sqrt(2) of its value (masked on the device)
       const int K = j + 1;
       const int nblk = krylov_nblk(N, nl);
       double2* hA = h->hA.as<double2>();
       double2* hB = h->hB.as<double2>();
-      for (int i0 = 0; i0 < K; i0 += 16) {
-        const int k = std::min(16, K - i0);
-        launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, 0, part);
-        launch_reduce(h->ctx, part, dc, nl, k, nblk, hA + i0, HS, 0);
-      }
-      if (K <= 16) {
-        launch_update(h->ctx, N, V, vstride, N, 0, K, hA, HS, w, N, dc, nl, nblk, 1, 0, part);
-        launch_reduce(h->ctx, part, dc, nl, K, nblk, hB, HS, 0);
-      } else {
-        for (int i0 = 0; i0 < K; i0 += 16)
-          launch_update(h->ctx, N, V, vstride, N, i0, std::min(16, K - i0), hA, HS, w, N, dc, nl, nblk, 0, 0, part);
+      int* flag = h->flag.as<int>();
+      for (int pass = 0; pass < 2; ++pass) {
+        double2* hh = pass == 0 ? hA : hB;
+        double2* nrm = pass == 0 ? h->nr.as<double2>() : h->nr2.as<double2>();
+        const int* mask = pass == 0 ? nullptr : flag;
         for (int i0 = 0; i0 < K; i0 += 16) {
           const int k = std::min(16, K - i0);
-          launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, 0, part);
-          launch_reduce(h->ctx, part, dc, nl, k, nblk, hB + i0, HS, 0);
+          const int wn = (pass == 0 && i0 + 16 >= K) ? 1 : 0;  // ||w||^2 before the update (slot K)
+          launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, wn, part, mask);
+          launch_reduce(h->ctx, part, dc, nl, k + wn, nblk, hh + i0, HS, 0);
         }
+        for (int i0 = 0; i0 < K; i0 += 16) {
+          const int k = std::min(16, K - i0);
+          const int wn = (i0 + 16 >= K) ? 1 : 0;
+          launch_update(h->ctx, N, V, vstride, N, i0, k, hh, HS, w, N, dc, nl, nblk, wn, part, mask);
+          if (wn) launch_reduce(h->ctx, part, dc, nl, 1, nblk, nrm, HS, 0);
+        }
+        if (pass == 0) launch_dgks(h->ctx, dc, nl, hA, HS, K, h->nr.as<double2>(), HS, flag);
       }
-      for (int i0 = 0; i0 < K; i0 += 16) {
-        const int k = std::min(16, K - i0);
-        const bool lastg = i0 + 16 >= K;
-        launch_update(h->ctx, N, V, vstride, N, i0, k, hB, HS, w, N, dc, nl, nblk, 0, lastg ? 1 : 0, part);
-        if (lastg) launch_reduce(h->ctx, part, dc, nl, 1, nblk, h->nr.as<double2>(), HS, 0);
-      }
-      launch_arnoldi_step(h->ctx, j, m, dc, nl, hA, hB, h->nr.as<double2>(), HS, h->Hh.as<double2>(),
-                          h->cs.as<double2>(), h->sn.as<double2>(), h->gv.as<double2>(), h->est.as<double>(),
-                          h->invhn.as<double>());
+      launch_arnoldi_step(h->ctx, j, m, dc, nl, hA, hB, h->nr.as<double2>(), h->nr2.as<double2>(), flag, HS,
+                          h->Hh.as<double2>(), h->cs.as<double2>(), h->sn.as<double2>(), h->gv.as<double2>(),
+                          h->est.as<double>(), h->invhn.as<double>());
       launch_scale_cols(h->ctx, N, w, N, w, N, h->invhn.as<double>(), dc, nl);
       ck(cudaMemcpyAsync(h->h_est, h->est.p, (size_t)h->rcap * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "est");
       sync(h);
@@ -931,9 +939,10 @@ int hz_clear(hz_handle* h) {
     sync(h);
     for (auto& H : h->hier) {
       H.lv.clear();
-      H.ab.reset();
-      H.ipiv.reset();
+      H.bandT.reset();
+      H.bandG.reset();
       H.bandwork.reset();
+      H.band = BandSolveOps();
       H.built = false;
     }
   });

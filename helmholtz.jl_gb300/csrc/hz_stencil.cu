@@ -455,73 +455,79 @@ void launch_prolong(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* ec,
 }
 
 // ---------------------------------------------------------------------------
-// Coarsest level: banded LU solve (LAPACK gbtrs order), FP64 arithmetic.
+// Coarsest level: blocked banded LU solve, FP64 arithmetic.
+//
+// The host folds each block of kl elimination steps of the band LU (row
+// interchanges included) into a dense window operator T_I, and each block of
+// the back substitution into G_I = [U_II^{-1} | -U_II^{-1} U_right]; a solve is
+// then N/kl sequential window mat-vecs per direction, each spread over the
+// whole GPU: one warp per (output row, column), lanes split the window sum.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_band_solve(long long N, int kl, int ku, const double2* __restrict__ ab,
-                                                    const int* __restrict__ ipiv, const cplx<T>* __restrict__ b,
-                                                    cplx<T>* __restrict__ x, long long ld, const int* __restrict__ cols,
-                                                    double2* gwork) {
-  extern __shared__ double2 smem[];
-  const int col = cols[blockIdx.x];
-  double2* v = gwork ? gwork + (long long)blockIdx.x * N : smem;
-  const cplx<T>* bc = b + (long long)col * ld;
-  cplx<T>* xc = x + (long long)col * ld;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (long long p = tid; p < N; p += nt) v[p] = mk<double>((double)bc[p].x, (double)bc[p].y);
-  __syncthreads();
-  const int kv = kl + ku;
-  const long long ldab = 2LL * kl + ku + 1;
-  // forward: L with the row interchanges applied step by step
-  for (long long jj = 0; jj < N - 1; ++jj) {
-    const int lm = (int)min((long long)kl, N - 1 - jj);
-    const long long l = ipiv[jj];
-    const double2 bj = v[jj];
-    const double2 bl = v[l];
-    __syncthreads();
-    const double2 piv = (l != jj) ? bl : bj;
-    const double2* Lc = ab + jj * ldab + kv;
-    for (int r = tid + 1; r <= lm; r += nt) {
-      const double2 val = (jj + r == l) ? bj : v[jj + r];
-      v[jj + r] = cfms<double>(Lc[r], piv, val);
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_band_block(long long N, long long s, int Win, int split,
+                                                    const double2* __restrict__ M, const double2* __restrict__ src0,
+                                                    const cplx<T>* __restrict__ b, long long ldb,
+                                                    const int* __restrict__ cols, const double2* __restrict__ src1,
+                                                    double2* __restrict__ dst, cplx<T>* __restrict__ xout,
+                                                    long long ldx, int ncols) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x;
+  const int ci = blockIdx.y * 8 + warp;
+  if (ci >= ncols) return;
+  const double2* Mr = M + (long long)i * Win;
+  const long long base = (long long)ci * N + s;
+  double ar = 0.0, ai = 0.0;
+  for (int k = lane; k < Win; k += 32) {
+    const double2 m = Mr[k];
+    double2 v;
+    if (k < split) {
+      v = src0[base + k];
+    } else if (MODE == 0) {
+      const cplx<T> bb = b[(long long)cols[ci] * ldb + s + k];
+      v = mk<double>((double)bb.x, (double)bb.y);
+    } else {
+      v = src1[base + k];
     }
-    if (tid == 0) v[jj] = piv;
-    __syncthreads();
+    ar = fma(m.x, v.x, ar);
+    ar = fma(-m.y, v.y, ar);
+    ai = fma(m.x, v.y, ai);
+    ai = fma(m.y, v.x, ai);
   }
-  // backward: U has kl + ku superdiagonals
-  for (long long jj = N - 1; jj >= 0; --jj) {
-    const double2* Uc = ab + jj * ldab + kv;  // Uc[i - jj] = U(i, jj), i <= jj
-    const double2 u = Uc[0];
-    const double2 bj = v[jj];
-    const double den = u.x * u.x + u.y * u.y;
-    const double2 xj = mk<double>((bj.x * u.x + bj.y * u.y) / den, (bj.y * u.x - bj.x * u.y) / den);
-    const long long lo = max(0LL, jj - kv);
-    for (long long i = lo + tid; i < jj; i += nt) v[i] = cfms<double>(Uc[i - jj], xj, v[i]);
-    if (tid == 0) xc[jj] = mk<T>((T)xj.x, (T)xj.y);
-    __syncthreads();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ar += __shfl_xor_sync(0xffffffffu, ar, o);
+    ai += __shfl_xor_sync(0xffffffffu, ai, o);
+  }
+  if (lane == 0) {
+    dst[base + i] = mk<double>(ar, ai);
+    if (MODE == 1) xout[(long long)cols[ci] * ldx + s + i] = mk<T>((T)ar, (T)ai);
   }
 }
 
-static constexpr long long kBandSmemMax = 200LL * 1024;
-
 template <typename T>
-void launch_band_solve(Ctx& ctx, long long N, int kl, int ku, const double2* ab, const int* ipiv, const cplx<T>* b,
-                       cplx<T>* x, long long ld, const int* cols, int ncols, double2* gwork) {
+void launch_band_solve(Ctx& ctx, const BandSolveOps& op, const cplx<T>* b, cplx<T>* x, long long ld, const int* cols,
+                       int ncols, double2* work) {
   if (ncols <= 0) return;
-  const long long bytes = N * (long long)sizeof(double2);
-  // the band factors once (shared through L2) plus each column in and out
-  const double bbytes = (double)N * (2.0 * kl + ku + 1) * sizeof(double2) + (double)ncols * N * 2 * sizeof(cplx<T>);
-  if (bytes <= kBandSmemMax) {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(k_band_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBandSmemMax);
-      attr_set = true;
-    }
-    HZ_LAUNCH(ctx, "band_solve", bbytes, k_band_solve<T>, ncols, 256, (size_t)bytes, N, kl, ku, ab, ipiv, b, x, ld, cols,
-              (double2*)nullptr);
-  } else {
-    if (!gwork) throw std::runtime_error("band_solve: coarsest level too large for shared memory and no workspace");
-    HZ_LAUNCH(ctx, "band_solve", bbytes, k_band_solve<T>, ncols, 256, 0, N, kl, ku, ab, ipiv, b, x, ld, cols, gwork);
+  const long long N = op.N;
+  double2* Y[2] = {work, work + (long long)ncols * N};
+  double2* X64 = work + 2LL * ncols * N;
+  const int nbk = (int)op.blocks.size();
+  const unsigned gy = (unsigned)((ncols + 7) / 8);
+  long long prev_end = 0;
+  for (int I = 0; I < nbk; ++I) {
+    const BandBlock& B = op.blocks[(size_t)I];
+    const int split = (I == 0) ? 0 : (int)(prev_end - B.s);
+    const double bytes = (double)B.W * B.W * sizeof(double2) + 2.0 * ncols * B.W * sizeof(double2);
+    HZ_LAUNCH(ctx, "band_forward", bytes, (k_band_block<T, 0>), dim3((unsigned)B.W, gy), 256, 0, N, B.s, B.W, split,
+              op.T + B.toff, Y[(I + 1) % 2], b, ld, cols, (const double2*)nullptr, Y[I % 2], (cplx<T>*)nullptr,
+              0LL, ncols);
+    prev_end = B.s + B.W;
+  }
+  for (int I = nbk - 1; I >= 0; --I) {
+    const BandBlock& B = op.blocks[(size_t)I];
+    const double bytes = (double)B.nb * B.Wb * sizeof(double2) + ncols * (B.Wb + 2.0 * B.nb) * sizeof(double2);
+    HZ_LAUNCH(ctx, "band_backward", bytes, (k_band_block<T, 1>), dim3((unsigned)B.nb, gy), 256, 0, N, B.s, B.Wb,
+              B.nb, op.G + B.goff, Y[I % 2], (const cplx<T>*)nullptr, 0LL, cols, X64, X64, x, ld, ncols);
   }
 }
 
@@ -548,9 +554,9 @@ template void launch_prolong<double>(Ctx&, const Grid&, const Grid&, const doubl
                                      double2*, long long, const int*, int);
 template void launch_prolong<float>(Ctx&, const Grid&, const Grid&, const float2*, long long, const float2*, float2*,
                                     long long, const int*, int);
-template void launch_band_solve<double>(Ctx&, long long, int, int, const double2*, const int*, const double2*,
-                                        double2*, long long, const int*, int, double2*);
-template void launch_band_solve<float>(Ctx&, long long, int, int, const double2*, const int*, const float2*, float2*,
-                                       long long, const int*, int, double2*);
+template void launch_band_solve<double>(Ctx&, const BandSolveOps&, const double2*, double2*, long long, const int*, int,
+                                        double2*);
+template void launch_band_solve<float>(Ctx&, const BandSolveOps&, const float2*, float2*, long long, const int*, int,
+                                       double2*);
 
 }  // namespace hz

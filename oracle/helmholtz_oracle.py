@@ -27,7 +27,7 @@ algorithms are restated here from the mathematics:
 * damped Jacobi relaxation x <- x + w D^{-1} (b - A x),
 * V/W cycles with a direct solve on the coarsest level,
 * right-preconditioned flexible GMRES(restart) per right-hand-side column,
-  classical Gram-Schmidt with one reorthogonalisation, Givens rotations,
+  classical Gram-Schmidt with DGKS selective reorthogonalisation, Givens rotations,
   relative-residual stopping test ||r_j|| <= tol * ||b_j||.
 
 Parity status: the operator assembly is pinned by the reference's own
@@ -369,10 +369,10 @@ class FGMRESResult:
 
 def fgmres(Hmul, prec, B: np.ndarray, restart: int, tol: float, max_outer: int) -> FGMRESResult:
     """Right-preconditioned flexible GMRES(restart), all columns batched but
-    mathematically independent.  Classical Gram-Schmidt with one
-    reorthogonalisation pass (CGS2); per-column Givens rotations; a column
+    mathematically independent; per-column Givens rotations; a column
     stops when its Arnoldi residual estimate drops to tol*||b_j||; the true
-    residual is recomputed at each restart."""
+    residual is recomputed at each restart.  Gram-Schmidt is classical with
+    the DGKS criterion: a second pass where ||w'||^2 < ||w||^2 / 2."""
     B = np.asarray(B, dtype=np.complex128)
     n, R = B.shape
     X = np.zeros_like(B)
@@ -405,11 +405,18 @@ def fgmres(Hmul, prec, B: np.ndarray, restart: int, tol: float, max_outer: int) 
                 break
             Z[j][:, lc] = prec(V[j][:, lc])
             w = Hmul(Z[j][:, lc])
-            h = np.zeros((j + 1, lc.size), dtype=np.complex128)
-            for _ in range(2):
-                hh = np.einsum("knc,nc->kc", V[: j + 1][:, :, lc].conj(), w)
-                w = w - np.einsum("knc,kc->nc", V[: j + 1][:, :, lc], hh)
-                h += hh
+            # classical Gram-Schmidt; a second pass only for the columns whose
+            # squared norm dropped below half (DGKS test)
+            Vl = V[: j + 1][:, :, lc]
+            before = np.sum(np.abs(w) ** 2, axis=0)
+            h = np.einsum("knc,nc->kc", Vl.conj(), w)
+            w = w - np.einsum("knc,kc->nc", Vl, h)
+            after = np.sum(np.abs(w) ** 2, axis=0)
+            redo = after < 0.5 * before
+            if redo.any():
+                h2 = np.einsum("knc,nc->kc", Vl[:, :, redo].conj(), w[:, redo])
+                w[:, redo] = w[:, redo] - np.einsum("knc,kc->nc", Vl[:, :, redo], h2)
+                h[:, redo] += h2
             hn = np.linalg.norm(w, axis=0)
             V[j + 1][:, lc] = w / np.where(hn > 0, hn, 1.0)
             col = np.zeros((j + 2, lc.size), dtype=np.complex128)

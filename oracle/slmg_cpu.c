@@ -12,8 +12,8 @@
  *   - the Multigrid.jl V/W cycle with damped Jacobi, full-weighting
  *     restriction and linear prolongation given as CSR matrices, and a
  *     direct (banded LU, partial pivoting) coarsest solve,
- *   - FGMRES(restart) per column with classical Gram-Schmidt and one
- *     reorthogonalisation, Givens rotations, relative-residual test,
+ *   - FGMRES(restart) per column with classical Gram-Schmidt and the DGKS
+ *     second pass (where ||w'||^2 < ||w||^2/2), Givens rotations, relative-residual test,
  *     the same algorithm as oracle/helmholtz_oracle.py:fgmres
  *     (src/ShiftedLaplacianMultigridSolver.jl:89 calls it as solveGMRES_MG).
  * The hierarchy (A_l, P_l, R_l) is assembled by the Python oracle.
@@ -325,6 +325,8 @@ int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const 
         const int q = lq[a];
         cplx* wv = Wk + (int64_t)a * n;
         for (int i = 0; i <= j; ++i) hv[q * (m + 1) + i] = 0;
+        double before = col_norm(wv, n);
+        before *= before;
         for (int pass = 0; pass < 2; ++pass) {
           cplx hh[64];
           for (int i = 0; i <= j; ++i) {
@@ -345,6 +347,10 @@ int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const 
             wv[p] = s;
           }
           for (int i = 0; i <= j; ++i) hv[q * (m + 1) + i] += hh[i];
+          if (pass == 0) {
+            double after = col_norm(wv, n);
+            if (!(after * after < 0.5 * before)) break; /* DGKS: second pass not needed */
+          }
         }
         double hnrm = col_norm(wv, n);
         cplx* vn = V + ((int64_t)(j + 1) * nc + q) * n;
