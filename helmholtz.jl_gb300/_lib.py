@@ -32,6 +32,7 @@ HZ_COARSE_GALERKIN = 0
 HZ_COARSE_REDISCRETIZE = 1
 HZ_OP_H = 0
 HZ_OP_SH = 1
+HZ_NOALLOC_MAX_COLS = 4096
 
 
 class hz_problem(C.Structure):
@@ -99,6 +100,7 @@ SIGNATURES = {
     "hz_solve": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.POINTER(hz_stats)]),
     "hz_column_stats": (C.c_int, [_vp, _dp, C.POINTER(C.c_int32), C.c_int32]),
     "hz_apply": (C.c_int, [_vp, C.c_int32, C.c_int32, _vp, _vp, C.c_int64, C.c_int32, C.c_int32]),
+    "hz_apply_noalloc": (C.c_int, [_vp, C.c_int32, C.c_int32, _vp, _vp, C.c_int64, C.c_int32]),
     "hz_clear": (C.c_int, [_vp]),
     "hz_copy": (C.c_int, [_vp, C.POINTER(_vp)]),
     "hz_stream": (_vp, [_vp]),

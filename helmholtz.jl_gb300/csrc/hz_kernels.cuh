@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/helmgpu.h"
 #include "hz_common.cuh"
 #include "hz_host.h"
 
@@ -87,6 +88,14 @@ struct BandSolveOps {
 template <typename T>
 void launch_band_solve(Ctx& ctx, const BandSolveOps& op, const cplx<T>* b, cplx<T>* x, long long ld, const int* cols,
                        int ncols, double2* work);
+
+// Allocation-free Y = A X on device memory for hz_apply_noalloc: the column
+// list lives in a static device array of kNoAllocMaxCols entries shared by all
+// calls on a device.  Returns 0, -1 (bad size) or -2 (CUDA error) with *err set.
+static constexpr int kNoAllocMaxCols = HZ_NOALLOC_MAX_COLS;
+static constexpr int kNoAllocMaxDevices = 64;
+int launch_fine_apply_noalloc(cudaStream_t stream, int dev, const FineOp& op, const double2* diag, const double2* x,
+                              double2* y, long long ld, int nrhs, std::string* err);
 
 // ---- setup kernels ---------------------------------------------------------
 void launch_probe_init(Ctx& ctx, const Grid& gc, int dim, double2* out, long long ld);

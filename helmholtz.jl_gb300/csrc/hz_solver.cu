@@ -932,6 +932,29 @@ int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, doubl
   });
 }
 
+int hz_apply_noalloc(hz_handle* h, int32_t op, int32_t transpose, const double* X, double* Y, int64_t n,
+                     int32_t nrhs) {
+  if (!h) return HZ_ERR_ARG;
+  return guarded(h, [&] {
+    if (!X || !Y) fail(HZ_ERR_ARG, "null X or Y");
+    if (n != h->g0.N) fail(HZ_ERR_ARG, "X has %lld rows, the grid has %lld nodes", (long long)n, h->g0.N);
+    if (nrhs < 1 || nrhs > HZ_NOALLOC_MAX_COLS)
+      fail(HZ_ERR_ARG, "hz_apply_noalloc takes 1 to %d columns (got %d)", HZ_NOALLOC_MAX_COLS, (int)nrhs);
+    if (op != HZ_OP_H && op != HZ_OP_SH) fail(HZ_ERR_ARG, "op must be HZ_OP_H or HZ_OP_SH");
+    if (transpose != 0 && transpose != 1) fail(HZ_ERR_ARG, "transpose must be 0 or 1");
+    set_device(h);
+    FineOp fop = h->fop;
+    fop.adj = transpose;
+    const double2* diag = (op == HZ_OP_H) ? h->diagH.as<double2>() : h->diagSH.as<double2>();
+    std::string err;
+    const int rc = launch_fine_apply_noalloc(h->ctx.stream, h->dev, fop, diag, reinterpret_cast<const double2*>(X),
+                                             reinterpret_cast<double2*>(Y), n, nrhs, &err);
+    if (rc == -1) fail(HZ_ERR_ARG, "%s", err.c_str());
+    if (rc != 0) fail(HZ_ERR_CUDA, "%s", err.c_str());
+    ck(cudaStreamSynchronize(h->ctx.stream), "stream sync");
+  });
+}
+
 int hz_clear(hz_handle* h) {
   if (!h) return HZ_ERR_ARG;
   return guarded(h, [&] {

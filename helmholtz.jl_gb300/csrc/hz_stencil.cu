@@ -8,7 +8,9 @@
 // src/ShiftedLaplacianMultigridSolver.jl:89.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <stdexcept>
+#include <string>
 
 #include "hz_launch.cuh"
 
@@ -529,6 +531,80 @@ void launch_band_solve(Ctx& ctx, const BandSolveOps& op, const cplx<T>* b, cplx<
     HZ_LAUNCH(ctx, "band_backward", bytes, (k_band_block<T, 1>), dim3((unsigned)B.nb, gy), 256, 0, N, B.s, B.Wb,
               B.nb, op.G + B.goff, Y[I % 2], (const cplx<T>*)nullptr, 0LL, cols, X64, X64, x, ld, ncols);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free operator apply (hz_apply_noalloc).  The column-index list
+// the stencil kernel reads is kept in a file-scope device array instead of a
+// per-call allocation.  Host code must not pass the symbol itself to a kernel
+// (in host code it is only a host-side stand-in); its device address is looked
+// up with cudaGetSymbolAddress once per device, with that device current.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) int g_noalloc_cols[kNoAllocMaxCols];
+
+__global__ void k_iota(int* __restrict__ out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i;
+}
+
+static int* noalloc_cols_address(int dev, std::string* err) {
+  static std::mutex mu;
+  static int* addr[kNoAllocMaxDevices] = {};
+  if (dev < 0 || dev >= kNoAllocMaxDevices) {
+    *err = "device ordinal out of range for the allocation-free entry point";
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    int* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_cols);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      *err = std::string("cudaGetSymbolAddress of the column-list scratch failed: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    addr[dev] = p;
+  }
+  return addr[dev];
+}
+
+int launch_fine_apply_noalloc(cudaStream_t stream, int dev, const FineOp& op, const double2* diag, const double2* x,
+                              double2* y, long long ld, int nrhs, std::string* err) {
+  if (nrhs < 1 || nrhs > kNoAllocMaxCols) {
+    *err = "nrhs must be in [1, " + std::to_string(kNoAllocMaxCols) + "] for the allocation-free apply";
+    return -1;
+  }
+  int* cols = noalloc_cols_address(dev, err);
+  if (!cols) return -2;
+  // every call rewrites the entries it reads: the array keeps the previous call's contents
+  k_iota<<<(nrhs + 255) / 256, 256, 0, stream>>>(cols, nrhs);
+  FineOpT<double> o;
+  o.nx = op.g.nx;
+  o.ny = op.g.ny;
+  o.nz = op.g.nz;
+  o.N = op.g.N;
+  for (int d = 0; d < 3; ++d) {
+    o.o[d] = op.o[d];
+    o.b[d] = op.b[d];
+  }
+  o.adj = op.adj;
+  const int TPB = 256;
+  const long long nbx = (op.g.N + TPB - 1) / TPB;
+  const int ch = chunks_for(nbx, nrhs);
+  const int cpb = (nrhs + ch - 1) / ch;
+  const dim3 grid((unsigned)nbx, (unsigned)ch);
+  if (op.g.nz > 1)
+    k_fine<double, double, double, MODE_APPLY, true><<<grid, TPB, 0, stream>>>(
+        o, diag, nullptr, x, (const double2*)nullptr, y, ld, cols, nrhs, cpb, 0.0);
+  else
+    k_fine<double, double, double, MODE_APPLY, false><<<grid, TPB, 0, stream>>>(
+        o, diag, nullptr, x, (const double2*)nullptr, y, ld, cols, nrhs, cpb, 0.0);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    *err = std::string("allocation-free apply launch failed: ") + cudaGetErrorString(e);
+    return -2;
+  }
+  return 0;
 }
 
 // explicit instantiations

@@ -145,6 +145,24 @@ int hz_column_stats(const hz_handle* h, double* relres, int32_t* iters, int32_t 
 int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, double* Y, int64_t n, int32_t nrhs,
              int32_t mem);
 
+/* Allocation-free variant of hz_apply, for callers that cannot allocate GPU
+ * memory at the time they apply the operator: an application whose own pool
+ * already holds the whole device, a solver loop whose memory footprint must
+ * stay fixed, or code that must avoid cudaMalloc's implicit device-wide
+ * synchronisation.  This entry point has no counterpart in the reference.
+ * X and Y are device pointers (n x nrhs column-major complex); the call
+ * allocates nothing: the column list the kernel needs lives in a static
+ * device array of HZ_NOALLOC_MAX_COLS entries (16 KiB, held by every GPU that
+ * loads the library until the process exits), so nrhs above that maximum is
+ * rejected with HZ_ERR_ARG.  The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress) with the device current; make that
+ * first call before any stream capture.  All calls on a device share the
+ * array: calls that overlap on the GPU (different handles or streams) race.
+ * Returns after the result is complete, like hz_apply. */
+#define HZ_NOALLOC_MAX_COLS 4096
+int hz_apply_noalloc(hz_handle* h, int32_t op, int32_t transpose, const double* X, double* Y, int64_t n,
+                     int32_t nrhs);
+
 /* Drop the multigrid hierarchy (clear!, src/ShiftedLaplacianMultigridSolver.jl:105-109). */
 int hz_clear(hz_handle* h);
 
