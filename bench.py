@@ -201,15 +201,18 @@ def kernel_table(lib, h):
     return rows
 
 
-def traffic_from_profiles(kernel: str, workload: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def traffic_ratio_from_profiles(kernel: str, workload: str):
+    """DRAM bytes / algorithmic bytes of `kernel` from the committed ncu
+    summary (a small case of the same workload; traffic scales with the
+    columns processed), or None."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     try:
         d = json.loads(p.read_text())
-        return d.get(workload, {}).get(kernel)
-    except (ValueError, OSError):
+        e = d.get(workload, {}).get(kernel)
+        return float(e["dram_over_algorithmic"]) if e else None
+    except (ValueError, OSError, KeyError, TypeError):
         return None
 
 
@@ -220,7 +223,9 @@ def run_ours(args, rank, ws, dist):
     hz = ge.load_package()
     L = hz._lib
     lib = L.load()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.nrhs > 0:
+        wl["nrhs"] = args.nrhs
     P = make_problem(wl, seed=1234)
     gam = gamma_of(P, wl["pad"], lib, hz)
     nrhs = wl["nrhs"]
@@ -363,6 +368,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nrhs", type=int, default=0, help="override the workload's RHS count (small profiling cases)")
     args = ap.parse_args()
     peak, peak_kind = load_peaks()
 
@@ -402,7 +408,8 @@ def main():
     roofline = None
     if dom:
         achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
-        tr = traffic_from_profiles(dom["name"], args.workload)
+        ratio = traffic_ratio_from_profiles(dom["name"], args.workload) if args.nrhs == 0 else None
+        tr = None if ratio is None else ratio * dom["bytes"] / dom["launches"]
         roofline = dict(bound="hbm", kernel=dom["name"], achieved=achieved, peak=peak, unit="GB/s",
                         frac=achieved / peak, peak_source=f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                         traffic=tr, avg_launch_ms=dom["ms"] / dom["timed"],
