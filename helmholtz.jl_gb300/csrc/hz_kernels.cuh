@@ -33,6 +33,7 @@ struct Ctx {
   void before(int id, cudaEvent_t* a);
   void after(int id, cudaEvent_t a, double bytes);
   void resolve();  // after a stream sync: fold pending event pairs into the table
+  void add_bytes(const char* name, double bytes) { alg_bytes[name_id(name)] += bytes; }
   void release();
 };
 
@@ -120,7 +121,8 @@ void launch_zero_cols(Ctx& ctx, long long N, cplx<T>* x, long long ld, const int
 // and are folded in a fixed order by launch_reduce (deterministic results).
 int krylov_nblk(long long N, int ncols);
 // slots i < K: conj(V_{i0+i}) . w ; slot K (want_norm): ||w||^2.  Columns with
-// mask[c] == 0 (mask may be null) yield zeros.
+// mask[c] == 0 (mask may be null) yield zeros; a masked launch adds no
+// algorithmic bytes (the caller adds those of the columns that took it).
 void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, long long ld, int i0, int K,
                  const double2* w, long long wld, const int* cols, int ncols, int nblk, int want_norm, double2* part,
                  const int* mask = nullptr);

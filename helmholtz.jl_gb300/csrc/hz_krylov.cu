@@ -142,7 +142,8 @@ void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, lon
                  const int* mask) {
   if (ncols <= 0) return;
   dim3 grid(nblk, ncols);
-  const double bytes = (double)N * ncols * (K + 1) * sizeof(double2);
+  // a masked pass is charged by the host once it knows which columns took it
+  const double bytes = mask ? 0.0 : (double)N * ncols * (K + 1) * sizeof(double2);
   switch (K) {
 #define HZ_DOTS_CASE(k)                                                                                     \
   case k:                                                                                                   \
@@ -162,7 +163,7 @@ void launch_update(Ctx& ctx, long long N, const double2* V, long long vstride, l
                    int want_norm, double2* part, const int* mask) {
   if (ncols <= 0) return;
   dim3 grid(nblk, ncols);
-  const double bytes = (double)N * ncols * (K + 2) * sizeof(double2);
+  const double bytes = mask ? 0.0 : (double)N * ncols * (K + 2) * sizeof(double2);
   switch (K) {
 #define HZ_UPD_CASE(k)                                                                                           \
   case k:                                                                                                        \

@@ -122,6 +122,8 @@ struct hz_handle {
   DBuf tmpA, tmpB;  // hz_apply staging
   double* h_est = nullptr;  // pinned
   double* h_nrm = nullptr;  // pinned
+  int* h_flag = nullptr;    // pinned copy of the second-pass flags
+  long long reorth = 0;     // second Gram-Schmidt passes taken (columns x steps)
   std::string err;
   double setup_time = 0, solve_time = 0;
   long long nprec = 0;
@@ -344,10 +346,13 @@ void ensure_workspace(hz_handle* h, int nrhs) {
   h->kcol.alloc((size_t)R * sizeof(int));
   if (h->h_est) cudaFreeHost(h->h_est);
   if (h->h_nrm) cudaFreeHost(h->h_nrm);
+  if (h->h_flag) cudaFreeHost(h->h_flag);
   h->h_est = nullptr;
   h->h_nrm = nullptr;
+  h->h_flag = nullptr;
   ck(cudaMallocHost(&h->h_est, (size_t)R * 8), "pinned est");
   ck(cudaMallocHost(&h->h_nrm, (size_t)R * 8), "pinned nrm");
+  ck(cudaMallocHost(&h->h_flag, (size_t)R * sizeof(int)), "pinned flags");
   // multigrid work buffers per level and orientation (allocated on demand in the cycle)
   h->rcap = R;
   h->mcap = m;
@@ -600,7 +605,16 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
                           h->est.as<double>(), h->invhn.as<double>());
       launch_scale_cols(h->ctx, N, w, N, w, N, h->invhn.as<double>(), dc, nl);
       ck(cudaMemcpyAsync(h->h_est, h->est.p, (size_t)h->rcap * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "est");
+      ck(cudaMemcpyAsync(h->h_flag, h->flag.p, (size_t)h->rcap * sizeof(int), cudaMemcpyDeviceToHost, h->ctx.stream),
+         "flags");
       sync(h);
+      {
+        int n2 = 0;  // columns that took the second Gram-Schmidt pass
+        for (int c : live) n2 += h->h_flag[c] ? 1 : 0;
+        h->ctx.add_bytes("krylov_dots", (double)N * n2 * (K + 1) * 16.0);
+        h->ctx.add_bytes("krylov_update", (double)N * n2 * (K + 2) * 16.0);
+        h->reorth += n2;
+      }
       std::vector<int> still;
       for (int c : live) {
         kcol[c] = j + 1;
@@ -821,6 +835,7 @@ int hz_destroy(hz_handle* h) {
   h->ctx.release();
   if (h->h_est) cudaFreeHost(h->h_est);
   if (h->h_nrm) cudaFreeHost(h->h_nrm);
+  if (h->h_flag) cudaFreeHost(h->h_flag);
   if (h->ctx.stream) cudaStreamDestroy(h->ctx.stream);
   delete h;
   return HZ_OK;

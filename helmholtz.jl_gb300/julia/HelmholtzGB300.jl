@@ -1,0 +1,267 @@
+# HelmholtzGB300: Julia binding of the helmgpu C ABI (include/helmgpu.h).
+#
+# Drop-in for the shifted-Laplacian multigrid path of Helmholtz.jl: the same
+# names and argument orders as src/ShiftedLaplacianMultigridSolver.jl and
+# src/GetHelmholtz.jl, with the solve running on one GB300 through ccall.
+# Matrices handed in by callers (ShiftedHT) are not read; the library
+# rebuilds the operator matrix-free from HelmholtzParam.
+#
+# Load with
+#     ENV["HELMGPU_LIB"] = "/path/to/libhelmgpu.so"   # optional
+#     include("HelmholtzGB300.jl"); using .HelmholtzGB300
+# Requires jInv (RegularMesh) and Multigrid (MGparam) as Helmholtz.jl does.
+module HelmholtzGB300
+
+using LinearAlgebra
+using SparseArrays
+using jInv.Mesh
+import jInv.LinearSolvers: AbstractSolver, solveLinearSystem, solveLinearSystem!
+import jInv.Utils.clear!
+using Multigrid: MGparam
+
+export HelmholtzParam, ShiftedLaplacianMultigridSolver, getShiftedLaplacianMultigridSolver, solveLinearSystem,
+       solveLinearSystem!, copySolver, clear!, getMaximalFrequency, getABL, getSommerfeldBC,
+       getAcousticPointSource, getHelmholtzFun, HzApply
+
+const libhelmgpu = get(ENV, "HELMGPU_LIB", joinpath(@__DIR__, "..", "libhelmgpu.so"))
+
+# ---- C structs (field order and types of include/helmgpu.h) -----------------
+struct HzProblem
+    dim::Int32
+    n::NTuple{3,Int64}
+    h::NTuple{3,Float64}
+    omega_re::Float64
+    omega_im::Float64
+    m::Ptr{Float64}
+    gamma::Ptr{Float64}
+    neumann_on_top::Int32
+    sommerfeld::Int32
+    order_neumann_bc::Int32
+end
+
+mutable struct HzOptions
+    levels::Int32
+    max_outer::Int32
+    rel_tol::Float64
+    relax_pre::Int32
+    relax_post::Int32
+    relax_param::Float64
+    cycle::Int32
+    krylov::Int32
+    inner::Int32
+    shift::Float64
+    precision::Int32
+    coarse_op::Int32
+    verbose::Int32
+    profile::Int32
+    device::Int32
+    reserved::NTuple{7,Int32}
+end
+HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 7))
+
+mutable struct HzStats
+    outer::Int32
+    n_prec::Int32
+    max_col_iters::Int32
+    converged_cols::Int32
+    max_relres::Float64
+    setup_time::Float64
+    solve_time::Float64
+    kernel_launches::Int64
+    h2d_bytes::Int64
+    d2h_bytes::Int64
+end
+HzStats() = HzStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0)
+
+const HZ_MEM_HOST = Int32(0)
+const HZ_PREC_FP64 = Int32(0)
+const HZ_PREC_MIXED = Int32(1)
+const HZ_OP_H = Int32(0)
+
+lasterror(h::Ptr{Cvoid}) = unsafe_string(ccall((:hz_last_error, libhelmgpu), Cstring, (Ptr{Cvoid},), h))
+function check(st::Integer, h::Ptr{Cvoid} = C_NULL)
+    st < 0 && throw(ErrorException("helmgpu error $st: " * lasterror(h)))
+    return st
+end
+
+# ---- Helmholtz problem ---------------------------------------------------------
+mutable struct HelmholtzParam      # src/Helmholtz.jl:13-20
+    Mesh::RegularMesh
+    gamma::Array{Float64}
+    m::Array{Float64}
+    omega::Union{Float64,ComplexF64}
+    NeumannOnTop::Bool
+    Sommerfeld::Bool
+end
+
+function hzproblem(p::HelmholtzParam, order::Int = 2)
+    M = p.Mesh
+    n = ntuple(i -> i <= M.dim ? Int64(M.n[i]) : Int64(0), 3)
+    h = ntuple(i -> i <= M.dim ? Float64(M.h[i]) : 0.0, 3)
+    w = ComplexF64(p.omega)
+    return HzProblem(Int32(M.dim), n, h, real(w), imag(w), pointer(p.m), pointer(p.gamma),
+                     Int32(p.NeumannOnTop), Int32(p.Sommerfeld), Int32(order))
+end
+
+getMaximalFrequency(m::Array{Float64}, M::RegularMesh) =
+    ccall((:hz_max_frequency, libhelmgpu), Float64, (Ptr{Float64}, Int64, Ptr{Float64}, Int32),
+          m, length(m), collect(Float64, M.h), Int32(M.dim))
+
+function getABL(n::Array{Int64}, NeumannAtFirstDim::Bool, ABLpad::Array{Int64}, ABLamp::Float64)
+    g = zeros(Float64, tuple(n...))
+    check(ccall((:hz_abl, libhelmgpu), Cint, (Int32, Ptr{Int64}, Int32, Ptr{Int64}, Float64, Ptr{Float64}),
+                Int32(length(n)), n, Int32(NeumannAtFirstDim), ABLpad, ABLamp, g))
+    return g
+end
+
+function getSommerfeldBC(Msh::RegularMesh, mNodal::Array{Float64}, omega::Float64, NeumannOnTop::Bool,
+                         orderNeumannBC = 2)
+    S = zeros(ComplexF64, tuple((Msh.n .+ 1)...))
+    check(ccall((:hz_sommerfeld, libhelmgpu), Cint,
+                (Int32, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Float64, Int32, Int32, Ptr{ComplexF64}),
+                Int32(Msh.dim), collect(Int64, Msh.n), collect(Float64, Msh.h), mNodal, omega,
+                Int32(NeumannOnTop), Int32(orderNeumannBC), S))
+    return S
+end
+
+function getAcousticPointSource(Minv::RegularMesh, TYPE, src = nothing)
+    if src === nothing
+        src = Minv.dim == 3 ? [div(Minv.n[1] + 1, 2); div(Minv.n[2] + 1, 2); 1] : [div(Minv.n[1] + 1, 2); 1]
+    end
+    q = zeros(ComplexF64, tuple((Minv.n .+ 1)...))
+    check(ccall((:hz_point_source, libhelmgpu), Cint, (Int32, Ptr{Int64}, Ptr{Float64}, Ptr{Int64}, Ptr{ComplexF64}),
+                Int32(Minv.dim), collect(Int64, Minv.n), collect(Float64, Minv.h), collect(Int64, src), q))
+    return convert(Array{TYPE}, q), src
+end
+
+# ---- solver ----------------------------------------------------------------------
+mutable struct ShiftedLaplacianMultigridSolver <: AbstractSolver   # src/ShiftedLaplacianMultigridSolver.jl:4-15
+    helmParam::HelmholtzParam
+    MG::MGparam
+    shift::Array{Float64}
+    Krylov::String
+    inner::Int64
+    doClear::Int64
+    verbose::Bool
+    setupTime::Real
+    nPrec::Int
+    solveTime::Real
+    precision::Int32            # HZ_PREC_FP64 (plain) or HZ_PREC_MIXED
+    handle::Ptr{Cvoid}
+end
+
+function getShiftedLaplacianMultigridSolver(helmParam::HelmholtzParam, MG::MGparam, shift::Array{Float64},
+                                            Krylov::String = "BiCGSTAB", inner::Int64 = 5, verbose::Bool = false;
+                                            precision::Int32 = HZ_PREC_FP64)
+    s = ShiftedLaplacianMultigridSolver(helmParam, MG, shift, Krylov, inner, 0, verbose, 0.0, 0, 0.0, precision,
+                                        C_NULL)
+    finalizer(release!, s)
+    return s
+end
+getShiftedLaplacianMultigridSolver(helmParam::HelmholtzParam, MG::MGparam, shift::Float64, Krylov::String = "BiCGSTAB",
+                                   inner::Int64 = 5, verbose::Bool = false; kw...) =
+    getShiftedLaplacianMultigridSolver(helmParam, MG, ones(MG.levels) * shift, Krylov, inner, verbose; kw...)
+
+function release!(s::ShiftedLaplacianMultigridSolver)
+    s.handle != C_NULL && ccall((:hz_destroy, libhelmgpu), Cint, (Ptr{Cvoid},), s.handle)
+    s.handle = C_NULL
+    return nothing
+end
+
+function options(s::ShiftedLaplacianMultigridSolver)
+    MG = s.MG
+    MG.relaxType == "Jac" || throw(ArgumentError("relaxType $(MG.relaxType): only \"Jac\" is built"))
+    MG.cycleType in ('V', 'W') || throw(ArgumentError("cycleType $(MG.cycleType): only 'V' and 'W' are built"))
+    s.Krylov == "GMRES" || throw(ArgumentError("Krylov $(s.Krylov): only \"GMRES\" (FGMRES) is built"))
+    o = HzOptions()
+    ccall((:hz_default_options, libhelmgpu), Cvoid, (Ref{HzOptions},), o)
+    o.levels = MG.levels
+    o.max_outer = MG.maxOuterIter
+    o.rel_tol = MG.relativeTol
+    o.relax_pre = MG.relaxPre
+    o.relax_post = MG.relaxPost
+    o.relax_param = MG.relaxParam
+    o.cycle = Int32(MG.cycleType)
+    o.inner = s.inner
+    o.shift = s.shift[1]
+    o.precision = s.precision
+    o.verbose = Int32(s.verbose)
+    return o
+end
+
+function ensure_handle!(s::ShiftedLaplacianMultigridSolver)
+    s.handle != C_NULL && return s.handle
+    prob = hzproblem(s.helmParam)
+    o = options(s)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve s begin
+        check(ccall((:hz_create, libhelmgpu), Cint, (Ref{HzProblem}, Ref{HzOptions}, Ref{Ptr{Cvoid}}), prob, o, h))
+    end
+    s.handle = h[]
+    return s.handle
+end
+
+# src/ShiftedLaplacianMultigridSolver.jl:33-102
+function solveLinearSystem(ShiftedHT, B, param::ShiftedLaplacianMultigridSolver, doTranspose::Int64 = 0)
+    if size(B, 2) == 1
+        B = vec(B)
+    end
+    if param.doClear == 1
+        clear!(param)
+    end
+    if norm(B) == 0.0
+        return zeros(eltype(B), size(B)), param
+    end
+    h = ensure_handle!(param)
+    Bc = convert(Array{ComplexF64}, B)
+    X = similar(Bc)
+    st = HzStats()
+    code = ccall((:hz_solve, libhelmgpu), Cint,
+                 (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Int64, Int32, Int32, Int32, Ref{HzStats}),
+                 h, Bc, X, size(Bc, 1), Int32(size(Bc, 2)), Int32(doTranspose), HZ_MEM_HOST, st)
+    check(code, h)
+    param.setupTime = st.setup_time
+    param.solveTime = st.solve_time
+    param.nPrec += st.outer
+    if code > 0
+        println("WARNING: MG solver reached maximum iterations without convergence")
+    end
+    return X, param
+end
+
+function solveLinearSystem!(A, B, X, param::ShiftedLaplacianMultigridSolver, doTranspose::Int64 = 0)
+    Y, param = solveLinearSystem(A, B, param, doTranspose)
+    X .= reshape(Y, size(X))
+    return X, param
+end
+
+function copySolver(s::ShiftedLaplacianMultigridSolver)   # src/ShiftedLaplacianMultigridSolver.jl:18-22
+    return getShiftedLaplacianMultigridSolver(s.helmParam, s.MG, s.shift, s.Krylov, s.inner, s.verbose;
+                                              precision = s.precision)
+end
+
+function clear!(s::ShiftedLaplacianMultigridSolver)        # src/ShiftedLaplacianMultigridSolver.jl:105-109
+    s.handle != C_NULL && check(ccall((:hz_clear, libhelmgpu), Cint, (Ptr{Cvoid},), s.handle), s.handle)
+    s.doClear = 0
+    return nothing
+end
+
+# getHelmholtzFun (src/GetHelmholtz.jl:85-95): y = H x on the GPU.  The sparse
+# ShiftedHT / ShiftMat arguments of the reference are replaced by the solver
+# that owns the problem; transpose = 1 gives H^H x (the doTranspose pair).
+struct HzApply
+    s::ShiftedLaplacianMultigridSolver
+    transpose::Int32
+end
+function (f::HzApply)(x::AbstractVecOrMat)
+    h = ensure_handle!(f.s)
+    xc = convert(Array{ComplexF64}, x)
+    y = similar(xc)
+    check(ccall((:hz_apply, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Int32, Int32, Ptr{ComplexF64}, Ptr{ComplexF64}, Int64, Int32, Int32),
+                h, HZ_OP_H, f.transpose, xc, y, size(xc, 1), Int32(size(xc, 2)), HZ_MEM_HOST), h)
+    return y
+end
+getHelmholtzFun(s::ShiftedLaplacianMultigridSolver, transpose::Integer = 0) = HzApply(s, Int32(transpose))
+
+end # module
