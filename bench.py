@@ -246,6 +246,8 @@ def run_ours(args, rank, ws, dist):
         o = L.hz_options()
         lib.hz_default_options(C.byref(o))
         o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, 200
+        if args.krylov == "bicgstab":
+            o.krylov, o.max_outer = L.HZ_KRYLOV_BICGSTAB, 2000
         o.precision = precision
         o.device = torch.cuda.current_device()
         hh = C.c_void_p()
@@ -369,6 +371,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nrhs", type=int, default=0, help="override the workload's RHS count (small profiling cases)")
+    ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
     args = ap.parse_args()
     peak, peak_kind = load_peaks()
 
@@ -425,6 +428,7 @@ def main():
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
                 vs_baseline=None, dtype="c64 V-cycle / c128 FGMRES", data="synthetic (seeded layered model)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
+                            krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB",
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
                             l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9)),
                 e2e=head.get("e2e"), gpu_launches=head["launches_per_step"] * args.steps,

@@ -466,7 +466,7 @@ def _options(s: ShiftedLaplacianMultigridSolver) -> L.hz_options:
     o.relax_post = int(MG.relaxPost)
     o.relax_param = MG.relaxParam
     o.cycle = ord(MG.cycleType)
-    o.krylov = L.HZ_KRYLOV_FGMRES
+    o.krylov = L.HZ_KRYLOV_BICGSTAB if s.Krylov == "BiCGSTAB" else L.HZ_KRYLOV_FGMRES
     o.inner = s.inner
     o.shift = float(s.shift[0])
     o.precision = L.HZ_PREC_MIXED if MG.precision == "mixed" else L.HZ_PREC_FP64
@@ -476,13 +476,13 @@ def _options(s: ShiftedLaplacianMultigridSolver) -> L.hz_options:
 
 def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
     _validate_mg(s.MG)
-    if s.Krylov != "GMRES":
-        raise NotImplementedError(f"Krylov {s.Krylov!r}: only FGMRES ('GMRES') is built")
+    if s.Krylov not in ("GMRES", "BiCGSTAB"):
+        raise NotImplementedError(f"Krylov {s.Krylov!r}: FGMRES ('GMRES') and 'BiCGSTAB' are built")
     if not np.all(s.shift == s.shift[0]):
         raise NotImplementedError("level-dependent shifts are not built")
     key = (id(s.helmParam), id(s.helmParam.m), id(s.helmParam.gamma), s.MG.levels, s.MG.maxOuterIter,
            s.MG.relativeTol, s.MG.relaxParam, int(s.MG.relaxPre), int(s.MG.relaxPost), s.MG.cycleType,
-           s.MG.precision, s.inner, float(s.shift[0]))
+           s.MG.precision, s.inner, float(s.shift[0]), s.Krylov)
     if s._handle is not None and s._key == key:
         return s._handle
     _release(s)

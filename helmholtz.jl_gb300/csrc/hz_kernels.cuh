@@ -12,6 +12,9 @@
 
 namespace hz {
 
+// Device ordinals the per-device caches of the library cover.
+static constexpr int kMaxDevices = 64;
+
 // Per-handle launch context: stream, launch counter and the optional
 // per-kernel event timer.
 struct Ctx {
@@ -83,6 +86,7 @@ void launch_prolong(Ctx& ctx, const Grid& gf, const Grid& gc, const cplx<T>* ec,
 struct BandSolveOps {
   long long N = 0;
   std::vector<BandBlock> blocks;
+  const BandBlock* dblocks = nullptr;  // device copy of blocks: one cooperative launch per solve
   const double2* T = nullptr;
   const double2* G = nullptr;
 };
@@ -160,6 +164,18 @@ void launch_cycle_init(Ctx& ctx, int m, const int* cols, int ncols, const double
 void launch_arnoldi_step(Ctx& ctx, int j, int m, const int* cols, int ncols, const double2* hA, const double2* hB,
                          const double2* nrm, const double2* nrm2, const int* flag, int hstride, double2* Hh,
                          double2* cs, double2* sn, double2* g, double* est, double* inv_hn);
+// BiCGSTAB per-column scalars sc[c*8 + k] (0 rho, 1 rho_prev, 2 alpha, 3 omega,
+// 4 beta) from reduced dots red[c*rstride + slot]: stage -1 init, 0 beta from
+// <rh,r>, 1 alpha from <rh,v>, 2 omega from (conj<t,s>, ||t||^2).
+void launch_bicg_scalars(Ctx& ctx, int stage, const int* cols, int ncols, const double2* red, int rstride,
+                         double2* sc);
+// mode 0: p = r + beta (p - omega v); mode 1: out = r - alpha v.  Blocks of N per column.
+void launch_bicg_vec(Ctx& ctx, int mode, long long N, const double2* r, double2* p, const double2* v, double2* out,
+                     const double2* sc, const int* cols, int ncols);
+// x += alpha ph + omega sh; r = s - omega t.
+template <typename TZ>
+void launch_bicg_xr(Ctx& ctx, long long N, double2* x, const cplx<TZ>* ph, const cplx<TZ>* sh, const double2* s,
+                    const double2* t, double2* r, const double2* sc, const int* cols, int ncols);
 // Back substitution R y = g for the first kcol[c] entries: y[c*m + i].
 void launch_lsq(Ctx& ctx, int m, const int* cols, int ncols, const int* kcol, const double2* Hh, const double2* g,
                 double2* y);

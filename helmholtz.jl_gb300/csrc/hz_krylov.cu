@@ -404,6 +404,107 @@ void launch_lsq(Ctx& ctx, int m, const int* cols, int ncols, const int* kcol, co
 }
 
 // ---------------------------------------------------------------------------
+// BiCGSTAB (right preconditioned) per-column vector updates and scalars
+// ---------------------------------------------------------------------------
+// Scalars per column c (complex, sc[c*8 + k]): 0 rho, 1 rho_prev, 2 alpha,
+// 3 omega, 4 beta.  red[c*rstride + slot] hold the reduced dot products.
+__global__ void k_bicg_scalars(int stage, const int* __restrict__ cols, int ncols, const double2* __restrict__ red,
+                               int rstride, double2* __restrict__ sc) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  double2* q = sc + (long long)c * 8;
+  const double2* d = red + (long long)c * rstride;
+  auto cdiv = [](double2 a, double2 b) {
+    const double den = b.x * b.x + b.y * b.y;
+    return mk<double>((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+  };
+  if (stage == -1) {  // start: rho_prev = alpha = omega = 1
+    q[1] = mk<double>(1, 0);
+    q[2] = mk<double>(1, 0);
+    q[3] = mk<double>(1, 0);
+  } else if (stage == 0) {  // d[0] = <rh, r>: beta = (rho/rho_prev)(alpha/omega)
+    const double2 rho = d[0];
+    q[4] = cmul<double>(cdiv(rho, q[1]), cdiv(q[2], q[3]));
+    q[0] = rho;
+    q[1] = rho;
+  } else if (stage == 1) {  // d[0] = <rh, v>: alpha = rho / <rh, v>
+    q[2] = cdiv(q[0], d[0]);
+  } else {  // d[0] = sum conj(s) t = conj(<t, s>), d[1] = ||t||^2: omega = <t, s> / ||t||^2
+    q[3] = mk<double>(d[0].x / d[1].x, -d[0].y / d[1].x);
+  }
+}
+
+void launch_bicg_scalars(Ctx& ctx, int stage, const int* cols, int ncols, const double2* red, int rstride,
+                         double2* sc) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "bicg_scalars", 0.0, k_bicg_scalars, (ncols + 127) / 128, 128, 0, stage, cols, ncols, red, rstride,
+            sc);
+}
+
+// mode 0: p = r + beta (p - omega v);  mode 1: s = r - alpha v (into out)
+__global__ void __launch_bounds__(256) k_bicg_vec(int mode, long long N, const double2* __restrict__ r,
+                                                  double2* __restrict__ p, const double2* __restrict__ v,
+                                                  double2* __restrict__ out, const double2* __restrict__ sc,
+                                                  const int* __restrict__ cols) {
+  const int c = cols[blockIdx.y];
+  const double2* q = sc + (long long)c * 8;
+  const long long off = (long long)c * N;
+  const double2 beta = q[4], omega = q[3], alpha = q[2];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const double2 ri = r[off + i], vi = v[off + i];
+    if (mode == 0) {
+      const double2 t = cfms<double>(omega, vi, p[off + i]);  // p - omega v
+      p[off + i] = cfma<double>(beta, t, ri);
+    } else {
+      out[off + i] = cfms<double>(alpha, vi, ri);
+    }
+  }
+}
+
+void launch_bicg_vec(Ctx& ctx, int mode, long long N, const double2* r, double2* p, const double2* v, double2* out,
+                     const double2* sc, const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  const int nb = krylov_nblk(N, ncols);
+  const double bytes = (double)N * ncols * (mode == 0 ? 4 : 3) * sizeof(double2);
+  HZ_LAUNCH(ctx, mode == 0 ? "bicg_p" : "bicg_s", bytes, k_bicg_vec, dim3(nb, ncols), 256, 0, mode, N, r, p, v, out,
+            sc, cols);
+}
+
+// x += alpha ph + omega sh ;  r = s - omega t   (ph, sh in the cycle precision)
+template <typename TZ>
+__global__ void __launch_bounds__(256) k_bicg_xr(long long N, double2* __restrict__ x, const cplx<TZ>* __restrict__ ph,
+                                                 const cplx<TZ>* __restrict__ sh, const double2* __restrict__ s,
+                                                 const double2* __restrict__ t, double2* __restrict__ r,
+                                                 const double2* __restrict__ sc, const int* __restrict__ cols) {
+  const int c = cols[blockIdx.y];
+  const double2* q = sc + (long long)c * 8;
+  const long long off = (long long)c * N;
+  const double2 alpha = q[2], omega = q[3];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const cplx<TZ> a = ph[off + i], b = sh[off + i];
+    double2 xi = x[off + i];
+    xi = cfma<double>(alpha, mk<double>((double)a.x, (double)a.y), xi);
+    xi = cfma<double>(omega, mk<double>((double)b.x, (double)b.y), xi);
+    x[off + i] = xi;
+    r[off + i] = cfms<double>(omega, t[off + i], s[off + i]);
+  }
+}
+
+template <typename TZ>
+void launch_bicg_xr(Ctx& ctx, long long N, double2* x, const cplx<TZ>* ph, const cplx<TZ>* sh, const double2* s,
+                    const double2* t, double2* r, const double2* sc, const int* cols, int ncols) {
+  if (ncols <= 0) return;
+  const int nb = krylov_nblk(N, ncols);
+  const double bytes = (double)N * ncols * (5 * sizeof(double2) + 2 * sizeof(cplx<TZ>));
+  HZ_LAUNCH(ctx, "bicg_xr", bytes, k_bicg_xr<TZ>, dim3(nb, ncols), 256, 0, N, x, ph, sh, s, t, r, sc, cols);
+}
+template void launch_bicg_xr<double>(Ctx&, long long, double2*, const double2*, const double2*, const double2*,
+                                     const double2*, double2*, const double2*, const int*, int);
+template void launch_bicg_xr<float>(Ctx&, long long, double2*, const float2*, const float2*, const double2*,
+                                    const double2*, double2*, const double2*, const int*, int);
+
+// ---------------------------------------------------------------------------
 // Setup kernels
 // ---------------------------------------------------------------------------
 // Galerkin probing: column k of the probe block is the indicator of the

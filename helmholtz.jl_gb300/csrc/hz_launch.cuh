@@ -22,13 +22,14 @@ static inline void check_launch(const char* name) {
 #define HZ_LAUNCH(ctx, name, bytes, kern, grid, block, smem, ...) \
   do {                                                          \
     static thread_local int _id = -1;                           \
+    const char* _nm = (name);                                   \
     if (_id < 0 || (size_t)_id >= (ctx).names.size() ||         \
-        (ctx).names[_id] != name)                               \
-      _id = (ctx).name_id(name);                                \
+        (ctx).names[_id] != _nm)                                \
+      _id = (ctx).name_id(_nm);                                 \
     cudaEvent_t _a = nullptr;                                   \
     (ctx).before(_id, &_a);                                     \
     kern<<<grid, block, smem, (ctx).stream>>>(__VA_ARGS__);     \
-    check_launch(name);                                         \
+    check_launch(_nm);                                          \
     (ctx).after(_id, _a, (double)(bytes));                      \
   } while (0)
 

@@ -97,7 +97,7 @@ struct Hierarchy {
   // coarsest LU (band, FP64) as blocked operators
   long long nc = 0;
   int kl = 0, ku = 0;
-  DBuf bandT, bandG, bandwork;
+  DBuf bandT, bandG, bandB, bandwork;
   BandSolveOps band;
 };
 
@@ -119,6 +119,7 @@ struct hz_handle {
   int mcap = 0;
   DBuf Bd, Xd, V, Z, part, hA, hB, nr, nr2, flag, Hh, cs, sn, gv, yv, est, invhn, bnorm, bnorm_inv, beta, beta_inv,
       cols, kcol;
+  DBuf bsc;         // BiCGSTAB per-column scalars
   DBuf tmpA, tmpB;  // hz_apply staging
   double* h_est = nullptr;  // pinned
   double* h_nrm = nullptr;  // pinned
@@ -251,6 +252,10 @@ void factor_coarsest(hz_handle* h, Hierarchy& H) {
   H.band.N = N;
   H.band.T = H.bandT.as<double2>();
   H.band.G = H.bandG.as<double2>();
+  H.bandB.alloc(H.band.blocks.size() * sizeof(BandBlock));
+  ck(cudaMemcpy(H.bandB.p, H.band.blocks.data(), H.band.blocks.size() * sizeof(BandBlock), cudaMemcpyHostToDevice),
+     "upload band blocks");
+  H.band.dblocks = H.bandB.as<BandBlock>();
 }
 
 void build_hierarchy(hz_handle* h, int adj) {
@@ -321,8 +326,9 @@ void ensure_workspace(hz_handle* h, int nrhs) {
   const size_t zb = mixed ? 8 : 16;
   h->Bd.alloc((size_t)R * N * 16);
   h->Xd.alloc((size_t)R * N * 16);
-  h->V.alloc((size_t)(m + 1) * R * N * 16);
-  h->Z.alloc((size_t)m * R * N * zb);
+  h->V.alloc((size_t)std::max(m + 1, 6) * R * N * 16);  // BiCGSTAB uses 6 FP64 blocks
+  h->Z.alloc((size_t)std::max(m, 2) * R * N * zb);
+  h->bsc.alloc((size_t)R * 8 * 16);
   const int nblk = krylov_nblk(N, 1);
   h->part.alloc((size_t)R * 18 * nblk * 16);
   const int HS = m + 2;
@@ -660,6 +666,120 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
   return std::min(outer, std::max(1, h->opt.max_outer));
 }
 
+// Right-preconditioned BiCGSTAB on H (or H^H), one multigrid cycle per
+// preconditioner application (solveBiCGSTAB_MG, src/ShiftedLaplacianMultigridSolver.jl:91-93).
+// Returns the iterations of the slowest column.
+int bicgstab(hz_handle* h, int adj, int nrhs) {
+  Hierarchy& H = h->hier[adj];
+  const long long N = h->g0.N;
+  const int HS = h->mcap + 2;
+  const bool mixed = h->opt.precision == HZ_PREC_MIXED;
+  const size_t zb = mixed ? 8 : 16;
+  double2* B = h->Bd.as<double2>();
+  double2* X = h->Xd.as<double2>();
+  const long long bs = (long long)h->rcap * N;  // one block of rcap columns
+  double2* V = h->V.as<double2>();
+  double2 *r = V, *rh = V + bs, *p = V + 2 * bs, *v = V + 3 * bs, *sv = V + 4 * bs, *t = V + 5 * bs;
+  char* ph = (char*)h->Z.p;
+  char* sh = (char*)h->Z.p + (size_t)bs * zb;
+  double2* part = h->part.as<double2>();
+  double2* red = h->hA.as<double2>();
+  double2* sc = h->bsc.as<double2>();
+  int* dc = h->cols.as<int>();
+  std::vector<int> all(nrhs);
+  for (int c = 0; c < nrhs; ++c) all[c] = c;
+  upload_cols(h, all);
+  std::vector<double> bn(nrhs, 0.0), rn(nrhs, 0.0);
+  col_norms(h, B, all, h->bnorm.as<double>(), h->bnorm_inv.as<double>(), bn.data());
+  launch_zero_cols<double>(h->ctx, N, X, N, dc, nrhs);
+  h->col_relres.assign(nrhs, 0.0);
+  h->col_iters.assign(nrhs, 0);
+  std::vector<int> act;
+  for (int c = 0; c < nrhs; ++c) {
+    if (!std::isfinite(bn[c])) fail(HZ_ERR_NUMERIC, "right-hand side column %d holds NaN or Inf", c);
+    if (bn[c] > 0) act.push_back(c);
+  }
+  if (act.empty()) return 0;
+  if (mixed)
+    ensure_level_buffers<float>(h, H, h->rcap);
+  else
+    ensure_level_buffers<double>(h, H, h->rcap);
+  const double tol = h->opt.rel_tol;
+  upload_cols(h, act);
+  int na = (int)act.size();
+  launch_cast_cols<double, double>(h->ctx, N, B, N, r, N, dc, na);   // r = b (x0 = 0)
+  launch_cast_cols<double, double>(h->ctx, N, B, N, rh, N, dc, na);  // shadow residual
+  launch_zero_cols<double>(h->ctx, N, p, N, dc, na);
+  launch_zero_cols<double>(h->ctx, N, v, N, dc, na);
+  launch_bicg_scalars(h->ctx, -1, dc, na, red, HS, sc);
+  const int maxit = std::max(1, h->opt.max_outer);
+  int it = 0;
+  for (; it <= maxit; ++it) {
+    na = (int)act.size();
+    int nblk = krylov_nblk(N, na);
+    // <rh, r> and ||r||^2 in one pass
+    launch_dots(h->ctx, N, rh, 0, N, 0, 1, r, N, dc, na, nblk, 1, part);
+    launch_reduce(h->ctx, part, dc, na, 2, nblk, red, HS, 0);
+    launch_norms(h->ctx, red, HS, 1, dc, na, h->beta.as<double>(), nullptr);
+    ck(cudaMemcpyAsync(h->h_nrm, h->beta.p, (size_t)h->rcap * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "norms");
+    sync(h);
+    std::vector<int> still;
+    for (int c : act) {
+      const double e = h->h_nrm[c];
+      if (!std::isfinite(e)) fail(HZ_ERR_NUMERIC, "BiCGSTAB breakdown (NaN/Inf) in column %d", c);
+      if (!(e / bn[c] <= tol)) still.push_back(c);
+    }
+    if (still.size() != act.size()) {
+      act.swap(still);
+      if (act.empty()) break;
+      upload_cols(h, act);
+      na = (int)act.size();
+      nblk = krylov_nblk(N, na);
+    }
+    if (it == maxit) break;
+    launch_bicg_scalars(h->ctx, 0, dc, na, red, HS, sc);
+    launch_bicg_vec(h->ctx, 0, N, r, p, v, nullptr, sc, dc, na);
+    precondition(h, H, p, ph, dc, na);
+    if (mixed)
+      apply_H<float>(h, adj, MODE_APPLY, (const float2*)ph, nullptr, v, dc, na);
+    else
+      apply_H<double>(h, adj, MODE_APPLY, (const double2*)ph, nullptr, v, dc, na);
+    launch_dots(h->ctx, N, rh, 0, N, 0, 1, v, N, dc, na, nblk, 0, part);
+    launch_reduce(h->ctx, part, dc, na, 1, nblk, red, HS, 0);
+    launch_bicg_scalars(h->ctx, 1, dc, na, red, HS, sc);
+    launch_bicg_vec(h->ctx, 1, N, r, nullptr, v, sv, sc, dc, na);
+    precondition(h, H, sv, sh, dc, na);
+    if (mixed)
+      apply_H<float>(h, adj, MODE_APPLY, (const float2*)sh, nullptr, t, dc, na);
+    else
+      apply_H<double>(h, adj, MODE_APPLY, (const double2*)sh, nullptr, t, dc, na);
+    launch_dots(h->ctx, N, sv, 0, N, 0, 1, t, N, dc, na, nblk, 1, part);
+    launch_reduce(h->ctx, part, dc, na, 2, nblk, red, HS, 0);
+    launch_bicg_scalars(h->ctx, 2, dc, na, red, HS, sc);
+    if (mixed)
+      launch_bicg_xr<float>(h->ctx, N, X, (const float2*)ph, (const float2*)sh, sv, t, r, sc, dc, na);
+    else
+      launch_bicg_xr<double>(h->ctx, N, X, (const double2*)ph, (const double2*)sh, sv, t, r, sc, dc, na);
+    for (int c : act) {
+      h->col_iters[c] += 1;
+      h->nprec += 2;
+    }
+  }
+  // true residuals of every nonzero column
+  std::vector<int> nz;
+  for (int c = 0; c < nrhs; ++c)
+    if (bn[c] > 0) nz.push_back(c);
+  upload_cols(h, nz);
+  apply_H<double>(h, adj, MODE_RESID, X, B, r, dc, (int)nz.size());
+  col_norms(h, r, nz, h->beta.as<double>(), nullptr, rn.data());
+  int worst = 0;
+  for (int c : nz) {
+    h->col_relres[c] = rn[c] / bn[c];
+    worst = std::max(worst, h->col_iters[c]);
+  }
+  return worst;
+}
+
 void init_fine(hz_handle* h) {
   const hz_problem& p = h->prob;
   const long long N = num_nodes(p);
@@ -719,8 +839,11 @@ void validate(const hz_problem* p, const hz_options* o) {
   if (!p->m || !p->gamma) fail(HZ_ERR_ARG, "m and gamma must be given");
   if (!(p->omega_re != 0.0)) fail(HZ_ERR_ARG, "omega must have a nonzero real part");
   if (o->levels < 1 || o->levels > 16) fail(HZ_ERR_ARG, "levels must be in [1, 16]");
-  if (o->inner < 1 || o->inner > 64) fail(HZ_ERR_ARG, "inner (restart length) must be in [1, 64]");
-  if (o->krylov != HZ_KRYLOV_FGMRES) fail(HZ_ERR_ARG, "only the FGMRES Krylov method is built");
+  // the restart length only matters for FGMRES (the reference passes 0 with BiCGSTAB)
+  if (o->krylov == HZ_KRYLOV_FGMRES && (o->inner < 1 || o->inner > 64))
+    fail(HZ_ERR_ARG, "inner (restart length) must be in [1, 64]");
+  if (o->inner < 0 || o->inner > 64) fail(HZ_ERR_ARG, "inner must be in [0, 64]");
+  if (o->krylov != HZ_KRYLOV_FGMRES && o->krylov != HZ_KRYLOV_BICGSTAB) fail(HZ_ERR_ARG, "unknown Krylov method");
   if (o->cycle != 'V' && o->cycle != 'W') fail(HZ_ERR_ARG, "cycle must be 'V' or 'W'");
   if (o->coarse_op != HZ_COARSE_GALERKIN) fail(HZ_ERR_ARG, "only Galerkin coarse operators are built");
   if (o->precision != HZ_PREC_FP64 && o->precision != HZ_PREC_MIXED) fail(HZ_ERR_ARG, "unknown precision");
@@ -862,7 +985,7 @@ int hz_solve(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, 
     h->setup_time += secs(t0, t1);
     copy_in(h, B, h->Bd.as<double2>(), n, nrhs, mem);
     const long long np0 = h->nprec;
-    int outer = fgmres(h, transpose, nrhs);
+    int outer = (h->opt.krylov == HZ_KRYLOV_BICGSTAB) ? bicgstab(h, transpose, nrhs) : fgmres(h, transpose, nrhs);
     copy_out(h, h->Xd.as<double2>(), X, n, nrhs, mem);
     sync(h);
     auto t2 = clk::now();
@@ -979,6 +1102,7 @@ int hz_clear(hz_handle* h) {
       H.lv.clear();
       H.bandT.reset();
       H.bandG.reset();
+      H.bandB.reset();
       H.bandwork.reset();
       H.band = BandSolveOps();
       H.built = false;

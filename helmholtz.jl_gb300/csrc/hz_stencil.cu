@@ -12,7 +12,11 @@
 #include <stdexcept>
 #include <string>
 
+#include <cooperative_groups.h>
+
 #include "hz_launch.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace hz {
 
@@ -506,29 +510,148 @@ __global__ void __launch_bounds__(256) k_band_block(long long N, long long s, in
   }
 }
 
+// All block steps of the solve in one cooperative launch: every warp takes
+// (row, column) items of the current window mat-vec, then the grid
+// synchronises before the next block step.  The launch is sized to the
+// co-resident capacity (cudaLaunchCooperativeKernel refuses a larger grid).
+template <typename T>
+__global__ void __launch_bounds__(256) k_band_coop(long long N, int nbk, const BandBlock* __restrict__ blocks,
+                                                   const double2* __restrict__ Tops, const double2* __restrict__ Gops,
+                                                   const cplx<T>* __restrict__ b, long long ldb,
+                                                   const int* __restrict__ cols, int ncols, double2* __restrict__ work,
+                                                   cplx<T>* __restrict__ x, long long ldx) {
+  cg::grid_group grid = cg::this_grid();
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  double2* const Y0 = work;
+  double2* const Y1 = work + (long long)ncols * N;
+  double2* const X64 = work + 2LL * ncols * N;
+  long long prev_end = 0;
+  for (int I = 0; I < nbk; ++I) {
+    const BandBlock B = blocks[I];
+    const int split = (I == 0) ? 0 : (int)(prev_end - B.s);
+    const double2* src0 = (I & 1) ? Y0 : Y1;  // output of block I-1
+    double2* dst = (I & 1) ? Y1 : Y0;
+    const long long items = (long long)B.W * ncols;
+    for (long long it = gw; it < items; it += nw) {
+      const int i = (int)(it % B.W), ci = (int)(it / B.W);
+      const double2* Mr = Tops + B.toff + (long long)i * B.W;
+      const long long base = (long long)ci * N + B.s;
+      double ar = 0.0, ai = 0.0;
+      for (int k = lane; k < B.W; k += 32) {
+        const double2 m = Mr[k];
+        double2 v;
+        if (k < split) {
+          v = src0[base + k];
+        } else {
+          const cplx<T> bb = b[(long long)cols[ci] * ldb + B.s + k];
+          v = mk<double>((double)bb.x, (double)bb.y);
+        }
+        ar = fma(m.x, v.x, ar);
+        ar = fma(-m.y, v.y, ar);
+        ai = fma(m.x, v.y, ai);
+        ai = fma(m.y, v.x, ai);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, o);
+        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+      }
+      if (lane == 0) dst[base + i] = mk<double>(ar, ai);
+    }
+    prev_end = B.s + B.W;
+    grid.sync();
+  }
+  for (int I = nbk - 1; I >= 0; --I) {
+    const BandBlock B = blocks[I];
+    const double2* yb = (I & 1) ? Y1 : Y0;
+    const long long items = (long long)B.nb * ncols;
+    for (long long it = gw; it < items; it += nw) {
+      const int i = (int)(it % B.nb), ci = (int)(it / B.nb);
+      const double2* Mr = Gops + B.goff + (long long)i * B.Wb;
+      const long long base = (long long)ci * N + B.s;
+      double ar = 0.0, ai = 0.0;
+      for (int k = lane; k < B.Wb; k += 32) {
+        const double2 m = Mr[k];
+        const double2 v = (k < B.nb) ? yb[base + k] : X64[base + k];
+        ar = fma(m.x, v.x, ar);
+        ar = fma(-m.y, v.y, ar);
+        ai = fma(m.x, v.y, ai);
+        ai = fma(m.y, v.x, ai);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, o);
+        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+      }
+      if (lane == 0) {
+        X64[base + i] = mk<double>(ar, ai);
+        x[(long long)cols[ci] * ldx + B.s + i] = mk<T>((T)ar, (T)ai);
+      }
+    }
+    grid.sync();
+  }
+}
+
 template <typename T>
 void launch_band_solve(Ctx& ctx, const BandSolveOps& op, const cplx<T>* b, cplx<T>* x, long long ld, const int* cols,
                        int ncols, double2* work) {
   if (ncols <= 0) return;
   const long long N = op.N;
+  const int nbk = (int)op.blocks.size();
+  double bytes = 0.0;
+  for (const BandBlock& B : op.blocks)
+    bytes += ((double)B.W * B.W + (double)B.nb * B.Wb) * sizeof(double2) +
+             ncols * (2.0 * B.W + B.Wb + 2.0 * B.nb) * sizeof(double2);
+  if (op.dblocks) {
+    // one cooperative launch, grid = co-resident capacity
+    static int capacity[kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < kMaxDevices && capacity[dev] == 0) {
+      int per_sm = 0, sms = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_band_coop<T>, 256, 0);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      capacity[dev] = std::max(1, std::min(per_sm, 4)) * std::max(1, sms);
+    }
+    const int grid = (dev >= 0 && dev < kMaxDevices) ? capacity[dev] : kSMs;
+    static thread_local int id = -1;
+    if (id < 0 || (size_t)id >= ctx.names.size() || ctx.names[id] != "band_solve") id = ctx.name_id("band_solve");
+    cudaEvent_t ev = nullptr;
+    ctx.before(id, &ev);
+    const BandBlock* blk = op.dblocks;
+    const double2* Tp = op.T;
+    const double2* Gp = op.G;
+    long long ldb = ld, ldx = ld;
+    void* args[] = {(void*)&N,    (void*)&nbk,  (void*)&blk,   (void*)&Tp,   (void*)&Gp, (void*)&b,
+                    (void*)&ldb,  (void*)&cols, (void*)&ncols, (void*)&work, (void*)&x,  (void*)&ldx};
+    const cudaError_t e =
+        cudaLaunchCooperativeKernel((const void*)k_band_coop<T>, dim3(grid), dim3(256), args, 0, ctx.stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw std::runtime_error(std::string("band_solve cooperative launch failed: ") + cudaGetErrorString(e));
+    }
+    ctx.after(id, ev, bytes);
+    return;
+  }
   double2* Y[2] = {work, work + (long long)ncols * N};
   double2* X64 = work + 2LL * ncols * N;
-  const int nbk = (int)op.blocks.size();
   const unsigned gy = (unsigned)((ncols + 7) / 8);
   long long prev_end = 0;
   for (int I = 0; I < nbk; ++I) {
     const BandBlock& B = op.blocks[(size_t)I];
     const int split = (I == 0) ? 0 : (int)(prev_end - B.s);
-    const double bytes = (double)B.W * B.W * sizeof(double2) + 2.0 * ncols * B.W * sizeof(double2);
-    HZ_LAUNCH(ctx, "band_forward", bytes, (k_band_block<T, 0>), dim3((unsigned)B.W, gy), 256, 0, N, B.s, B.W, split,
+    const double fb = (double)B.W * B.W * sizeof(double2) + 2.0 * ncols * B.W * sizeof(double2);
+    HZ_LAUNCH(ctx, "band_forward", fb, (k_band_block<T, 0>), dim3((unsigned)B.W, gy), 256, 0, N, B.s, B.W, split,
               op.T + B.toff, Y[(I + 1) % 2], b, ld, cols, (const double2*)nullptr, Y[I % 2], (cplx<T>*)nullptr,
               0LL, ncols);
     prev_end = B.s + B.W;
   }
   for (int I = nbk - 1; I >= 0; --I) {
     const BandBlock& B = op.blocks[(size_t)I];
-    const double bytes = (double)B.nb * B.Wb * sizeof(double2) + ncols * (B.Wb + 2.0 * B.nb) * sizeof(double2);
-    HZ_LAUNCH(ctx, "band_backward", bytes, (k_band_block<T, 1>), dim3((unsigned)B.nb, gy), 256, 0, N, B.s, B.Wb,
+    const double bb = (double)B.nb * B.Wb * sizeof(double2) + ncols * (B.Wb + 2.0 * B.nb) * sizeof(double2);
+    HZ_LAUNCH(ctx, "band_backward", bb, (k_band_block<T, 1>), dim3((unsigned)B.nb, gy), 256, 0, N, B.s, B.Wb,
               B.nb, op.G + B.goff, Y[I % 2], (const cplx<T>*)nullptr, 0LL, cols, X64, X64, x, ld, ncols);
   }
 }

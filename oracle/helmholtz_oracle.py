@@ -461,6 +461,54 @@ def fgmres(Hmul, prec, B: np.ndarray, restart: int, tol: float, max_outer: int) 
     return FGMRESResult(X=X, iters=iters, outer=outer, relres=relres, converged=conv)
 
 
+def bicgstab(Hmul, prec, B: np.ndarray, tol: float, max_iter: int) -> FGMRESResult:
+    """Right-preconditioned BiCGSTAB (van der Vorst 1992), the Krylov method
+    of solveBiCGSTAB_MG (src/ShiftedLaplacianMultigridSolver.jl:91-93, the
+    reference's default), all columns batched but independent.  Two
+    preconditioner applications per iteration; a column stops when
+    ||r||/||b|| <= tol (r updated recursively, true residual at the end).
+    ``iters`` counts iterations, ``outer`` the maximum over the columns."""
+    B = np.asarray(B, dtype=np.complex128)
+    n, R = B.shape
+    X = np.zeros_like(B)
+    bnorm = np.linalg.norm(B, axis=0)
+    live = bnorm > 0
+    r = B.copy()
+    rh = r.copy()
+    p = np.zeros_like(B)
+    v = np.zeros_like(B)
+    rho_prev = np.ones(R, dtype=np.complex128)
+    alpha = np.ones(R, dtype=np.complex128)
+    omega = np.ones(R, dtype=np.complex128)
+    iters = np.zeros(R, dtype=np.int64)
+    for _ in range(max_iter):
+        c = np.nonzero(live)[0]
+        if c.size == 0:
+            break
+        rho = np.sum(rh[:, c].conj() * r[:, c], axis=0)
+        beta = (rho / rho_prev[c]) * (alpha[c] / omega[c])
+        p[:, c] = r[:, c] + beta * (p[:, c] - omega[c] * v[:, c])
+        ph = prec(p[:, c])
+        v[:, c] = Hmul(ph)
+        alpha[c] = rho / np.sum(rh[:, c].conj() * v[:, c], axis=0)
+        s = r[:, c] - alpha[c] * v[:, c]
+        sh = prec(s)
+        t = Hmul(sh)
+        omega[c] = np.sum(t.conj() * s, axis=0) / np.sum(np.abs(t) ** 2, axis=0)
+        X[:, c] += alpha[c] * ph + omega[c] * sh
+        r[:, c] = s - omega[c] * t
+        rho_prev[c] = rho
+        iters[c] += 1
+        rel = np.linalg.norm(r[:, c], axis=0) / bnorm[c]
+        live[c[rel <= tol]] = False
+    relres = np.zeros(R)
+    nz = bnorm > 0
+    if nz.any():
+        relres[nz] = np.linalg.norm(B[:, nz] - Hmul(X[:, nz]), axis=0) / bnorm[nz]
+    return FGMRESResult(X=X, iters=iters, outer=int(iters.max(initial=0)), relres=relres,
+                        converged=relres <= tol * 1.0001)
+
+
 @dataclass
 class SLMGSolution:
     X: np.ndarray
@@ -471,7 +519,7 @@ class SLMGSolution:
 def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Sommerfeld: bool, B: np.ndarray,
                levels: int, shift: float = 0.5, relax_w: float = 0.8, pre: int = 1, post: int = 1,
                restart: int = 10, tol: float = 1e-8, max_outer: int = 100, cycle: str = "V",
-               transpose: bool = False) -> SLMGSolution:
+               transpose: bool = False, krylov: str = "GMRES") -> SLMGSolution:
     """Plain FP64 SLMG: FGMRES(restart) on H (or H^H when ``transpose``),
     right-preconditioned by one multigrid cycle on SH = H + i*s*w^2*diag(m)
     (or SH^H), src/ShiftedLaplacianMultigridSolver.jl:33-102."""
@@ -485,7 +533,11 @@ def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Somme
     vec = B2.ndim == 1
     if vec:
         B2 = B2[:, None]
-    res = fgmres(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle), B2, restart, tol, max_outer)
+    if krylov == "BiCGSTAB":
+        res = bicgstab(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle), B2, tol, max_outer)
+    else:
+        res = fgmres(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle), B2, restart, tol,
+                     max_outer)
     X = res.X[:, 0] if vec else res.X
     return SLMGSolution(X=X, result=res, hier=hier)
 

@@ -158,3 +158,40 @@ def test_clear_and_copy(hz, O):
     S2 = hz.copySolver(S)
     X3, S2 = hz.solveLinearSystem(None, B, S2)
     np.testing.assert_array_equal(X1, X3)
+
+
+def _bicg_solver(hz, P, levels, tol, precision="fp64", max_iter=400):
+    MG = hz.getMGparam(complex, int, levels, 1, max_iter, tol, "Jac", 0.8, 1, 1, "V", "Julia", 0.5, 0.0,
+                       precision=precision)
+    return hz.getShiftedLaplacianMultigridSolver(PB.hz_param(hz, P), MG, 0.5, "BiCGSTAB", 0)
+
+
+@pytest.mark.parametrize("precision,tol,bound", [("fp64", 1e-8, 1e-6), ("mixed", 1e-6, 1e-4)])
+def test_bicgstab_2d(hz, O, precision, tol, bound):
+    """solveBiCGSTAB_MG path (src/ShiftedLaplacianMultigridSolver.jl:91-93, the reference's default Krylov)."""
+    P = PB.gradient_2d((64, 64), pad=8)
+    n = P["m"].size
+    B = PB.rhs(n, 4, seed=3)
+    B[:, 2] = 0.0
+    S = _bicg_solver(hz, P, 3, tol, precision)
+    X, S = hz.solveLinearSystem(None, B, S)
+    Xref = O.direct_solve(P["H"], B)
+    assert not np.any(X[:, 2])
+    for c in (0, 1, 3):
+        assert _rel(X[:, c], Xref[:, c]) <= bound
+    assert np.max(S.last_relres) <= tol
+    if precision == "fp64":
+        sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=3, tol=tol, max_outer=400,
+                           krylov="BiCGSTAB")
+        # same algorithm in FP64: iteration counts agree up to rounding of the stopping test
+        assert np.all(np.abs(S.last_iters.astype(int) - sol.result.iters.astype(int)) <= 1)
+
+
+def test_bicgstab_3d_transpose(hz, O):
+    P = PB.layered((24, 24, 24), seed=9, pad=3, ellipsoid=True)
+    n = P["m"].size
+    B = PB.rhs(n, 2, seed=4)
+    S = _bicg_solver(hz, P, 3, 1e-8)
+    X, S = hz.solveLinearSystem(None, B, S, 1)
+    Xref = O.direct_solve(P["H"].conj().T.tocsr(), B)
+    assert _rel(X, Xref) <= 1e-6
