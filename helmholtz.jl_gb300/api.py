@@ -359,6 +359,7 @@ class MGparam:
     high: float = 0.0
     transferType: str = "FullWeighting"
     precision: str = "fp64"  # "fp64" or "mixed" (complex-FP32 cycle)
+    coarseOperator: str = "Galerkin"  # or "Rediscretize" (src/ShiftedLaplacianMultigridSolver.jl:51-62)
     doTranspose: int = 0
     _hier: dict = field(default_factory=dict, repr=False)
 
@@ -366,7 +367,8 @@ class MGparam:
 _SUPPORTED_COARSE = {"Julia", "MUMPS", "NoMUMPS", "BandLU"}
 
 
-def getMGparam(*args, transferType: str | None = None, precision: str = "fp64") -> MGparam:
+def getMGparam(*args, transferType: str | None = None, precision: str = "fp64",
+               coarseOperator: str = "Galerkin") -> MGparam:
     """Positional forms of Multigrid.jl getMGparam:
     (TYPE, ITYPE, levels, numCores, maxIter, relativeTol, relaxType, relaxParam,
      relaxPre, relaxPost, cycleType, coarseSolveType[, low, high[, transferType]])
@@ -382,7 +384,7 @@ def getMGparam(*args, transferType: str | None = None, precision: str = "fp64") 
     high = a[11] if len(a) > 11 else 0.0
     tt = a[12] if len(a) > 12 else (transferType or "FullWeighting")
     mg = MGparam(int(levels), int(numCores), int(maxIter), float(tol), str(relaxType), float(relaxParam), pre, post,
-                 str(cycle), str(coarse), float(low), float(high), str(tt), precision)
+                 str(cycle), str(coarse), float(low), float(high), str(tt), precision, coarseOperator)
     return mg
 
 
@@ -399,6 +401,8 @@ def _validate_mg(MG: MGparam):
         raise NotImplementedError("level-dependent relaxation counts are not built")
     if MG.precision not in ("fp64", "mixed"):
         raise ValueError("precision must be 'fp64' or 'mixed'")
+    if MG.coarseOperator not in ("Galerkin", "Rediscretize"):
+        raise ValueError("coarseOperator must be 'Galerkin' or 'Rediscretize'")
 
 
 @dataclass
@@ -470,6 +474,7 @@ def _options(s: ShiftedLaplacianMultigridSolver) -> L.hz_options:
     o.inner = s.inner
     o.shift = float(s.shift[0])
     o.precision = L.HZ_PREC_MIXED if MG.precision == "mixed" else L.HZ_PREC_FP64
+    o.coarse_op = L.HZ_COARSE_REDISCRETIZE if MG.coarseOperator == "Rediscretize" else L.HZ_COARSE_GALERKIN
     o.verbose = int(bool(s.verbose))
     return o
 
@@ -482,7 +487,7 @@ def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
         raise NotImplementedError("level-dependent shifts are not built")
     key = (id(s.helmParam), id(s.helmParam.m), id(s.helmParam.gamma), s.MG.levels, s.MG.maxOuterIter,
            s.MG.relativeTol, s.MG.relaxParam, int(s.MG.relaxPre), int(s.MG.relaxPost), s.MG.cycleType,
-           s.MG.precision, s.inner, float(s.shift[0]), s.Krylov)
+           s.MG.precision, s.inner, float(s.shift[0]), s.Krylov, s.MG.coarseOperator)
     if s._handle is not None and s._key == key:
         return s._handle
     _release(s)

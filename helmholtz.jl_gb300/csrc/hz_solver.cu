@@ -86,6 +86,15 @@ struct Level {
   long long ld = 0;  // leading dimension of the RHS blocks of this level
   // Galerkin coefficients (levels >= 1): FP64 master and FP32 copy
   DBuf coef64, coef32, dinv64, dinv32;
+  // 5/7-point (fine-kind) level: level 0, or a re-discretised coarse level
+  bool fine = false;
+  FineOp fop{};
+  const double2* fd64 = nullptr;  // diag(SH), 1/diag(SH) in FP64 and FP32
+  const double2* fi64 = nullptr;
+  const float2* fd32 = nullptr;
+  const float2* fi32 = nullptr;
+  DBuf own_d64, own_i64, own_d32, own_i32;  // storage of a re-discretised level
+  std::vector<double> m, gamma;              // restricted nodal m and shifted gamma (host)
   // work buffers (precision of the cycle): x/t ping-pong, r residual, b right-hand side
   DBuf x, t, r, b;
 };
@@ -176,6 +185,70 @@ void sync(hz_handle* h) {
   h->ctx.resolve();
 }
 
+// Diagonals of H and SH on the node grid of problem p (5/7-point Laplacian
+// diagonal with the boundary-row rule, plus the mass/Sommerfeld term, plus the
+// shift i s w^2 m for SH) and 1/diag(SH).
+void fine_diagonals(const hz_problem& p, double s, std::vector<std::complex<double>>& dH,
+                    std::vector<std::complex<double>>& dSH, std::vector<std::complex<double>>& iSH) {
+  const long long N = num_nodes(p);
+  const Grid g = make_grid(p);
+  std::vector<std::complex<double>> mass((size_t)N);
+  int st = hz_helmholtz_mass(&p, reinterpret_cast<double*>(mass.data()));
+  if (st != HZ_OK) fail(st, "invalid problem (mass term)");
+  const double BC = p.order_neumann_bc == 1 ? 1.0 : 2.0;
+  const double w2 = p.omega_re * p.omega_re;  // the shift uses real omega (GetHelmholtzShiftOP)
+  dH.resize((size_t)N);
+  dSH.resize((size_t)N);
+  iSH.resize((size_t)N);
+  for (long long q = 0; q < N; ++q) {
+    const int i = (int)(q % g.nx), j = (int)((q / g.nx) % g.ny), k = (int)(q / ((long long)g.nx * g.ny));
+    const int pos[3] = {i, j, k};
+    const int nn[3] = {g.nx, g.ny, g.nz};
+    double lap = 0.0;
+    for (int d = 0; d < p.dim; ++d) {
+      const bool bnd = pos[d] == 0 || pos[d] == nn[d] - 1;
+      lap += (bnd ? BC : 2.0) / (p.h[d] * p.h[d]);
+    }
+    dH[(size_t)q] = lap + mass[(size_t)q];
+    dSH[(size_t)q] = dH[(size_t)q] + std::complex<double>(0.0, s * w2 * p.m[q]);
+    iSH[(size_t)q] = 1.0 / dSH[(size_t)q];
+  }
+}
+
+FineOp make_fineop(const hz_problem& p, int adj) {
+  FineOp f{};
+  f.g = make_grid(p);
+  const double BC = p.order_neumann_bc == 1 ? 1.0 : 2.0;
+  for (int d = 0; d < 3; ++d) {
+    const double hd = d < p.dim ? p.h[d] : 1.0;
+    f.o[d] = 1.0 / (hd * hd);
+    f.b[d] = BC / (hd * hd);
+  }
+  f.adj = adj;
+  return f;
+}
+
+// Full-weighting average of a nodal field onto the next coarser grid
+// (weights of P^T normalised to sum 1 at every coarse node).
+std::vector<double> restrict_nodal(const std::vector<double>& f, const Grid& gf, const Grid& gc, int dim) {
+  std::vector<double> c((size_t)gc.N);
+  for (long long q = 0; q < gc.N; ++q) {
+    const int I = (int)(q % gc.nx), J = (int)((q / gc.nx) % gc.ny), K = (int)(q / ((long long)gc.nx * gc.ny));
+    double acc = 0.0, wsum = 0.0;
+    for (int dk = (dim == 3 ? -1 : 0); dk <= (dim == 3 ? 1 : 0); ++dk)
+      for (int dj = -1; dj <= 1; ++dj)
+        for (int di = -1; di <= 1; ++di) {
+          const int fi = 2 * I + di, fj = 2 * J + dj, fk = 2 * K + dk;
+          if (fi < 0 || fi >= gf.nx || fj < 0 || fj >= gf.ny || fk < 0 || fk >= gf.nz) continue;
+          const double wgt = (di ? 0.5 : 1.0) * (dj ? 0.5 : 1.0) * (dk ? 0.5 : 1.0);
+          acc += wgt * f[(size_t)(fi + (long long)gf.nx * (fj + (long long)gf.ny * fk))];
+          wsum += wgt;
+        }
+    c[(size_t)q] = acc / wsum;
+  }
+  return c;
+}
+
 // ---- hierarchy setup -------------------------------------------------------
 
 // Stencil offsets per level are all within one node; the banded storage uses
@@ -191,11 +264,10 @@ void factor_coarsest(hz_handle* h, Hierarchy& H) {
   const int ns = dim == 3 ? 27 : 9;
   // gather the stencil coefficients of the coarsest level on the host
   std::vector<std::complex<double>> coef((size_t)ns * N, 0.0);
-  if (H.lv.size() == 1) {
-    // single-level hierarchy: the fine operator itself (5/7-point)
+  if (L.fine) {
+    // 5/7-point coarsest level (single-level hierarchy or re-discretised levels)
     std::vector<std::complex<double>> d((size_t)N);
-    ck(cudaMemcpy(d.data(), h->diagSH.p, N * 16, cudaMemcpyDeviceToHost), "copy diag");
-    const double BC = h->prob.order_neumann_bc == 1 ? 1.0 : 2.0;
+    ck(cudaMemcpy(d.data(), L.fd64, N * 16, cudaMemcpyDeviceToHost), "copy diag");
     for (long long p = 0; p < N; ++p) {
       const int i = (int)(p % g.nx), j = (int)((p / g.nx) % g.ny), k = (int)(p / ((long long)g.nx * g.ny));
       const int center = dim == 3 ? 13 : 4;
@@ -203,7 +275,7 @@ void factor_coarsest(hz_handle* h, Hierarchy& H) {
       const int pos[3] = {i, j, k};
       const int nn[3] = {g.nx, g.ny, g.nz};
       for (int ax = 0; ax < dim; ++ax) {
-        const double o = 1.0 / (h->prob.h[ax] * h->prob.h[ax]), b = BC * o;
+        const double o = L.fop.o[ax], b = L.fop.b[ax];
         const int q = pos[ax], n = nn[ax];
         double cl, cr;
         if (!H.adj) {
@@ -269,7 +341,61 @@ void build_hierarchy(hz_handle* h, int adj) {
   auto l0 = std::make_unique<Level>();
   l0->g = h->g0;
   l0->ld = h->g0.N;
+  l0->fine = true;
+  l0->fop = h->fop;
+  l0->fop.adj = adj;
+  l0->fd64 = h->diagSH.as<double2>();
+  l0->fi64 = h->dinvSH.as<double2>();
+  l0->fd32 = h->diagSH32.as<float2>();
+  l0->fi32 = h->dinvSH32.as<float2>();
   H.lv.push_back(std::move(l0));
+  if (h->opt.coarse_op == HZ_COARSE_REDISCRETIZE) {
+    // the alternative MGsetup path of src/ShiftedLaplacianMultigridSolver.jl:51-62:
+    // shift folded into gamma (getShiftedHelmholtzParam), m and gamma restricted
+    // to each coarse mesh, operator re-assembled there (h doubles per level)
+    const double sre = h->opt.shift * h->prob.omega_re;
+    std::vector<double> mf = h->m, gf(h->gamma.size());
+    for (size_t q = 0; q < gf.size(); ++q) gf[q] = h->gamma[q] + sre;
+    hz_problem pl = h->prob;
+    for (int l = 1; l < L; ++l) {
+      Level& F = *H.lv[l - 1];
+      auto C = std::make_unique<Level>();
+      C->g = coarsen(F.g, dim);
+      C->ld = C->g.N;
+      C->m = restrict_nodal(l == 1 ? mf : F.m, F.g, C->g, dim);
+      C->gamma = restrict_nodal(l == 1 ? gf : F.gamma, F.g, C->g, dim);
+      for (int d = 0; d < dim; ++d) {
+        pl.n[d] /= 2;
+        pl.h[d] *= 2.0;
+      }
+      pl.m = C->m.data();
+      pl.gamma = C->gamma.data();
+      std::vector<std::complex<double>> dH, dSH, iSH;
+      fine_diagonals(pl, 0.0, dH, dSH, iSH);  // the shift is already in gamma
+      const long long Nc = C->g.N;
+      C->own_d64.alloc((size_t)Nc * 16);
+      C->own_i64.alloc((size_t)Nc * 16);
+      ck(cudaMemcpy(C->own_d64.p, dSH.data(), Nc * 16, cudaMemcpyHostToDevice), "upload coarse diag");
+      ck(cudaMemcpy(C->own_i64.p, iSH.data(), Nc * 16, cudaMemcpyHostToDevice), "upload coarse inverse diag");
+      C->fine = true;
+      C->fop = make_fineop(pl, adj);
+      C->fd64 = C->own_d64.as<double2>();
+      C->fi64 = C->own_i64.as<double2>();
+      if (mixed) {
+        C->own_d32.alloc((size_t)Nc * 8);
+        C->own_i32.alloc((size_t)Nc * 8);
+        launch_cast<float, double>(h->ctx, C->fd64, C->own_d32.as<float2>(), Nc);
+        launch_cast<float, double>(h->ctx, C->fi64, C->own_i32.as<float2>(), Nc);
+        C->fd32 = C->own_d32.as<float2>();
+        C->fi32 = C->own_i32.as<float2>();
+      }
+      H.lv.push_back(std::move(C));
+    }
+    sync(h);
+    factor_coarsest(h, H);
+    H.built = true;
+    return;
+  }
   FineOp fop = h->fop;
   fop.adj = adj;
   DBuf pin, pf, pg;
@@ -384,12 +510,12 @@ void ensure_level_buffers(hz_handle* h, Hierarchy& H, int R) {
 
 // ---- multigrid cycle -----------------------------------------------------------
 
-template <typename T> const cplx<T>* fine_diag(hz_handle* h);
-template <> const double2* fine_diag<double>(hz_handle* h) { return h->diagSH.as<double2>(); }
-template <> const float2* fine_diag<float>(hz_handle* h) { return h->diagSH32.as<float2>(); }
-template <typename T> const cplx<T>* fine_dinv(hz_handle* h);
-template <> const double2* fine_dinv<double>(hz_handle* h) { return h->dinvSH.as<double2>(); }
-template <> const float2* fine_dinv<float>(hz_handle* h) { return h->dinvSH32.as<float2>(); }
+template <typename T> const cplx<T>* fine_diag(const Level& L);
+template <> const double2* fine_diag<double>(const Level& L) { return L.fd64; }
+template <> const float2* fine_diag<float>(const Level& L) { return L.fd32; }
+template <typename T> const cplx<T>* fine_dinv(const Level& L);
+template <> const double2* fine_dinv<double>(const Level& L) { return L.fi64; }
+template <> const float2* fine_dinv<float>(const Level& L) { return L.fi32; }
 template <typename T> const cplx<T>* lev_coef(Level& L);
 template <> const double2* lev_coef<double>(Level& L) { return L.coef64.as<double2>(); }
 template <> const float2* lev_coef<float>(Level& L) { return L.coef32.as<float2>(); }
@@ -403,10 +529,8 @@ void lev_op(hz_handle* h, Hierarchy& H, int l, int mode, const cplx<T>* x, const
             const int* cols, int nc) {
   Level& L = *H.lv[l];
   const double w = h->opt.relax_param;
-  if (l == 0) {
-    FineOp fop = h->fop;
-    fop.adj = H.adj;
-    launch_fine<T, T, TB>(h->ctx, mode, fop, fine_diag<T>(h), fine_dinv<T>(h), x, b, y, L.ld, cols, nc, w);
+  if (L.fine) {
+    launch_fine<T, T, TB>(h->ctx, mode, L.fop, fine_diag<T>(L), fine_dinv<T>(L), x, b, y, L.ld, cols, nc, w);
   } else {
     launch_rap<T, TB>(h->ctx, mode, L.g, lev_coef<T>(L), L.g.N, lev_dinv<T>(L), x, b, y, L.ld, cols, nc, w);
   }
@@ -415,8 +539,8 @@ void lev_op(hz_handle* h, Hierarchy& H, int l, int mode, const cplx<T>* x, const
 template <typename T, typename TB>
 void lev_jacobi0(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* y, const int* cols, int nc) {
   Level& L = *H.lv[l];
-  const cplx<T>* dinv = (l == 0) ? fine_dinv<T>(h) : lev_dinv<T>(L);
-  launch_jacobi0<T, TB>(h->ctx, L.g, dinv, l == 0 ? H.adj : 0, b, y, L.ld, cols, nc, h->opt.relax_param);
+  const cplx<T>* dinv = L.fine ? fine_dinv<T>(L) : lev_dinv<T>(L);
+  launch_jacobi0<T, TB>(h->ctx, L.g, dinv, L.fine ? L.fop.adj : 0, b, y, L.ld, cols, nc, h->opt.relax_param);
 }
 
 // x_out = cycle(b) on level l with zero initial guess.
@@ -784,36 +908,9 @@ void init_fine(hz_handle* h) {
   const hz_problem& p = h->prob;
   const long long N = num_nodes(p);
   h->g0 = make_grid(p);
-  FineOp f{};
-  f.g = h->g0;
-  const double BC = p.order_neumann_bc == 1 ? 1.0 : 2.0;
-  for (int d = 0; d < 3; ++d) {
-    const double hd = d < p.dim ? p.h[d] : 1.0;
-    f.o[d] = 1.0 / (hd * hd);
-    f.b[d] = BC / (hd * hd);
-  }
-  f.adj = 0;
-  h->fop = f;
-  // diagonals on the host in FP64
-  std::vector<std::complex<double>> mass((size_t)N), dH((size_t)N), dSH((size_t)N), iSH((size_t)N);
-  int st = hz_helmholtz_mass(&h->prob, reinterpret_cast<double*>(mass.data()));
-  if (st != HZ_OK) fail(st, "invalid problem (mass term)");
-  const Grid g = h->g0;
-  const double s = h->opt.shift;
-  const double w2 = p.omega_re * p.omega_re;  // shift uses real omega (GetHelmholtzShiftOP)
-  for (long long q = 0; q < N; ++q) {
-    const int i = (int)(q % g.nx), j = (int)((q / g.nx) % g.ny), k = (int)(q / ((long long)g.nx * g.ny));
-    const int pos[3] = {i, j, k};
-    const int nn[3] = {g.nx, g.ny, g.nz};
-    double lap = 0.0;
-    for (int d = 0; d < p.dim; ++d) {
-      const bool bnd = pos[d] == 0 || pos[d] == nn[d] - 1;
-      lap += (bnd ? BC : 2.0) / (p.h[d] * p.h[d]);
-    }
-    dH[(size_t)q] = lap + mass[(size_t)q];
-    dSH[(size_t)q] = dH[(size_t)q] + std::complex<double>(0.0, s * w2 * p.m[q]);
-    iSH[(size_t)q] = 1.0 / dSH[(size_t)q];
-  }
+  h->fop = make_fineop(p, 0);
+  std::vector<std::complex<double>> dH, dSH, iSH;
+  fine_diagonals(p, h->opt.shift, dH, dSH, iSH);
   h->diagH.alloc((size_t)N * 16);
   h->diagSH.alloc((size_t)N * 16);
   h->dinvSH.alloc((size_t)N * 16);
@@ -845,7 +942,8 @@ void validate(const hz_problem* p, const hz_options* o) {
   if (o->inner < 0 || o->inner > 64) fail(HZ_ERR_ARG, "inner must be in [0, 64]");
   if (o->krylov != HZ_KRYLOV_FGMRES && o->krylov != HZ_KRYLOV_BICGSTAB) fail(HZ_ERR_ARG, "unknown Krylov method");
   if (o->cycle != 'V' && o->cycle != 'W') fail(HZ_ERR_ARG, "cycle must be 'V' or 'W'");
-  if (o->coarse_op != HZ_COARSE_GALERKIN) fail(HZ_ERR_ARG, "only Galerkin coarse operators are built");
+  if (o->coarse_op != HZ_COARSE_GALERKIN && o->coarse_op != HZ_COARSE_REDISCRETIZE)
+    fail(HZ_ERR_ARG, "coarse_op must be HZ_COARSE_GALERKIN or HZ_COARSE_REDISCRETIZE");
   if (o->precision != HZ_PREC_FP64 && o->precision != HZ_PREC_MIXED) fail(HZ_ERR_ARG, "unknown precision");
   if (o->precision == HZ_PREC_MIXED && o->levels < 2) fail(HZ_ERR_ARG, "mixed precision needs at least 2 levels");
   if (!(o->rel_tol > 0)) fail(HZ_ERR_ARG, "rel_tol must be > 0");

@@ -332,6 +332,38 @@ def build_hierarchy(SH: sp.csr_matrix, M: RegularMesh, nlevels: int) -> Hierarch
     return hier
 
 
+def restrict_nodal(v: np.ndarray, fine_cells) -> np.ndarray:
+    """Full-weighting average of a nodal field: (P^T v) / (P^T 1)."""
+    P = prolongation(fine_cells)
+    return (P.T @ v) / (P.T @ np.ones(P.shape[0]))
+
+
+def build_hierarchy_rediscretized(M: RegularMesh, m, gamma, omega: float, shift: float, NeumannOnTop: bool,
+                                  Sommerfeld: bool, nlevels: int, transpose: bool = False) -> Hierarchy:
+    """The alternative MGsetup path of src/ShiftedLaplacianMultigridSolver.jl:51-62:
+    the shift is folded into gamma (getShiftedHelmholtzParam, src/Helmholtz.jl:32-34),
+    m and gamma are restricted to every coarse mesh and the operator is
+    re-assembled there with GetHelmholtzOperator; P and R as in the Galerkin path."""
+    hier = Hierarchy()
+    m_l = np.asarray(m, dtype=np.float64).ravel(order="F")
+    g_l = np.asarray(gamma, dtype=np.float64).ravel(order="F") + shift * float(np.real(omega))
+    M_l = M
+    for lev in range(nlevels):
+        A = GetHelmholtzOperator(M_l, m_l, omega, g_l, NeumannOnTop, Sommerfeld)
+        if transpose:
+            A = A.conj().T.tocsr()
+        L = Level(cells=np.array(M_l.n), A=A, dinv=1.0 / A.diagonal())
+        if lev < nlevels - 1:
+            P = prolongation(M_l.n)
+            L.P, L.R = P, (P.T / (2.0 ** M.dim)).tocsr()
+            m_l = restrict_nodal(m_l, M_l.n)
+            g_l = restrict_nodal(g_l, M_l.n)
+            M_l = getRegularMesh(M_l.domain, M_l.n // 2)
+        hier.levels.append(L)
+    hier.lu = spla.splu(hier.levels[-1].A.tocsc())
+    return hier
+
+
 def jacobi(L: Level, x: np.ndarray, b: np.ndarray, w: float, sweeps: int) -> np.ndarray:
     for _ in range(sweeps):
         x = x + w * (L.dinv[:, None] * (b - L.A @ x))
@@ -519,7 +551,7 @@ class SLMGSolution:
 def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Sommerfeld: bool, B: np.ndarray,
                levels: int, shift: float = 0.5, relax_w: float = 0.8, pre: int = 1, post: int = 1,
                restart: int = 10, tol: float = 1e-8, max_outer: int = 100, cycle: str = "V",
-               transpose: bool = False, krylov: str = "GMRES") -> SLMGSolution:
+               transpose: bool = False, krylov: str = "GMRES", coarse: str = "galerkin") -> SLMGSolution:
     """Plain FP64 SLMG: FGMRES(restart) on H (or H^H when ``transpose``),
     right-preconditioned by one multigrid cycle on SH = H + i*s*w^2*diag(m)
     (or SH^H), src/ShiftedLaplacianMultigridSolver.jl:33-102."""
@@ -528,7 +560,10 @@ def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Somme
     if transpose:
         H = H.conj().T.tocsr()
         SH = SH.conj().T.tocsr()
-    hier = build_hierarchy(SH, M, levels)
+    if coarse == "rediscretize":
+        hier = build_hierarchy_rediscretized(M, m, gamma, omega, shift, NeumannOnTop, Sommerfeld, levels, transpose)
+    else:
+        hier = build_hierarchy(SH, M, levels)
     B2 = np.asarray(B, dtype=np.complex128)
     vec = B2.ndim == 1
     if vec:

@@ -195,3 +195,31 @@ def test_bicgstab_3d_transpose(hz, O):
     X, S = hz.solveLinearSystem(None, B, S, 1)
     Xref = O.direct_solve(P["H"].conj().T.tocsr(), B)
     assert _rel(X, Xref) <= 1e-6
+
+
+@pytest.mark.parametrize("precision,tol,bound", [("fp64", 1e-8, 1e-6), ("mixed", 1e-6, 1e-4)])
+def test_rediscretized_coarse_levels(hz, O, precision, tol, bound):
+    """The re-discretised hierarchy (src/ShiftedLaplacianMultigridSolver.jl:51-62)."""
+    P = PB.gradient_2d((64, 64), pad=8)
+    n = P["m"].size
+    B = PB.rhs(n, 3, seed=13)
+    MG = hz.getMGparam(complex, int, 3, 1, 100, tol, "Jac", 0.8, 1, 1, "V", "Julia", 0.5, 0.0, precision=precision,
+                       coarseOperator="Rediscretize")
+    S = hz.getShiftedLaplacianMultigridSolver(PB.hz_param(hz, P), MG, 0.5, "GMRES", 10)
+    X, S = hz.solveLinearSystem(None, B, S)
+    assert _rel(X, O.direct_solve(P["H"], B)) <= bound
+    if precision == "fp64":
+        sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=3, tol=tol, max_outer=100,
+                           coarse="rediscretize")
+        assert np.all(np.abs(S.last_iters.astype(int) - sol.result.iters.astype(int)) <= 1)
+        Xt, S = hz.solveLinearSystem(None, B, S, 1)
+        assert _rel(Xt, O.direct_solve(P["H"].conj().T.tocsr(), B)) <= bound
+
+
+def test_rediscretized_3d(hz, O):
+    P = PB.layered((32, 32, 32), seed=6, pad=4, ellipsoid=True)
+    B = PB.rhs(P["m"].size, 2, seed=4)
+    MG = hz.getMGparam(complex, int, 3, 1, 100, 1e-8, "Jac", 0.8, 1, 1, "V", "Julia", coarseOperator="Rediscretize")
+    S = hz.getShiftedLaplacianMultigridSolver(PB.hz_param(hz, P), MG, 0.5, "GMRES", 10)
+    X, S = hz.solveLinearSystem(None, B, S)
+    assert _rel(X, O.direct_solve(P["H"], B)) <= 1e-6
