@@ -103,6 +103,11 @@ int launch_fine_apply_noalloc(cudaStream_t stream, int dev, const FineOp& op, co
                               double2* y, long long ld, int nrhs, std::string* err);
 
 // ---- setup kernels ---------------------------------------------------------
+// Fine-level diagonals on the device from nodal m and gamma (device arrays):
+// diag(H), diag(SH) with the shift i*shift*Re(w)^2*m, and 1/diag(SH).
+void launch_fine_setup(Ctx& ctx, const Grid& g, int dim, const double* h, double wr, double wi, double shift, double BC,
+                       int neumann_on_top, int sommerfeld, const double* m, const double* gamma, double2* dH,
+                       double2* dSH, double2* iSH);
 void launch_probe_init(Ctx& ctx, const Grid& gc, int dim, double2* out, long long ld);
 void launch_probe_scatter(Ctx& ctx, const Grid& gc, int dim, const double2* y, long long ld, double2* coef,
                           long long cld);

@@ -505,6 +505,67 @@ template void launch_bicg_xr<float>(Ctx&, long long, double2*, const float2*, co
                                     const double2*, double2*, const double2*, const int*, int);
 
 // ---------------------------------------------------------------------------
+// Operator setup on the device (src/GetHelmholtz.jl:33-50, 81-83, 222-247)
+// ---------------------------------------------------------------------------
+// Per node: Sommerfeld term summed over the boundary faces the node lies on
+// (top face skipped when NeumannOnTop; same face order as the host helper),
+// mass = -w^2 m (1 - i gamma / Re w) - Somm, diag(H) = Laplacian diagonal + mass,
+// diag(SH) = diag(H) + i s (Re w)^2 m, and 1/diag(SH).
+__global__ void k_fine_setup(Grid g, int dim, double h0, double h1, double h2, double wr, double wi, double s,
+                             double BC, int neumann_on_top, int sommerfeld, const double* __restrict__ m,
+                             const double* __restrict__ gamma, double2* __restrict__ dH, double2* __restrict__ dSH,
+                             double2* __restrict__ iSH) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= g.N) return;
+  const int i = (int)(p % g.nx);
+  const long long t = p / g.nx;
+  const int j = (int)(t % g.ny);
+  const int k = (int)(t / g.ny);
+  const double mp = m[p], gp = gamma[p];
+  // -w^2 m (1 - i gamma / Re w), w complex
+  const double w2r = wr * wr - wi * wi, w2i = 2.0 * wr * wi;
+  const double a = 1.0, b = -gp / wr;  // (1 + i b)
+  double mr = -(w2r * a - w2i * b) * mp;
+  double mi = -(w2r * b + w2i * a) * mp;
+  if (sommerfeld) {
+    // Somm += -i w (BC/h_d) sqrt(m) on each face; host order: 2D top, bottom, x-high, x-low;
+    // 3D top, bottom, y-low, y-high, x-low, x-high
+    const double sq = sqrt(mp);
+    double si = 0.0;
+    if (dim == 2) {
+      if (!neumann_on_top && j == 0) si += -wr * (BC / h1) * sq;
+      if (j == g.ny - 1) si += -wr * (BC / h1) * sq;
+      if (i == g.nx - 1) si += -wr * (BC / h0) * sq;
+      if (i == 0) si += -wr * (BC / h0) * sq;
+    } else {
+      if (!neumann_on_top && k == 0) si += -wr * (BC / h2) * sq;
+      if (k == g.nz - 1) si += -wr * (BC / h2) * sq;
+      if (j == 0) si += -wr * (BC / h1) * sq;
+      if (j == g.ny - 1) si += -wr * (BC / h1) * sq;
+      if (i == 0) si += -wr * (BC / h0) * sq;
+      if (i == g.nx - 1) si += -wr * (BC / h0) * sq;
+    }
+    mi -= si;
+  }
+  double lap = ((i == 0 || i == g.nx - 1) ? BC : 2.0) / (h0 * h0) + ((j == 0 || j == g.ny - 1) ? BC : 2.0) / (h1 * h1);
+  if (dim == 3) lap += ((k == 0 || k == g.nz - 1) ? BC : 2.0) / (h2 * h2);
+  const double hr = lap + mr, hi = mi;
+  dH[p] = mk<double>(hr, hi);
+  const double sr = hr, shi = hi + s * wr * wr * mp;
+  dSH[p] = mk<double>(sr, shi);
+  const double den = sr * sr + shi * shi;
+  iSH[p] = mk<double>(sr / den, -shi / den);
+}
+
+void launch_fine_setup(Ctx& ctx, const Grid& g, int dim, const double* h, double wr, double wi, double shift, double BC,
+                       int neumann_on_top, int sommerfeld, const double* m, const double* gamma, double2* dH,
+                       double2* dSH, double2* iSH) {
+  const long long nb = (g.N + 255) / 256;
+  HZ_LAUNCH(ctx, "fine_setup", (double)g.N * (2 * 8 + 3 * 16), k_fine_setup, (unsigned)nb, 256, 0, g, dim, h[0], h[1],
+            dim == 3 ? h[2] : 1.0, wr, wi, shift, BC, neumann_on_top, sommerfeld, m, gamma, dH, dSH, iSH);
+}
+
+// ---------------------------------------------------------------------------
 // Setup kernels
 // ---------------------------------------------------------------------------
 // Galerkin probing: column k of the probe block is the indicator of the

@@ -909,14 +909,21 @@ void init_fine(hz_handle* h) {
   const long long N = num_nodes(p);
   h->g0 = make_grid(p);
   h->fop = make_fineop(p, 0);
-  std::vector<std::complex<double>> dH, dSH, iSH;
-  fine_diagonals(p, h->opt.shift, dH, dSH, iSH);
+  // operator setup on the device: upload m and gamma, compute the diagonals there
   h->diagH.alloc((size_t)N * 16);
   h->diagSH.alloc((size_t)N * 16);
   h->dinvSH.alloc((size_t)N * 16);
-  ck(cudaMemcpy(h->diagH.p, dH.data(), N * 16, cudaMemcpyHostToDevice), "upload diagH");
-  ck(cudaMemcpy(h->diagSH.p, dSH.data(), N * 16, cudaMemcpyHostToDevice), "upload diagSH");
-  ck(cudaMemcpy(h->dinvSH.p, iSH.data(), N * 16, cudaMemcpyHostToDevice), "upload dinvSH");
+  {
+    DBuf dm, dg;
+    dm.alloc((size_t)N * 8);
+    dg.alloc((size_t)N * 8);
+    ck(cudaMemcpyAsync(dm.p, p.m, N * 8, cudaMemcpyHostToDevice, h->ctx.stream), "upload m");
+    ck(cudaMemcpyAsync(dg.p, p.gamma, N * 8, cudaMemcpyHostToDevice, h->ctx.stream), "upload gamma");
+    launch_fine_setup(h->ctx, h->g0, p.dim, p.h, p.omega_re, p.omega_im, h->opt.shift,
+                      p.order_neumann_bc == 1 ? 1.0 : 2.0, p.neumann_on_top, p.sommerfeld, dm.as<double>(),
+                      dg.as<double>(), h->diagH.as<double2>(), h->diagSH.as<double2>(), h->dinvSH.as<double2>());
+    sync(h);
+  }
   if (h->opt.precision == HZ_PREC_MIXED) {
     h->diagSH32.alloc((size_t)N * 8);
     h->dinvSH32.alloc((size_t)N * 8);

@@ -223,3 +223,25 @@ def test_rediscretized_3d(hz, O):
     S = hz.getShiftedLaplacianMultigridSolver(PB.hz_param(hz, P), MG, 0.5, "GMRES", 10)
     X, S = hz.solveLinearSystem(None, B, S)
     assert _rel(X, O.direct_solve(P["H"], B)) <= 1e-6
+
+
+def test_multi_frequency_farming(hz, O):
+    """Several frequencies x shots in batches: one hierarchy per frequency, reused across batches."""
+    from helmholtz_jl_gb300.farm import solve_frequencies
+    P = PB.gradient_2d((64, 32), pad=6)
+    Mo = P["M"]
+    M = hz.getRegularMesh(Mo.domain, Mo.n)
+    n = P["m"].size
+    B = PB.rhs(n, 5, seed=17)
+    params, refs = [], []
+    for scale in (0.6, 1.0):
+        w = P["w"] * scale
+        gam = hz.getABL(Mo.n + 1, True, [6, 6], 0.95 * w).ravel(order="F") + 0.01 * w
+        params.append(hz.HelmholtzParam(M, gam, P["m"], w, True, True))
+        refs.append(O.GetHelmholtzOperator(Mo, P["m"], w, gam, True, True))
+    MG = hz.getMGparam(complex, int, 3, 1, 100, 1e-8, "Jac", 0.8, 1, 1, "V", "Julia")
+    res = solve_frequencies(params, B, MG, batch=2)
+    for k in range(2):
+        Xref = O.direct_solve(refs[k], B)
+        assert _rel(res.X[k], Xref) <= 1e-6
+        assert np.all(res.relres[k] <= 1e-8) and np.all(res.iters[k] > 0)
