@@ -249,6 +249,8 @@ def run_ours(args, rank, ws, dist):
         if args.krylov == "bicgstab":
             o.krylov, o.max_outer = L.HZ_KRYLOV_BICGSTAB, 2000
         o.precision = precision
+        if precision == L.HZ_PREC_MIXED and args.outer == "emulated":
+            o.outer_arith = L.HZ_OUTER_EMULATED
         o.device = torch.cuda.current_device()
         hh = C.c_void_p()
         L.check(lib.hz_create(C.byref(prob), C.byref(o), C.byref(hh)))
@@ -372,6 +374,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nrhs", type=int, default=0, help="override the workload's RHS count (small profiling cases)")
     ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
+    ap.add_argument("--outer", default="emulated", choices=["fp64", "emulated"],
+                    help="outer Krylov arithmetic of the mixed form: native FP64 or FP64 emulated with FP32 pairs")
     args = ap.parse_args()
     peak, peak_kind = load_peaks()
 
@@ -426,9 +430,13 @@ def main():
     plain = results.get("fp64")
     line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
-                vs_baseline=None, dtype="c64 V-cycle / c128 FGMRES", data="synthetic (seeded layered model)",
+                vs_baseline=None,
+                dtype=("c64 V-cycle / c128 outer" + (" (emulated by FP32 pairs)" if args.outer == "emulated" else "")
+                       if args.precision != "fp64" else "c128"),
+                data="synthetic (seeded layered model)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
                             krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB",
+                            outer_arithmetic=args.outer,
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
                             l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9)),
                 e2e=head.get("e2e"), gpu_launches=head["launches_per_step"] * args.steps,

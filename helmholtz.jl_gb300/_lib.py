@@ -26,6 +26,8 @@ HZ_MEM_HOST = 0
 HZ_MEM_DEVICE = 1
 HZ_PREC_FP64 = 0
 HZ_PREC_MIXED = 1
+HZ_OUTER_FP64 = 0
+HZ_OUTER_EMULATED = 1
 HZ_KRYLOV_FGMRES = 0
 HZ_KRYLOV_BICGSTAB = 1
 HZ_COARSE_GALERKIN = 0
@@ -67,7 +69,8 @@ class hz_options(C.Structure):
         ("verbose", C.c_int32),
         ("profile", C.c_int32),
         ("device", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("outer_arith", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 

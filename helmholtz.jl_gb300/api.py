@@ -360,6 +360,7 @@ class MGparam:
     transferType: str = "FullWeighting"
     precision: str = "fp64"  # "fp64" or "mixed" (complex-FP32 cycle)
     coarseOperator: str = "Galerkin"  # or "Rediscretize" (src/ShiftedLaplacianMultigridSolver.jl:51-62)
+    outerArithmetic: str = "fp64"     # or "emulated": FP64 emulated with FP32 pairs (mixed form, FGMRES)
     doTranspose: int = 0
     _hier: dict = field(default_factory=dict, repr=False)
 
@@ -368,7 +369,7 @@ _SUPPORTED_COARSE = {"Julia", "MUMPS", "NoMUMPS", "BandLU"}
 
 
 def getMGparam(*args, transferType: str | None = None, precision: str = "fp64",
-               coarseOperator: str = "Galerkin") -> MGparam:
+               coarseOperator: str = "Galerkin", outerArithmetic: str = "fp64") -> MGparam:
     """Positional forms of Multigrid.jl getMGparam:
     (TYPE, ITYPE, levels, numCores, maxIter, relativeTol, relaxType, relaxParam,
      relaxPre, relaxPost, cycleType, coarseSolveType[, low, high[, transferType]])
@@ -384,7 +385,8 @@ def getMGparam(*args, transferType: str | None = None, precision: str = "fp64",
     high = a[11] if len(a) > 11 else 0.0
     tt = a[12] if len(a) > 12 else (transferType or "FullWeighting")
     mg = MGparam(int(levels), int(numCores), int(maxIter), float(tol), str(relaxType), float(relaxParam), pre, post,
-                 str(cycle), str(coarse), float(low), float(high), str(tt), precision, coarseOperator)
+                 str(cycle), str(coarse), float(low), float(high), str(tt), precision, coarseOperator,
+                 outerArithmetic)
     return mg
 
 
@@ -403,6 +405,8 @@ def _validate_mg(MG: MGparam):
         raise ValueError("precision must be 'fp64' or 'mixed'")
     if MG.coarseOperator not in ("Galerkin", "Rediscretize"):
         raise ValueError("coarseOperator must be 'Galerkin' or 'Rediscretize'")
+    if MG.outerArithmetic not in ("fp64", "emulated"):
+        raise ValueError("outerArithmetic must be 'fp64' or 'emulated'")
 
 
 @dataclass
@@ -475,6 +479,7 @@ def _options(s: ShiftedLaplacianMultigridSolver) -> L.hz_options:
     o.shift = float(s.shift[0])
     o.precision = L.HZ_PREC_MIXED if MG.precision == "mixed" else L.HZ_PREC_FP64
     o.coarse_op = L.HZ_COARSE_REDISCRETIZE if MG.coarseOperator == "Rediscretize" else L.HZ_COARSE_GALERKIN
+    o.outer_arith = L.HZ_OUTER_EMULATED if MG.outerArithmetic == "emulated" else L.HZ_OUTER_FP64
     o.verbose = int(bool(s.verbose))
     return o
 
@@ -487,7 +492,7 @@ def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
         raise NotImplementedError("level-dependent shifts are not built")
     key = (id(s.helmParam), id(s.helmParam.m), id(s.helmParam.gamma), s.MG.levels, s.MG.maxOuterIter,
            s.MG.relativeTol, s.MG.relaxParam, int(s.MG.relaxPre), int(s.MG.relaxPost), s.MG.cycleType,
-           s.MG.precision, s.inner, float(s.shift[0]), s.Krylov, s.MG.coarseOperator)
+           s.MG.precision, s.inner, float(s.shift[0]), s.Krylov, s.MG.coarseOperator, s.MG.outerArithmetic)
     if s._handle is not None and s._key == key:
         return s._handle
     _release(s)

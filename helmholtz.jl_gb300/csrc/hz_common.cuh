@@ -14,6 +14,10 @@ namespace hz {
 template <typename T> struct cvec;
 template <> struct cvec<double> { using type = double2; };
 template <> struct cvec<float> { using type = float2; };
+// Emulated-FP64 complex (float4: re_hi, im_hi, re_lo, im_lo); as a right-hand
+// side of a complex-FP32 kernel only .x/.y (the high parts) are read.
+struct df64_tag {};
+template <> struct cvec<df64_tag> { using type = float4; };
 template <typename T> using cplx = typename cvec<T>::type;
 
 template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T re, T im) {

@@ -102,6 +102,36 @@ static constexpr int kNoAllocMaxDevices = 64;
 int launch_fine_apply_noalloc(cudaStream_t stream, int dev, const FineOp& op, const double2* diag, const double2* x,
                               double2* y, long long ld, int nrhs, std::string* err);
 
+// ---- emulated-FP64 outer FGMRES (hz_df64.cu) ---------------------------------
+// w = H z with z complex FP32, accumulated in df64; w a df64 vector (TO =
+// float4) or rounded to FP64 (TO = double2); dHd = diag(H) in df64.
+template <typename TO>
+void launch_fine_df64(Ctx& ctx, const FineOp& op, const float4* dHd, const float2* z, TO* y, long long ld,
+                      const int* cols, int ncols);
+void launch_dots_df(Ctx& ctx, long long N, const float4* V, long long vstride, long long ld, int i0, int K,
+                    const float4* w, long long wld, const int* cols, int ncols, int nblk, int want_norm,
+                    double2* part, const int* mask = nullptr);
+void launch_update_df(Ctx& ctx, long long N, const float4* V, long long vstride, long long ld, int i0, int K,
+                      const double2* h, int hstride, float4* w, long long wld, const int* cols, int ncols, int nblk,
+                      int want_norm, double2* part, const int* mask = nullptr);
+// y = s[c] x (FP64 x into df64 y; may run in place on the same memory)
+void launch_to_df(Ctx& ctx, long long N, const double2* x, long long xld, float4* y, long long yld, const double* s,
+                  const int* cols, int ncols);
+void launch_scale_df(Ctx& ctx, long long N, float4* w, long long ld, const double* s, const int* cols, int ncols);
+void launch_diag_to_df(Ctx& ctx, long long N, const double2* d, float4* out);
+// Coarsest solve as a dense emulated-FP64 product x = Ainv b (Ainv column-major
+// df64); part holds dense_df_splits(N, ncols) * ncols * N FP64 values.
+int dense_df_splits(long long N, int ncols);
+void launch_dense_df(Ctx& ctx, long long N, const float4* Ainv, const float2* b, float2* x, long long ld,
+                     const int* cols, int ncols, double2* part);
+void launch_identity(Ctx& ctx, long long N, double2* e);
+void launch_inplace_df(Ctx& ctx, long long n, double2* a);
+// Coarsest solve with the block operators stored as df64 (op.T / op.G point to
+// float4 arrays); work holds 3 * ncols * N df64 values.
+template <typename T>
+void launch_band_solve_df(Ctx& ctx, const BandSolveOps& op, const cplx<T>* b, cplx<T>* x, long long ld,
+                          const int* cols, int ncols, float4* work);
+
 // ---- setup kernels ---------------------------------------------------------
 // Fine-level diagonals on the device from nodal m and gamma (device arrays):
 // diag(H), diag(SH) with the shift i*shift*Re(w)^2*m, and 1/diag(SH).

@@ -726,6 +726,8 @@ template void launch_cast_cols<double, float>(Ctx&, long long, const float2*, lo
                                               const int*, int);
 template void launch_cast_cols<double, double>(Ctx&, long long, const double2*, long long, double2*, long long,
                                                const int*, int);
+template void launch_cast_cols<float, df64_tag>(Ctx&, long long, const float4*, long long, float2*, long long,
+                                                const int*, int);
 template void launch_zero_cols<double>(Ctx&, long long, double2*, long long, const int*, int);
 template void launch_zero_cols<float>(Ctx&, long long, float2*, long long, const int*, int);
 

@@ -108,6 +108,9 @@ struct Hierarchy {
   int kl = 0, ku = 0;
   DBuf bandT, bandG, bandB, bandwork;
   BandSolveOps band;
+  bool band_df = false;   // block operators stored as df64
+  bool dense_df = false;  // coarsest solve as a dense df64 product with A^{-1}
+  DBuf dense;             // A^{-1} (column-major, df64)
 };
 
 }  // namespace
@@ -122,6 +125,7 @@ struct hz_handle {
   FineOp fop{};
   // fine-level diagonals: H, SH (FP64), 1/diag(SH) (FP64), FP32 copies of SH
   DBuf diagH, diagSH, dinvSH, diagSH32, dinvSH32;
+  DBuf diagHdf;  // diag(H) in df64 (emulated-FP64 outer arithmetic)
   Hierarchy hier[2];
   // FGMRES workspace
   int rcap = 0;
@@ -249,6 +253,10 @@ std::vector<double> restrict_nodal(const std::vector<double>& f, const Grid& gf,
   return c;
 }
 
+// Largest coarsest level solved through a dense inverse in the emulated mode
+// (A^{-1} takes N^2 x 16 bytes: 1 GiB at this size).
+static constexpr long long kDenseCoarseMax = 8192;
+
 // ---- hierarchy setup -------------------------------------------------------
 
 // Stencil offsets per level are all within one node; the banded storage uses
@@ -317,6 +325,54 @@ void factor_coarsest(hz_handle* h, Hierarchy& H) {
   H.nc = N;
   H.kl = kl;
   H.ku = ku;
+  H.band_df = h->opt.precision == HZ_PREC_MIXED && h->opt.outer_arith == HZ_OUTER_EMULATED;
+  H.dense_df = H.band_df && N <= kDenseCoarseMax;
+  if (H.dense_df) {
+    // emulated-FP64 cycles on a small coarsest level: compute A^{-1} once in FP64
+    // (the blocked band solve applied to the identity), store it as df64 and
+    // apply it as one dense product per cycle
+    DBuf dT, dG, dB, E, W, dc;
+    dT.alloc(T.size() * 16);
+    dG.alloc(G.size() * 16);
+    ck(cudaMemcpy(dT.p, T.data(), T.size() * 16, cudaMemcpyHostToDevice), "upload band forward operators");
+    ck(cudaMemcpy(dG.p, G.data(), G.size() * 16, cudaMemcpyHostToDevice), "upload band backward operators");
+    dB.alloc(H.band.blocks.size() * sizeof(BandBlock));
+    ck(cudaMemcpy(dB.p, H.band.blocks.data(), H.band.blocks.size() * sizeof(BandBlock), cudaMemcpyHostToDevice),
+       "upload band blocks");
+    BandSolveOps ops;
+    ops.N = N;
+    ops.blocks = H.band.blocks;
+    ops.dblocks = dB.as<BandBlock>();
+    ops.T = dT.as<double2>();
+    ops.G = dG.as<double2>();
+    std::vector<int> all((size_t)N);
+    for (long long c = 0; c < N; ++c) all[(size_t)c] = (int)c;
+    dc.alloc((size_t)N * sizeof(int));
+    ck(cudaMemcpy(dc.p, all.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice), "upload identity columns");
+    E.alloc((size_t)N * N * 16);
+    W.alloc((size_t)3 * N * N * 16);
+    H.dense.alloc((size_t)N * N * 16);
+    launch_identity(h->ctx, N, E.as<double2>());
+    launch_band_solve<double>(h->ctx, ops, E.as<double2>(), H.dense.as<double2>(), N, dc.as<int>(), (int)N,
+                              W.as<double2>());
+    launch_inplace_df(h->ctx, N * N, H.dense.as<double2>());
+    sync(h);
+    H.band.N = N;
+    return;
+  }
+  if (H.band_df) {
+    // emulated-FP64 solves: each FP64 entry stored as a (hi, lo) float pair
+    auto to_df = [](std::vector<std::complex<double>>& v) {
+      for (auto& z : v) {
+        const float rh = (float)z.real(), ih = (float)z.imag();
+        const float rl = (float)(z.real() - (double)rh), il = (float)(z.imag() - (double)ih);
+        float f[4] = {rh, ih, rl, il};
+        std::memcpy(&z, f, sizeof(f));
+      }
+    };
+    to_df(T);
+    to_df(G);
+  }
   H.bandT.alloc(T.size() * 16);
   H.bandG.alloc(G.size() * 16);
   ck(cudaMemcpy(H.bandT.p, T.data(), T.size() * 16, cudaMemcpyHostToDevice), "upload band forward operators");
@@ -505,7 +561,12 @@ void ensure_level_buffers(hz_handle* h, Hierarchy& H, int R) {
       L.r.alloc(bytes);
     }
   }
-  H.bandwork.alloc((size_t)3 * R * H.nc * 16);
+  // band work: 3 vectors per column; the dense product's split-K partials need
+  // splits(ncols) * ncols vectors, largest over the active column counts
+  long long wcols = 3LL * R;
+  if (H.dense_df)
+    for (int nc = 1; nc <= R; ++nc) wcols = std::max(wcols, (long long)dense_df_splits(H.nc, nc) * nc);
+  H.bandwork.alloc((size_t)wcols * H.nc * 16);
 }
 
 // ---- multigrid cycle -----------------------------------------------------------
@@ -550,7 +611,14 @@ void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out
   const int last = (int)H.lv.size() - 1;
   if (l == last) {
     if (!std::is_same<T, TB>::value) fail(HZ_ERR_STATE, "single-level mixed hierarchy is not supported");
-    launch_band_solve<T>(h->ctx, H.band, (const cplx<T>*)b, out, L.ld, cols, nc, H.bandwork.as<double2>());
+    if (H.dense_df)
+      launch_dense_df(h->ctx, H.nc, H.dense.as<float4>(), (const float2*)b, (float2*)out, L.ld, cols, nc,
+                      H.bandwork.as<double2>());
+    else if (H.band_df)
+      launch_band_solve_df<float>(h->ctx, H.band, (const float2*)b, (float2*)out, L.ld, cols, nc,
+                                  H.bandwork.as<float4>());
+    else
+      launch_band_solve<T>(h->ctx, H.band, (const cplx<T>*)b, out, L.ld, cols, nc, H.bandwork.as<double2>());
     return;
   }
   Level& C = *H.lv[l + 1];
@@ -686,9 +754,16 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
   else
     ensure_level_buffers<double>(h, H, h->rcap);
   const double tol = h->opt.rel_tol;
+  // emulated-FP64 outer arithmetic: the basis V holds df64 values (float4, same size as double2)
+  const bool df = mixed && h->opt.outer_arith == HZ_OUTER_EMULATED;
+  float4* Vd = reinterpret_cast<float4*>(V);
+  auto Vdj = [&](int j) { return Vd + (long long)j * vstride * N; };
   // r0 = b (x0 = 0): V_0 = b / ||b||
   upload_cols(h, act);
-  launch_scale_cols(h->ctx, N, B, N, Vj(0), N, h->bnorm_inv.as<double>(), dc, (int)act.size());
+  if (df)
+    launch_to_df(h->ctx, N, B, N, Vdj(0), N, h->bnorm_inv.as<double>(), dc, (int)act.size());
+  else
+    launch_scale_cols(h->ctx, N, B, N, Vj(0), N, h->bnorm_inv.as<double>(), dc, (int)act.size());
   launch_cycle_init(h->ctx, m, dc, (int)act.size(), h->bnorm.as<double>(), h->gv.as<double2>());
   std::vector<int> kcol(h->rcap, 0);
   int outer = 0;
@@ -698,12 +773,20 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
     for (int j = 0; j < m && !live.empty(); ++j) {
       upload_cols(h, live);
       const int nl = (int)live.size();
-      precondition(h, H, Vj(j), Zj(j), dc, nl);
       double2* w = Vj(j + 1);
-      if (mixed)
-        apply_H<float>(h, adj, MODE_APPLY, (const float2*)Zj(j), nullptr, w, dc, nl);
-      else
-        apply_H<double>(h, adj, MODE_APPLY, (const double2*)Zj(j), nullptr, w, dc, nl);
+      if (df) {
+        // the cycle reads the high parts of the df64 basis vector as its FP32 right-hand side
+        mg_cycle<float, df64_tag>(h, H, 0, Vdj(j), (float2*)Zj(j), dc, nl);
+        FineOp fop = h->fop;
+        fop.adj = adj;
+        launch_fine_df64(h->ctx, fop, h->diagHdf.as<float4>(), (const float2*)Zj(j), Vdj(j + 1), N, dc, nl);
+      } else {
+        precondition(h, H, Vj(j), Zj(j), dc, nl);
+        if (mixed)
+          apply_H<float>(h, adj, MODE_APPLY, (const float2*)Zj(j), nullptr, w, dc, nl);
+        else
+          apply_H<double>(h, adj, MODE_APPLY, (const double2*)Zj(j), nullptr, w, dc, nl);
+      }
       // classical Gram-Schmidt with the DGKS test: pass 1 (dots + ||w||^2,
       // update + ||w'||^2) for every column, pass 2 only for the columns whose
       // norm dropped below 1/sqrt(2) of its value (masked on the device)
@@ -719,13 +802,19 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
         for (int i0 = 0; i0 < K; i0 += 16) {
           const int k = std::min(16, K - i0);
           const int wn = (pass == 0 && i0 + 16 >= K) ? 1 : 0;  // ||w||^2 before the update (slot K)
-          launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, wn, part, mask);
+          if (df)
+            launch_dots_df(h->ctx, N, Vd, vstride, N, i0, k, Vdj(j + 1), N, dc, nl, nblk, wn, part, mask);
+          else
+            launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, wn, part, mask);
           launch_reduce(h->ctx, part, dc, nl, k + wn, nblk, hh + i0, HS, 0);
         }
         for (int i0 = 0; i0 < K; i0 += 16) {
           const int k = std::min(16, K - i0);
           const int wn = (i0 + 16 >= K) ? 1 : 0;
-          launch_update(h->ctx, N, V, vstride, N, i0, k, hh, HS, w, N, dc, nl, nblk, wn, part, mask);
+          if (df)
+            launch_update_df(h->ctx, N, Vd, vstride, N, i0, k, hh, HS, Vdj(j + 1), N, dc, nl, nblk, wn, part, mask);
+          else
+            launch_update(h->ctx, N, V, vstride, N, i0, k, hh, HS, w, N, dc, nl, nblk, wn, part, mask);
           if (wn) launch_reduce(h->ctx, part, dc, nl, 1, nblk, nrm, HS, 0);
         }
         if (pass == 0) launch_dgks(h->ctx, dc, nl, hA, HS, K, h->nr.as<double2>(), HS, flag);
@@ -733,7 +822,10 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
       launch_arnoldi_step(h->ctx, j, m, dc, nl, hA, hB, h->nr.as<double2>(), h->nr2.as<double2>(), flag, HS,
                           h->Hh.as<double2>(), h->cs.as<double2>(), h->sn.as<double2>(), h->gv.as<double2>(),
                           h->est.as<double>(), h->invhn.as<double>());
-      launch_scale_cols(h->ctx, N, w, N, w, N, h->invhn.as<double>(), dc, nl);
+      if (df)
+        launch_scale_df(h->ctx, N, Vdj(j + 1), N, h->invhn.as<double>(), dc, nl);
+      else
+        launch_scale_cols(h->ctx, N, w, N, w, N, h->invhn.as<double>(), dc, nl);
       ck(cudaMemcpyAsync(h->h_est, h->est.p, (size_t)h->rcap * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "est");
       ck(cudaMemcpyAsync(h->h_flag, h->flag.p, (size_t)h->rcap * sizeof(int), cudaMemcpyDeviceToHost, h->ctx.stream),
          "flags");
@@ -784,7 +876,10 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
     if (act.empty()) break;
     if (outer == std::max(1, h->opt.max_outer)) break;
     upload_cols(h, act);
-    launch_scale_cols(h->ctx, N, Vj(0), N, Vj(0), N, h->beta_inv.as<double>(), dc, (int)act.size());
+    if (df)  // r (FP64) -> V_0 (df64) in place
+      launch_to_df(h->ctx, N, Vj(0), N, Vdj(0), N, h->beta_inv.as<double>(), dc, (int)act.size());
+    else
+      launch_scale_cols(h->ctx, N, Vj(0), N, Vj(0), N, h->beta_inv.as<double>(), dc, (int)act.size());
     launch_cycle_init(h->ctx, m, dc, (int)act.size(), h->beta.as<double>(), h->gv.as<double2>());
   }
   return std::min(outer, std::max(1, h->opt.max_outer));
@@ -829,6 +924,10 @@ int bicgstab(hz_handle* h, int adj, int nrhs) {
   else
     ensure_level_buffers<double>(h, H, h->rcap);
   const double tol = h->opt.rel_tol;
+  // emulated-FP64 arithmetic for H z (rounded to FP64: the BiCGSTAB vectors stay FP64)
+  const bool emu = mixed && h->opt.outer_arith == HZ_OUTER_EMULATED;
+  FineOp fopa = h->fop;
+  fopa.adj = adj;
   upload_cols(h, act);
   int na = (int)act.size();
   launch_cast_cols<double, double>(h->ctx, N, B, N, r, N, dc, na);   // r = b (x0 = 0)
@@ -864,7 +963,9 @@ int bicgstab(hz_handle* h, int adj, int nrhs) {
     launch_bicg_scalars(h->ctx, 0, dc, na, red, HS, sc);
     launch_bicg_vec(h->ctx, 0, N, r, p, v, nullptr, sc, dc, na);
     precondition(h, H, p, ph, dc, na);
-    if (mixed)
+    if (emu)
+      launch_fine_df64<double2>(h->ctx, fopa, h->diagHdf.as<float4>(), (const float2*)ph, v, N, dc, na);
+    else if (mixed)
       apply_H<float>(h, adj, MODE_APPLY, (const float2*)ph, nullptr, v, dc, na);
     else
       apply_H<double>(h, adj, MODE_APPLY, (const double2*)ph, nullptr, v, dc, na);
@@ -873,7 +974,9 @@ int bicgstab(hz_handle* h, int adj, int nrhs) {
     launch_bicg_scalars(h->ctx, 1, dc, na, red, HS, sc);
     launch_bicg_vec(h->ctx, 1, N, r, nullptr, v, sv, sc, dc, na);
     precondition(h, H, sv, sh, dc, na);
-    if (mixed)
+    if (emu)
+      launch_fine_df64<double2>(h->ctx, fopa, h->diagHdf.as<float4>(), (const float2*)sh, t, N, dc, na);
+    else if (mixed)
       apply_H<float>(h, adj, MODE_APPLY, (const float2*)sh, nullptr, t, dc, na);
     else
       apply_H<double>(h, adj, MODE_APPLY, (const double2*)sh, nullptr, t, dc, na);
@@ -924,6 +1027,10 @@ void init_fine(hz_handle* h) {
                       dg.as<double>(), h->diagH.as<double2>(), h->diagSH.as<double2>(), h->dinvSH.as<double2>());
     sync(h);
   }
+  if (h->opt.precision == HZ_PREC_MIXED && h->opt.outer_arith == HZ_OUTER_EMULATED) {
+    h->diagHdf.alloc((size_t)N * 16);
+    launch_diag_to_df(h->ctx, N, h->diagH.as<double2>(), h->diagHdf.as<float4>());
+  }
   if (h->opt.precision == HZ_PREC_MIXED) {
     h->diagSH32.alloc((size_t)N * 8);
     h->dinvSH32.alloc((size_t)N * 8);
@@ -953,6 +1060,9 @@ void validate(const hz_problem* p, const hz_options* o) {
     fail(HZ_ERR_ARG, "coarse_op must be HZ_COARSE_GALERKIN or HZ_COARSE_REDISCRETIZE");
   if (o->precision != HZ_PREC_FP64 && o->precision != HZ_PREC_MIXED) fail(HZ_ERR_ARG, "unknown precision");
   if (o->precision == HZ_PREC_MIXED && o->levels < 2) fail(HZ_ERR_ARG, "mixed precision needs at least 2 levels");
+  if (o->outer_arith != HZ_OUTER_FP64 && o->outer_arith != HZ_OUTER_EMULATED) fail(HZ_ERR_ARG, "unknown outer_arith");
+  if (o->outer_arith == HZ_OUTER_EMULATED && o->precision != HZ_PREC_MIXED)
+    fail(HZ_ERR_ARG, "emulated-FP64 outer arithmetic is part of the mixed form (precision = HZ_PREC_MIXED)");
   if (!(o->rel_tol > 0)) fail(HZ_ERR_ARG, "rel_tol must be > 0");
 }
 
@@ -1208,6 +1318,9 @@ int hz_clear(hz_handle* h) {
       H.bandT.reset();
       H.bandG.reset();
       H.bandB.reset();
+      H.dense.reset();
+      H.dense_df = false;
+      H.band_df = false;
       H.bandwork.reset();
       H.band = BandSolveOps();
       H.built = false;

@@ -510,10 +510,14 @@ __global__ void __launch_bounds__(256) k_band_block(long long N, long long s, in
   }
 }
 
-// All block steps of the solve in one cooperative launch: every warp takes
-// (row, column) items of the current window mat-vec, then the grid
-// synchronises before the next block step.  The launch is sized to the
-// co-resident capacity (cudaLaunchCooperativeKernel refuses a larger grid).
+// All block steps of the solve in one cooperative launch.  A warp item is one
+// row of the current window operator for BCW columns: the row entries are
+// loaded once and feed BCW independent accumulators (more loads in flight per
+// warp than one column per item).  The grid synchronises between block steps;
+// the launch is sized to the co-resident capacity (cudaLaunchCooperativeKernel
+// refuses a larger grid rather than deadlocking).
+static constexpr int BCW = 1;  // one column per item: more items in flight per step
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_band_coop(long long N, int nbk, const BandBlock* __restrict__ blocks,
                                                    const double2* __restrict__ Tops, const double2* __restrict__ Gops,
@@ -527,38 +531,49 @@ __global__ void __launch_bounds__(256) k_band_coop(long long N, int nbk, const B
   double2* const Y0 = work;
   double2* const Y1 = work + (long long)ncols * N;
   double2* const X64 = work + 2LL * ncols * N;
+  const int ngrp = (ncols + BCW - 1) / BCW;
   long long prev_end = 0;
   for (int I = 0; I < nbk; ++I) {
     const BandBlock B = blocks[I];
     const int split = (I == 0) ? 0 : (int)(prev_end - B.s);
     const double2* src0 = (I & 1) ? Y0 : Y1;  // output of block I-1
     double2* dst = (I & 1) ? Y1 : Y0;
-    const long long items = (long long)B.W * ncols;
+    const long long items = (long long)B.W * ngrp;
     for (long long it = gw; it < items; it += nw) {
-      const int i = (int)(it % B.W), ci = (int)(it / B.W);
+      const int i = (int)(it % B.W), c0 = (int)(it / B.W) * BCW;
       const double2* Mr = Tops + B.toff + (long long)i * B.W;
-      const long long base = (long long)ci * N + B.s;
-      double ar = 0.0, ai = 0.0;
+      double ar[BCW], ai[BCW];
+#pragma unroll
+      for (int c = 0; c < BCW; ++c) ar[c] = ai[c] = 0.0;
       for (int k = lane; k < B.W; k += 32) {
         const double2 m = Mr[k];
-        double2 v;
-        if (k < split) {
-          v = src0[base + k];
-        } else {
-          const cplx<T> bb = b[(long long)cols[ci] * ldb + B.s + k];
-          v = mk<double>((double)bb.x, (double)bb.y);
+#pragma unroll
+        for (int c = 0; c < BCW; ++c) {
+          const int ci = c0 + c;
+          if (ci < ncols) {
+            double2 v;
+            if (k < split) {
+              v = src0[(long long)ci * N + B.s + k];
+            } else {
+              const cplx<T> bb = b[(long long)cols[ci] * ldb + B.s + k];
+              v = mk<double>((double)bb.x, (double)bb.y);
+            }
+            ar[c] = fma(m.x, v.x, ar[c]);
+            ar[c] = fma(-m.y, v.y, ar[c]);
+            ai[c] = fma(m.x, v.y, ai[c]);
+            ai[c] = fma(m.y, v.x, ai[c]);
+          }
         }
-        ar = fma(m.x, v.x, ar);
-        ar = fma(-m.y, v.y, ar);
-        ai = fma(m.x, v.y, ai);
-        ai = fma(m.y, v.x, ai);
       }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        ar += __shfl_xor_sync(0xffffffffu, ar, o);
-        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+      for (int c = 0; c < BCW; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          ar[c] += __shfl_xor_sync(0xffffffffu, ar[c], o);
+          ai[c] += __shfl_xor_sync(0xffffffffu, ai[c], o);
+        }
+        if (lane == 0 && c0 + c < ncols) dst[(long long)(c0 + c) * N + B.s + i] = mk<double>(ar[c], ai[c]);
       }
-      if (lane == 0) dst[base + i] = mk<double>(ar, ai);
     }
     prev_end = B.s + B.W;
     grid.sync();
@@ -566,28 +581,40 @@ __global__ void __launch_bounds__(256) k_band_coop(long long N, int nbk, const B
   for (int I = nbk - 1; I >= 0; --I) {
     const BandBlock B = blocks[I];
     const double2* yb = (I & 1) ? Y1 : Y0;
-    const long long items = (long long)B.nb * ncols;
+    const long long items = (long long)B.nb * ngrp;
     for (long long it = gw; it < items; it += nw) {
-      const int i = (int)(it % B.nb), ci = (int)(it / B.nb);
+      const int i = (int)(it % B.nb), c0 = (int)(it / B.nb) * BCW;
       const double2* Mr = Gops + B.goff + (long long)i * B.Wb;
-      const long long base = (long long)ci * N + B.s;
-      double ar = 0.0, ai = 0.0;
+      double ar[BCW], ai[BCW];
+#pragma unroll
+      for (int c = 0; c < BCW; ++c) ar[c] = ai[c] = 0.0;
       for (int k = lane; k < B.Wb; k += 32) {
         const double2 m = Mr[k];
-        const double2 v = (k < B.nb) ? yb[base + k] : X64[base + k];
-        ar = fma(m.x, v.x, ar);
-        ar = fma(-m.y, v.y, ar);
-        ai = fma(m.x, v.y, ai);
-        ai = fma(m.y, v.x, ai);
+#pragma unroll
+        for (int c = 0; c < BCW; ++c) {
+          const int ci = c0 + c;
+          if (ci < ncols) {
+            const long long q = (long long)ci * N + B.s + k;
+            const double2 v = (k < B.nb) ? yb[q] : X64[q];
+            ar[c] = fma(m.x, v.x, ar[c]);
+            ar[c] = fma(-m.y, v.y, ar[c]);
+            ai[c] = fma(m.x, v.y, ai[c]);
+            ai[c] = fma(m.y, v.x, ai[c]);
+          }
+        }
       }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        ar += __shfl_xor_sync(0xffffffffu, ar, o);
-        ai += __shfl_xor_sync(0xffffffffu, ai, o);
-      }
-      if (lane == 0) {
-        X64[base + i] = mk<double>(ar, ai);
-        x[(long long)cols[ci] * ldx + B.s + i] = mk<T>((T)ar, (T)ai);
+      for (int c = 0; c < BCW; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          ar[c] += __shfl_xor_sync(0xffffffffu, ar[c], o);
+          ai[c] += __shfl_xor_sync(0xffffffffu, ai[c], o);
+        }
+        const int ci = c0 + c;
+        if (lane == 0 && ci < ncols) {
+          X64[(long long)ci * N + B.s + i] = mk<double>(ar[c], ai[c]);
+          x[(long long)cols[ci] * ldx + B.s + i] = mk<T>((T)ar[c], (T)ai[c]);
+        }
       }
     }
     grid.sync();
@@ -741,6 +768,7 @@ int launch_fine_apply_noalloc(cudaStream_t stream, int dev, const FineOp& op, co
 HZ_INST_T_TB(double, double)
 HZ_INST_T_TB(float, float)
 HZ_INST_T_TB(float, double)
+HZ_INST_T_TB(float, df64_tag)
 template void launch_fine<double, float, double>(Ctx&, int, const FineOp&, const double2*, const double2*,
                                                  const float2*, const double2*, double2*, long long, const int*, int,
                                                  double);

@@ -55,9 +55,10 @@ mutable struct HzOptions
     verbose::Int32
     profile::Int32
     device::Int32
-    reserved::NTuple{7,Int32}
+    outer_arith::Int32
+    reserved::NTuple{6,Int32}
 end
-HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 7))
+HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 6))
 
 mutable struct HzStats
     outer::Int32

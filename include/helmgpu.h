@@ -43,6 +43,12 @@ extern "C" {
 #define HZ_PREC_FP64 0
 #define HZ_PREC_MIXED 1 /* complex-FP32 V-cycle, FP64 coarsest LU */
 
+/* outer FGMRES arithmetic: native FP64, or FP64 emulated with pairs of FP32
+ * (basis stored as hi+lo, error-free FP32 transformations; ~2^-48 relative),
+ * which runs on the FP32 pipe.  The true residual is native FP64 either way. */
+#define HZ_OUTER_FP64 0
+#define HZ_OUTER_EMULATED 1
+
 #define HZ_KRYLOV_FGMRES 0
 #define HZ_KRYLOV_BICGSTAB 1
 
@@ -88,7 +94,8 @@ typedef struct hz_options {
   int32_t verbose;
   int32_t profile;       /* 1: time every kernel launch with CUDA events */
   int32_t device;        /* CUDA device ordinal */
-  int32_t reserved[7];
+  int32_t outer_arith;   /* FGMRES outer arithmetic: HZ_OUTER_FP64 (native) or HZ_OUTER_EMULATED */
+  int32_t reserved[6];
 } hz_options;
 
 typedef struct hz_stats {

@@ -245,3 +245,30 @@ def test_multi_frequency_farming(hz, O):
         Xref = O.direct_solve(refs[k], B)
         assert _rel(res.X[k], Xref) <= 1e-6
         assert np.all(res.relres[k] <= 1e-8) and np.all(res.iters[k] > 0)
+
+
+@pytest.mark.parametrize("case", ["2d", "3d", "2d_transpose"])
+def test_emulated_fp64_outer_matches_native(hz, O, case):
+    """Mixed form with the outer FGMRES in FP64 emulated by FP32 pairs: same
+    accuracy bound as the native-FP64 mixed form and about the same iterations."""
+    if case == "3d":
+        P = PB.layered((32, 32, 32), seed=6, pad=4, ellipsoid=True)
+    else:
+        P = PB.layered((128, 64), seed=3, pad=8, lengths=[2.0, 1.0])
+    tr = 1 if case == "2d_transpose" else 0
+    B = PB.rhs(P["m"].size, 4, seed=23)
+    B[:, 1] = 0.0
+    its = {}
+    for arith in ("fp64", "emulated"):
+        MG = hz.getMGparam(complex, int, 3, 1, 60, 1e-6, "Jac", 0.8, 1, 1, "V", "Julia", precision="mixed",
+                           outerArithmetic=arith)
+        S = hz.getShiftedLaplacianMultigridSolver(PB.hz_param(hz, P), MG, 0.5, "GMRES", 10)
+        X, S = hz.solveLinearSystem(None, B, S, tr)
+        Href = P["H"].conj().T.tocsr() if tr else P["H"]
+        Xref = O.direct_solve(Href, B)
+        assert not np.any(X[:, 1])
+        for c in (0, 2, 3):
+            assert _rel(X[:, c], Xref[:, c]) <= 1e-4
+            assert np.linalg.norm(Href @ X[:, c] - B[:, c]) / np.linalg.norm(B[:, c]) <= 1e-6 * 1.0001
+        its[arith] = S.last_iters.astype(int)
+    assert np.all(np.abs(its["emulated"] - its["fp64"]) <= 2), its
