@@ -35,6 +35,11 @@ METRIC = "RHS solved/s to rel. residual 1e-6 on 1 GB300: learned+mixed vs plain 
 # Synthetic seeded workloads (shapes, sizes and value distributions of the
 # measured configurations; no external dataset is needed).
 WORKLOADS = {
+    # configs[0]: 2D 129 x 129 on [0,1]^2, v = 1.5 + 3 z with the v = 4.5 ellipse, one source
+    # at (0.5, 2h), absorbing layer 16, 3 levels, FGMRES(10) to 1e-8
+    "c1": dict(name="2D 129x129 gradient+ellipse, 1 source, 3 levels, FGMRES(10) tol 1e-8",
+               cells=(128, 128), h=1.0 / 128, nrhs=1, levels=3, pad=16, ellipsoid=False, tol=1e-8,
+               model="gradient_ellipse"),
     # 2D 1025 x 513 nodes, h = 10 m, 12 seeded layers in [1.5, 4.5] km/s,
     # absorbing layer 32 cells, 64 sources along the surface row, 5 levels
     "c2": dict(name="2D 1025x513 layered, 64 surface sources, 5 levels, FGMRES(10) tol 1e-6",
@@ -51,10 +56,17 @@ WORKLOADS = {
 def make_problem(wl: dict, seed: int):
     """Seeded layered (+ ellipsoid) velocity model, 10 points per wavelength,
     attenuation 0.01 w plus a quadratic absorbing layer of amplitude 0.95 w."""
-    sys.path.insert(0, str(ROOT / "oracle"))
     cells = wl["cells"]
     dim = len(cells)
     nodes = [c + 1 for c in cells]
+    if wl.get("model") == "gradient_ellipse":
+        h = np.full(dim, wl["h"])
+        X, Z = np.meshgrid(h[0] * np.arange(nodes[0]), h[1] * np.arange(nodes[1]), indexing="ij")
+        v = 1.5 + 3.0 * Z
+        v[((X - 0.5) / 0.15) ** 2 + ((Z - 0.6) / 0.08) ** 2 <= 1.0] = 4.5
+        m = (1.0 / v**2).ravel(order="F")
+        w = (0.1 * 2 * np.pi) / (h.max() * np.sqrt(m.max()))
+        return dict(dim=dim, cells=cells, nodes=nodes, h=h, m=m, w=w)
     rng = np.random.default_rng(seed)
     # layered model with depth along the last axis
     nl = 12
@@ -85,7 +97,9 @@ def sources(P: dict, nrhs: int, seed: int) -> np.ndarray:
     N = int(np.prod(nodes))
     B = np.zeros((N, nrhs), dtype=np.complex128, order="F")
     amp = 1.0 / float(np.linalg.norm(P["h"])) ** 2
-    if P["dim"] == 2:
+    if P["dim"] == 2 and nrhs == 1:
+        B[(nodes[0] - 1) // 2 + nodes[0] * 2, 0] = amp  # (0.5, 2h)
+    elif P["dim"] == 2:
         xs = np.linspace(nodes[0] * 0.05, nodes[0] * 0.95, nrhs).astype(np.int64)
         for c in range(nrhs):
             B[int(xs[c]) + nodes[0] * 1, c] = amp

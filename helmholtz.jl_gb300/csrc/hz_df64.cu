@@ -642,6 +642,63 @@ void launch_inplace_df(Ctx& ctx, long long n, double2* a) {
   HZ_LAUNCH(ctx, "cast", (double)n * 32.0, k_inplace_df, (unsigned)nb, 256, 0, n, a);
 }
 
+// ---- solution update x += sum_i y_i Z_i (Z complex FP32, x FP64) -----------------
+__global__ void __launch_bounds__(256) k_update_x_df(long long N, const float2* __restrict__ Z, long long zstride,
+                                                     long long ld, const int* __restrict__ kcol,
+                                                     const double2* __restrict__ y, int ystride,
+                                                     double2* __restrict__ x, long long xld,
+                                                     const int* __restrict__ cols) {
+  const int c = cols[blockIdx.y];
+  const int k = kcol[c];
+  float yrh[KG], yrl[KG], yih[KG], yil[KG];
+#pragma unroll
+  for (int s = 0; s < KG; ++s) {
+    const double2 v = (s < k) ? y[(long long)c * ystride + s] : mk<double>(0, 0);
+    split(v.x, yrh[s], yrl[s]);
+    split(v.y, yih[s], yil[s]);
+  }
+  double2* xc = x + (long long)c * xld;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
+    DAcc re, im;
+    re.init(0.f, 0.f);
+    im.init(0.f, 0.f);
+#pragma unroll
+    for (int s = 0; s < KG; ++s) {
+      if (s < k) {
+        const float2 z = Z[((long long)s * zstride + c) * ld + p];
+        // (yr + i yi)(zr + i zi)
+        re.mac1(yrh[s], yrl[s], z.x);
+        re.mac1(-yih[s], -yil[s], z.y);
+        im.mac1(yrh[s], yrl[s], z.y);
+        im.mac1(yih[s], yil[s], z.x);
+      }
+    }
+    for (int s = KG; s < k; ++s) {  // restart lengths above KG
+      const double2 v = y[(long long)c * ystride + s];
+      float a, b2, e, f;
+      split(v.x, a, b2);
+      split(v.y, e, f);
+      const float2 z = Z[((long long)s * zstride + c) * ld + p];
+      re.mac1(a, b2, z.x);
+      re.mac1(-e, -f, z.y);
+      im.mac1(a, b2, z.y);
+      im.mac1(e, f, z.x);
+    }
+    const double2 xv = xc[p];
+    xc[p] = mk<double>(xv.x + re.to_double(), xv.y + im.to_double());
+  }
+}
+
+void launch_update_x_df(Ctx& ctx, long long N, const float2* Z, long long zstride, long long ld, const int* kcol,
+                        const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols,
+                        long long zcols) {
+  if (ncols <= 0) return;
+  const int nb = std::max(1, std::min((int)((N + 255) / 256), 8 * kSMs / std::max(ncols, 1) + 1));
+  const double bytes = (double)N * (ncols * 2.0 * 16.0 + zcols * 8.0);
+  HZ_LAUNCH(ctx, "update_x", bytes, k_update_x_df, dim3(nb, ncols), 256, 0, N, Z, zstride, ld, kcol, y, ystride, x,
+            xld, cols);
+}
+
 // ---- conversions and scaling -------------------------------------------------
 // y[:, c] = s[c] * x[:, c]: FP64 x into a df64 y (the start vector of a cycle)
 __global__ void __launch_bounds__(256) k_to_df(long long N, const double2* __restrict__ x, long long xld,

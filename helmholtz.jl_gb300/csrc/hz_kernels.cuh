@@ -119,6 +119,10 @@ void launch_to_df(Ctx& ctx, long long N, const double2* x, long long xld, float4
                   const int* cols, int ncols);
 void launch_scale_df(Ctx& ctx, long long N, float4* w, long long ld, const double* s, const int* cols, int ncols);
 void launch_diag_to_df(Ctx& ctx, long long N, const double2* d, float4* out);
+// x += sum_{i<kcol[c]} y_i Z_i with the products and their sum in df64, x FP64.
+void launch_update_x_df(Ctx& ctx, long long N, const float2* Z, long long zstride, long long ld, const int* kcol,
+                        const double2* y, int ystride, double2* x, long long xld, const int* cols, int ncols,
+                        long long zcols);
 // Coarsest solve as a dense emulated-FP64 product x = Ainv b (Ainv column-major
 // df64); part holds dense_df_splits(N, ncols) * ncols * N FP64 values.
 int dense_df_splits(long long N, int ncols);

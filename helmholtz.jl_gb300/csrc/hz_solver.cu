@@ -857,7 +857,10 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
                h->yv.as<double2>());
     long long zcols = 0;
     for (int c : act) zcols += kcol[c];
-    if (mixed)
+    if (df)
+      launch_update_x_df(h->ctx, N, (const float2*)h->Z.p, vstride, N, h->kcol.as<int>(), h->yv.as<double2>(), m, X,
+                         N, dc, (int)act.size(), zcols);
+    else if (mixed)
       launch_update_x<float>(h->ctx, N, (const float2*)h->Z.p, vstride, N, h->kcol.as<int>(), h->yv.as<double2>(), m,
                              X, N, dc, (int)act.size(), zcols);
     else
