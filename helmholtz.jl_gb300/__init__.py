@@ -13,6 +13,7 @@ from .api import (GetHelmholtzOperator, GetHelmholtzShiftOP, HelmholtzOperator, 
                   getShiftedHelmholtzParam, getShiftedLaplacianMultigridSolver, getSommerfeldBC, getTopPointSrc,
                   helmholtz_mass, loc2cs, solveLinearSystem, solveLinearSystemInPlace)
 from . import _lib  # noqa: F401
+from . import learned  # noqa: F401
 
 __all__ = [
     "GetHelmholtzOperator", "GetHelmholtzShiftOP", "HelmholtzOperator", "HelmholtzParam", "MGparam", "RegularMesh",

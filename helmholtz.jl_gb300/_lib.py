@@ -110,6 +110,20 @@ SIGNATURES = {
     "hz_kernel_times": (C.c_int, [_vp, C.c_int32, C.c_char_p, C.c_int32, _i64p, _i64p, _dp, _dp]),
     "hz_reset_kernel_times": (C.c_int, [_vp]),
     "hz_set_profile": (C.c_int, [_vp, C.c_int32]),
+    "hz_net_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(_vp)]),
+    "hz_net_destroy": (C.c_int, [_vp]),
+    "hz_net_num_params": (C.c_int64, []),
+    "hz_net_layer_shape": (C.c_int, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "hz_net_get_weights": (C.c_int, [_vp, _vp]),
+    "hz_net_set_weights": (C.c_int, [_vp, _vp]),
+    "hz_net_forward": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int32, C.c_int32]),
+    "hz_net_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _dp, _vp]),
+    "hz_net_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_double,
+                               C.c_int32, _dp]),
+    "hz_attach_net": (C.c_int, [_vp, _vp, C.c_int32, C.c_double]),
+    "hz_learned_stats": (C.c_int, [_vp, _i64p, C.POINTER(C.c_int32)]),
+    "hz_collect_pairs": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64,
+                                   _vp, _vp, _dp, _dp, _i64p]),
     "hz_max_frequency": (C.c_double, [_dp, C.c_int64, _dp, C.c_int32]),
     "hz_abl": (C.c_int, [C.c_int32, _i64p, C.c_int32, _i64p, C.c_double, _dp]),
     "hz_sommerfeld": (C.c_int, [C.c_int32, _i64p, _dp, _dp, C.c_double, C.c_int32, C.c_int32, _dp]),

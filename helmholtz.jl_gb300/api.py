@@ -427,6 +427,7 @@ class ShiftedLaplacianMultigridSolver:
     last_stats: object = field(default=None, repr=False)
     last_relres: np.ndarray | None = field(default=None, repr=False)
     last_iters: np.ndarray | None = field(default=None, repr=False)
+    learned: object = field(default=None, repr=False)  # (CoarseNet, level, stag_ratio): learned.attach
 
     def __del__(self):
         _release(self)
@@ -502,6 +503,9 @@ def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
     L.check(L.load().hz_create(C.byref(p), C.byref(o), C.byref(h)))
     s._handle = h
     s._key = key
+    if s.learned is not None:
+        from .learned import _apply
+        _apply(s)
     return h
 
 

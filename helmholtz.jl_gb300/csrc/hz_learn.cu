@@ -1,0 +1,839 @@
+// Learned coarse-grid correction: a small 2D convolutional encoder-decoder
+// with BF16 weights and activations and FP32 accumulation, trained on the GPU
+// by the kernels of this file, and applied inside the multigrid cycle in place
+// of the coarse-grid correction below a chosen level.
+//
+// Network (grids g0 -> g1 -> g2 -> g3 by node coarsening n -> (n-1)/2+1; NHWC
+// activations, channel counts padded to multiples of 16 for the tensor cores):
+//   e0 = relu(conv(x,  4 -> 16))          on g0
+//   e1 = relu(conv(R e0, 16 -> 32))       on g1     R: full weighting per channel
+//   e2 = relu(conv(R e1, 32 -> 64))       on g2
+//   e3 = relu(conv(R e2, 64 -> 64))       on g3
+//   d2 = relu(conv([P e3, e2], 128 -> 64)) on g2    P: bilinear prolongation per channel
+//   d1 = relu(conv([P d2, e1],  96 -> 32)) on g1
+//   d0 = relu(conv([P d1, e0],  48 -> 16)) on g0
+//   y  = conv(d0, 16 -> 2)                on g0     (Re, Im)
+// No biases: the map is positively homogeneous, and the solver feeds it the
+// residual scaled to unit RMS and scales the output back.  The skip tensors
+// e0, e1, e2 are written straight into the upper channels of the concatenation
+// buffers, so the decoder needs no copies.
+//
+// Convolutions (3x3, zero padding) are implicit GEMMs on the tensor cores
+// (mma.sync m16n8k16, BF16 x BF16 -> FP32): one warp computes 16 nodes x 8*NT
+// output channels, the 9 taps x Cin/16 K-steps reading the input rows and the
+// weight rows straight from L1/L2.  The data gradient is the same kernel with
+// flipped taps and transposed weights; the weight gradient is an FP32
+// reduction over the nodes.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <stdexcept>
+#include <vector>
+
+#include "hz_launch.cuh"
+#include "hz_learn.h"
+
+namespace hz {
+
+using bf16 = __nv_bfloat16;
+
+namespace {
+
+struct LayerSpec {
+  int cin, cout, cinp, coutp, lev;
+};
+// the 8 convolutions in forward order; cinp: input channels padded to 16, coutp: outputs padded to 8
+constexpr LayerSpec kSpec[CoarseNet::kLayers] = {
+    {4, 16, 16, 16, 0},    {16, 32, 16, 32, 1}, {32, 64, 32, 64, 2}, {64, 64, 64, 64, 3},
+    {128, 64, 128, 64, 2}, {96, 32, 96, 32, 1}, {48, 16, 48, 16, 0}, {16, 2, 16, 8, 0},
+};
+inline int round16(int c) { return (c + 15) / 16 * 16; }
+
+// activation slots: buffer, grid level and channel count
+enum Slot { X = 0, C0, R0, C1, R1, C2, R2, E3, D2, D1, D0, NSLOT };
+constexpr int kSlotLev[NSLOT] = {0, 0, 1, 1, 2, 2, 3, 3, 2, 1, 0};
+constexpr int kSlotCh[NSLOT] = {16, 48, 16, 96, 32, 128, 64, 64, 64, 32, 16};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// conv3x3 on the tensor cores
+//   in  [B][N] rows of ldi bf16, channels i_off .. i_off+Cin (Cin multiple of 16)
+//   w   [Cout][9][Cin] bf16
+//   out [B][N] rows of ldo, channels o_off + co (bf16, or FP32 into out32)
+// epilogue: optional ReLU; optional mask: zero where mask[row*ldm + m_off + co] <= 0
+// for co >= mask_lo.  grid.z splits Cout in chunks of 8*NT.
+// ---------------------------------------------------------------------------
+template <int NT>
+__global__ void __launch_bounds__(128) k_conv_mma(int nx, int ny, int Cin, int Cout, const bf16* __restrict__ in,
+                                                  int ldi, int i_off, const bf16* __restrict__ w,
+                                                  bf16* __restrict__ out, float* __restrict__ out32, int ldo,
+                                                  int o_off, int relu, const bf16* __restrict__ mask, int ldm,
+                                                  int m_off, int mask_lo) {
+  const int N = nx * ny;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int p0 = (blockIdx.x * 4 + warp) * 16;
+  const int bidx = blockIdx.y;
+  const int co0 = blockIdx.z * 8 * NT;
+  if (p0 >= N) return;
+  const int g = lane >> 2, tq = lane & 3;
+  const bf16* inb = in + (long long)bidx * N * ldi + i_off;
+  const int pa = p0 + g, pb = p0 + g + 8;
+  const int ia = pa % nx, ja = pa / nx, ib = pb % nx, jb = pb / nx;
+  float acc[NT][4];
+#pragma unroll
+  for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+  for (int t = 0; t < 9; ++t) {
+    const int dx = t % 3 - 1, dy = t / 3 - 1;
+    const bool va = pa < N && ia + dx >= 0 && ia + dx < nx && ja + dy >= 0 && ja + dy < ny;
+    const bool vb = pb < N && ib + dx >= 0 && ib + dx < nx && jb + dy >= 0 && jb + dy < ny;
+    const bf16* ra = inb + (long long)(va ? (pa + dx + dy * nx) : 0) * ldi;
+    const bf16* rb = inb + (long long)(vb ? (pb + dx + dy * nx) : 0) * ldi;
+    for (int c0 = 0; c0 < Cin; c0 += 16) {
+      const int ca = c0 + tq * 2;
+      const unsigned a0 = va ? *reinterpret_cast<const unsigned*>(ra + ca) : 0u;
+      const unsigned a1 = vb ? *reinterpret_cast<const unsigned*>(rb + ca) : 0u;
+      const unsigned a2 = va ? *reinterpret_cast<const unsigned*>(ra + ca + 8) : 0u;
+      const unsigned a3 = vb ? *reinterpret_cast<const unsigned*>(rb + ca + 8) : 0u;
+#pragma unroll
+      for (int n = 0; n < NT; ++n) {
+        const int co = co0 + n * 8 + g;
+        unsigned b0 = 0u, b1 = 0u;
+        if (co < Cout) {
+          const bf16* wr = w + ((long long)co * 9 + t) * Cin + ca;
+          b0 = *reinterpret_cast<const unsigned*>(wr);
+          b1 = *reinterpret_cast<const unsigned*>(wr + 8);
+        }
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+            "{%0,%1,%2,%3};\n"
+            : "+f"(acc[n][0]), "+f"(acc[n][1]), "+f"(acc[n][2]), "+f"(acc[n][3])
+            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+      }
+    }
+  }
+#pragma unroll
+  for (int n = 0; n < NT; ++n) {
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const int p = hh ? pb : pa;
+      if (p >= N) continue;
+      const long long row = (long long)bidx * N + p;
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int co = co0 + n * 8 + tq * 2 + e;
+        if (co >= Cout) continue;
+        float v = acc[n][hh * 2 + e];
+        if (relu) v = fmaxf(v, 0.f);
+        if (mask && co >= mask_lo && !(__bfloat162float(mask[row * ldm + m_off + co]) > 0.f)) v = 0.f;
+        if (out32)
+          out32[row * ldo + o_off + co] = v;
+        else
+          out[row * ldo + o_off + co] = __float2bfloat16_rn(v);
+      }
+    }
+  }
+}
+
+static void conv_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi,
+                        int i_off, int Cout, const bf16* w, bf16* out, float* out32, int ldo, int o_off, int relu,
+                        const bf16* mask, int ldm, int m_off, int mask_lo) {
+  if (Cin % 16 != 0 || (ldi % 2) || (i_off % 2)) throw std::runtime_error("conv: channel layout not aligned");
+  const int N = nx * ny;
+  const int tiles = (N + 15) / 16;
+  const int NT = Cout <= 8 ? 1 : Cout <= 16 ? 2 : Cout <= 32 ? 4 : 8;
+  const dim3 grid((unsigned)((tiles + 3) / 4), (unsigned)B, (unsigned)((Cout + 8 * NT - 1) / (8 * NT)));
+  const double bytes = (double)B * N * (Cin * 2.0 + Cout * (out32 ? 4.0 : 2.0)) + 9.0 * Cin * Cout * 2.0;
+  switch (NT) {
+    case 1:
+      HZ_LAUNCH(ctx, name, bytes, k_conv_mma<1>, grid, 128, 0, nx, ny, Cin, Cout, in, ldi, i_off, w, out, out32, ldo,
+                o_off, relu, mask, ldm, m_off, mask_lo);
+      break;
+    case 2:
+      HZ_LAUNCH(ctx, name, bytes, k_conv_mma<2>, grid, 128, 0, nx, ny, Cin, Cout, in, ldi, i_off, w, out, out32, ldo,
+                o_off, relu, mask, ldm, m_off, mask_lo);
+      break;
+    case 4:
+      HZ_LAUNCH(ctx, name, bytes, k_conv_mma<4>, grid, 128, 0, nx, ny, Cin, Cout, in, ldi, i_off, w, out, out32, ldo,
+                o_off, relu, mask, ldm, m_off, mask_lo);
+      break;
+    default:
+      HZ_LAUNCH(ctx, name, bytes, k_conv_mma<8>, grid, 128, 0, nx, ny, Cin, Cout, in, ldi, i_off, w, out, out32, ldo,
+                o_off, relu, mask, ldm, m_off, mask_lo);
+      break;
+  }
+}
+
+// weights of the data-gradient convolution: wt[ci][t][co] = w[co][8 - t][ci],
+// co padded from Cout to K (zero rows)
+__global__ void k_wflip(int Cout, int Cin, int K, const bf16* __restrict__ w, bf16* __restrict__ wt) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= Cin * 9 * K) return;
+  const int co = idx % K, t = (idx / K) % 9, ci = idx / (K * 9);
+  wt[idx] = (co < Cout) ? w[((long long)co * 9 + (8 - t)) * Cin + ci] : __float2bfloat16_rn(0.f);
+}
+
+// weight gradient dw[co][t][ci] += sum over the nodes of a chunk of
+// dout[n][co] * in[n + off_t][ci]  (FP32; one thread per weight, atomics per chunk)
+__global__ void __launch_bounds__(256) k_wgrad(int nx, int ny, int B, int Cin, int Cout, const bf16* __restrict__ in,
+                                               int ldi, int i_off, const bf16* __restrict__ dout, int ldd, int d_off,
+                                               float* __restrict__ dw, int chunk) {
+  const int N = nx * ny;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= Cout * 9 * Cin) return;
+  const int ci = idx % Cin, t = (idx / Cin) % 9, co = idx / (Cin * 9);
+  const int dx = t % 3 - 1, dy = t / 3 - 1;
+  const long long n0 = (long long)blockIdx.y * chunk;
+  const long long n1 = min((long long)N * B, n0 + chunk);
+  float acc = 0.f;
+  for (long long q = n0; q < n1; ++q) {
+    const int p = (int)(q % N);
+    const int i = p % nx + dx, j = p / nx + dy;
+    if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
+    const float d = __bfloat162float(dout[q * ldd + d_off + co]);
+    const float x = __bfloat162float(in[(q + dx + (long long)dy * nx) * ldi + i_off + ci]);
+    acc = fmaf(d, x, acc);
+  }
+  atomicAdd(&dw[idx], acc);
+}
+
+// Per-channel resampling between grid levels (NHWC bf16, FP32 arithmetic).
+// mode 0, restriction (fine -> coarse): full weighting with weights 1, 1/2 per
+// axis, normalised by the weights that fall inside the grid.
+// mode 1, prolongation (coarse -> fine): bilinear, (c[i0] + c[i1]) / 2 per axis
+// with i0 = i / 2, i1 = (i + 1) / 2.
+// transpose = 1 applies the adjoint (fine <- coarse for mode 0, coarse <- fine for
+// mode 1).  The result, zeroed where mask <= 0 (mask may be null), is written or,
+// with accum, added to out (rounded to bf16 once).
+__device__ __forceinline__ float fw_wsum(int I, int J, int nxf, int nyf) {
+  const float sx = 1.f + (2 * I - 1 >= 0 ? 0.5f : 0.f) + (2 * I + 1 < nxf ? 0.5f : 0.f);
+  const float sy = 1.f + (2 * J - 1 >= 0 ? 0.5f : 0.f) + (2 * J + 1 < nyf ? 0.5f : 0.f);
+  return sx * sy;
+}
+
+__global__ void k_resample(int mode, int transpose, int nxf, int nyf, int nxc, int nyc, int B, int C,
+                           const bf16* __restrict__ in, int ldi, int i_off, bf16* __restrict__ out, int ldo, int o_off,
+                           int accum, const bf16* __restrict__ mask, int ldm, int m_off) {
+  const int Nf = nxf * nyf, Nc = nxc * nyc;
+  const bool to_coarse = (mode == 0) != (transpose != 0);
+  const int No = to_coarse ? Nc : Nf, Ni = to_coarse ? Nf : Nc;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)B * No * C) return;
+  const int c = (int)(idx % C);
+  const long long q = idx / C;
+  const int b = (int)(q / No), po = (int)(q % No);
+  const bf16* ib = in + (long long)b * Ni * ldi + i_off + c;
+  auto rd = [&](int p) { return __bfloat162float(ib[(long long)p * ldi]); };
+  float v = 0.f;
+  if (mode == 0 && !transpose) {  // restriction
+    const int I = po % nxc, J = po / nxc;
+    for (int dj = -1; dj <= 1; ++dj)
+      for (int di = -1; di <= 1; ++di) {
+        const int fi = 2 * I + di, fj = 2 * J + dj;
+        if (fi < 0 || fi >= nxf || fj < 0 || fj >= nyf) continue;
+        v += (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) * rd(fi + fj * nxf);
+      }
+    v /= fw_wsum(I, J, nxf, nyf);
+  } else if (mode == 0) {  // adjoint of the restriction: fine <- coarse parents I with |i - 2I| <= 1
+    const int i = po % nxf, j = po / nxf;
+    for (int J = j / 2 - 1; J <= j / 2 + 1; ++J)
+      for (int I = i / 2 - 1; I <= i / 2 + 1; ++I) {
+        if (I < 0 || I >= nxc || J < 0 || J >= nyc) continue;
+        const int di = i - 2 * I, dj = j - 2 * J;
+        if (di < -1 || di > 1 || dj < -1 || dj > 1) continue;
+        v += (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) / fw_wsum(I, J, nxf, nyf) * rd(I + J * nxc);
+      }
+  } else if (!transpose) {  // prolongation
+    const int i = po % nxf, j = po / nxf;
+    const int i0 = i >> 1, i1 = (i + 1) >> 1, j0 = j >> 1, j1 = (j + 1) >> 1;
+    v = 0.25f * (rd(i0 + j0 * nxc) + rd(i1 + j0 * nxc) + rd(i0 + j1 * nxc) + rd(i1 + j1 * nxc));
+  } else {  // adjoint of the prolongation: coarse <- fine children
+    const int I = po % nxc, J = po / nxc;
+    for (int fj = 2 * J - 1; fj <= 2 * J + 1; ++fj)
+      for (int fi = 2 * I - 1; fi <= 2 * I + 1; ++fi) {
+        if (fi < 0 || fi >= nxf || fj < 0 || fj >= nyf) continue;
+        v += (fi == 2 * I ? 1.f : 0.5f) * (fj == 2 * J ? 1.f : 0.5f) * rd(fi + fj * nxf);
+      }
+  }
+  const long long row = (long long)b * No + po;
+  if (mask && !(__bfloat162float(mask[row * ldm + m_off + c]) > 0.f)) v = 0.f;
+  const long long o = row * ldo + o_off + c;
+  if (accum) v += __bfloat162float(out[o]);
+  out[o] = __float2bfloat16_rn(v);
+}
+
+static void resample(Ctx& ctx, int mode, int transpose, const int* gx, const int* gy, int lf, int B, int C,
+                     const bf16* in, int ldi, int i_off, bf16* out, int ldo, int o_off, int accum,
+                     const bf16* mask = nullptr, int ldm = 0, int m_off = 0) {
+  const int nxf = gx[lf], nyf = gy[lf], nxc = gx[lf + 1], nyc = gy[lf + 1];
+  const bool to_coarse = (mode == 0) != (transpose != 0);
+  const long long no = to_coarse ? (long long)nxc * nyc : (long long)nxf * nyf;
+  const long long ni = to_coarse ? (long long)nxf * nyf : (long long)nxc * nyc;
+  const long long total = (long long)B * no * C;
+  HZ_LAUNCH(ctx, "net_resample", (double)B * (no + ni) * C * 2.0, k_resample, (unsigned)((total + 255) / 256), 256, 0,
+            mode, transpose, nxf, nyf, nxc, nyc, B, C, in, ldi, i_off, out, ldo, o_off, accum, mask, ldm, m_off);
+}
+
+// input assembly: X[b][p][0..16) = (x4[b][p][0..4), 0...) in bf16
+__global__ void k_pack_in(long long BN, const float4* __restrict__ x4, bf16* __restrict__ x16) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= BN) return;
+  const float4 v = x4[i];
+  __align__(16) __nv_bfloat162 q[8];
+  q[0] = __floats2bfloat162_rn(v.x, v.y);
+  q[1] = __floats2bfloat162_rn(v.z, v.w);
+#pragma unroll
+  for (int k = 2; k < 8; ++k) q[k] = __floats2bfloat162_rn(0.f, 0.f);
+  uint4* dst = reinterpret_cast<uint4*>(x16 + i * 16);
+  dst[0] = *reinterpret_cast<uint4*>(&q[0]);
+  dst[1] = *reinterpret_cast<uint4*>(&q[4]);
+}
+
+// loss_b = ||y_b - t_b||^2 / ||t_b||^2 (channels 0, 1 of y) accumulated as the
+// batch mean into *loss, and the output gradient dy = 2 (y - t) / ||t_b||^2 / B
+// as bf16 into 16-channel rows (channels 2..15 zero).
+__global__ void __launch_bounds__(256) k_loss(int N, int B, const float* __restrict__ y, const float* __restrict__ t,
+                                              bf16* __restrict__ dy, double* __restrict__ loss) {
+  const int b = blockIdx.x;
+  __shared__ double sh_e[256], sh_t[256];
+  double e = 0.0, tt = 0.0;
+  for (int p = threadIdx.x; p < N; p += blockDim.x) {
+    const long long r = (long long)b * N + p;
+    for (int c = 0; c < 2; ++c) {
+      const double tv = t[r * 2 + c];
+      const double d = (double)y[r * 8 + c] - tv;
+      e += d * d;
+      tt += tv * tv;
+    }
+  }
+  sh_e[threadIdx.x] = e;
+  sh_t[threadIdx.x] = tt;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sh_e[threadIdx.x] += sh_e[threadIdx.x + s];
+      sh_t[threadIdx.x] += sh_t[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  const double tn = sh_t[0] > 0.0 ? sh_t[0] : 1.0;
+  if (threadIdx.x == 0) atomicAdd(loss, sh_e[0] / tn / B);
+  const double sc = 2.0 / tn / B;
+  for (int p = threadIdx.x; p < N; p += blockDim.x) {
+    const long long r = (long long)b * N + p;
+    __align__(16) __nv_bfloat162 q[8];
+    q[0] = __floats2bfloat162_rn((float)(sc * ((double)y[r * 8] - t[r * 2])),
+                                 (float)(sc * ((double)y[r * 8 + 1] - t[r * 2 + 1])));
+#pragma unroll
+    for (int k = 1; k < 8; ++k) q[k] = __floats2bfloat162_rn(0.f, 0.f);
+    uint4* dst = reinterpret_cast<uint4*>(dy + r * 16);
+    dst[0] = *reinterpret_cast<uint4*>(&q[0]);
+    dst[1] = *reinterpret_cast<uint4*>(&q[4]);
+  }
+}
+
+// Adam on the FP32 master weights; the BF16 copy is refreshed in the same pass
+__global__ void k_adam(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, bf16* __restrict__ wb, float lr, float b1, float b2, float eps, float c1,
+                       float c2) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    wb[i] = __float2bfloat16_rn(wi);
+  }
+}
+
+__global__ void k_f2bf(long long n, const float* __restrict__ a, bf16* __restrict__ b) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = __float2bfloat16_rn(a[i]);
+}
+
+// mini-batch gather of training pairs: rows perm[k] of x (4 floats per node) and t (2 per node)
+__global__ void k_gather_pairs(int B, long long N, const int* __restrict__ perm, const float4* __restrict__ x,
+                               const float2* __restrict__ t, float4* __restrict__ bx, float2* __restrict__ bt) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)B * N) return;
+  const int k = (int)(i / N);
+  const long long p = i % N;
+  const long long src = (long long)perm[k] * N + p;
+  bx[i] = x[src];
+  bt[i] = t[src];
+}
+
+// ---------------------------------------------------------------------------
+// CoarseNet
+// ---------------------------------------------------------------------------
+long long CoarseNet::num_params() {
+  long long n = 0;
+  for (const auto& L : kSpec) n += (long long)L.cout * 9 * L.cin;
+  return n;
+}
+
+void CoarseNet::layer_shape(int l, int* cin, int* cout) {
+  *cin = kSpec[l].cin;
+  *cout = kSpec[l].cout;
+}
+
+bool CoarseNet::supports(long long nx, long long ny) {
+  return nx >= 9 && ny >= 9 && (nx - 1) % 8 == 0 && (ny - 1) % 8 == 0 && nx * ny < (1LL << 30);
+}
+
+static void cuda_ok(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw std::runtime_error(std::string("coarse net: ") + what + ": " + cudaGetErrorString(e));
+  }
+}
+
+template <typename P> static void dalloc(P** p, size_t bytes) {
+  cuda_ok(cudaMalloc(reinterpret_cast<void**>(p), bytes), "cudaMalloc");
+}
+template <typename P> static void dfree(P*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+CoarseNet::CoarseNet(unsigned seed) {
+  cuda_ok(cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking), "stream");
+  long long off = 0;
+  for (int l = 0; l < kLayers; ++l) {
+    woff_[l] = off;
+    off += (long long)kSpec[l].coutp * 9 * kSpec[l].cinp;
+  }
+  wtotal_ = off;
+  dalloc(&w32_, off * 4);
+  dalloc(&wbf_, off * 2);
+  dalloc(&g32_, off * 4);
+  dalloc(&m_, off * 4);
+  dalloc(&v_, off * 4);
+  // He-normal initialisation (last layer scaled down), from a seeded host generator
+  std::vector<float> w((size_t)num_params());
+  std::mt19937 rng(seed);
+  size_t k = 0;
+  for (int l = 0; l < kLayers; ++l) {
+    const auto& L = kSpec[l];
+    std::normal_distribution<float> nd(0.f, std::sqrt(2.0f / (9.0f * L.cin)) * (l == kLayers - 1 ? 0.5f : 1.0f));
+    for (long long q = 0; q < (long long)L.cout * 9 * L.cin; ++q) w[k++] = nd(rng);
+  }
+  set_weights(w.data());
+}
+
+CoarseNet::~CoarseNet() {
+  release_acts();
+  dfree(w32_);
+  dfree(wbf_);
+  dfree(g32_);
+  dfree(m_);
+  dfree(v_);
+  dfree(wt_);
+  dfree(x4_);
+  dfree(scale_);
+  dfree(loss_);
+  dfree(bx_);
+  dfree(bt_);
+  dfree(perm_);
+  ctx.release();
+  if (ctx.stream) cudaStreamDestroy(ctx.stream);
+}
+
+void CoarseNet::set_weights(const float* host) {
+  std::vector<float> w((size_t)wtotal_, 0.f);
+  size_t k = 0;
+  for (int l = 0; l < kLayers; ++l) {
+    const auto& L = kSpec[l];
+    for (int co = 0; co < L.cout; ++co)
+      for (int t = 0; t < 9; ++t)
+        for (int ci = 0; ci < L.cin; ++ci) w[(size_t)(woff_[l] + ((long long)co * 9 + t) * L.cinp + ci)] = host[k++];
+  }
+  cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
+  cuda_ok(cudaMemcpy(w32_, w.data(), wtotal_ * 4, cudaMemcpyHostToDevice), "upload weights");
+  cuda_ok(cudaMemset(m_, 0, wtotal_ * 4), "adam m");
+  cuda_ok(cudaMemset(v_, 0, wtotal_ * 4), "adam v");
+  step_ = 0;
+  k_f2bf<<<256, 256, 0, ctx.stream>>>(wtotal_, w32_, wbf_);
+  cuda_ok(cudaGetLastError(), "weights to bf16");
+  cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
+}
+
+static void unpack_padded(const std::vector<float>& w, const long long* woff, float* host) {
+  size_t k = 0;
+  for (int l = 0; l < CoarseNet::kLayers; ++l) {
+    const auto& L = kSpec[l];
+    for (int co = 0; co < L.cout; ++co)
+      for (int t = 0; t < 9; ++t)
+        for (int ci = 0; ci < L.cin; ++ci) host[k++] = w[(size_t)(woff[l] + ((long long)co * 9 + t) * L.cinp + ci)];
+  }
+}
+
+void CoarseNet::get_weights(float* host) const {
+  std::vector<float> w((size_t)wtotal_);
+  cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
+  cuda_ok(cudaMemcpy(w.data(), w32_, wtotal_ * 4, cudaMemcpyDeviceToHost), "download weights");
+  unpack_padded(w, woff_, host);
+}
+
+void CoarseNet::get_grad(float* host) const {
+  std::vector<float> w((size_t)wtotal_);
+  cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
+  cuda_ok(cudaMemcpy(w.data(), g32_, wtotal_ * 4, cudaMemcpyDeviceToHost), "download gradient");
+  unpack_padded(w, woff_, host);
+}
+
+void CoarseNet::release_acts() {
+  for (int i = 0; i < NSLOT; ++i) {
+    dfree(act_[i]);
+    dfree(grd_[i]);
+  }
+  dfree(y32_);
+  nx_ = ny_ = B_ = 0;
+  grads_ = false;
+}
+
+void CoarseNet::ensure(int nx, int ny, int B, bool grads) {
+  if (!supports(nx, ny)) throw std::runtime_error("coarse net: grid must have (n - 1) divisible by 8, n >= 9");
+  if (nx == nx_ && ny == ny_ && B <= B_ && (grads_ || !grads)) return;
+  cudaDeviceSynchronize();  // buffers may be in use on the caller's stream
+  release_acts();
+  nx_ = nx;
+  ny_ = ny;
+  B_ = B;
+  grads_ = grads;
+  gx_[0] = nx;
+  gy_[0] = ny;
+  for (int l = 1; l < 4; ++l) {
+    gx_[l] = (gx_[l - 1] - 1) / 2 + 1;
+    gy_[l] = (gy_[l - 1] - 1) / 2 + 1;
+  }
+  for (int i = 0; i < NSLOT; ++i) {
+    const size_t n = (size_t)B * gx_[kSlotLev[i]] * gy_[kSlotLev[i]] * kSlotCh[i];
+    dalloc(&act_[i], n * 2);
+    if (grads) dalloc(&grd_[i], n * 2);
+  }
+  dalloc(&y32_, (size_t)B * nx * ny * 8 * 4);
+  if (!loss_) dalloc(&loss_, 8);
+}
+
+float* CoarseNet::input_staging(int nx, int ny, int B) {
+  const long long need = (long long)B * nx * ny * 4;
+  if (need > x4cap_) {
+    cudaDeviceSynchronize();
+    dfree(x4_);
+    dalloc(&x4_, need * 4);
+    x4cap_ = need;
+  }
+  return x4_;
+}
+
+float* CoarseNet::scale_staging(int B) {
+  if (B > scalecap_) {
+    cudaDeviceSynchronize();
+    dfree(scale_);
+    dalloc(&scale_, (size_t)B * 4);
+    scalecap_ = B;
+  }
+  return scale_;
+}
+
+void CoarseNet::conv_fwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi, int i_off, bf16* out, int ldo,
+                         int o_off, int relu, float* out32) {
+  const auto& L = kSpec[l];
+  conv_launch(c, "net_conv_fwd", gx_[lev], gy_[lev], B, L.cinp, in, ldi, i_off, L.coutp, wbf_ + woff_[l], out, out32,
+              ldo, o_off, relu, nullptr, 0, 0, 0);
+}
+
+void CoarseNet::forward(Ctx& c, const float* x4, int nx, int ny, int B, bool train) {
+  ensure(nx, ny, B, train || (grads_ && nx == nx_ && ny == ny_));
+  const long long BN0 = (long long)B * nx * ny;
+  HZ_LAUNCH(c, "net_pack_in", (double)BN0 * 48.0, k_pack_in, (unsigned)((BN0 + 255) / 256), 256, 0, BN0,
+            reinterpret_cast<const float4*>(x4), act_[X]);
+  // encoder (skips written into the upper channels of the concatenation buffers)
+  conv_fwd(c, 0, 0, B, act_[X], 16, 0, act_[C0], 48, 32, 1, nullptr);
+  resample(c, 0, 0, gx_, gy_, 0, B, 16, act_[C0], 48, 32, act_[R0], 16, 0, 0);
+  conv_fwd(c, 1, 1, B, act_[R0], 16, 0, act_[C1], 96, 64, 1, nullptr);
+  resample(c, 0, 0, gx_, gy_, 1, B, 32, act_[C1], 96, 64, act_[R1], 32, 0, 0);
+  conv_fwd(c, 2, 2, B, act_[R1], 32, 0, act_[C2], 128, 64, 1, nullptr);
+  resample(c, 0, 0, gx_, gy_, 2, B, 64, act_[C2], 128, 64, act_[R2], 64, 0, 0);
+  conv_fwd(c, 3, 3, B, act_[R2], 64, 0, act_[E3], 64, 0, 1, nullptr);
+  // decoder
+  resample(c, 1, 0, gx_, gy_, 2, B, 64, act_[E3], 64, 0, act_[C2], 128, 0, 0);
+  conv_fwd(c, 4, 2, B, act_[C2], 128, 0, act_[D2], 64, 0, 1, nullptr);
+  resample(c, 1, 0, gx_, gy_, 1, B, 64, act_[D2], 64, 0, act_[C1], 96, 0, 0);
+  conv_fwd(c, 5, 1, B, act_[C1], 96, 0, act_[D1], 32, 0, 1, nullptr);
+  resample(c, 1, 0, gx_, gy_, 0, B, 32, act_[D1], 32, 0, act_[C0], 48, 0, 0);
+  conv_fwd(c, 6, 0, B, act_[C0], 48, 0, act_[D0], 16, 0, 1, nullptr);
+  conv_fwd(c, 7, 0, B, act_[D0], 16, 0, nullptr, 8, 0, 0, y32_);
+}
+
+// Weight gradient of layer l (in: its input, dout: gradient of its output), then
+// the data gradient into din (null: skipped), masked for channels >= mask_lo by
+// the input activation (ReLU derivative of the skip tensors).
+void CoarseNet::conv_bwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi, int i_off, const bf16* dout, int ldd,
+                         int d_off, bf16* din, int ldn, int n_off, const bf16* mask, int ldm, int mask_lo) {
+  const auto& L = kSpec[l];
+  const int nx = gx_[lev], ny = gy_[lev];
+  const long long nodes = (long long)nx * ny * B;
+  const int total = L.coutp * 9 * L.cinp;
+  const int chunk = (int)std::max<long long>(256, (nodes + 65534) / 65535);  // grid.y <= 65535
+  const dim3 grid((unsigned)((total + 255) / 256), (unsigned)((nodes + chunk - 1) / chunk));
+  HZ_LAUNCH(c, "net_wgrad", (double)nodes * (L.cinp + L.coutp) * 2.0, k_wgrad, grid, 256, 0, nx, ny, B, L.cinp,
+            L.coutp, in, ldi, i_off, dout, ldd, d_off, g32_ + woff_[l], chunk);
+  if (!din) return;
+  const int K = round16(L.coutp);
+  const int tot = L.cinp * 9 * K;
+  HZ_LAUNCH(c, "net_wflip", (double)tot * 4.0, k_wflip, (unsigned)((tot + 255) / 256), 256, 0, L.coutp, L.cinp, K,
+            wbf_ + woff_[l], wt_);
+  conv_launch(c, "net_conv_bwd", nx, ny, B, K, dout, ldd, d_off, L.cinp, wt_, din, nullptr, ldn, n_off, 0, mask, ldm,
+              i_off, mask_lo);
+}
+
+double CoarseNet::backward(Ctx& c, const float* t, int nx, int ny, int B) {
+  if (nx != nx_ || ny != ny_ || B > B_ || !grads_) throw std::runtime_error("coarse net: backward needs forward");
+  if (!wt_) {
+    long long mx = 0;
+    for (const auto& L : kSpec) mx = std::max(mx, (long long)L.cinp * 9 * round16(L.coutp));
+    dalloc(&wt_, mx * 2);
+  }
+  const int N0 = nx * ny;
+  cuda_ok(cudaMemsetAsync(loss_, 0, 8, c.stream), "loss reset");
+  cuda_ok(cudaMemsetAsync(g32_, 0, wtotal_ * 4, c.stream), "grad reset");
+  bf16* gY = grd_[X];  // the input needs no gradient: its slot holds dL/dy (16 channels)
+  HZ_LAUNCH(c, "net_loss", (double)N0 * B * 72.0, k_loss, B, 256, 0, N0, B, y32_, t, gY, loss_);
+  conv_bwd(c, 7, 0, B, act_[D0], 16, 0, gY, 16, 0, grd_[D0], 16, 0, act_[D0], 16, 0);
+  conv_bwd(c, 6, 0, B, act_[C0], 48, 0, grd_[D0], 16, 0, grd_[C0], 48, 0, act_[C0], 48, 32);
+  resample(c, 1, 1, gx_, gy_, 0, B, 32, grd_[C0], 48, 0, grd_[D1], 32, 0, 0, act_[D1], 32, 0);
+  conv_bwd(c, 5, 1, B, act_[C1], 96, 0, grd_[D1], 32, 0, grd_[C1], 96, 0, act_[C1], 96, 64);
+  resample(c, 1, 1, gx_, gy_, 1, B, 64, grd_[C1], 96, 0, grd_[D2], 64, 0, 0, act_[D2], 64, 0);
+  conv_bwd(c, 4, 2, B, act_[C2], 128, 0, grd_[D2], 64, 0, grd_[C2], 128, 0, act_[C2], 128, 64);
+  resample(c, 1, 1, gx_, gy_, 2, B, 64, grd_[C2], 128, 0, grd_[E3], 64, 0, 0, act_[E3], 64, 0);
+  conv_bwd(c, 3, 3, B, act_[R2], 64, 0, grd_[E3], 64, 0, grd_[R2], 64, 0, nullptr, 0, 0);
+  resample(c, 0, 1, gx_, gy_, 2, B, 64, grd_[R2], 64, 0, grd_[C2], 128, 64, 1, act_[C2], 128, 64);
+  conv_bwd(c, 2, 2, B, act_[R1], 32, 0, grd_[C2], 128, 64, grd_[R1], 32, 0, nullptr, 0, 0);
+  resample(c, 0, 1, gx_, gy_, 1, B, 32, grd_[R1], 32, 0, grd_[C1], 96, 64, 1, act_[C1], 96, 64);
+  conv_bwd(c, 1, 1, B, act_[R0], 16, 0, grd_[C1], 96, 64, grd_[R0], 16, 0, nullptr, 0, 0);
+  resample(c, 0, 1, gx_, gy_, 0, B, 16, grd_[R0], 16, 0, grd_[C0], 48, 32, 1, act_[C0], 48, 32);
+  conv_bwd(c, 0, 0, B, act_[X], 16, 0, grd_[C0], 48, 32, nullptr, 0, 0, nullptr, 0, 0);
+  double l = 0.0;
+  cuda_ok(cudaMemcpyAsync(&l, loss_, 8, cudaMemcpyDeviceToHost, c.stream), "loss");
+  cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+  c.resolve();
+  return l;
+}
+
+void CoarseNet::adam(Ctx& c, double lr) {
+  ++step_;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)step_), c2 = 1.f - std::pow(b2, (float)step_);
+  HZ_LAUNCH(c, "net_adam", (double)wtotal_ * 22.0, k_adam, 304, 256, 0, wtotal_, w32_, g32_, m_, v_, wbf_, (float)lr,
+            b1, b2, 1e-8f, c1, c2);
+}
+
+void CoarseNet::train(Ctx& c, const float* x, const float* t, int nx, int ny, long long nsamples, int batch,
+                      int epochs, double lr, unsigned seed, double* loss_hist) {
+  if (batch < 1 || nsamples < 1 || epochs < 1) throw std::runtime_error("coarse net: bad training sizes");
+  if (nsamples >= (1LL << 31)) throw std::runtime_error("coarse net: too many training pairs");
+  batch = (int)std::min<long long>(batch, nsamples);
+  const long long N = (long long)nx * ny;
+  if ((long long)batch * N * 4 > bcap_) {
+    cudaDeviceSynchronize();
+    dfree(bx_);
+    dfree(bt_);
+    dalloc(&bx_, (size_t)batch * N * 16);
+    dalloc(&bt_, (size_t)batch * N * 8);
+    bcap_ = (long long)batch * N * 4;
+  }
+  cudaDeviceSynchronize();
+  dfree(perm_);
+  dalloc(&perm_, (size_t)nsamples * sizeof(int));
+  ensure(nx, ny, batch, true);
+  std::mt19937 rng(seed);
+  std::vector<int> perm((size_t)nsamples);
+  const long long steps_per_epoch = nsamples / batch;
+  const long long total = steps_per_epoch * epochs;
+  long long it = 0;
+  for (int ep = 0; ep < epochs; ++ep) {
+    std::iota(perm.begin(), perm.end(), 0);
+    std::shuffle(perm.begin(), perm.end(), rng);
+    cuda_ok(cudaMemcpyAsync(perm_, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream), "perm");
+    double sum = 0.0;
+    for (long long s = 0; s < steps_per_epoch; ++s, ++it) {
+      const long long tot = (long long)batch * N;
+      HZ_LAUNCH(c, "net_gather", (double)tot * 48.0, k_gather_pairs, (unsigned)((tot + 255) / 256), 256, 0, batch, N,
+                perm_ + s * batch, reinterpret_cast<const float4*>(x), reinterpret_cast<const float2*>(t),
+                reinterpret_cast<float4*>(bx_), reinterpret_cast<float2*>(bt_));
+      forward(c, bx_, nx, ny, batch, true);
+      sum += backward(c, bt_, nx, ny, batch);
+      // cosine decay to lr / 20
+      const double f = total > 1 ? (double)it / (double)(total - 1) : 1.0;
+      adam(c, lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(M_PI * f))));
+    }
+    if (loss_hist) loss_hist[ep] = sum / (double)std::max<long long>(1, steps_per_epoch);
+  }
+  cuda_ok(cudaStreamSynchronize(c.stream), "sync");
+  c.resolve();
+}
+
+// ---------------------------------------------------------------------------
+// Solver-side packing
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_col_rms(long long N, const cplx<T>* __restrict__ b, long long ld,
+                                                 const int* __restrict__ cols, float* __restrict__ scale) {
+  const int k = blockIdx.x;
+  const cplx<T>* col = b + (long long)(cols ? cols[k] : k) * ld;
+  double s = 0.0;
+  for (long long p = threadIdx.x; p < N; p += blockDim.x) {
+    const double re = (double)col[p].x, im = (double)col[p].y;
+    s += re * re + im * im;
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) scale[k] = (float)sqrt(sh[0] / (double)N);
+}
+
+template <typename T>
+__global__ void k_net_pack(long long N, const cplx<T>* __restrict__ b, long long ld, const int* __restrict__ cols,
+                           int nc, const float2* __restrict__ feat, int conj, const float* __restrict__ scale,
+                           float4* __restrict__ x4) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)nc * N) return;
+  const int k = (int)(i / N);
+  const long long p = i % N;
+  const float s = scale[k];
+  const float inv = s > 0.f ? 1.f / s : 0.f;
+  const cplx<T> v = b[(long long)cols[k] * ld + p];
+  const float2 f = feat[p];
+  x4[i] = make_float4((float)v.x * inv, (conj ? -(float)v.y : (float)v.y) * inv, f.x, f.y);
+}
+
+template <typename T>
+__global__ void k_net_unpack(long long N, const float* __restrict__ y, const float* __restrict__ scale, double h2,
+                             int conj, cplx<T>* __restrict__ out, long long ld, const int* __restrict__ cols, int nc) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)nc * N) return;
+  const int k = (int)(i / N);
+  const long long p = i % N;
+  const double s = (double)scale[k] * h2;
+  const float2 v = *reinterpret_cast<const float2*>(y + i * 8);
+  out[(long long)cols[k] * ld + p] = mk<T>((T)(s * v.x), (T)(conj ? -s * v.y : s * v.y));
+}
+
+template <typename T>
+void launch_net_pack(Ctx& ctx, long long N, const cplx<T>* b, long long ld, const int* cols, int nc,
+                     const float2* feat, int conj, float* scale, float* x4) {
+  HZ_LAUNCH(ctx, "net_col_rms", (double)nc * N * sizeof(cplx<T>), k_col_rms<T>, nc, 256, 0, N, b, ld, cols, scale);
+  const long long tot = (long long)nc * N;
+  HZ_LAUNCH(ctx, "net_pack", (double)tot * (sizeof(cplx<T>) + 24.0), k_net_pack<T>, (unsigned)((tot + 255) / 256),
+            256, 0, N, b, ld, cols, nc, feat, conj, scale, reinterpret_cast<float4*>(x4));
+}
+
+template <typename T>
+void launch_net_unpack(Ctx& ctx, long long N, const float* y, const float* scale, double h2, int conj, cplx<T>* out,
+                       long long ld, const int* cols, int nc) {
+  const long long tot = (long long)nc * N;
+  HZ_LAUNCH(ctx, "net_unpack", (double)tot * (8.0 + sizeof(cplx<T>)), k_net_unpack<T>, (unsigned)((tot + 255) / 256),
+            256, 0, N, y, scale, h2, conj, out, ld, cols, nc);
+}
+
+template void launch_net_pack<float>(Ctx&, long long, const float2*, long long, const int*, int, const float2*, int,
+                                     float*, float*);
+template void launch_net_pack<double>(Ctx&, long long, const double2*, long long, const int*, int, const float2*, int,
+                                      float*, float*);
+template void launch_net_unpack<float>(Ctx&, long long, const float*, const float*, double, int, float2*, long long,
+                                       const int*, int);
+template void launch_net_unpack<double>(Ctx&, long long, const float*, const float*, double, int, double2*,
+                                        long long, const int*, int);
+
+__global__ void k_pair_pack(long long N, const double2* __restrict__ r, const double2* __restrict__ e, int nc,
+                            const float2* __restrict__ feat, double h2, const float* __restrict__ scale,
+                            float4* __restrict__ x4, float2* __restrict__ t2) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)nc * N) return;
+  const int k = (int)(i / N);
+  const long long p = i % N;
+  const double s = (double)scale[k];
+  const double inv = s > 0.0 ? 1.0 / s : 0.0;
+  const double2 rv = r[i], ev = e[i];
+  const float2 f = feat[p];
+  x4[i] = make_float4((float)(rv.x * inv), (float)(rv.y * inv), f.x, f.y);
+  t2[i] = make_float2((float)(ev.x * inv / h2), (float)(ev.y * inv / h2));
+}
+
+void launch_pair_pack(Ctx& ctx, long long N, const double2* r, const double2* e, int nc, const float2* feat, double h2,
+                      float* scale, float* x4, float* t2) {
+  HZ_LAUNCH(ctx, "net_col_rms", (double)nc * N * 16.0, k_col_rms<double>, nc, 256, 0, N, r, N, (const int*)nullptr,
+            scale);
+  const long long tot = (long long)nc * N;
+  HZ_LAUNCH(ctx, "net_pair_pack", (double)tot * 64.0, k_pair_pack, (unsigned)((tot + 255) / 256), 256, 0, N, r, e, nc,
+            feat, h2, scale, reinterpret_cast<float4*>(x4), reinterpret_cast<float2*>(t2));
+}
+
+__global__ void k_gather_cols(long long N, const double2* __restrict__ src, long long ld, const int* __restrict__ cols,
+                              int nc, double2* __restrict__ dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)nc * N) return;
+  dst[i] = src[(long long)cols[i / N] * ld + i % N];
+}
+
+void launch_gather_cols(Ctx& ctx, long long N, const double2* src, long long ld, const int* cols, int nc,
+                        double2* dst) {
+  const long long tot = (long long)nc * N;
+  HZ_LAUNCH(ctx, "net_capture", (double)tot * 32.0, k_gather_cols, (unsigned)((tot + 255) / 256), 256, 0, N, src, ld,
+            cols, nc, dst);
+}
+
+__global__ void k_axpy_compact(long long n, const double2* __restrict__ e, double2* __restrict__ x) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 a = x[i], b = e[i];
+  x[i] = make_double2(a.x + b.x, a.y + b.y);
+}
+
+void launch_axpy_compact(Ctx& ctx, long long N, int nc, const double2* e, double2* x) {
+  const long long tot = (long long)nc * N;
+  HZ_LAUNCH(ctx, "net_axpy", (double)tot * 48.0, k_axpy_compact, (unsigned)((tot + 255) / 256), 256, 0, tot, e, x);
+}
+
+__global__ void __launch_bounds__(256) k_diff_norms(long long N, const double2* __restrict__ a,
+                                                    const double2* __restrict__ b, double* __restrict__ out) {
+  const int k = blockIdx.x;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (long long p = threadIdx.x; p < N; p += blockDim.x) {
+    const double2 u = a[(long long)k * N + p], v = b[(long long)k * N + p];
+    const double dx = u.x - v.x, dy = u.y - v.y;
+    s0 += dx * dx + dy * dy;
+    s1 += u.x * u.x + u.y * u.y;
+    s2 += v.x * v.x + v.y * v.y;
+  }
+  __shared__ double sh[3][256];
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 3; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) out[3 * k + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+void launch_diff_norms(Ctx& ctx, long long N, int nc, const double2* a, const double2* b, double* out) {
+  HZ_LAUNCH(ctx, "net_norms", (double)nc * N * 32.0, k_diff_norms, nc, 256, 0, N, a, b, out);
+}
+
+}  // namespace hz

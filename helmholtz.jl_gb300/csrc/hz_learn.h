@@ -1,0 +1,108 @@
+// Learned coarse-grid correction: network object and the launch helpers the
+// solver uses to feed it (implemented in hz_learn.cu).
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "hz_kernels.cuh"
+
+namespace hz {
+
+// 2D convolutional encoder-decoder (BF16 weights and activations, FP32
+// accumulation on the tensor cores) that maps a normalised coarse residual and
+// the medium to the normalised coarse error.
+//   input  x [B][N][4] FP32: Re r/s, Im r/s, w^2 m h^2, gamma / w   (s = RMS of r)
+//   output y [B][N][8] FP32: Re, Im of e / (h^2 s) in channels 0, 1
+// N = nx * ny nodes, axis 1 (nx) fastest; nx - 1 and ny - 1 divisible by 8.
+// Weights exchanged with the host are FP32, layer after layer, each layer
+// [cout][9][cin] with tap t = 3 * (dy + 1) + (dx + 1).
+class CoarseNet {
+ public:
+  static constexpr int kLayers = 8;
+  explicit CoarseNet(unsigned seed);
+  ~CoarseNet();
+  CoarseNet(const CoarseNet&) = delete;
+  CoarseNet& operator=(const CoarseNet&) = delete;
+
+  static long long num_params();
+  static bool supports(long long nx, long long ny);
+  static void layer_shape(int l, int* cin, int* cout);
+
+  void get_weights(float* host) const;
+  void set_weights(const float* host);
+  void get_grad(float* host) const;
+
+  // forward pass on c.stream; x4 on the device; result in output(); train keeps
+  // the activations and allocates their gradients for backward()
+  void forward(Ctx& c, const float* x4, int nx, int ny, int B, bool train = false);
+  const float* output() const { return y32_; }
+  float* input_staging(int nx, int ny, int B);  // [B][N][4] FP32 buffer the solver packs into
+  float* scale_staging(int B);                  // per-sample scale factors
+  // loss and weight gradient after forward(); t [B][N][2] FP32 on the device
+  double backward(Ctx& c, const float* t, int nx, int ny, int B);
+  void adam(Ctx& c, double lr);
+  // Adam steps over nsamples pairs (device x [S][N][4], t [S][N][2]) in shuffled
+  // mini-batches; epoch-mean losses into loss_hist (host, epochs entries)
+  void train(Ctx& c, const float* x, const float* t, int nx, int ny, long long nsamples, int batch, int epochs,
+             double lr, unsigned seed, double* loss_hist);
+
+  Ctx ctx;  // own stream and launch table (training, standalone inference)
+
+ private:
+  void ensure(int nx, int ny, int B, bool grads);
+  void release_acts();
+  void conv_fwd(Ctx& c, int l, int lev, int B, const __nv_bfloat16* in, int ldi, int i_off, __nv_bfloat16* out,
+                int ldo, int o_off, int relu, float* out32);
+  void conv_bwd(Ctx& c, int l, int lev, int B, const __nv_bfloat16* in, int ldi, int i_off,
+                const __nv_bfloat16* dout, int ldd, int d_off, __nv_bfloat16* din, int ldn, int n_off,
+                const __nv_bfloat16* mask, int ldm, int mask_lo);
+
+  long long woff_[kLayers] = {};
+  long long wtotal_ = 0;
+  float* w32_ = nullptr;
+  __nv_bfloat16* wbf_ = nullptr;
+  __nv_bfloat16* wt_ = nullptr;  // flipped weights of the data-gradient convolutions
+  float* g32_ = nullptr;
+  float* m_ = nullptr;
+  float* v_ = nullptr;
+  long long step_ = 0;
+  // activations (forward) and their gradients, bf16
+  int nx_ = 0, ny_ = 0, B_ = 0;
+  bool grads_ = false;
+  int gx_[4] = {}, gy_[4] = {};
+  __nv_bfloat16* act_[11] = {};
+  __nv_bfloat16* grd_[11] = {};
+  float* y32_ = nullptr;
+  float* x4_ = nullptr;
+  long long x4cap_ = 0;
+  float* scale_ = nullptr;
+  int scalecap_ = 0;
+  double* loss_ = nullptr;
+  // training staging
+  float* bx_ = nullptr;
+  float* bt_ = nullptr;
+  int* perm_ = nullptr;
+  long long bcap_ = 0;
+};
+
+// Column RMS s_k of the active columns of b (one level, ld-strided), then the
+// network input x[k][p] = (b/s, feat[p]) (conj: the adjoint solve feeds conj(b)).
+template <typename T>
+void launch_net_pack(Ctx& ctx, long long N, const cplx<T>* b, long long ld, const int* cols, int nc,
+                     const float2* feat, int conj, float* scale, float* x4);
+// out[cols[k]] = s_k h2 (y0 + i y1) (conj: conjugated)
+template <typename T>
+void launch_net_unpack(Ctx& ctx, long long N, const float* y, const float* scale, double h2, int conj, cplx<T>* out,
+                       long long ld, const int* cols, int nc);
+// Training pairs from compact FP64 columns r, e (k = 0..nc): x as in launch_net_pack
+// and t = e / (h2 s_k); scale receives s_k.
+void launch_pair_pack(Ctx& ctx, long long N, const double2* r, const double2* e, int nc, const float2* feat,
+                      double h2, float* scale, float* x4, float* t2);
+// Compact-column helpers (FP64): gather active columns, x += e, and per-column
+// sums |a - b|^2, |a|^2 and |b|^2 into out[3k], out[3k+1], out[3k+2].
+void launch_gather_cols(Ctx& ctx, long long N, const double2* src, long long ld, const int* cols, int nc,
+                        double2* dst);
+void launch_axpy_compact(Ctx& ctx, long long N, int nc, const double2* e, double2* x);
+void launch_diff_norms(Ctx& ctx, long long N, int nc, const double2* a, const double2* b, double* out);
+
+}  // namespace hz

@@ -25,6 +25,7 @@
 #include "../../include/helmgpu.h"
 #include "hz_host.h"
 #include "hz_kernels.cuh"
+#include "hz_learn.h"
 
 namespace {
 
@@ -144,6 +145,21 @@ struct hz_handle {
   std::vector<double> col_relres;
   std::vector<int> col_iters;
   long long h2d = 0, d2h = 0;
+  // learned coarse-grid correction (the network is owned by the caller)
+  hz::CoarseNet* net = nullptr;
+  int net_level = 0;         // level whose correction the network computes
+  double net_stag = 0.5;     // restart-cycle residual ratio above which the plain cycle takes over
+  bool net_active = false;   // network in use by the running solve
+  long long net_calls = 0;   // network applications (blocks of columns)
+  int net_fallbacks = 0;     // solves that fell back to the plain cycle
+  int net_feat_level = -1;
+  double net_h2 = 0.0;       // hx * hy of the network level
+  DBuf net_feat;             // per node of the network level: (w^2 m hx hy, gamma / w), float2
+  // capture of the right-hand sides handed to one level (training pairs)
+  bool cap_on = false;
+  int cap_level = 0;
+  long long cap_count = 0, cap_max = 0;
+  DBuf cap_buf;
 };
 
 namespace {
@@ -261,8 +277,11 @@ static constexpr long long kDenseCoarseMax = 8192;
 
 // Stencil offsets per level are all within one node; the banded storage uses
 // kl = ku = nx*ny + nx + 1 (3D) or nx + 1 (2D).
-void factor_coarsest(hz_handle* h, Hierarchy& H) {
-  Level& L = *H.lv.back();
+// Banded LU of one level's operator (host, FP64) and the dense block operators
+// of its blocked solve.
+void band_factor_level(hz_handle* h, const Hierarchy& H, const Level& L, std::vector<BandBlock>& blocks,
+                       std::vector<std::complex<double>>& T, std::vector<std::complex<double>>& G, int& kl_out,
+                       int& ku_out) {
   const Grid g = L.g;
   const int dim = h->prob.dim;
   const long long N = g.N;
@@ -317,11 +336,20 @@ void factor_coarsest(hz_handle* h, Hierarchy& H) {
   }
   std::vector<int> ipiv((size_t)N);
   int info = band_lu_factor(N, kl, ku, ab.data(), ipiv.data());
-  if (info != 0) fail(HZ_ERR_NUMERIC, "coarsest-level LU: zero pivot in column %d", info);
+  if (info != 0) fail(HZ_ERR_NUMERIC, "banded LU of a %lld-node level: zero pivot in column %d", N, info);
   // dense block operators of the blocked banded solve, block size kl
+  blocks.clear();
+  band_block_operators(N, kl, ku, ab.data(), ipiv.data(), std::max(kl, 1), blocks, T, G);
+  kl_out = kl;
+  ku_out = ku;
+}
+
+void factor_coarsest(hz_handle* h, Hierarchy& H) {
+  Level& L = *H.lv.back();
+  const long long N = L.g.N;
+  int kl = 0, ku = 0;
   std::vector<std::complex<double>> T, G;
-  H.band.blocks.clear();
-  band_block_operators(N, kl, ku, ab.data(), ipiv.data(), std::max(kl, 1), H.band.blocks, T, G);
+  band_factor_level(h, H, L, H.band.blocks, T, G, kl, ku);
   H.nc = N;
   H.kl = kl;
   H.ku = ku;
@@ -604,11 +632,64 @@ void lev_jacobi0(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* 
   launch_jacobi0<T, TB>(h->ctx, L.g, dinv, L.fine ? L.fop.adj : 0, b, y, L.ld, cols, nc, h->opt.relax_param);
 }
 
+// Network input features on level l: the medium restricted l times by nodal
+// full weighting, as w^2 m hx hy and gamma / w (w = Re omega).
+const float2* net_features(hz_handle* h, int l) {
+  if (h->net_feat_level == l) return h->net_feat.as<float2>();
+  Grid g = h->g0;
+  std::vector<double> m = h->m, gm = h->gamma;
+  double hx = h->prob.h[0], hy = h->prob.h[1];
+  for (int k = 0; k < l; ++k) {
+    const Grid c = coarsen(g, 2);
+    m = restrict_nodal(m, g, c, 2);
+    gm = restrict_nodal(gm, g, c, 2);
+    g = c;
+    hx *= 2.0;
+    hy *= 2.0;
+  }
+  const double w = h->prob.omega_re;
+  std::vector<float2> f((size_t)g.N);
+  for (long long p = 0; p < g.N; ++p) f[(size_t)p] = make_float2((float)(w * w * m[p] * hx * hy), (float)(gm[p] / w));
+  h->net_feat.alloc((size_t)g.N * sizeof(float2));
+  ck(cudaMemcpy(h->net_feat.p, f.data(), (size_t)g.N * sizeof(float2), cudaMemcpyHostToDevice), "upload features");
+  h->net_feat_level = l;
+  h->net_h2 = hx * hy;
+  return h->net_feat.as<float2>();
+}
+
+// out = e_l for the active columns of b_l by the network: the coarse-grid
+// correction below level l - 1 replaced by one inference (the adjoint solve
+// feeds conj(b) and conjugates the result).
+template <typename T>
+void learned_correction(hz_handle* h, Hierarchy& H, int l, const cplx<T>* b, cplx<T>* out, const int* cols, int nc) {
+  Level& L = *H.lv[l];
+  hz::CoarseNet* net = h->net;
+  const float2* feat = net_features(h, l);
+  float* x4 = net->input_staging(L.g.nx, L.g.ny, nc);
+  float* sc = net->scale_staging(nc);
+  launch_net_pack<T>(h->ctx, L.g.N, b, L.ld, cols, nc, feat, H.adj, sc, x4);
+  net->forward(h->ctx, x4, L.g.nx, L.g.ny, nc);
+  launch_net_unpack<T>(h->ctx, L.g.N, net->output(), sc, h->net_h2, H.adj, out, L.ld, cols, nc);
+  h->net_calls += 1;
+}
+
+// Record the right-hand sides handed to the capture level (FP64 cycles only).
+template <typename TB>
+void capture_rhs(hz_handle* h, Level& L, const cplx<TB>* b, const int* cols, int nc) {
+  if constexpr (std::is_same<TB, double>::value) {
+    const int k = (int)std::min<long long>(h->cap_max - h->cap_count, nc);
+    if (k <= 0) return;
+    launch_gather_cols(h->ctx, L.g.N, b, L.ld, cols, k, h->cap_buf.as<double2>() + h->cap_count * L.g.N);
+    h->cap_count += k;
+  }
+}
+
 // x_out = cycle(b) on level l with zero initial guess.
 template <typename T, typename TB>
 void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out, const int* cols, int nc) {
   Level& L = *H.lv[l];
   const int last = (int)H.lv.size() - 1;
+  if (h->cap_on && l == h->cap_level) capture_rhs<TB>(h, L, b, cols, nc);
   if (l == last) {
     if (!std::is_same<T, TB>::value) fail(HZ_ERR_STATE, "single-level mixed hierarchy is not supported");
     if (H.dense_df)
@@ -659,7 +740,10 @@ void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out
       lev_op<T, TB>(h, H, l, MODE_RESID, cur, b, rb, cols, nc);
       launch_restrict<T>(h->ctx, L.g, C.g, rb, L.ld, C.b.as<cplx<T>>(), C.ld, cols, nc);
     }
-    mg_cycle<T, T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+    if (h->net_active && l + 1 == h->net_level)
+      learned_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+    else
+      mg_cycle<T, T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
     launch_prolong<T>(h->ctx, L.g, C.g, C.x.as<cplx<T>>(), C.ld, zero_guess ? nullptr : cur, cur, L.ld, cols, nc);
     zero_guess = false;
   }
@@ -749,6 +833,14 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
     if (bn[c] > 0) act.push_back(c);
   }
   if (act.empty()) return 0;
+  // the network (a nonlinear preconditioner: FGMRES only) serves until a restart
+  // cycle reduces some column's residual by less than net_stag
+  struct NetScope {
+    hz_handle* h;
+    ~NetScope() { h->net_active = false; }
+  } net_scope{h};
+  h->net_active = h->net != nullptr;
+  std::vector<double> prev = bn;
   if (mixed)
     ensure_level_buffers<float>(h, H, h->rcap);
   else
@@ -875,6 +967,16 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
       if (!std::isfinite(rn[c])) fail(HZ_ERR_NUMERIC, "residual of column %d is NaN or Inf", c);
       if (!(h->col_relres[c] <= tol)) next.push_back(c);
     }
+    if (h->net_active) {
+      for (int c : next)
+        if (!(rn[c] <= h->net_stag * prev[c])) {
+          h->net_active = false;
+          h->net_fallbacks += 1;
+          if (h->opt.verbose) fprintf(stderr, "helmgpu: learned correction stagnated, plain cycle takes over\n");
+          break;
+        }
+    }
+    for (int c : act) prev[c] = rn[c];
     act.swap(next);
     if (act.empty()) break;
     if (outer == std::max(1, h->opt.max_outer)) break;
@@ -1103,6 +1205,28 @@ int guarded(hz_handle* h, F&& f) {
     g_thread_error = e.what();
     return HZ_ERR_CUDA;
   }
+}
+
+}  // namespace
+
+// A trained or training coarse-correction network on one device.
+struct hz_net {
+  int dev = 0;
+  std::unique_ptr<hz::CoarseNet> net;
+};
+
+namespace {
+
+Grid level_grid(const hz_handle* h, int level) {
+  Grid g = h->g0;
+  for (int k = 0; k < level; ++k) g = coarsen(g, h->prob.dim);
+  return g;
+}
+
+void check_net_grid(long long nx, long long ny, int batch) {
+  if (!hz::CoarseNet::supports(nx, ny))
+    fail(HZ_ERR_ARG, "network grid %lldx%lld: node counts must be 8k+1 (k >= 1)", nx, ny);
+  if (batch < 1) fail(HZ_ERR_ARG, "batch must be >= 1");
 }
 
 }  // namespace
@@ -1377,6 +1501,246 @@ int hz_set_profile(hz_handle* h, int32_t on) {
   h->ctx.resolve();
   h->ctx.profile = on != 0;
   return HZ_OK;
+}
+
+// ---- learned coarse-grid correction -------------------------------------------
+
+int hz_net_create(int32_t seed, int32_t device, hz_net** out) {
+  if (!out) return HZ_ERR_ARG;
+  *out = nullptr;
+  auto n = std::make_unique<hz_net>();
+  int st = guarded(nullptr, [&] {
+    int cnt = 0;
+    if (cudaGetDeviceCount(&cnt) != cudaSuccess || cnt == 0) {
+      cudaGetLastError();
+      fail(HZ_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= cnt) fail(HZ_ERR_ARG, "device %d out of range", device);
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    n->dev = device;
+    n->net = std::make_unique<hz::CoarseNet>((unsigned)seed);
+  });
+  if (st == HZ_OK) *out = n.release();
+  return st;
+}
+
+int hz_net_destroy(hz_net* net) {
+  if (!net) return HZ_OK;
+  cudaSetDevice(net->dev);
+  delete net;
+  return HZ_OK;
+}
+
+int64_t hz_net_num_params(void) { return hz::CoarseNet::num_params(); }
+
+int hz_net_layer_shape(int32_t layer, int32_t* cin, int32_t* cout) {
+  if (layer < 0 || layer >= hz::CoarseNet::kLayers || !cin || !cout) return HZ_ERR_ARG;
+  int a = 0, b = 0;
+  hz::CoarseNet::layer_shape(layer, &a, &b);
+  *cin = a;
+  *cout = b;
+  return HZ_OK;
+}
+
+int hz_net_get_weights(hz_net* net, float* w) {
+  if (!net || !w) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    net->net->get_weights(w);
+  });
+}
+
+int hz_net_set_weights(hz_net* net, const float* w) {
+  if (!net || !w) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    net->net->set_weights(w);
+  });
+}
+
+int hz_net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, int32_t batch, int32_t mem) {
+  if (!net || !x || !y) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    check_net_grid(nx, ny, batch);
+    if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "mem must be HZ_MEM_HOST or HZ_MEM_DEVICE");
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    hz::CoarseNet& c = *net->net;
+    const long long N = nx * ny;
+    const float* dx = x;
+    if (mem == HZ_MEM_HOST) {
+      float* st = c.input_staging((int)nx, (int)ny, batch);
+      ck(cudaMemcpyAsync(st, x, (size_t)batch * N * 16, cudaMemcpyHostToDevice, c.ctx.stream), "copy x");
+      dx = st;
+    }
+    c.forward(c.ctx, dx, (int)nx, (int)ny, batch);
+    ck(cudaMemcpy2DAsync(y, 8, c.output(), 32, 8, (size_t)batch * N,
+                         mem == HZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c.ctx.stream),
+       "copy y");
+    ck(cudaStreamSynchronize(c.ctx.stream), "sync");
+    c.ctx.resolve();
+  });
+}
+
+int hz_net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int32_t batch, int32_t mem,
+                    double* loss, float* grad) {
+  if (!net || !x || !t) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    check_net_grid(nx, ny, batch);
+    if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "mem must be HZ_MEM_HOST or HZ_MEM_DEVICE");
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    hz::CoarseNet& c = *net->net;
+    const long long N = nx * ny;
+    DBuf bx, bt;
+    const float* dx = x;
+    const float* dt = t;
+    if (mem == HZ_MEM_HOST) {
+      bx.alloc((size_t)batch * N * 16);
+      bt.alloc((size_t)batch * N * 8);
+      ck(cudaMemcpyAsync(bx.p, x, (size_t)batch * N * 16, cudaMemcpyHostToDevice, c.ctx.stream), "copy x");
+      ck(cudaMemcpyAsync(bt.p, t, (size_t)batch * N * 8, cudaMemcpyHostToDevice, c.ctx.stream), "copy t");
+      dx = bx.as<float>();
+      dt = bt.as<float>();
+    }
+    c.forward(c.ctx, dx, (int)nx, (int)ny, batch, true);
+    const double l = c.backward(c.ctx, dt, (int)nx, (int)ny, batch);
+    if (loss) *loss = l;
+    if (grad) c.get_grad(grad);
+  });
+}
+
+int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t npairs, int32_t batch,
+                 int32_t epochs, double lr, int32_t seed, double* loss_hist) {
+  if (!net || !x || !t) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    check_net_grid(nx, ny, batch);
+    if (npairs < 1 || epochs < 1) fail(HZ_ERR_ARG, "npairs and epochs must be >= 1");
+    if (!(lr > 0)) fail(HZ_ERR_ARG, "lr must be > 0");
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    hz::CoarseNet& c = *net->net;
+    c.train(c.ctx, x, t, (int)nx, (int)ny, npairs, batch, epochs, lr, (unsigned)seed, loss_hist);
+  });
+}
+
+int hz_attach_net(hz_handle* h, hz_net* net, int32_t level, double stag_ratio) {
+  if (!h) return HZ_ERR_ARG;
+  return guarded(h, [&] {
+    if (!net) {
+      h->net = nullptr;
+      h->net_level = 0;
+      return;
+    }
+    if (h->prob.dim != 2) fail(HZ_ERR_ARG, "the learned correction is 2D only");
+    if (h->opt.krylov != HZ_KRYLOV_FGMRES)
+      fail(HZ_ERR_ARG, "the learned correction is a nonlinear preconditioner: it needs FGMRES");
+    if (level < 1 || level >= h->opt.levels) fail(HZ_ERR_ARG, "level must be in [1, levels - 1]");
+    if (!(stag_ratio > 0)) fail(HZ_ERR_ARG, "stag_ratio must be > 0");
+    if (net->dev != h->dev) fail(HZ_ERR_ARG, "network and solver live on different devices");
+    const Grid g = level_grid(h, level);
+    check_net_grid(g.nx, g.ny, 1);
+    h->net = net->net.get();
+    h->net_level = level;
+    h->net_stag = stag_ratio;
+  });
+}
+
+int hz_learned_stats(const hz_handle* h, int64_t* net_calls, int32_t* fallbacks) {
+  if (!h) return HZ_ERR_ARG;
+  if (net_calls) *net_calls = h->net_calls;
+  if (fallbacks) *fallbacks = h->net_fallbacks;
+  return HZ_OK;
+}
+
+int hz_collect_pairs(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, int32_t mem, int32_t level,
+                     int32_t sweeps, int64_t max_pairs, float* x_out, float* t_out, double* plain_err,
+                     double* target_relres, int64_t* count) {
+  if (!h) return HZ_ERR_ARG;
+  return guarded(h, [&] {
+    if (!x_out || !t_out || !count) fail(HZ_ERR_ARG, "null output");
+    if (h->opt.precision != HZ_PREC_FP64) fail(HZ_ERR_ARG, "training pairs come from the FP64 solver");
+    if (h->prob.dim != 2) fail(HZ_ERR_ARG, "the learned correction is 2D only");
+    if (level < 1 || level >= h->opt.levels) fail(HZ_ERR_ARG, "level must be in [1, levels - 1]");
+    if (sweeps < 1 || max_pairs < 1) fail(HZ_ERR_ARG, "sweeps and max_pairs must be >= 1");
+    const Grid g = level_grid(h, level);
+    check_net_grid(g.nx, g.ny, 1);
+    set_device(h);
+    const long long N = g.N;
+    h->cap_buf.alloc((size_t)max_pairs * N * 16);
+    hz::CoarseNet* saved = h->net;
+    h->net = nullptr;
+    h->cap_on = true;
+    h->cap_level = level;
+    h->cap_count = 0;
+    h->cap_max = max_pairs;
+    const int rc = hz_solve(h, B, X, n, nrhs, 0, mem, nullptr);
+    h->cap_on = false;
+    h->net = saved;
+    if (rc < 0) fail(rc, "%s", h->err.c_str());
+    Hierarchy& H = h->hier[0];
+    const long long cnt = h->cap_count;
+    const int R = h->rcap;
+    // targets: exact solves with a banded LU of the capture level's operator
+    // (plain cycles as a stationary iteration need not converge on coarse levels)
+    Level& Lv = *H.lv[level];
+    std::vector<std::complex<double>> bT, bG;
+    BandSolveOps lu;
+    int kl = 0, ku = 0;
+    band_factor_level(h, H, Lv, lu.blocks, bT, bG, kl, ku);
+    DBuf dT, dG, dB, bw;
+    dT.alloc(bT.size() * 16);
+    dG.alloc(bG.size() * 16);
+    dB.alloc(lu.blocks.size() * sizeof(BandBlock));
+    ck(cudaMemcpy(dT.p, bT.data(), bT.size() * 16, cudaMemcpyHostToDevice), "upload band forward operators");
+    ck(cudaMemcpy(dG.p, bG.data(), bG.size() * 16, cudaMemcpyHostToDevice), "upload band backward operators");
+    ck(cudaMemcpy(dB.p, lu.blocks.data(), lu.blocks.size() * sizeof(BandBlock), cudaMemcpyHostToDevice),
+       "upload band blocks");
+    lu.N = N;
+    lu.T = dT.as<double2>();
+    lu.G = dG.as<double2>();
+    lu.dblocks = dB.as<BandBlock>();
+    bw.alloc((size_t)3 * R * N * 16);
+    DBuf xe, res, ev, x1, idc, sc, nrm;
+    xe.alloc((size_t)R * N * 16);
+    res.alloc((size_t)R * N * 16);
+    ev.alloc((size_t)R * N * 16);
+    x1.alloc((size_t)R * N * 16);
+    sc.alloc((size_t)R * 4);
+    nrm.alloc((size_t)R * 6 * 8);
+    idc.alloc((size_t)R * sizeof(int));
+    std::vector<int> seq(R);
+    for (int c = 0; c < R; ++c) seq[c] = c;
+    ck(cudaMemcpy(idc.p, seq.data(), R * sizeof(int), cudaMemcpyHostToDevice), "upload cols");
+    const int* dc = idc.as<int>();
+    const float2* feat = net_features(h, level);
+    std::vector<double> hn((size_t)R * 6);
+    double worst = 0.0;
+    for (long long i0 = 0; i0 < cnt; i0 += R) {
+      const int k = (int)std::min<long long>(R, cnt - i0);
+      const double2* r = h->cap_buf.as<double2>() + i0 * N;
+      double2* xd = xe.as<double2>();
+      // one plain cycle from this level (what the network replaces), then the exact solve
+      mg_cycle<double, double>(h, H, level, r, x1.as<double2>(), dc, k);
+      launch_band_solve<double>(h->ctx, lu, r, xd, N, dc, k, bw.as<double2>());
+      for (int s = 1; s < sweeps; ++s) {  // iterative refinement with the same factors
+        lev_op<double, double>(h, H, level, MODE_RESID, xd, r, res.as<double2>(), dc, k);
+        launch_band_solve<double>(h->ctx, lu, res.as<double2>(), ev.as<double2>(), N, dc, k, bw.as<double2>());
+        launch_axpy_compact(h->ctx, N, k, ev.as<double2>(), xd);
+      }
+      lev_op<double, double>(h, H, level, MODE_RESID, xd, r, res.as<double2>(), dc, k);
+      launch_diff_norms(h->ctx, N, k, res.as<double2>(), r, nrm.as<double>());
+      launch_diff_norms(h->ctx, N, k, x1.as<double2>(), xd, nrm.as<double>() + 3 * R);
+      launch_pair_pack(h->ctx, N, r, xd, k, feat, h->net_h2, sc.as<float>(), x_out + i0 * N * 4, t_out + i0 * N * 2);
+      ck(cudaMemcpyAsync(hn.data(), nrm.p, (size_t)R * 6 * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "norms");
+      sync(h);
+      for (int c = 0; c < k; ++c) {
+        const double rr = hn[3 * c + 2] > 0 ? std::sqrt(hn[3 * c + 1] / hn[3 * c + 2]) : 0.0;
+        worst = std::max(worst, rr);
+        const double* q = hn.data() + 3 * R + 3 * c;
+        if (plain_err) plain_err[i0 + c] = q[2] > 0 ? std::sqrt(q[0] / q[2]) : 0.0;
+      }
+    }
+    *count = cnt;
+    if (target_relres) *target_relres = worst;
+  });
 }
 
 }  // extern "C"

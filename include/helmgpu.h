@@ -191,6 +191,67 @@ int hz_reset_kernel_times(hz_handle* h);
 /* Turn per-launch CUDA-event timing on (1) or off (0) (options.profile at create time). */
 int hz_set_profile(hz_handle* h, int32_t on);
 
+/* ---- learned coarse-grid correction ------------------------------------------
+ * No counterpart in the reference: the reference's multigrid always recurses to
+ * its coarsest LU.  A small 2D convolutional encoder-decoder (BF16 weights and
+ * activations, FP32 accumulation on the tensor cores; 8 layers of 3x3
+ * convolutions, 16-32-64-64 channels over four grid levels) replaces the
+ * coarse-grid correction below one multigrid level.  It is trained on the GPU
+ * by the library's own forward and backward kernels on (residual, error) pairs
+ * the FP64 solver produces (hz_collect_pairs).
+ *
+ * Pair / input layout on a network grid of nx x ny nodes (axis 1 fastest, node
+ * counts 8k+1): x [batch][nx*ny][4] FP32 = (Re r/s, Im r/s, w^2 m hx hy, gamma/w)
+ * with s the RMS of r over the grid and hx, hy the level's cell sizes;
+ * target / output [batch][nx*ny][2] FP32 = (Re, Im) of e / (hx hy s).
+ * Weights (FP32 on the host): layer after layer, each [cout][9][cin] with tap
+ * index 3 (dy + 1) + (dx + 1), dx along axis 1.  Loss: mean over the batch of
+ * ||y - t||^2 / ||t||^2. */
+typedef struct hz_net hz_net;
+
+/* New network with seeded He-normal weights on a device. */
+int hz_net_create(int32_t seed, int32_t device, hz_net** out);
+int hz_net_destroy(hz_net* net);
+/* Number of weights (FP32 values of hz_net_get_weights). */
+int64_t hz_net_num_params(void);
+/* Input and output channels of layer 0..7. */
+int hz_net_layer_shape(int32_t layer, int32_t* cin, int32_t* cout);
+int hz_net_get_weights(hz_net* net, float* w);
+/* Replaces the weights (and resets the optimiser state). */
+int hz_net_set_weights(hz_net* net, const float* w);
+/* y = net(x) for a batch (x, y on the host or the device: mem). */
+int hz_net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, int32_t batch, int32_t mem);
+/* Loss and its gradient with respect to the weights (host array laid out like
+ * the weights; may be NULL) for one batch; the weights are unchanged. */
+int hz_net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int32_t batch, int32_t mem,
+                    double* loss, float* grad);
+/* Adam over npairs device-resident pairs (x, t as above) in shuffled
+ * mini-batches for epochs passes, learning rate lr with cosine decay to lr/20;
+ * loss_hist (host, epochs entries, may be NULL) gets the mean loss per epoch. */
+int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t npairs, int32_t batch,
+                 int32_t epochs, double lr, int32_t seed, double* loss_hist);
+/* Use the network for the coarse-grid correction of multigrid level `level`
+ * (1 .. levels-1; 2D, FGMRES only: the network is a nonlinear preconditioner).
+ * A restart cycle that reduces some column's residual by less than stag_ratio
+ * hands the rest of that solve to the plain cycle.  net = NULL detaches.  The
+ * handle does not own the network; keep it alive while attached, and use one
+ * network with one solve at a time. */
+int hz_attach_net(hz_handle* h, hz_net* net, int32_t level, double stag_ratio);
+/* Network applications (blocks of columns) and fallbacks to the plain cycle so far. */
+int hz_learned_stats(const hz_handle* h, int64_t* net_calls, int32_t* fallbacks);
+/* Training pairs: solves H X = B (FP64 preconditioner, no network) like
+ * hz_solve while recording the right-hand side r that each cycle hands to
+ * `level` (at most max_pairs columns), then computes the target e = A^{-1} r on
+ * that level with a banded LU of its operator (FP64) followed by sweeps - 1
+ * steps of iterative refinement.
+ * x_out [max_pairs][N][4] and t_out [max_pairs][N][2] are DEVICE FP32 arrays in
+ * the layout above; plain_err (host, may be NULL) gets ||e1 - e|| / ||e|| of one
+ * plain cycle e1 per pair, target_relres (may be NULL) the largest
+ * ||r - A e|| / ||r|| of the targets, count the pairs written. */
+int hz_collect_pairs(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, int32_t mem, int32_t level,
+                     int32_t sweeps, int64_t max_pairs, float* x_out, float* t_out, double* plain_err,
+                     double* target_relres, int64_t* count);
+
 /* ---- host-side discretisation helpers (no GPU needed) ---------------------- */
 
 /* getMaximalFrequency (src/GetHelmholtz.jl:75-79): 0.2*pi / (max(h) sqrt(max(m))). */

@@ -1,0 +1,190 @@
+"""GPU tests of the learned coarse-grid correction.
+
+* The network kernels (BF16 tensor-core convolutions, FP32 accumulation)
+  against the CPU oracle (oracle/coarse_net.py, BF16 rounding emulated at the
+  same points): forward output to relative L2 error <= 1e-2, loss to <= 1e-3,
+  the weight gradient of every layer to <= 3e-2 (relative L2; the residual
+  difference comes from FP32 summation order flipping a BF16 rounding).
+* Training on pairs the FP64 solver produces lowers the loss and beats the
+  "no correction" baseline on held-out pairs.
+* Inside FGMRES (outer FP64, stopping residual 1e-6) the learned form reaches
+  the same stopping residual with error <= 1e-4 against the direct solution,
+  takes fewer iterations than the same cycle without any correction below the
+  network's level, and hands over to the plain cycle when it stagnates.
+"""
+import numpy as np
+import pytest
+
+import coarse_net as CN
+import problems as PB
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+
+def _x(seed, B=3, ny=17, nx=33):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(B, ny, nx, 4)).astype(np.float32)
+    x[..., 2] = rng.uniform(0.5, 6.0, size=(B, ny, nx))   # w^2 m h^2
+    x[..., 3] = rng.uniform(0.01, 0.9, size=(B, ny, nx))  # gamma / w
+    t = rng.normal(size=(B, ny, nx, 2)).astype(np.float32)
+    return x, t
+
+
+def test_forward_matches_oracle(hz):
+    net = hz.learned.CoarseNet(seed=11)
+    w = net.get_weights()
+    x, _ = _x(1)
+    y = net.forward(x)
+    yo, _ = CN.forward(w, x.astype(np.float64), emulate=True)
+    for b in range(x.shape[0]):
+        assert _rel(y[b], yo[b]) <= 1e-2, b
+    # the device path gives the same bits as the host path
+    import torch
+    yd = net.forward(torch.from_numpy(x).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(yd, y)
+
+
+def test_weights_roundtrip(hz):
+    net = hz.learned.CoarseNet(seed=2)
+    w = CN.he_init(9)
+    net.set_weights(w)
+    np.testing.assert_array_equal(net.get_weights(), w)
+    with pytest.raises(ValueError):
+        net.set_weights(w[:-1])
+
+
+def test_gradient_matches_oracle(hz):
+    net = hz.learned.CoarseNet(seed=5)
+    w = net.get_weights()
+    x, t = _x(2, B=2)
+    loss, g = net.gradient(x, t)
+    yo, cache = CN.forward(w, x.astype(np.float64), emulate=True)
+    lo, go = CN.backward(cache, t.astype(np.float64))
+    assert abs(loss - lo) <= 1e-3 * lo
+    offs = np.cumsum([0] + [9 * a * b for a, b in CN.LAYERS])
+    for k in range(8):
+        a, b = g[offs[k]:offs[k + 1]], go[offs[k]:offs[k + 1]]
+        assert _rel(a, b) <= 3e-2, (k, _rel(a, b))
+    # the weights are unchanged by a gradient evaluation
+    np.testing.assert_array_equal(net.get_weights(), w)
+
+
+def _sources(n_nodes, nx, ny, h, k, seed, pad):
+    """k unit point sources (1/(hx hy) at one node) at seeded positions outside the absorbing layer."""
+    rng = np.random.default_rng(seed)
+    B = np.zeros((n_nodes, k), dtype=np.complex128)
+    for c in range(k):
+        i = rng.integers(pad, nx - pad)
+        j = rng.integers(1, ny - pad)
+        B[i + j * nx, c] = 1.0 / (h[0] * h[1])
+    return B
+
+
+def _solver(hz, P, precision, levels=5, tol=1e-6, max_outer=60):
+    MG = hz.getMGparam(complex, int, levels, 1, max_outer, tol, "Jac", 0.8, 1, 1, "V", "Julia", 0.5, 0.0,
+                       precision=precision)
+    return hz.getShiftedLaplacianMultigridSolver(PB.hz_param(hz, P), MG, 0.5, "GMRES", 10)
+
+
+@pytest.fixture(scope="module")
+def trained(hz):
+    """A network trained on pairs from three seeded layered+inclusion models (129x129 nodes, level 2 = 33x33)."""
+    import torch
+    xs, ts, pes = [], [], []
+    for seed in (21, 22, 23):
+        P = PB.layered((128, 128), seed=seed, pad=16, ellipsoid=True)
+        S = _solver(hz, P, "fp64")
+        nx = ny = 129
+        B = _sources(nx * ny, nx, ny, P["M"].h, 6, seed, 16)
+        d = hz.learned.collect_pairs(S, B, level=2, sweeps=2, max_pairs=240)
+        assert d["target_relres"] < 1e-10
+        assert d["x"].shape[1:] == (33, 33, 4)
+        xs.append(d["x"])
+        ts.append(d["t"])
+        pes.append(d["plain_err"])
+    x = torch.cat(xs).contiguous()
+    t = torch.cat(ts).contiguous()
+    net = hz.learned.CoarseNet(seed=1)
+    hist = net.train(x, t, epochs=40, batch=32, lr=2e-3, seed=3)
+    return net, x, t, np.concatenate(pes), hist
+
+
+def test_training_lowers_loss(hz, trained):
+    net, x, t, plain_err, hist = trained
+    assert np.all(np.isfinite(hist))
+    assert hist[-1] < 0.5 * hist[0], hist
+    # on the training pairs the network beats "no correction" (relative error 1)
+    err = hz.learned.pair_errors(net, x, t)
+    print(f"loss {hist[0]:.3f} -> {hist[-1]:.3f}; median pair error: network {np.median(err):.3f}, "
+          f"one plain cycle {np.median(plain_err):.3f}")
+    assert np.median(err) < 0.7, np.median(err)
+
+
+def test_learned_solve_gains_over_no_correction(hz, O, trained):
+    net = trained[0]
+    P = PB.layered((128, 128), seed=101, pad=16, ellipsoid=True)  # held-out model
+    nx = ny = 129
+    B = _sources(nx * ny, nx, ny, P["M"].h, 4, 101, 16)
+    Xref = O.direct_solve(P["H"], B)
+    iters = {}
+    for name, weights in (("learned", None), ("zero", np.zeros(CN.num_params(), np.float32))):
+        S = _solver(hz, P, "mixed")
+        use = net
+        if weights is not None:
+            use = hz.learned.CoarseNet(seed=0)
+            use.set_weights(weights)
+        hz.learned.attach(S, use, level=2, stag_ratio=1e9)  # no fallback: measure the network alone
+        X, S = hz.solveLinearSystem(None, B, S)
+        calls, fb = hz.learned.learned_stats(S)
+        assert calls > 0 and fb == 0
+        iters[name] = int(S.last_iters.max())
+        if name == "learned":
+            assert S.last_relres.max() <= 1e-6
+            for c in range(B.shape[1]):
+                assert _rel(X[:, c], Xref[:, c]) <= 1e-4
+    S = _solver(hz, P, "mixed")
+    hz.solveLinearSystem(None, B, S)
+    iters["plain"] = int(S.last_iters.max())
+    print("iterations (max over columns):", iters)
+    assert iters["learned"] < iters["zero"], iters
+
+
+def test_learned_fp64_and_adjoint(hz, O, trained):
+    """FP64 cycle with the network, and the adjoint solve (conjugated network input/output)."""
+    net = trained[0]
+    P = PB.layered((128, 128), seed=102, pad=16, ellipsoid=True)
+    B = _sources(129 * 129, 129, 129, P["M"].h, 2, 102, 16)
+    S = _solver(hz, P, "fp64")
+    hz.learned.attach(S, net, level=2, stag_ratio=1e9)
+    X, S = hz.solveLinearSystem(None, B, S)
+    assert S.last_relres.max() <= 1e-6
+    Xa, S = hz.solveLinearSystem(None, B, S, 1)
+    assert S.last_relres.max() <= 1e-6
+    HH = P["H"].conj().T.tocsr()
+    for c in range(2):
+        assert np.linalg.norm(HH @ Xa[:, c] - B[:, c]) / np.linalg.norm(B[:, c]) <= 1e-6 * 1.0001
+
+
+def test_stagnation_falls_back_to_plain_cycle(hz, O):
+    """A network that gives no correction stagnates; the plain cycle finishes the solve."""
+    P = PB.layered((128, 128), seed=103, pad=16, ellipsoid=True)
+    B = _sources(129 * 129, 129, 129, P["M"].h, 3, 103, 16)
+    net = hz.learned.CoarseNet(seed=0)
+    net.set_weights(np.zeros(CN.num_params(), np.float32))
+    S = _solver(hz, P, "mixed")
+    hz.learned.attach(S, net, level=2, stag_ratio=0.05)
+    X, S = hz.solveLinearSystem(None, B, S)
+    calls, fb = hz.learned.learned_stats(S)
+    assert fb == 1 and calls > 0
+    assert S.last_relres.max() <= 1e-6
+    Xref = O.direct_solve(P["H"], B)
+    for c in range(3):
+        assert _rel(X[:, c], Xref[:, c]) <= 1e-4
+    # detach: plain solve, no further network calls
+    hz.learned.attach(S, None)
+    hz.solveLinearSystem(None, B, S)
+    assert hz.learned.learned_stats(S)[0] == calls
