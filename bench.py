@@ -6,7 +6,7 @@ One step = one hz_solve of the whole right-hand-side block of the workload
 complex-FP32 V-cycle inside the FP64 FGMRES ("mixed"); the plain FP64 form of
 the same solver is timed in the same process for the ratio the metric names.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c2|c3|c5]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1|c2|c3|c4|c5]
   python bench.py --impl reference ...   # CPU reference path (C oracle, all host threads)
 
 Under torchrun each rank solves its own seeded block of right-hand sides
@@ -47,6 +47,12 @@ WORKLOADS = {
     # 3D 129^3 nodes layered + ellipsoid, absorbing layer 12, 4x4 surface sources, 4 levels
     "c3": dict(name="3D 129^3 layered+ellipsoid, 16 surface sources, 4 levels, FGMRES(10) tol 1e-6",
                cells=(128, 128, 128), h=0.010, nrhs=16, levels=4, pad=12, ellipsoid=True, tol=1e-6),
+    # 2D 513 x 513 layered + inclusion models, learned coarse correction below level 2: trained on
+    # pairs from seeded training models, evaluated on held-out seeds x 32 random-position sources
+    "c4": dict(name="2D 513x513 layered+inclusion, learned coarse correction below level 2, 32 random sources, "
+                    "5 levels, FGMRES(10) tol 1e-6",
+               cells=(512, 512), h=0.010, nrhs=32, levels=5, pad=32, ellipsoid=True, tol=1e-6, learned=True,
+               net_level=2),
     # 3D 257^3 nodes (16,974,593 unknowns per RHS), absorbing layer 16, 32 surface sources
     "c5": dict(name="3D 257^3 layered+ellipsoid, 32 surface sources, 5 levels, FGMRES(10) tol 1e-6",
                cells=(256, 256, 256), h=0.010, nrhs=32, levels=5, pad=16, ellipsoid=True, tol=1e-6),
@@ -351,6 +357,121 @@ def run_ours(args, rank, ws, dist):
     return results, wl, P
 
 
+def random_sources(P: dict, nrhs: int, seed: int, pad: int) -> np.ndarray:
+    """Delta sources q = 1/||h||^2 at seeded random nodes outside the absorbing layer (2D)."""
+    rng = np.random.default_rng(seed)
+    nx, nz = P["nodes"]
+    B = np.zeros((nx * nz, nrhs), dtype=np.complex128, order="F")
+    amp = 1.0 / float(np.linalg.norm(P["h"])) ** 2
+    for c in range(nrhs):
+        i = int(rng.integers(pad, nx - pad))
+        j = int(rng.integers(1, nz - pad))
+        B[i + nx * j, c] = amp
+    return B
+
+
+def run_learned(args, rank, ws, dist):
+    """Learned-correction workload: pairs from seeded training models (FP64
+    solver), GPU training of the network, then per held-out model one step =
+    solver setup + solve of its 32 right-hand sides (setup included in every arm)."""
+    import torch
+    import __graft_entry__ as ge
+    ge._load_build_module().build()
+    hz = ge.load_package()
+    L = hz._lib
+    lib = L.load()
+    wl = dict(WORKLOADS[args.workload])
+    if args.nrhs > 0:
+        wl["nrhs"] = args.nrhs
+    level = wl["net_level"]
+
+    def solver(P, precision, outer="fp64", max_outer=200):
+        M = hz.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
+        gam = gamma_of(P, wl["pad"], lib, hz)
+        param = hz.HelmholtzParam(M, gam, P["m"], P["w"], True, True)
+        MG = hz.getMGparam(complex, int, wl["levels"], 1, max_outer, wl["tol"], "Jac", 0.8, 1, 1, "V", "Julia",
+                           0.5, 0.0, precision=precision, outerArithmetic=outer)
+        return hz.getShiftedLaplacianMultigridSolver(param, MG, 0.5, "GMRES", 10)
+
+    # 1. training pairs from the FP64 solver on seeded training models
+    t0 = time.perf_counter()
+    xs, ts, pes = [], [], []
+    for s in range(args.train_models):
+        P = make_problem(wl, seed=10_000 + 97 * rank + s)
+        S = solver(P, "fp64")
+        B = random_sources(P, args.train_rhs, seed=20_000 + s, pad=wl["pad"])
+        d = hz.learned.collect_pairs(S, B, level=level, sweeps=2, max_pairs=args.pairs_per_model)
+        xs.append(d["x"].clone())
+        ts.append(d["t"].clone())
+        pes.append(d["plain_err"])
+        del S, d
+    x = torch.cat(xs).contiguous()
+    t = torch.cat(ts).contiguous()
+    del xs, ts
+    collect_s = time.perf_counter() - t0
+    # 2. training (the library's forward/backward/Adam kernels)
+    net = hz.learned.CoarseNet(seed=1)
+    t0 = time.perf_counter()
+    hist = net.train(x, t, epochs=args.train_epochs, batch=32, lr=2e-3, seed=3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    train_err = float(np.median(hz.learned.pair_errors(net, x[:512], t[:512])))
+    npairs = int(x.shape[0])
+    del x, t
+    torch.cuda.empty_cache()
+    # held-out pairs: the network against one plain cycle from the same level
+    P = make_problem(wl, seed=90_000 + rank)
+    d = hz.learned.collect_pairs(solver(P, "fp64"), random_sources(P, 8, seed=90_001, pad=wl["pad"]), level=level,
+                                 sweeps=2, max_pairs=400)
+    held = dict(pairs=int(d["x"].shape[0]), net_median=float(np.median(hz.learned.pair_errors(net, d["x"], d["t"]))),
+                plain_cycle_median=float(np.median(d["plain_err"])))
+    del d
+    # 3. timed arms on held-out models
+    arms = [("learned_mixed", "mixed", True), ("mixed", "mixed", False), ("fp64", "fp64", False)]
+    res = {}
+    nrhs = wl["nrhs"]
+    for name, prec, use_net in arms:
+        nsteps = args.steps if name != "fp64" else max(1, args.plain_steps)
+        tot, iters, relres, fb, calls, launches = 0.0, [], [], 0, 0, 0
+        clk = None
+        for k in range(args.warmup + nsteps):
+            P = make_problem(wl, seed=50_000 + 1000 * rank + k)
+            B = random_sources(P, nrhs, seed=60_000 + k, pad=wl["pad"])
+            Bd = torch.from_numpy(np.ascontiguousarray(B.T)).to("cuda")
+            S = solver(P, prec, outer=args.outer if prec == "mixed" else "fp64")
+            torch.cuda.synchronize()
+            barrier(dist)
+            sampler = ClockSampler(torch.cuda.current_device()) if k == args.warmup else None
+            if sampler:
+                sampler.__enter__()
+            t0 = time.perf_counter()
+            if use_net:
+                hz.learned.attach(S, net, level=level, stag_ratio=args.stag_ratio)
+            X, S = hz.solveLinearSystem(None, Bd.t(), S)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            if sampler:
+                sampler.__exit__()
+                clk = sampler.summary()
+            if k >= args.warmup:
+                tot += dt
+                iters.append(float(np.mean(S.last_iters)))
+                relres.append(float(np.max(S.last_relres)))
+                launches += int(S.last_stats.kernel_launches)
+                c_, f_ = hz.learned.learned_stats(S)
+                calls += c_
+                fb += f_
+            del S, X, Bd
+        tot = max_over_ranks(dist, tot)
+        res[name] = dict(rhs_per_s=nrhs * ws * nsteps / tot, ms_per_step=1000.0 * tot / nsteps,
+                         mean_iters=float(np.mean(iters)), max_relres=float(np.max(relres)), fallbacks=fb,
+                         net_calls=calls, launches_per_step=launches // nsteps, clocks=clk)
+    info = dict(train_models=args.train_models, train_pairs=npairs, epochs=args.train_epochs,
+                loss_first=float(hist[0]), loss_last=float(hist[-1]), collect_s=collect_s, train_s=train_s,
+                train_pair_error_median=train_err, heldout=held)
+    return res, info, wl
+
+
 def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4):
     """C oracle (threaded CSR SLMG, plain FP64) on a bounded sample of the
     workload: the full grid and operator, a few of its right-hand sides."""
@@ -390,6 +511,11 @@ def main():
     ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
     ap.add_argument("--outer", default="emulated", choices=["fp64", "emulated"],
                     help="outer Krylov arithmetic of the mixed form: native FP64 or FP64 emulated with FP32 pairs")
+    ap.add_argument("--train-models", type=int, default=24, help="learned workload: seeded training models")
+    ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
+    ap.add_argument("--pairs-per-model", type=int, default=160)
+    ap.add_argument("--train-epochs", type=int, default=30)
+    ap.add_argument("--stag-ratio", type=float, default=0.5)
     args = ap.parse_args()
     peak, peak_kind = load_peaks()
 
@@ -419,6 +545,26 @@ def main():
         return
 
     rank, ws, dist = dist_setup()
+    if WORKLOADS[args.workload].get("learned"):
+        res, info, wl = run_learned(args, rank, ws, dist)
+        if rank != 0:
+            return
+        head = res["learned_mixed"]
+        line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
+                    warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
+                    vs_baseline=None, dtype="c64 V-cycle + bf16 network / c128 outer",
+                    data="synthetic (seeded layered+inclusion models, random source positions)",
+                    config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
+                                krylov="FGMRES(10)", outer_arithmetic=args.outer, learned=True,
+                                net_level=wl["net_level"], stag_ratio=args.stag_ratio,
+                                step="solver setup + solve of one held-out model's right-hand sides",
+                                l2="inputs larger than L2 (one step touches > 1 GB)"),
+                    gpu_launches=head["launches_per_step"] * args.steps, clocks=head["clocks"],
+                    learned_over_plain_fp64=head["rhs_per_s"] / res["fp64"]["rhs_per_s"],
+                    learned_over_mixed=head["rhs_per_s"] / res["mixed"]["rhs_per_s"],
+                    arms=res, training=info)
+        print(json.dumps(line))
+        return
     results, wl, P = run_ours(args, rank, ws, dist)
     if rank != 0:
         return

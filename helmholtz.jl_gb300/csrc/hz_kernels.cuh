@@ -26,6 +26,7 @@ struct Ctx {
   std::vector<long long> timed;    // launches with an event pair (profiling on)
   std::vector<double> total_ms;    // event-timed milliseconds per kernel
   std::vector<double> alg_bytes;   // algorithmic bytes per kernel (all launches)
+  std::vector<double> alg_flops;   // algorithmic flops per kernel (tensor-core kernels; 0 elsewhere)
   struct Pending {
     int id;
     cudaEvent_t a, b;
@@ -37,6 +38,7 @@ struct Ctx {
   void after(int id, cudaEvent_t a, double bytes);
   void resolve();  // after a stream sync: fold pending event pairs into the table
   void add_bytes(const char* name, double bytes) { alg_bytes[name_id(name)] += bytes; }
+  void add_flops(const char* name, double flops) { alg_flops[name_id(name)] += flops; }
   void release();
 };
 

@@ -67,56 +67,99 @@ constexpr int kSlotCh[NSLOT] = {16, 48, 16, 96, 32, 128, 64, 64, 64, 32, 16};
 //   out [B][N] rows of ldo, channels o_off + co (bf16, or FP32 into out32)
 // epilogue: optional ReLU; optional mask: zero where mask[row*ldm + m_off + co] <= 0
 // for co >= mask_lo.  grid.z splits Cout in chunks of 8*NT.
+//
+// A CTA (4 warps) owns 64 consecutive nodes of one sample.  Per 16-channel
+// chunk it stages, with 16-byte loads, the three strips of input rows the
+// 3x3 taps reach (66 rows each: rows p0 + dy*nx - 1 .. p0 + dy*nx + 64) and
+// the chunk of the weights, then every warp runs 9 taps x NT MMAs for its 16
+// nodes.  Shared rows are padded to 24 bf16 (12 words), so the 8 rows of a
+// fragment load start in 8 different bank groups.  Taps that leave the grid
+// read zeros (checked per node and tap), which is the zero padding.
 // ---------------------------------------------------------------------------
+constexpr int kConvTile = 64;               // nodes per CTA
+constexpr int kConvStrip = kConvTile + 2;   // rows per strip
+constexpr int kConvCK = 16;                 // channels per staged chunk
+constexpr int kConvSR = kConvCK + 8;        // padded shared row (bf16)
+
+__device__ __forceinline__ unsigned lds32(const bf16* p) { return *reinterpret_cast<const unsigned*>(p); }
+
 template <int NT>
 __global__ void __launch_bounds__(128) k_conv_mma(int nx, int ny, int Cin, int Cout, const bf16* __restrict__ in,
                                                   int ldi, int i_off, const bf16* __restrict__ w,
                                                   bf16* __restrict__ out, float* __restrict__ out32, int ldo,
                                                   int o_off, int relu, const bf16* __restrict__ mask, int ldm,
                                                   int m_off, int mask_lo) {
+  __shared__ __align__(16) bf16 s_in[3 * kConvStrip * kConvSR];
+  __shared__ __align__(16) bf16 s_w[8 * NT * 9 * kConvSR];
   const int N = nx * ny;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const int p0 = (blockIdx.x * 4 + warp) * 16;
+  const int p0 = blockIdx.x * kConvTile;
   const int bidx = blockIdx.y;
   const int co0 = blockIdx.z * 8 * NT;
-  if (p0 >= N) return;
   const int g = lane >> 2, tq = lane & 3;
+  const int la = warp * 16 + g;  // local node of fragment rows g (and g + 8)
+  const int pa = p0 + la, pb = pa + 8;
+  const bool active = p0 + warp * 16 < N;
+  // per-tap validity of the two nodes (bit t)
+  unsigned ma = 0u, mb = 0u;
+  {
+    const int ia = pa % nx, ja = pa / nx, ib = pb % nx, jb = pb / nx;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const int dx = t % 3 - 1, dy = t / 3 - 1;
+      if (pa < N && ia + dx >= 0 && ia + dx < nx && ja + dy >= 0 && ja + dy < ny) ma |= 1u << t;
+      if (pb < N && ib + dx >= 0 && ib + dx < nx && jb + dy >= 0 && jb + dy < ny) mb |= 1u << t;
+    }
+  }
   const bf16* inb = in + (long long)bidx * N * ldi + i_off;
-  const int pa = p0 + g, pb = p0 + g + 8;
-  const int ia = pa % nx, ja = pa / nx, ib = pb % nx, jb = pb / nx;
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
   float acc[NT][4];
 #pragma unroll
   for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
-  for (int t = 0; t < 9; ++t) {
-    const int dx = t % 3 - 1, dy = t / 3 - 1;
-    const bool va = pa < N && ia + dx >= 0 && ia + dx < nx && ja + dy >= 0 && ja + dy < ny;
-    const bool vb = pb < N && ib + dx >= 0 && ib + dx < nx && jb + dy >= 0 && jb + dy < ny;
-    const bf16* ra = inb + (long long)(va ? (pa + dx + dy * nx) : 0) * ldi;
-    const bf16* rb = inb + (long long)(vb ? (pb + dx + dy * nx) : 0) * ldi;
-    for (int c0 = 0; c0 < Cin; c0 += 16) {
-      const int ca = c0 + tq * 2;
-      const unsigned a0 = va ? *reinterpret_cast<const unsigned*>(ra + ca) : 0u;
-      const unsigned a1 = vb ? *reinterpret_cast<const unsigned*>(rb + ca) : 0u;
-      const unsigned a2 = va ? *reinterpret_cast<const unsigned*>(ra + ca + 8) : 0u;
-      const unsigned a3 = vb ? *reinterpret_cast<const unsigned*>(rb + ca + 8) : 0u;
+  for (int c0 = 0; c0 < Cin; c0 += kConvCK) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * kConvStrip * 2; e += blockDim.x) {
+      const int h = e & 1, rr = e >> 1;
+      const int sidx = rr / kConvStrip, k = rr % kConvStrip;
+      const int gr = p0 + (sidx - 1) * nx - 1 + k;
+      uint4 v = zero;
+      if (gr >= 0 && gr < N) v = *reinterpret_cast<const uint4*>(inb + (long long)gr * ldi + c0 + 8 * h);
+      *reinterpret_cast<uint4*>(s_in + rr * kConvSR + 8 * h) = v;
+    }
+    for (int e = threadIdx.x; e < 8 * NT * 9 * 2; e += blockDim.x) {
+      const int h = e & 1, rr = e >> 1;
+      const int co = rr / 9, t = rr % 9;
+      uint4 v = zero;
+      if (co0 + co < Cout) v = *reinterpret_cast<const uint4*>(w + ((long long)(co0 + co) * 9 + t) * Cin + c0 + 8 * h);
+      *reinterpret_cast<uint4*>(s_w + rr * kConvSR + 8 * h) = v;
+    }
+    __syncthreads();
+    if (active) {
 #pragma unroll
-      for (int n = 0; n < NT; ++n) {
-        const int co = co0 + n * 8 + g;
-        unsigned b0 = 0u, b1 = 0u;
-        if (co < Cout) {
-          const bf16* wr = w + ((long long)co * 9 + t) * Cin + ca;
-          b0 = *reinterpret_cast<const unsigned*>(wr);
-          b1 = *reinterpret_cast<const unsigned*>(wr + 8);
+      for (int t = 0; t < 9; ++t) {
+        const int dx = t % 3 - 1, dy = t / 3 - 1;
+        const bf16* ra = s_in + ((dy + 1) * kConvStrip + la + dx + 1) * kConvSR + tq * 2;
+        const bf16* rb = ra + 8 * kConvSR;
+        const bool va = (ma >> t) & 1u, vb = (mb >> t) & 1u;
+        const unsigned a0 = va ? lds32(ra) : 0u;
+        const unsigned a1 = vb ? lds32(rb) : 0u;
+        const unsigned a2 = va ? lds32(ra + 8) : 0u;
+        const unsigned a3 = vb ? lds32(rb + 8) : 0u;
+#pragma unroll
+        for (int n = 0; n < NT; ++n) {
+          const bf16* wr = s_w + ((n * 8 + g) * 9 + t) * kConvSR + tq * 2;
+          const unsigned b0 = lds32(wr), b1 = lds32(wr + 8);
+          asm volatile(
+              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+              "{%0,%1,%2,%3};\n"
+              : "+f"(acc[n][0]), "+f"(acc[n][1]), "+f"(acc[n][2]), "+f"(acc[n][3])
+              : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
         }
-        asm volatile(
-            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-            "{%0,%1,%2,%3};\n"
-            : "+f"(acc[n][0]), "+f"(acc[n][1]), "+f"(acc[n][2]), "+f"(acc[n][3])
-            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
       }
     }
   }
+  if (!active) return;
 #pragma unroll
   for (int n = 0; n < NT; ++n) {
 #pragma unroll
@@ -143,12 +186,13 @@ __global__ void __launch_bounds__(128) k_conv_mma(int nx, int ny, int Cin, int C
 static void conv_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi,
                         int i_off, int Cout, const bf16* w, bf16* out, float* out32, int ldo, int o_off, int relu,
                         const bf16* mask, int ldm, int m_off, int mask_lo) {
-  if (Cin % 16 != 0 || (ldi % 2) || (i_off % 2)) throw std::runtime_error("conv: channel layout not aligned");
+  if (Cin % 16 != 0 || (ldi % 8) || (i_off % 8) || (Cin % 16))
+    throw std::runtime_error("conv: channel layout not aligned");
   const int N = nx * ny;
-  const int tiles = (N + 15) / 16;
   const int NT = Cout <= 8 ? 1 : Cout <= 16 ? 2 : Cout <= 32 ? 4 : 8;
-  const dim3 grid((unsigned)((tiles + 3) / 4), (unsigned)B, (unsigned)((Cout + 8 * NT - 1) / (8 * NT)));
+  const dim3 grid((unsigned)((N + kConvTile - 1) / kConvTile), (unsigned)B, (unsigned)((Cout + 8 * NT - 1) / (8 * NT)));
   const double bytes = (double)B * N * (Cin * 2.0 + Cout * (out32 ? 4.0 : 2.0)) + 9.0 * Cin * Cout * 2.0;
+  ctx.add_flops(name, 2.0 * 9.0 * Cin * Cout * (double)N * B);
   switch (NT) {
     case 1:
       HZ_LAUNCH(ctx, name, bytes, k_conv_mma<1>, grid, 128, 0, nx, ny, Cin, Cout, in, ldi, i_off, w, out, out32, ldo,
@@ -178,28 +222,105 @@ __global__ void k_wflip(int Cout, int Cin, int K, const bf16* __restrict__ w, bf
   wt[idx] = (co < Cout) ? w[((long long)co * 9 + (8 - t)) * Cin + ci] : __float2bfloat16_rn(0.f);
 }
 
-// weight gradient dw[co][t][ci] += sum over the nodes of a chunk of
-// dout[n][co] * in[n + off_t][ci]  (FP32; one thread per weight, atomics per chunk)
-__global__ void __launch_bounds__(256) k_wgrad(int nx, int ny, int B, int Cin, int Cout, const bf16* __restrict__ in,
-                                               int ldi, int i_off, const bf16* __restrict__ dout, int ldd, int d_off,
-                                               float* __restrict__ dw, int chunk) {
+// Weight gradient on the tensor cores: dw[co][t][ci] += sum_n dout[n][co] * in[n + off_t][ci],
+// a GEMM with M = Cout, N = Cin and K = the nodes.  One CTA (4 warps) owns one
+// tap t (blockIdx.z) and a range of kc nodes (blockIdx.y); it stages KS-node
+// slices of the input rows (zeroed where the tap leaves the grid, so the
+// zero padding is exact) and of the output-gradient rows in shared memory,
+// runs m16n8k16 MMAs over 16-node K-steps (warp w owns the 16x8 output tiles
+// w, w+4, ...), and adds its partial sums to dw with one atomic per weight.
+// Row strides in shared memory are padded by 8 bf16 so the four node rows a
+// fragment load touches fall in different banks.
+constexpr int kWgKS = 64;        // nodes per staged slice
+constexpr int kWgMaxTiles = 16;  // 16x8 tiles per warp (Cout <= 64, Cin <= 128)
+
+__device__ __forceinline__ unsigned pack2(bf16 lo, bf16 hi) {
+  return (unsigned)__bfloat16_as_ushort(lo) | ((unsigned)__bfloat16_as_ushort(hi) << 16);
+}
+
+__global__ void __launch_bounds__(128) k_wgrad_mma(int nx, int ny, int total, int Cin, int Cout,
+                                                   const bf16* __restrict__ in, int ldi, const bf16* __restrict__ dout,
+                                                   int ldd, int d_off, float* __restrict__ dw, int kc) {
+  extern __shared__ __align__(16) unsigned char wg_smem[];
   const int N = nx * ny;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= Cout * 9 * Cin) return;
-  const int ci = idx % Cin, t = (idx / Cin) % 9, co = idx / (Cin * 9);
+  const int t = blockIdx.z;
   const int dx = t % 3 - 1, dy = t / 3 - 1;
-  const long long n0 = (long long)blockIdx.y * chunk;
-  const long long n1 = min((long long)N * B, n0 + chunk);
-  float acc = 0.f;
-  for (long long q = n0; q < n1; ++q) {
-    const int p = (int)(q % N);
-    const int i = p % nx + dx, j = p / nx + dy;
-    if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
-    const float d = __bfloat162float(dout[q * ldd + d_off + co]);
-    const float x = __bfloat162float(in[(q + dx + (long long)dy * nx) * ldi + i_off + ci]);
-    acc = fmaf(d, x, acc);
+  const int C16 = (Cout + 15) / 16 * 16;
+  const int sIn = Cin + 8, sD = C16 + 8;
+  bf16* s_in = reinterpret_cast<bf16*>(wg_smem);
+  bf16* s_d = s_in + kWgKS * sIn;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, tq = lane & 3;
+  const int NTn = Cin / 8, T = (C16 / 16) * NTn;
+  float acc[kWgMaxTiles][4];
+#pragma unroll
+  for (int k = 0; k < kWgMaxTiles; ++k) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.f;
+  const int q0 = blockIdx.y * kc;
+  const int q1 = min(total, q0 + kc);
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+  for (int qs = q0; qs < q1; qs += kWgKS) {
+    __syncthreads();
+    const int cin8 = Cin / 8, cd8 = C16 / 8;
+    for (int e = threadIdx.x; e < kWgKS * cin8; e += blockDim.x) {
+      const int r = e / cin8, c8 = e % cin8;
+      const int q = qs + r;
+      uint4 v = zero;
+      if (q < q1) {
+        const int p = q % N;
+        const int i = p % nx + dx, j = p / nx + dy;
+        if (i >= 0 && i < nx && j >= 0 && j < ny)
+          v = *reinterpret_cast<const uint4*>(in + (long long)(q + dx + dy * nx) * ldi + c8 * 8);
+      }
+      *reinterpret_cast<uint4*>(s_in + r * sIn + c8 * 8) = v;
+    }
+    for (int e = threadIdx.x; e < kWgKS * cd8; e += blockDim.x) {
+      const int r = e / cd8, c8 = e % cd8;
+      const int q = qs + r;
+      uint4 v = zero;
+      if (q < q1 && c8 * 8 < Cout) v = *reinterpret_cast<const uint4*>(dout + (long long)q * ldd + d_off + c8 * 8);
+      *reinterpret_cast<uint4*>(s_d + r * sD + c8 * 8) = v;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int kb = 0; kb < kWgKS; kb += 16) {
+      const bf16* d0 = s_d + (kb + tq * 2) * sD;
+      const bf16* i0 = s_in + (kb + tq * 2) * sIn;
+#pragma unroll
+      for (int k = 0; k < kWgMaxTiles; ++k) {
+        const int tile = warp + 4 * k;
+        if (tile < T) {
+          const int co = (tile / NTn) * 16 + g;
+          const int ci = (tile % NTn) * 8 + g;
+          const unsigned a0 = pack2(d0[co], d0[sD + co]);
+          const unsigned a1 = pack2(d0[co + 8], d0[sD + co + 8]);
+          const unsigned a2 = pack2(d0[8 * sD + co], d0[9 * sD + co]);
+          const unsigned a3 = pack2(d0[8 * sD + co + 8], d0[9 * sD + co + 8]);
+          const unsigned b0 = pack2(i0[ci], i0[sIn + ci]);
+          const unsigned b1 = pack2(i0[8 * sIn + ci], i0[9 * sIn + ci]);
+          asm volatile(
+              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+              "{%0,%1,%2,%3};\n"
+              : "+f"(acc[k][0]), "+f"(acc[k][1]), "+f"(acc[k][2]), "+f"(acc[k][3])
+              : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+      }
+    }
   }
-  atomicAdd(&dw[idx], acc);
+#pragma unroll
+  for (int k = 0; k < kWgMaxTiles; ++k) {
+    const int tile = warp + 4 * k;
+    if (tile >= T) break;
+    const int co = (tile / NTn) * 16 + g;
+    const int ci = (tile % NTn) * 8 + tq * 2;
+    if (co < Cout) {
+      atomicAdd(&dw[((long long)co * 9 + t) * Cin + ci], acc[k][0]);
+      atomicAdd(&dw[((long long)co * 9 + t) * Cin + ci + 1], acc[k][1]);
+    }
+    if (co + 8 < Cout) {
+      atomicAdd(&dw[((long long)(co + 8) * 9 + t) * Cin + ci], acc[k][2]);
+      atomicAdd(&dw[((long long)(co + 8) * 9 + t) * Cin + ci + 1], acc[k][3]);
+    }
+  }
 }
 
 // Per-channel resampling between grid levels (NHWC bf16, FP32 arithmetic).
@@ -210,10 +331,27 @@ __global__ void __launch_bounds__(256) k_wgrad(int nx, int ny, int B, int Cin, i
 // transpose = 1 applies the adjoint (fine <- coarse for mode 0, coarse <- fine for
 // mode 1).  The result, zeroed where mask <= 0 (mask may be null), is written or,
 // with accum, added to out (rounded to bf16 once).
-__device__ __forceinline__ float fw_wsum(int I, int J, int nxf, int nyf) {
-  const float sx = 1.f + (2 * I - 1 >= 0 ? 0.5f : 0.f) + (2 * I + 1 < nxf ? 0.5f : 0.f);
-  const float sy = 1.f + (2 * J - 1 >= 0 ? 0.5f : 0.f) + (2 * J + 1 < nyf ? 0.5f : 0.f);
-  return sx * sy;
+
+// One thread per (node, 8 channels): 16-byte loads and stores (every channel
+// count and offset is a multiple of 8).
+struct F8 {
+  float v[8];
+};
+__device__ __forceinline__ void ld8(const bf16* p, F8& f) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float2 x = __bfloat1622float2(h[k]);
+    f.v[2 * k] = x.x;
+    f.v[2 * k + 1] = x.y;
+  }
+}
+__device__ __forceinline__ void axpy8(float a, const bf16* p, F8& acc) {
+  F8 f;
+  ld8(p, f);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc.v[k] = fmaf(a, f.v[k], acc.v[k]);
 }
 
 __global__ void k_resample(int mode, int transpose, int nxf, int nyf, int nxc, int nyc, int B, int C,
@@ -222,23 +360,30 @@ __global__ void k_resample(int mode, int transpose, int nxf, int nyf, int nxc, i
   const int Nf = nxf * nyf, Nc = nxc * nyc;
   const bool to_coarse = (mode == 0) != (transpose != 0);
   const int No = to_coarse ? Nc : Nf, Ni = to_coarse ? Nf : Nc;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)B * No * C) return;
-  const int c = (int)(idx % C);
-  const long long q = idx / C;
-  const int b = (int)(q / No), po = (int)(q % No);
+  const int C8 = C / 8;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * No * C8) return;
+  const int c = (idx % C8) * 8;
+  const int q = idx / C8;
+  const int b = q / No, po = q % No;
   const bf16* ib = in + (long long)b * Ni * ldi + i_off + c;
-  auto rd = [&](int p) { return __bfloat162float(ib[(long long)p * ldi]); };
-  float v = 0.f;
+  F8 acc;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc.v[k] = 0.f;
   if (mode == 0 && !transpose) {  // restriction
     const int I = po % nxc, J = po / nxc;
+    float wsum = 0.f;
     for (int dj = -1; dj <= 1; ++dj)
       for (int di = -1; di <= 1; ++di) {
         const int fi = 2 * I + di, fj = 2 * J + dj;
         if (fi < 0 || fi >= nxf || fj < 0 || fj >= nyf) continue;
-        v += (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) * rd(fi + fj * nxf);
+        const float wg = (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f);
+        axpy8(wg, ib + (long long)(fi + fj * nxf) * ldi, acc);
+        wsum += wg;
       }
-    v /= fw_wsum(I, J, nxf, nyf);
+    const float inv = 1.f / wsum;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc.v[k] *= inv;
   } else if (mode == 0) {  // adjoint of the restriction: fine <- coarse parents I with |i - 2I| <= 1
     const int i = po % nxf, j = po / nxf;
     for (int J = j / 2 - 1; J <= j / 2 + 1; ++J)
@@ -246,35 +391,59 @@ __global__ void k_resample(int mode, int transpose, int nxf, int nyf, int nxc, i
         if (I < 0 || I >= nxc || J < 0 || J >= nyc) continue;
         const int di = i - 2 * I, dj = j - 2 * J;
         if (di < -1 || di > 1 || dj < -1 || dj > 1) continue;
-        v += (di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) / fw_wsum(I, J, nxf, nyf) * rd(I + J * nxc);
+        const float sx = 1.f + (2 * I - 1 >= 0 ? 0.5f : 0.f) + (2 * I + 1 < nxf ? 0.5f : 0.f);
+        const float sy = 1.f + (2 * J - 1 >= 0 ? 0.5f : 0.f) + (2 * J + 1 < nyf ? 0.5f : 0.f);
+        axpy8((di ? 0.5f : 1.f) * (dj ? 0.5f : 1.f) / (sx * sy), ib + (long long)(I + J * nxc) * ldi, acc);
       }
   } else if (!transpose) {  // prolongation
     const int i = po % nxf, j = po / nxf;
     const int i0 = i >> 1, i1 = (i + 1) >> 1, j0 = j >> 1, j1 = (j + 1) >> 1;
-    v = 0.25f * (rd(i0 + j0 * nxc) + rd(i1 + j0 * nxc) + rd(i0 + j1 * nxc) + rd(i1 + j1 * nxc));
+    axpy8(1.f, ib + (long long)(i0 + j0 * nxc) * ldi, acc);
+    axpy8(1.f, ib + (long long)(i1 + j0 * nxc) * ldi, acc);
+    axpy8(1.f, ib + (long long)(i0 + j1 * nxc) * ldi, acc);
+    axpy8(1.f, ib + (long long)(i1 + j1 * nxc) * ldi, acc);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc.v[k] *= 0.25f;
   } else {  // adjoint of the prolongation: coarse <- fine children
     const int I = po % nxc, J = po / nxc;
     for (int fj = 2 * J - 1; fj <= 2 * J + 1; ++fj)
       for (int fi = 2 * I - 1; fi <= 2 * I + 1; ++fi) {
         if (fi < 0 || fi >= nxf || fj < 0 || fj >= nyf) continue;
-        v += (fi == 2 * I ? 1.f : 0.5f) * (fj == 2 * J ? 1.f : 0.5f) * rd(fi + fj * nxf);
+        axpy8((fi == 2 * I ? 1.f : 0.5f) * (fj == 2 * J ? 1.f : 0.5f), ib + (long long)(fi + fj * nxf) * ldi, acc);
       }
   }
   const long long row = (long long)b * No + po;
-  if (mask && !(__bfloat162float(mask[row * ldm + m_off + c]) > 0.f)) v = 0.f;
-  const long long o = row * ldo + o_off + c;
-  if (accum) v += __bfloat162float(out[o]);
-  out[o] = __float2bfloat16_rn(v);
+  if (mask) {
+    F8 mk;
+    ld8(mask + row * ldm + m_off + c, mk);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (!(mk.v[k] > 0.f)) acc.v[k] = 0.f;
+  }
+  bf16* o = out + row * ldo + o_off + c;
+  if (accum) {
+    F8 old;
+    ld8(o, old);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc.v[k] += old.v[k];
+  }
+  __align__(16) __nv_bfloat162 r[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r[k] = __floats2bfloat162_rn(acc.v[2 * k], acc.v[2 * k + 1]);
+  *reinterpret_cast<uint4*>(o) = *reinterpret_cast<const uint4*>(r);
 }
 
 static void resample(Ctx& ctx, int mode, int transpose, const int* gx, const int* gy, int lf, int B, int C,
                      const bf16* in, int ldi, int i_off, bf16* out, int ldo, int o_off, int accum,
                      const bf16* mask = nullptr, int ldm = 0, int m_off = 0) {
+  if (C % 8 || ldi % 8 || i_off % 8 || ldo % 8 || o_off % 8 || (mask && (ldm % 8 || m_off % 8)))
+    throw std::runtime_error("resample: channel layout not aligned");
   const int nxf = gx[lf], nyf = gy[lf], nxc = gx[lf + 1], nyc = gy[lf + 1];
   const bool to_coarse = (mode == 0) != (transpose != 0);
   const long long no = to_coarse ? (long long)nxc * nyc : (long long)nxf * nyf;
   const long long ni = to_coarse ? (long long)nxf * nyf : (long long)nxc * nyc;
-  const long long total = (long long)B * no * C;
+  const long long total = (long long)B * no * (C / 8);
+  if (total >= (1LL << 31)) throw std::runtime_error("resample: batch too large");
   HZ_LAUNCH(ctx, "net_resample", (double)B * (no + ni) * C * 2.0, k_resample, (unsigned)((total + 255) / 256), 256, 0,
             mode, transpose, nxf, nyf, nxc, nyc, B, C, in, ldi, i_off, out, ldo, o_off, accum, mask, ldm, m_off);
 }
@@ -582,11 +751,17 @@ void CoarseNet::conv_bwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi,
   const auto& L = kSpec[l];
   const int nx = gx_[lev], ny = gy_[lev];
   const long long nodes = (long long)nx * ny * B;
-  const int total = L.coutp * 9 * L.cinp;
-  const int chunk = (int)std::max<long long>(256, (nodes + 65534) / 65535);  // grid.y <= 65535
-  const dim3 grid((unsigned)((total + 255) / 256), (unsigned)((nodes + chunk - 1) / chunk));
-  HZ_LAUNCH(c, "net_wgrad", (double)nodes * (L.cinp + L.coutp) * 2.0, k_wgrad, grid, 256, 0, nx, ny, B, L.cinp,
-            L.coutp, in, ldi, i_off, dout, ldd, d_off, g32_ + woff_[l], chunk);
+  if (nodes >= (1LL << 31)) throw std::runtime_error("coarse net: batch too large for the weight gradient");
+  if (L.cinp % 8 || L.cinp > 128 || L.coutp > 64 || ldi % 8 || ldd % 8 || d_off % 8 || i_off != 0)
+    throw std::runtime_error("coarse net: weight-gradient layout not supported");
+  // node range per CTA: enough CTAs (9 taps x chunks) for a few waves, few atomics
+  long long kc = (nodes + 134) / 135;
+  kc = std::max<long long>(kWgKS, (kc + kWgKS - 1) / kWgKS * kWgKS);
+  const dim3 grid(1u, (unsigned)((nodes + kc - 1) / kc), 9u);
+  const size_t smem = (size_t)kWgKS * ((L.cinp + 8) + (round16(L.coutp) + 8)) * 2;
+  c.add_flops("net_wgrad", 2.0 * 9.0 * L.cinp * L.coutp * (double)nodes);
+  HZ_LAUNCH(c, "net_wgrad", (double)nodes * (L.cinp + L.coutp) * 2.0 * 9.0, k_wgrad_mma, grid, 128, smem, nx, ny,
+            (int)nodes, L.cinp, L.coutp, in, ldi, dout, ldd, d_off, g32_ + woff_[l], (int)kc);
   if (!din) return;
   const int K = round16(L.coutp);
   const int tot = L.cinp * 9 * K;

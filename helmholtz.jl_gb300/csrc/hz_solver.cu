@@ -1463,34 +1463,50 @@ int hz_copy(const hz_handle* h, hz_handle** out) {
 
 void* hz_stream(hz_handle* h) { return h ? (void*)h->ctx.stream : nullptr; }
 
+static int ctx_times(Ctx& c, int dev, int32_t idx, char* name, int32_t name_len, int64_t* launches,
+                     int64_t* timed_launches, double* total_ms, double* alg_bytes, double* alg_flops) {
+  cudaSetDevice(dev);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  c.resolve();
+  const int n = (int)c.names.size();
+  if (idx < 0 || idx >= n) return n;
+  if (name && name_len > 0) {
+    std::strncpy(name, c.names[idx].c_str(), (size_t)name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (launches) *launches = c.counts[idx];
+  if (timed_launches) *timed_launches = c.timed[idx];
+  if (total_ms) *total_ms = c.total_ms[idx];
+  if (alg_bytes) *alg_bytes = c.alg_bytes[idx];
+  if (alg_flops) *alg_flops = c.alg_flops[idx];
+  return n;
+}
+
+static void ctx_reset(Ctx& c, int dev) {
+  cudaSetDevice(dev);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  c.resolve();
+  std::fill(c.counts.begin(), c.counts.end(), 0);
+  std::fill(c.timed.begin(), c.timed.end(), 0);
+  std::fill(c.total_ms.begin(), c.total_ms.end(), 0.0);
+  std::fill(c.alg_bytes.begin(), c.alg_bytes.end(), 0.0);
+  std::fill(c.alg_flops.begin(), c.alg_flops.end(), 0.0);
+}
+
 int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                     int64_t* timed_launches, double* total_ms, double* alg_bytes) {
   if (!h) return HZ_ERR_ARG;
-  cudaSetDevice(h->dev);
-  if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
-  h->ctx.resolve();
-  const int n = (int)h->ctx.names.size();
-  if (idx < 0 || idx >= n) return n;
-  if (name && name_len > 0) {
-    std::strncpy(name, h->ctx.names[idx].c_str(), (size_t)name_len - 1);
-    name[name_len - 1] = 0;
-  }
-  if (launches) *launches = h->ctx.counts[idx];
-  if (timed_launches) *timed_launches = h->ctx.timed[idx];
-  if (total_ms) *total_ms = h->ctx.total_ms[idx];
-  if (alg_bytes) *alg_bytes = h->ctx.alg_bytes[idx];
-  return n;
+  return ctx_times(h->ctx, h->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes, nullptr);
+}
+
+int hz_kernel_flops(hz_handle* h, int32_t idx, double* alg_flops) {
+  if (!h) return HZ_ERR_ARG;
+  return ctx_times(h->ctx, h->dev, idx, nullptr, 0, nullptr, nullptr, nullptr, nullptr, alg_flops);
 }
 
 int hz_reset_kernel_times(hz_handle* h) {
   if (!h) return HZ_ERR_ARG;
-  cudaSetDevice(h->dev);
-  if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
-  h->ctx.resolve();
-  std::fill(h->ctx.counts.begin(), h->ctx.counts.end(), 0);
-  std::fill(h->ctx.timed.begin(), h->ctx.timed.end(), 0);
-  std::fill(h->ctx.total_ms.begin(), h->ctx.total_ms.end(), 0.0);
-  std::fill(h->ctx.alg_bytes.begin(), h->ctx.alg_bytes.end(), 0.0);
+  ctx_reset(h->ctx, h->dev);
   return HZ_OK;
 }
 
@@ -1619,6 +1635,29 @@ int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_
     hz::CoarseNet& c = *net->net;
     c.train(c.ctx, x, t, (int)nx, (int)ny, npairs, batch, epochs, lr, (unsigned)seed, loss_hist);
   });
+}
+
+int hz_net_set_profile(hz_net* net, int32_t on) {
+  if (!net) return HZ_ERR_ARG;
+  cudaSetDevice(net->dev);
+  Ctx& c = net->net->ctx;
+  cudaStreamSynchronize(c.stream);
+  c.resolve();
+  c.profile = on != 0;
+  return HZ_OK;
+}
+
+int hz_net_kernel_times(hz_net* net, int32_t idx, char* name, int32_t name_len, int64_t* launches,
+                        int64_t* timed_launches, double* total_ms, double* alg_bytes, double* alg_flops) {
+  if (!net) return HZ_ERR_ARG;
+  return ctx_times(net->net->ctx, net->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes,
+                   alg_flops);
+}
+
+int hz_net_reset_kernel_times(hz_net* net) {
+  if (!net) return HZ_ERR_ARG;
+  ctx_reset(net->net->ctx, net->dev);
+  return HZ_OK;
 }
 
 int hz_attach_net(hz_handle* h, hz_net* net, int32_t level, double stag_ratio) {

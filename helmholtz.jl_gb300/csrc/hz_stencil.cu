@@ -31,6 +31,7 @@ int Ctx::name_id(const char* name) {
   timed.push_back(0);
   total_ms.push_back(0.0);
   alg_bytes.push_back(0.0);
+  alg_flops.push_back(0.0);
   return (int)names.size() - 1;
 }
 

@@ -108,6 +108,29 @@ class CoarseNet:
         L.check(L.load().hz_net_gradient(self._h, px, pt, nx, ny, B, mem, C.byref(loss), g.ctypes.data))
         return loss.value, g
 
+    def set_profile(self, on: bool) -> None:
+        """Time every kernel launch of the network's own stream with CUDA events."""
+        L.check(L.load().hz_net_set_profile(self._h, int(bool(on))))
+
+    def kernel_times(self) -> list[dict]:
+        """Launch table of the network's stream: name, launches, timed launches,
+        milliseconds, algorithmic bytes and flops per kernel."""
+        lib = L.load()
+        n = lib.hz_net_kernel_times(self._h, -1, None, 0, None, None, None, None, None)
+        rows = []
+        for i in range(n):
+            name = C.create_string_buffer(64)
+            la, lt = C.c_int64(), C.c_int64()
+            ms, by, fl = C.c_double(), C.c_double(), C.c_double()
+            lib.hz_net_kernel_times(self._h, i, name, 64, C.byref(la), C.byref(lt), C.byref(ms), C.byref(by),
+                                    C.byref(fl))
+            rows.append(dict(name=name.value.decode(), launches=la.value, timed=lt.value, ms=ms.value,
+                             bytes=by.value, flops=fl.value))
+        return rows
+
+    def reset_kernel_times(self) -> None:
+        L.check(L.load().hz_net_reset_kernel_times(self._h))
+
     def train(self, x, t, epochs: int = 10, batch: int = 32, lr: float = 2e-3, seed: int = 0) -> np.ndarray:
         """Adam over the pairs (CUDA tensors) for epochs passes; returns the mean loss per epoch."""
         if not (_is_device_array(x) and _is_device_array(t)):

@@ -188,6 +188,9 @@ void* hz_stream(hz_handle* h);
 int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                     int64_t* timed_launches, double* total_ms, double* alg_bytes);
 int hz_reset_kernel_times(hz_handle* h);
+/* Algorithmic flops of entry idx of the launch table (the tensor-core kernels
+ * of the learned correction; 0 for the memory-bound kernels). */
+int hz_kernel_flops(hz_handle* h, int32_t idx, double* alg_flops);
 /* Turn per-launch CUDA-event timing on (1) or off (0) (options.profile at create time). */
 int hz_set_profile(hz_handle* h, int32_t on);
 
@@ -230,6 +233,12 @@ int hz_net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int
  * loss_hist (host, epochs entries, may be NULL) gets the mean loss per epoch. */
 int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t npairs, int32_t batch,
                  int32_t epochs, double lr, int32_t seed, double* loss_hist);
+/* Launch table of the network's own stream (training, standalone inference),
+ * as hz_kernel_times plus the algorithmic flops; profiling on/off and reset. */
+int hz_net_set_profile(hz_net* net, int32_t on);
+int hz_net_kernel_times(hz_net* net, int32_t idx, char* name, int32_t name_len, int64_t* launches,
+                        int64_t* timed_launches, double* total_ms, double* alg_bytes, double* alg_flops);
+int hz_net_reset_kernel_times(hz_net* net);
 /* Use the network for the coarse-grid correction of multigrid level `level`
  * (1 .. levels-1; 2D, FGMRES only: the network is a nonlinear preconditioner).
  * A restart cycle that reduces some column's residual by less than stag_ratio
