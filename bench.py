@@ -385,7 +385,7 @@ def run_learned(args, rank, ws, dist):
         wl["nrhs"] = args.nrhs
     level = wl["net_level"]
 
-    def solver(P, precision, outer="fp64", max_outer=200):
+    def solver(P, precision, outer="fp64", max_outer=60):
         M = hz.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
         gam = gamma_of(P, wl["pad"], lib, hz)
         param = hz.HelmholtzParam(M, gam, P["m"], P["w"], True, True)
@@ -431,8 +431,8 @@ def run_learned(args, rank, ws, dist):
     res = {}
     nrhs = wl["nrhs"]
     for name, prec, use_net in arms:
-        nsteps = args.steps if name != "fp64" else max(1, args.plain_steps)
-        tot, iters, relres, fb, calls, launches = 0.0, [], [], 0, 0, 0
+        nsteps = args.steps
+        tot, iters, relres, fb, calls, launches, conv = 0.0, [], [], 0, 0, 0, 0
         clk = None
         for k in range(args.warmup + nsteps):
             P = make_problem(wl, seed=50_000 + 1000 * rank + k)
@@ -457,6 +457,7 @@ def run_learned(args, rank, ws, dist):
                 tot += dt
                 iters.append(float(np.mean(S.last_iters)))
                 relres.append(float(np.max(S.last_relres)))
+                conv += int(np.sum(S.last_relres <= wl["tol"]))
                 launches += int(S.last_stats.kernel_launches)
                 c_, f_ = hz.learned.learned_stats(S)
                 calls += c_
@@ -465,6 +466,7 @@ def run_learned(args, rank, ws, dist):
         tot = max_over_ranks(dist, tot)
         res[name] = dict(rhs_per_s=nrhs * ws * nsteps / tot, ms_per_step=1000.0 * tot / nsteps,
                          mean_iters=float(np.mean(iters)), max_relres=float(np.max(relres)), fallbacks=fb,
+                         converged_cols=conv, cols=nrhs * nsteps, converged_rhs_per_s=conv * ws / tot,
                          net_calls=calls, launches_per_step=launches // nsteps, clocks=clk)
     info = dict(train_models=args.train_models, train_pairs=npairs, epochs=args.train_epochs,
                 loss_first=float(hist[0]), loss_last=float(hist[-1]), collect_s=collect_s, train_s=train_s,
@@ -511,11 +513,13 @@ def main():
     ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
     ap.add_argument("--outer", default="emulated", choices=["fp64", "emulated"],
                     help="outer Krylov arithmetic of the mixed form: native FP64 or FP64 emulated with FP32 pairs")
-    ap.add_argument("--train-models", type=int, default=24, help="learned workload: seeded training models")
+    ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
     ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
-    ap.add_argument("--pairs-per-model", type=int, default=160)
-    ap.add_argument("--train-epochs", type=int, default=30)
-    ap.add_argument("--stag-ratio", type=float, default=0.5)
+    ap.add_argument("--pairs-per-model", type=int, default=200)
+    ap.add_argument("--train-epochs", type=int, default=20)
+    ap.add_argument("--stag-ratio", type=float, default=0.95,
+                    help="learned workload: a restart cycle reducing a residual by less than this hands over "
+                         "to the plain cycle")
     args = ap.parse_args()
     peak, peak_kind = load_peaks()
 
@@ -550,7 +554,9 @@ def main():
         if rank != 0:
             return
         head = res["learned_mixed"]
-        line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
+        # the metric counts right-hand sides solved to the tolerance: columns that
+        # did not converge within the restart limit count as time spent, not as solved
+        line = dict(metric=METRIC, value=head["converged_rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                     warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
                     vs_baseline=None, dtype="c64 V-cycle + bf16 network / c128 outer",
                     data="synthetic (seeded layered+inclusion models, random source positions)",
@@ -560,8 +566,10 @@ def main():
                                 step="solver setup + solve of one held-out model's right-hand sides",
                                 l2="inputs larger than L2 (one step touches > 1 GB)"),
                     gpu_launches=head["launches_per_step"] * args.steps, clocks=head["clocks"],
-                    learned_over_plain_fp64=head["rhs_per_s"] / res["fp64"]["rhs_per_s"],
-                    learned_over_mixed=head["rhs_per_s"] / res["mixed"]["rhs_per_s"],
+                    learned_over_plain_fp64=(head["converged_rhs_per_s"] / res["fp64"]["converged_rhs_per_s"]
+                                             if res["fp64"]["converged_rhs_per_s"] > 0 else None),
+                    learned_over_mixed=(head["converged_rhs_per_s"] / res["mixed"]["converged_rhs_per_s"]
+                                        if res["mixed"]["converged_rhs_per_s"] > 0 else None),
                     arms=res, training=info)
         print(json.dumps(line))
         return

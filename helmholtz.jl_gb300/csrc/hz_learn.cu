@@ -83,6 +83,20 @@ constexpr int kConvSR = kConvCK + 8;        // padded shared row (bf16)
 
 __device__ __forceinline__ unsigned lds32(const bf16* p) { return *reinterpret_cast<const unsigned*>(p); }
 
+// ldmatrix: four (two) 8x8 b16 matrices from shared memory, rows addressed by
+// lanes 0-7, 8-15, 16-23, 24-31 (0-7, 8-15); lane l receives row l/4, columns
+// 2(l%4), 2(l%4)+1 of matrix i in register i -- the m16n8k16 fragment layout.
+__device__ __forceinline__ void ldsm_x4(const bf16* p, unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2(const bf16* p, unsigned& r0, unsigned& r1) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(a));
+}
+
 template <int NT>
 __global__ void __launch_bounds__(128) k_conv_mma(int nx, int ny, int Cin, int Cout, const bf16* __restrict__ in,
                                                   int ldi, int i_off, const bf16* __restrict__ w,
@@ -136,25 +150,40 @@ __global__ void __launch_bounds__(128) k_conv_mma(int nx, int ny, int Cin, int C
     }
     __syncthreads();
     if (active) {
+      // ldmatrix row addresses of this lane: A matrix m = lane/8 covers nodes
+      // warp*16 + 8(m&1) + lane%8 and channels 8(m>>1)..; B matrix m covers the
+      // weight rows of output channel 8(n + (m>>1)) + lane%8, channels 8(m&1)..
+      const int lm = lane >> 3, lr = lane & 7;
+      const int a_node = warp * 16 + (lm & 1) * 8 + lr;
+      const int a_col = (lm >> 1) * 8;
+      const int b_row = (lm >> 1) * 8 + lr;
+      const int b_col = (lm & 1) * 8;
 #pragma unroll
       for (int t = 0; t < 9; ++t) {
         const int dx = t % 3 - 1, dy = t / 3 - 1;
-        const bf16* ra = s_in + ((dy + 1) * kConvStrip + la + dx + 1) * kConvSR + tq * 2;
-        const bf16* rb = ra + 8 * kConvSR;
-        const bool va = (ma >> t) & 1u, vb = (mb >> t) & 1u;
-        const unsigned a0 = va ? lds32(ra) : 0u;
-        const unsigned a1 = vb ? lds32(rb) : 0u;
-        const unsigned a2 = va ? lds32(ra + 8) : 0u;
-        const unsigned a3 = vb ? lds32(rb + 8) : 0u;
+        unsigned a0, a1, a2, a3;
+        ldsm_x4(s_in + ((dy + 1) * kConvStrip + a_node + dx + 1) * kConvSR + a_col, a0, a1, a2, a3);
+        // lane's A rows are its own nodes pa (a0, a2) and pb (a1, a3): zero the taps off the grid
+        if (!((ma >> t) & 1u)) a0 = a2 = 0u;
+        if (!((mb >> t) & 1u)) a1 = a3 = 0u;
 #pragma unroll
-        for (int n = 0; n < NT; ++n) {
-          const bf16* wr = s_w + ((n * 8 + g) * 9 + t) * kConvSR + tq * 2;
-          const unsigned b0 = lds32(wr), b1 = lds32(wr + 8);
+        for (int n = 0; n < NT; n += 2) {
+          unsigned b0, b1, b2 = 0u, b3 = 0u;
+          if (n + 1 < NT)
+            ldsm_x4(s_w + ((n * 8 + b_row) * 9 + t) * kConvSR + b_col, b0, b1, b2, b3);
+          else
+            ldsm_x2(s_w + ((n * 8 + (lr & 7)) * 9 + t) * kConvSR + (lm & 1) * 8, b0, b1);
           asm volatile(
               "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
               "{%0,%1,%2,%3};\n"
               : "+f"(acc[n][0]), "+f"(acc[n][1]), "+f"(acc[n][2]), "+f"(acc[n][3])
               : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+          if (n + 1 < NT)
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                "{%0,%1,%2,%3};\n"
+                : "+f"(acc[n + 1][0]), "+f"(acc[n + 1][1]), "+f"(acc[n + 1][2]), "+f"(acc[n + 1][3])
+                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b2), "r"(b3));
         }
       }
     }

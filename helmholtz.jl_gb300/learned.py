@@ -189,7 +189,7 @@ def collect_pairs(solver: ShiftedLaplacianMultigridSolver, B, level: int = 2, sw
 
 
 def attach(solver: ShiftedLaplacianMultigridSolver, net: CoarseNet | None, level: int = 2,
-           stag_ratio: float = 0.5) -> None:
+           stag_ratio: float = 0.95) -> None:
     """Use `net` for the coarse-grid correction of `level` in every later solve
     (FGMRES only); net=None detaches.  A restart cycle that reduces a column's
     residual by less than stag_ratio hands that solve to the plain cycle."""
