@@ -21,7 +21,8 @@ using Multigrid: MGparam
 
 export HelmholtzParam, ShiftedLaplacianMultigridSolver, getShiftedLaplacianMultigridSolver, solveLinearSystem,
        solveLinearSystem!, copySolver, clear!, getMaximalFrequency, getABL, getSommerfeldBC,
-       getAcousticPointSource, getHelmholtzFun, HzApply
+       getAcousticPointSource, getHelmholtzFun, HzApply,
+       CoarseNet, netWeights, setNetWeights!, netForward, netGradient, netTrain!, collectPairs!, attachNet!
 
 const libhelmgpu = get(ENV, "HELMGPU_LIB", joinpath(@__DIR__, "..", "libhelmgpu.so"))
 
@@ -78,6 +79,13 @@ const HZ_MEM_HOST = Int32(0)
 const HZ_PREC_FP64 = Int32(0)
 const HZ_PREC_MIXED = Int32(1)
 const HZ_OP_H = Int32(0)
+const HZ_MEM_DEVICE = Int32(1)
+const HZ_OUTER_FP64 = Int32(0)
+const HZ_OUTER_EMULATED = Int32(1)
+const HZ_KRYLOV_FGMRES = Int32(0)
+const HZ_KRYLOV_BICGSTAB = Int32(1)
+const HZ_COARSE_GALERKIN = Int32(0)
+const HZ_COARSE_REDISCRETIZE = Int32(1)
 
 lasterror(h::Ptr{Cvoid}) = unsafe_string(ccall((:hz_last_error, libhelmgpu), Cstring, (Ptr{Cvoid},), h))
 function check(st::Integer, h::Ptr{Cvoid} = C_NULL)
@@ -148,14 +156,20 @@ mutable struct ShiftedLaplacianMultigridSolver <: AbstractSolver   # src/Shifted
     nPrec::Int
     solveTime::Real
     precision::Int32            # HZ_PREC_FP64 (plain) or HZ_PREC_MIXED
+    outerArith::Int32           # HZ_OUTER_FP64 or HZ_OUTER_EMULATED (mixed form only)
+    coarseOp::Int32             # HZ_COARSE_GALERKIN or HZ_COARSE_REDISCRETIZE
     handle::Ptr{Cvoid}
+    net::Any                    # attached CoarseNet (or nothing), its level and stagnation ratio
+    netLevel::Int32
+    netStag::Float64
 end
 
 function getShiftedLaplacianMultigridSolver(helmParam::HelmholtzParam, MG::MGparam, shift::Array{Float64},
                                             Krylov::String = "BiCGSTAB", inner::Int64 = 5, verbose::Bool = false;
-                                            precision::Int32 = HZ_PREC_FP64)
+                                            precision::Int32 = HZ_PREC_FP64, outerArith::Int32 = HZ_OUTER_FP64,
+                                            coarseOp::Int32 = HZ_COARSE_GALERKIN)
     s = ShiftedLaplacianMultigridSolver(helmParam, MG, shift, Krylov, inner, 0, verbose, 0.0, 0, 0.0, precision,
-                                        C_NULL)
+                                        outerArith, coarseOp, C_NULL, nothing, Int32(0), 0.95)
     finalizer(release!, s)
     return s
 end
@@ -173,7 +187,8 @@ function options(s::ShiftedLaplacianMultigridSolver)
     MG = s.MG
     MG.relaxType == "Jac" || throw(ArgumentError("relaxType $(MG.relaxType): only \"Jac\" is built"))
     MG.cycleType in ('V', 'W') || throw(ArgumentError("cycleType $(MG.cycleType): only 'V' and 'W' are built"))
-    s.Krylov == "GMRES" || throw(ArgumentError("Krylov $(s.Krylov): only \"GMRES\" (FGMRES) is built"))
+    s.Krylov in ("GMRES", "BiCGSTAB") ||
+        throw(ArgumentError("Krylov $(s.Krylov): \"GMRES\" (FGMRES) and \"BiCGSTAB\" are built"))
     o = HzOptions()
     ccall((:hz_default_options, libhelmgpu), Cvoid, (Ref{HzOptions},), o)
     o.levels = MG.levels
@@ -186,6 +201,9 @@ function options(s::ShiftedLaplacianMultigridSolver)
     o.inner = s.inner
     o.shift = s.shift[1]
     o.precision = s.precision
+    o.outer_arith = s.outerArith
+    o.coarse_op = s.coarseOp
+    o.krylov = s.Krylov == "BiCGSTAB" ? HZ_KRYLOV_BICGSTAB : HZ_KRYLOV_FGMRES
     o.verbose = Int32(s.verbose)
     return o
 end
@@ -199,6 +217,7 @@ function ensure_handle!(s::ShiftedLaplacianMultigridSolver)
         check(ccall((:hz_create, libhelmgpu), Cint, (Ref{HzProblem}, Ref{HzOptions}, Ref{Ptr{Cvoid}}), prob, o, h))
     end
     s.handle = h[]
+    s.net === nothing || attach_handle!(s)
     return s.handle
 end
 
@@ -238,7 +257,8 @@ end
 
 function copySolver(s::ShiftedLaplacianMultigridSolver)   # src/ShiftedLaplacianMultigridSolver.jl:18-22
     return getShiftedLaplacianMultigridSolver(s.helmParam, s.MG, s.shift, s.Krylov, s.inner, s.verbose;
-                                              precision = s.precision)
+                                              precision = s.precision, outerArith = s.outerArith,
+                                              coarseOp = s.coarseOp)
 end
 
 function clear!(s::ShiftedLaplacianMultigridSolver)        # src/ShiftedLaplacianMultigridSolver.jl:105-109
@@ -264,5 +284,85 @@ function (f::HzApply)(x::AbstractVecOrMat)
     return y
 end
 getHelmholtzFun(s::ShiftedLaplacianMultigridSolver, transpose::Integer = 0) = HzApply(s, Int32(transpose))
+
+# ---- learned coarse-grid correction (no counterpart in the reference) ------------
+# Arrays are Julia column-major (4, nx, ny, batch) for inputs and (2, nx, ny, batch)
+# for targets / outputs (Float32): the C layout [batch][nx*ny][channels].
+mutable struct CoarseNet
+    ptr::Ptr{Cvoid}
+end
+function CoarseNet(seed::Integer = 0, device::Integer = 0)
+    p = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hz_net_create, libhelmgpu), Cint, (Int32, Int32, Ref{Ptr{Cvoid}}), seed, device, p))
+    net = CoarseNet(p[])
+    finalizer(n -> (n.ptr != C_NULL && ccall((:hz_net_destroy, libhelmgpu), Cint, (Ptr{Cvoid},), n.ptr);
+                    n.ptr = C_NULL), net)
+    return net
+end
+function netWeights(net::CoarseNet)
+    w = Vector{Float32}(undef, ccall((:hz_net_num_params, libhelmgpu), Int64, ()))
+    check(ccall((:hz_net_get_weights, libhelmgpu), Cint, (Ptr{Cvoid}, Ptr{Float32}), net.ptr, w))
+    return w
+end
+setNetWeights!(net::CoarseNet, w::Vector{Float32}) =
+    check(ccall((:hz_net_set_weights, libhelmgpu), Cint, (Ptr{Cvoid}, Ptr{Float32}), net.ptr, w))
+function netForward(net::CoarseNet, x::Array{Float32,4})
+    _, nx, ny, b = size(x)
+    y = Array{Float32}(undef, 2, nx, ny, b)
+    check(ccall((:hz_net_forward, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Int64, Int64, Int32, Int32),
+                net.ptr, x, y, nx, ny, Int32(b), HZ_MEM_HOST))
+    return y
+end
+function netGradient(net::CoarseNet, x::Array{Float32,4}, t::Array{Float32,4})
+    _, nx, ny, b = size(x)
+    g = similar(netWeights(net))
+    loss = Ref{Float64}(0.0)
+    check(ccall((:hz_net_gradient, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Int64, Int64, Int32, Int32, Ref{Float64}, Ptr{Float32}),
+                net.ptr, x, t, nx, ny, Int32(b), HZ_MEM_HOST, loss, g))
+    return loss[], g
+end
+# x, t: DEVICE pointers (e.g. from CUDA.jl CuArrays) to npairs pairs
+function netTrain!(net::CoarseNet, x::Ptr{Float32}, t::Ptr{Float32}, nx::Integer, ny::Integer, npairs::Integer;
+                   batch::Integer = 32, epochs::Integer = 20, lr::Float64 = 2e-3, seed::Integer = 0)
+    hist = zeros(Float64, epochs)
+    check(ccall((:hz_net_train, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Int64, Int64, Int64, Int32, Int32, Float64, Int32,
+                 Ptr{Float64}),
+                net.ptr, x, t, nx, ny, npairs, Int32(batch), Int32(epochs), lr, Int32(seed), hist))
+    return hist
+end
+# solves with the FP64 solver s while recording the pairs of `level` into the DEVICE
+# arrays x (4 x nx x ny x maxPairs) and t (2 x nx x ny x maxPairs); returns (count, plainErr, X)
+function collectPairs!(s::ShiftedLaplacianMultigridSolver, B::AbstractVecOrMat, level::Integer, maxPairs::Integer,
+                       x::Ptr{Float32}, t::Ptr{Float32}; sweeps::Integer = 2)
+    h = ensure_handle!(s)
+    Bc = convert(Matrix{ComplexF64}, reshape(B, size(B, 1), :))
+    X = similar(Bc)
+    pe = zeros(Float64, maxPairs)
+    rr = Ref{Float64}(0.0)
+    cnt = Ref{Int64}(0)
+    check(ccall((:hz_collect_pairs, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Int64, Int32, Int32, Int32, Int32, Int64,
+                 Ptr{Float32}, Ptr{Float32}, Ptr{Float64}, Ref{Float64}, Ref{Int64}),
+                h, Bc, X, size(Bc, 1), Int32(size(Bc, 2)), HZ_MEM_HOST, Int32(level), Int32(sweeps), maxPairs,
+                x, t, pe, rr, cnt), h)
+    return cnt[], pe[1:cnt[]], X
+end
+# use net for the coarse-grid correction of `level` in the later solves of s (FGMRES only);
+# net = nothing detaches
+function attachNet!(s::ShiftedLaplacianMultigridSolver, net, level::Integer = 2, stagRatio::Float64 = 0.95)
+    s.net = net
+    s.netLevel = Int32(level)
+    s.netStag = stagRatio
+    s.handle != C_NULL && attach_handle!(s)
+    return s
+end
+function attach_handle!(s::ShiftedLaplacianMultigridSolver)
+    p = s.net === nothing ? C_NULL : s.net.ptr
+    check(ccall((:hz_attach_net, libhelmgpu), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Int32, Float64),
+                s.handle, p, s.netLevel, s.netStag), s.handle)
+end
 
 end # module
