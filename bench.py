@@ -266,6 +266,7 @@ def run_ours(args, rank, ws, dist):
         o = L.hz_options()
         lib.hz_default_options(C.byref(o))
         o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, 200
+        o.cycle = ord(args.cycle)
         if args.krylov == "bicgstab":
             o.krylov, o.max_outer = L.HZ_KRYLOV_BICGSTAB, 2000
         o.precision = precision
@@ -389,8 +390,8 @@ def run_learned(args, rank, ws, dist):
         M = hz.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
         gam = gamma_of(P, wl["pad"], lib, hz)
         param = hz.HelmholtzParam(M, gam, P["m"], P["w"], True, True)
-        MG = hz.getMGparam(complex, int, wl["levels"], 1, max_outer, wl["tol"], "Jac", 0.8, 1, 1, "V", "Julia",
-                           0.5, 0.0, precision=precision, outerArithmetic=outer)
+        MG = hz.getMGparam(complex, int, wl["levels"], 1, max_outer, wl["tol"], "Jac", 0.8, 1, 1, args.cycle,
+                           "Julia", 0.5, 0.0, precision=precision, outerArithmetic=outer)
         return hz.getShiftedLaplacianMultigridSolver(param, MG, 0.5, "GMRES", 10)
 
     # 1. training pairs from the FP64 solver on seeded training models
@@ -513,6 +514,8 @@ def main():
     ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
     ap.add_argument("--outer", default="emulated", choices=["fp64", "emulated"],
                     help="outer Krylov arithmetic of the mixed form: native FP64 or FP64 emulated with FP32 pairs")
+    ap.add_argument("--cycle", default="V", choices=["V", "W", "K"],
+                    help="multigrid cycle (K: two FGMRES steps per coarse level)")
     ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
     ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
     ap.add_argument("--pairs-per-model", type=int, default=200)
@@ -561,7 +564,7 @@ def main():
                     vs_baseline=None, dtype="c64 V-cycle + bf16 network / c128 outer",
                     data="synthetic (seeded layered+inclusion models, random source positions)",
                     config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
-                                krylov="FGMRES(10)", outer_arithmetic=args.outer, learned=True,
+                                krylov="FGMRES(10)", cycle=args.cycle, outer_arithmetic=args.outer, learned=True,
                                 net_level=wl["net_level"], stag_ratio=args.stag_ratio,
                                 step="solver setup + solve of one held-out model's right-hand sides",
                                 l2="inputs larger than L2 (one step touches > 1 GB)"),
@@ -603,7 +606,7 @@ def main():
                        if args.precision != "fp64" else "c128"),
                 data="synthetic (seeded layered model)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
-                            krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB",
+                            krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB", cycle=args.cycle,
                             outer_arithmetic=args.outer,
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
                             l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9)),

@@ -393,8 +393,8 @@ def getMGparam(*args, transferType: str | None = None, precision: str = "fp64",
 def _validate_mg(MG: MGparam):
     if MG.relaxType != "Jac":
         raise NotImplementedError(f"relaxType {MG.relaxType!r}: only damped Jacobi ('Jac') is built")
-    if MG.cycleType not in ("V", "W"):
-        raise NotImplementedError(f"cycleType {MG.cycleType!r}: only 'V' and 'W' cycles are built")
+    if MG.cycleType not in ("V", "W", "K"):
+        raise NotImplementedError(f"cycleType {MG.cycleType!r}: only 'V', 'W' and 'K' cycles are built")
     if MG.coarseSolveType not in _SUPPORTED_COARSE:
         raise NotImplementedError(f"coarseSolveType {MG.coarseSolveType!r} is not built (direct band LU only)")
     if MG.transferType != "FullWeighting":

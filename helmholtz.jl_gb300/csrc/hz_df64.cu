@@ -62,6 +62,13 @@ struct DAcc {
     lo = __fadd_rn(lo, __fadd_rn(t, e));
     lo = __fmaf_rn(al, b, lo);
   }
+  // += x (an FP32 value) with the rounding error of the sum kept in lo
+  __device__ __forceinline__ void add(float x) {
+    float s, t;
+    two_sum(hi, x, s, t);
+    hi = s;
+    lo = __fadd_rn(lo, t);
+  }
   __device__ __forceinline__ void renorm() { quick_two_sum(hi, lo, hi, lo); }
   __device__ __forceinline__ double to_double() const { return (double)hi + (double)lo; }
 };
@@ -550,8 +557,13 @@ template void launch_band_solve_df<float>(Ctx&, const BandSolveOps&, const float
 // Ainv is column-major N x N in df64 (A^{-1}(i, k) at k*N + i), computed once in
 // FP64.  Thread = one row i and DCB columns; the k range is split KS ways
 // (partials in FP64, folded by k_dense_fold), so every SM has work even for a
-// few columns.  B and X are the cycle's complex FP32 columns.
+// few columns.  B and X are the cycle's complex FP32 columns.  Both FP32 parts
+// of each A^{-1} entry multiply b; products are summed in FP32 over blocks of
+// kDenseBlk rows and every block sum joins a double-float accumulator, so the
+// rounding error is that of a 32-term FP32 sum per block, far below the FP32
+// rounding of the result the cycle receives.
 static constexpr int DCB = 8;
+static constexpr int kDenseBlk = 32;  // rows per FP32 partial sum
 
 __global__ void __launch_bounds__(256) k_dense_df(long long N, int ncols, int kchunk, const float4* __restrict__ Ainv,
                                                   const float2* __restrict__ b, long long ldb,
@@ -569,15 +581,32 @@ __global__ void __launch_bounds__(256) k_dense_df(long long N, int ncols, int kc
     im[c].init(0.f, 0.f);
     bc[c] = b + (long long)cols[min(c0 + c, ncols - 1)] * ldb;
   }
-  for (long long k = k0; k < k1; ++k) {
-    const float4 a = Ainv[k * N + i];
+  // blocks of kDenseBlk rows summed in FP32 (hi and lo parts of A^-1 both
+  // applied), each block sum folded into the double-float accumulators
+  for (long long kb = k0; kb < k1; kb += kDenseBlk) {
+    const long long ke = min(k1, kb + kDenseBlk);
+    float sr[DCB], si[DCB];
+#pragma unroll
+    for (int c = 0; c < DCB; ++c) sr[c] = si[c] = 0.f;
+    for (long long k = kb; k < ke; ++k) {
+      const float4 a = Ainv[k * N + i];
+#pragma unroll
+      for (int c = 0; c < DCB; ++c) {
+        const float2 v = bc[c][k];  // same address across the warp: broadcast
+        sr[c] = __fmaf_rn(a.x, v.x, sr[c]);
+        sr[c] = __fmaf_rn(-a.y, v.y, sr[c]);
+        si[c] = __fmaf_rn(a.x, v.y, si[c]);
+        si[c] = __fmaf_rn(a.y, v.x, si[c]);
+        sr[c] = __fmaf_rn(a.z, v.x, sr[c]);
+        sr[c] = __fmaf_rn(-a.w, v.y, sr[c]);
+        si[c] = __fmaf_rn(a.z, v.y, si[c]);
+        si[c] = __fmaf_rn(a.w, v.x, si[c]);
+      }
+    }
 #pragma unroll
     for (int c = 0; c < DCB; ++c) {
-      const float2 v = bc[c][k];  // same address across the warp: broadcast
-      re[c].mac1(a.x, a.z, v.x);
-      re[c].mac1(-a.y, -a.w, v.y);
-      im[c].mac1(a.x, a.z, v.y);
-      im[c].mac1(a.y, a.w, v.x);
+      re[c].add(sr[c]);
+      im[c].add(si[c]);
     }
   }
 #pragma unroll

@@ -138,6 +138,30 @@ template <typename T>
 void launch_band_solve_df(Ctx& ctx, const BandSolveOps& op, const cplx<T>* b, cplx<T>* x, long long ld,
                           const int* cols, int ncols, float4* work);
 
+// ---- K-cycle (hz_kcycle.cu) ------------------------------------------------------
+// Two-step FGMRES on a coarse level, per-column scalars ks[c*8 + slot] on the
+// device (0 beta^2, 1 h00, 2 h10^2, 3 h01, 4 h11, 5 h21^2, 6 y0, 7 y1); part
+// holds 3 * ncols * kcycle_nblk(N) partial sums.
+int kcycle_nblk(long long N);
+// slots base.. : conj(V_s) . W for s < nd, then ||W||^2 when want_norm
+template <typename T>
+void launch_kc_sums(Ctx& ctx, long long N, long long ld, const int* cols, int nc, int nd, int want_norm,
+                    const cplx<T>* V0, const cplx<T>* V1, const cplx<T>* W, double2* part, double2* ks, int base);
+// W -= sum_{s<nd} ks[hb+s] V_s, ||W||^2 into slot norm_slot
+template <typename T>
+void launch_kc_update(Ctx& ctx, long long N, long long ld, const int* cols, int nc, int nd, int hb, double2* ks,
+                      const cplx<T>* V0, const cplx<T>* V1, cplx<T>* W, double2* part, int norm_slot);
+// Y = X / sqrt(ks[slot])
+template <typename T>
+void launch_kc_scale(Ctx& ctx, long long N, long long ld, const int* cols, int nc, const double2* ks, int slot,
+                     const cplx<T>* X, cplx<T>* Y);
+// X = y0 Z0 + y1 Z1
+template <typename T>
+void launch_kc_combine(Ctx& ctx, long long N, long long ld, const int* cols, int nc, const double2* ks,
+                       const cplx<T>* Z0, const cplx<T>* Z1, cplx<T>* X);
+// the 3x2 least-squares problem of each column -> y0, y1
+void launch_kc_lsq(Ctx& ctx, const int* cols, int nc, double2* ks);
+
 // ---- setup kernels ---------------------------------------------------------
 // Fine-level diagonals on the device from nodal m and gamma (device arrays):
 // diag(H), diag(SH) with the shift i*shift*Re(w)^2*m, and 1/diag(SH).

@@ -98,6 +98,8 @@ struct Level {
   std::vector<double> m, gamma;              // restricted nodal m and shifted gamma (host)
   // work buffers (precision of the cycle): x/t ping-pong, r residual, b right-hand side
   DBuf x, t, r, b;
+  // K-cycle on this level: V0, V1, Z0, Z1, W blocks, per-column scalars, partial sums
+  DBuf kv, ks, kp;
 };
 
 struct Hierarchy {
@@ -588,6 +590,11 @@ void ensure_level_buffers(hz_handle* h, Hierarchy& H, int R) {
       L.t.alloc(bytes);
       L.r.alloc(bytes);
     }
+    if (h->opt.cycle == 'K' && l > 0 && l + 1 < H.lv.size()) {
+      L.kv.alloc(5 * bytes);
+      L.ks.alloc((size_t)R * 8 * 16);
+      L.kp.alloc((size_t)R * 3 * kcycle_nblk(L.g.N) * 16);
+    }
   }
   // band work: 3 vectors per column; the dense product's split-K partials need
   // splits(ncols) * ncols vectors, largest over the active column counts
@@ -673,6 +680,41 @@ void learned_correction(hz_handle* h, Hierarchy& H, int l, const cplx<T>* b, cpl
   h->net_calls += 1;
 }
 
+template <typename T, typename TB>
+void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out, const int* cols, int nc);
+
+// out = e_k for the active columns of b_k by the K-cycle: two FGMRES steps on
+// level k's operator, right-preconditioned by level k's own cycle (zero
+// initial guess; Multigrid.jl cycleType 'K').
+template <typename T>
+void kcycle_correction(hz_handle* h, Hierarchy& H, int k, const cplx<T>* b, cplx<T>* out, const int* cols, int nc) {
+  Level& L = *H.lv[k];
+  Ctx& c = h->ctx;
+  const long long N = L.g.N, ld = L.ld, vs = (long long)h->rcap * ld;
+  cplx<T>* base = L.kv.as<cplx<T>>();
+  cplx<T>* V0 = base;
+  cplx<T>* V1 = base + vs;
+  cplx<T>* Z0 = base + 2 * vs;
+  cplx<T>* Z1 = base + 3 * vs;
+  cplx<T>* W = base + 4 * vs;
+  double2* ks = L.ks.as<double2>();
+  double2* part = L.kp.as<double2>();
+  const cplx<T>* none = nullptr;
+  launch_kc_sums<T>(c, N, ld, cols, nc, 0, 1, none, none, b, part, ks, 0);  // beta^2
+  launch_kc_scale<T>(c, N, ld, cols, nc, ks, 0, b, V0);
+  mg_cycle<T, T>(h, H, k, V0, Z0, cols, nc);
+  lev_op<T, T>(h, H, k, MODE_APPLY, Z0, none, W, cols, nc);
+  launch_kc_sums<T>(c, N, ld, cols, nc, 1, 0, V0, none, W, part, ks, 1);  // h00
+  launch_kc_update<T>(c, N, ld, cols, nc, 1, 1, ks, V0, none, W, part, 2);  // W -= h00 V0, h10^2
+  launch_kc_scale<T>(c, N, ld, cols, nc, ks, 2, W, V1);
+  mg_cycle<T, T>(h, H, k, V1, Z1, cols, nc);
+  lev_op<T, T>(h, H, k, MODE_APPLY, Z1, none, W, cols, nc);
+  launch_kc_sums<T>(c, N, ld, cols, nc, 2, 0, V0, V1, W, part, ks, 3);  // h01, h11
+  launch_kc_update<T>(c, N, ld, cols, nc, 2, 3, ks, V0, V1, W, part, 5);  // h21^2
+  launch_kc_lsq(c, cols, nc, ks);
+  launch_kc_combine<T>(c, N, ld, cols, nc, ks, Z0, Z1, out);
+}
+
 // Record the right-hand sides handed to the capture level (FP64 cycles only).
 template <typename TB>
 void capture_rhs(hz_handle* h, Level& L, const cplx<TB>* b, const int* cols, int nc) {
@@ -742,6 +784,8 @@ void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out
     }
     if (h->net_active && l + 1 == h->net_level)
       learned_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+    else if (h->opt.cycle == 'K' && l + 1 < last)
+      kcycle_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
     else
       mg_cycle<T, T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
     launch_prolong<T>(h->ctx, L.g, C.g, C.x.as<cplx<T>>(), C.ld, zero_guess ? nullptr : cur, cur, L.ld, cols, nc);
@@ -1160,7 +1204,9 @@ void validate(const hz_problem* p, const hz_options* o) {
     fail(HZ_ERR_ARG, "inner (restart length) must be in [1, 64]");
   if (o->inner < 0 || o->inner > 64) fail(HZ_ERR_ARG, "inner must be in [0, 64]");
   if (o->krylov != HZ_KRYLOV_FGMRES && o->krylov != HZ_KRYLOV_BICGSTAB) fail(HZ_ERR_ARG, "unknown Krylov method");
-  if (o->cycle != 'V' && o->cycle != 'W') fail(HZ_ERR_ARG, "cycle must be 'V' or 'W'");
+  if (o->cycle != 'V' && o->cycle != 'W' && o->cycle != 'K') fail(HZ_ERR_ARG, "cycle must be 'V', 'W' or 'K'");
+  if (o->cycle == 'K' && o->krylov != HZ_KRYLOV_FGMRES)
+    fail(HZ_ERR_ARG, "the K-cycle is a nonlinear preconditioner: it needs FGMRES");
   if (o->coarse_op != HZ_COARSE_GALERKIN && o->coarse_op != HZ_COARSE_REDISCRETIZE)
     fail(HZ_ERR_ARG, "coarse_op must be HZ_COARSE_GALERKIN or HZ_COARSE_REDISCRETIZE");
   if (o->precision != HZ_PREC_FP64 && o->precision != HZ_PREC_MIXED) fail(HZ_ERR_ARG, "unknown precision");

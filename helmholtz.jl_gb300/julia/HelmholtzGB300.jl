@@ -186,7 +186,8 @@ end
 function options(s::ShiftedLaplacianMultigridSolver)
     MG = s.MG
     MG.relaxType == "Jac" || throw(ArgumentError("relaxType $(MG.relaxType): only \"Jac\" is built"))
-    MG.cycleType in ('V', 'W') || throw(ArgumentError("cycleType $(MG.cycleType): only 'V' and 'W' are built"))
+    MG.cycleType in ('V', 'W', 'K') ||
+        throw(ArgumentError("cycleType $(MG.cycleType): only 'V', 'W' and 'K' are built"))
     s.Krylov in ("GMRES", "BiCGSTAB") ||
         throw(ArgumentError("Krylov $(s.Krylov): \"GMRES\" (FGMRES) and \"BiCGSTAB\" are built"))
     o = HzOptions()

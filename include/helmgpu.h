@@ -85,7 +85,7 @@ typedef struct hz_options {
   int32_t relax_pre;     /* Jacobi sweeps before the coarse correction */
   int32_t relax_post;    /* Jacobi sweeps after the coarse correction */
   double relax_param;    /* Jacobi damping w */
-  int32_t cycle;         /* 'V' or 'W' */
+  int32_t cycle;         /* 'V', 'W' or 'K' (K: two FGMRES steps per coarse level; FGMRES outer only) */
   int32_t krylov;        /* HZ_KRYLOV_* */
   int32_t inner;         /* FGMRES restart length */
   double shift;          /* s in SH = H + i s w^2 diag(m) */

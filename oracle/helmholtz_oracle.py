@@ -370,8 +370,39 @@ def jacobi(L: Level, x: np.ndarray, b: np.ndarray, w: float, sweeps: int) -> np.
     return x
 
 
+def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int) -> np.ndarray:
+    """K-cycle coarse correction on level ``lev`` (Multigrid.jl cycleType 'K',
+    used by test/ShiftedLaplacianTest.jl:137-140, restated): two steps of FGMRES
+    on that level's operator from a zero guess, right-preconditioned by the
+    level's own cycle, per column (least squares of the 3x2 Hessenberg matrix)."""
+    A = hier.levels[lev].A
+    b = b.reshape(b.shape[0], -1)
+    out = np.zeros_like(b)
+    beta = np.linalg.norm(b, axis=0)
+    V0 = b / np.where(beta > 0, beta, 1.0)
+    Z0 = mg_cycle(hier, lev, V0, w, pre, post, "K")
+    W = A @ Z0
+    h00 = np.sum(np.conj(V0) * W, axis=0)
+    W = W - h00 * V0
+    h10 = np.linalg.norm(W, axis=0)
+    V1 = W / np.where(h10 > 0, h10, 1.0) * (h10 > 0)
+    Z1 = mg_cycle(hier, lev, V1, w, pre, post, "K")
+    W = A @ Z1
+    h01 = np.sum(np.conj(V0) * W, axis=0)
+    h11 = np.sum(np.conj(V1) * W, axis=0)
+    W = W - h01 * V0 - h11 * V1
+    h21 = np.linalg.norm(W, axis=0)
+    for c in range(b.shape[1]):
+        if beta[c] == 0:
+            continue
+        Hm = np.array([[h00[c], h01[c]], [h10[c], h11[c]], [0.0, h21[c]]], dtype=np.complex128)
+        y = np.linalg.lstsq(Hm, np.array([beta[c], 0.0, 0.0], dtype=np.complex128), rcond=None)[0]
+        out[:, c] = y[0] * Z0[:, c] + y[1] * Z1[:, c]
+    return out
+
+
 def mg_cycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int, cycle: str = "V") -> np.ndarray:
-    """One V (or W) cycle with zero initial guess on level ``lev``."""
+    """One V, W or K cycle with zero initial guess on level ``lev``."""
     L = hier.levels[lev]
     if lev == len(hier.levels) - 1:
         return hier.lu.solve(b)
@@ -381,7 +412,10 @@ def mg_cycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post:
     for _ in range(ncalls):
         r = b - L.A @ x
         bc = L.R @ r
-        xc = mg_cycle(hier, lev + 1, bc, w, pre, post, cycle)
+        if cycle == "K" and lev + 1 < len(hier.levels) - 1:
+            xc = kcycle(hier, lev + 1, bc, w, pre, post).reshape(bc.shape)
+        else:
+            xc = mg_cycle(hier, lev + 1, bc, w, pre, post, cycle)
         x = x + L.P @ xc
     x = jacobi(L, x, b, w, post)
     return x
