@@ -70,7 +70,8 @@ class hz_options(C.Structure):
         ("profile", C.c_int32),
         ("device", C.c_int32),
         ("outer_arith", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("cuda_graph", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 

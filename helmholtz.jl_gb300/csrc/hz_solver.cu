@@ -11,14 +11,17 @@
 // preconditioned by one cycle on SH), src/GetHelmholtz.jl:33-50,81-95
 // (operator assembly, shift, getHelmholtzFun).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -52,6 +55,10 @@ void ck(cudaError_t e, const char* what) {
   }
 }
 
+// Device (re)allocations so far in this process: a captured CUDA graph holds
+// raw pointers, so graphs captured before the latest allocation are dropped.
+std::atomic<long long> g_alloc_gen{0};
+
 // Owning device buffer.
 struct DBuf {
   void* p = nullptr;
@@ -76,6 +83,7 @@ struct DBuf {
       fail(HZ_ERR_ALLOC, "cudaMalloc of %.3f GB failed: %s", b / 1e9, cudaGetErrorString(e));
     }
     bytes = b;
+    g_alloc_gen.fetch_add(1);
   }
   template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
 };
@@ -157,6 +165,18 @@ struct hz_handle {
   int net_feat_level = -1;
   double net_h2 = 0.0;       // hx * hy of the network level
   DBuf net_feat;             // per node of the network level: (w^2 m hx hy, gamma / w), float2
+  // CUDA graphs of the preconditioner application, one per (orientation, basis
+  // index, active columns, form); launch-table deltas of the captured kernels
+  struct CycleGraph {
+    cudaGraphExec_t exec = nullptr;
+    long long seen = 0;      // applications with this key (captured on the second)
+    long long launches = 0;  // kernels in the graph
+    double bytes = 0.0;
+    std::vector<std::pair<int, long long>> counts;
+  };
+  std::map<std::tuple<int, int, int, int>, CycleGraph> graphs;
+  long long graph_gen = -1;
+  bool graphs_off = false;  // a capture failed: eager launches from then on
   // capture of the right-hand sides handed to one level (training pairs)
   bool cap_on = false;
   int cap_level = 0;
@@ -846,6 +866,88 @@ void col_norms(hz_handle* h, const double2* x, const std::vector<int>& cols, dou
   }
 }
 
+void drop_graphs(hz_handle* h) {
+  for (auto& kv : h->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  h->graphs.clear();
+}
+
+// Run body (the launches of one preconditioner application) through a CUDA
+// graph: captured on the second application with the same key, replayed from
+// then on.  The graph's kernels keep their launch counts in the table; with
+// profiling on, a replay is timed as one "vcycle_graph" entry carrying the
+// algorithmic bytes of all its kernels.  A failed capture (an API the graph
+// cannot hold) turns graphs off for the handle and runs the body eagerly.
+template <typename F>
+void cycle_graph(hz_handle* h, int adj, int j, int nl, int form, F&& body) {
+  if (!h->opt.cuda_graph || h->graphs_off || h->net_active || h->cap_on) {
+    body();
+    return;
+  }
+  const long long gen = g_alloc_gen.load();
+  if (gen != h->graph_gen) {
+    drop_graphs(h);
+    h->graph_gen = gen;
+  }
+  Ctx& c = h->ctx;
+  auto& cg = h->graphs[std::make_tuple(adj, j, nl, form)];
+  if (!cg.exec) {
+    if (++cg.seen < 2) {
+      body();
+      return;
+    }
+    const bool prof = c.profile;
+    c.profile = false;
+    const std::vector<long long> counts0 = c.counts;
+    const std::vector<double> bytes0 = c.alg_bytes;
+    const long long l0 = c.launches;
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      try {
+        body();
+      } catch (...) {
+        ok = false;
+      }
+      const cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+      ok = ok && e == cudaSuccess && g != nullptr;
+    }
+    if (ok && cudaGraphInstantiate(&cg.exec, g, 0) != cudaSuccess) {
+      ok = false;
+      cg.exec = nullptr;
+    }
+    if (g) cudaGraphDestroy(g);
+    c.profile = prof;
+    // capture recorded the kernels in the launch table without running them: move the deltas to the graph
+    cg.launches = c.launches - l0;
+    c.launches = l0;
+    cg.counts.clear();
+    cg.bytes = 0.0;
+    for (size_t i = 0; i < c.counts.size(); ++i) {
+      const long long c0 = i < counts0.size() ? counts0[i] : 0;
+      const double b0 = i < bytes0.size() ? bytes0[i] : 0.0;
+      if (c.counts[i] != c0) cg.counts.push_back({(int)i, c.counts[i] - c0});
+      cg.bytes += c.alg_bytes[i] - b0;
+      c.counts[i] = c0;
+      c.alg_bytes[i] = b0;
+    }
+    if (!ok) {
+      cudaGetLastError();
+      h->graphs_off = true;
+      if (h->opt.verbose) fprintf(stderr, "helmgpu: CUDA graph capture failed, cycles run eagerly\n");
+      body();
+      return;
+    }
+  }
+  const int gid = c.name_id("vcycle_graph");
+  cudaEvent_t a = nullptr;
+  c.before(gid, &a);
+  ck(cudaGraphLaunch(cg.exec, c.stream), "cudaGraphLaunch");
+  c.after(gid, a, cg.bytes);
+  c.launches += cg.launches - 1;  // after() counted the graph as one launch
+  for (auto& pc : cg.counts) c.counts[pc.first] += pc.second;
+}
+
 // FGMRES(m) on H (or H^H) right-preconditioned by one multigrid cycle.
 int fgmres(hz_handle* h, int adj, int nrhs) {
   Hierarchy& H = h->hier[adj];
@@ -912,12 +1014,12 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
       double2* w = Vj(j + 1);
       if (df) {
         // the cycle reads the high parts of the df64 basis vector as its FP32 right-hand side
-        mg_cycle<float, df64_tag>(h, H, 0, Vdj(j), (float2*)Zj(j), dc, nl);
+        cycle_graph(h, adj, j, nl, 2, [&] { mg_cycle<float, df64_tag>(h, H, 0, Vdj(j), (float2*)Zj(j), dc, nl); });
         FineOp fop = h->fop;
         fop.adj = adj;
         launch_fine_df64(h->ctx, fop, h->diagHdf.as<float4>(), (const float2*)Zj(j), Vdj(j + 1), N, dc, nl);
       } else {
-        precondition(h, H, Vj(j), Zj(j), dc, nl);
+        cycle_graph(h, adj, j, nl, mixed ? 1 : 0, [&] { precondition(h, H, Vj(j), Zj(j), dc, nl); });
         if (mixed)
           apply_H<float>(h, adj, MODE_APPLY, (const float2*)Zj(j), nullptr, w, dc, nl);
         else
@@ -1301,6 +1403,7 @@ void hz_default_options(hz_options* o) {
   o->shift = 0.5;
   o->precision = HZ_PREC_FP64;
   o->coarse_op = HZ_COARSE_GALERKIN;
+  o->cuda_graph = 1;
 }
 
 int hz_create(const hz_problem* prob, const hz_options* opt, hz_handle** out) {
@@ -1343,6 +1446,7 @@ int hz_destroy(hz_handle* h) {
   if (!h) return HZ_OK;
   cudaSetDevice(h->dev);
   if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
+  drop_graphs(h);
   h->ctx.release();
   if (h->h_est) cudaFreeHost(h->h_est);
   if (h->h_nrm) cudaFreeHost(h->h_nrm);
@@ -1486,6 +1590,7 @@ int hz_clear(hz_handle* h) {
   return guarded(h, [&] {
     set_device(h);
     sync(h);
+    drop_graphs(h);
     for (auto& H : h->hier) {
       H.lv.clear();
       H.bandT.reset();

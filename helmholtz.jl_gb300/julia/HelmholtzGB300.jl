@@ -57,9 +57,10 @@ mutable struct HzOptions
     profile::Int32
     device::Int32
     outer_arith::Int32
-    reserved::NTuple{6,Int32}
+    cuda_graph::Int32
+    reserved::NTuple{5,Int32}
 end
-HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 6))
+HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 5))
 
 mutable struct HzStats
     outer::Int32

@@ -95,7 +95,8 @@ typedef struct hz_options {
   int32_t profile;       /* 1: time every kernel launch with CUDA events */
   int32_t device;        /* CUDA device ordinal */
   int32_t outer_arith;   /* FGMRES outer arithmetic: HZ_OUTER_FP64 (native) or HZ_OUTER_EMULATED */
-  int32_t reserved[6];
+  int32_t cuda_graph;    /* 1 (default): replay each FGMRES preconditioner application from a CUDA graph */
+  int32_t reserved[5];
 } hz_options;
 
 typedef struct hz_stats {
