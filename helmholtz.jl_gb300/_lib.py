@@ -122,6 +122,9 @@ SIGNATURES = {
     "hz_net_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_double,
                                C.c_int32, _dp]),
     "hz_kernel_flops": (C.c_int, [_vp, C.c_int32, _dp]),
+    "hz_net_save": (C.c_int, [_vp, C.c_char_p]),
+    "hz_net_load": (C.c_int, [_vp, C.c_char_p]),
+    "hz_net_file_info": (C.c_int, [C.c_char_p, _i64p, _i64p]),
     "hz_net_set_profile": (C.c_int, [_vp, C.c_int32]),
     "hz_net_kernel_times": (C.c_int, [_vp, C.c_int32, C.c_char_p, C.c_int32, _i64p, _i64p, _dp, _dp, _dp]),
     "hz_net_reset_kernel_times": (C.c_int, [_vp]),

@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 #include <random>
@@ -685,6 +686,113 @@ void CoarseNet::get_grad(float* host) const {
   cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
   cuda_ok(cudaMemcpy(w.data(), g32_, wtotal_ * 4, cudaMemcpyDeviceToHost), "download gradient");
   unpack_padded(w, woff_, host);
+}
+
+// ---- file format -----------------------------------------------------------
+// "HZCNET01" | u32 version | u32 layers | layers x (i32 cin, i32 cout) |
+// i64 nparams | i64 adam step | f32 weights[n] | f32 m[n] | f32 v[n]
+// (little-endian; weights and moments unpadded, layer after layer [cout][9][cin])
+static const char kNetMagic[8] = {'H', 'Z', 'C', 'N', 'E', 'T', '0', '1'};
+static constexpr unsigned kNetVersion = 1;
+
+static void download_unpadded(const float* dev, long long total, const long long* woff, float* host) {
+  std::vector<float> w((size_t)total);
+  cuda_ok(cudaMemcpy(w.data(), dev, total * 4, cudaMemcpyDeviceToHost), "download");
+  unpack_padded(w, woff, host);
+}
+
+static void upload_unpadded(const float* host, long long total, const long long* woff, float* dev) {
+  std::vector<float> w((size_t)total, 0.f);
+  size_t k = 0;
+  for (int l = 0; l < CoarseNet::kLayers; ++l) {
+    const auto& L = kSpec[l];
+    for (int co = 0; co < L.cout; ++co)
+      for (int t = 0; t < 9; ++t)
+        for (int ci = 0; ci < L.cin; ++ci) w[(size_t)(woff[l] + ((long long)co * 9 + t) * L.cinp + ci)] = host[k++];
+  }
+  cuda_ok(cudaMemcpy(dev, w.data(), total * 4, cudaMemcpyHostToDevice), "upload");
+}
+
+void CoarseNet::save(const char* path) const {
+  cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
+  const long long n = num_params();
+  std::vector<float> w((size_t)n), m((size_t)n), v((size_t)n);
+  download_unpadded(w32_, wtotal_, woff_, w.data());
+  download_unpadded(m_, wtotal_, woff_, m.data());
+  download_unpadded(v_, wtotal_, woff_, v.data());
+  FILE* f = std::fopen(path, "wb");
+  if (!f) throw std::runtime_error(std::string("coarse net: cannot write ") + path);
+  const unsigned hdr[2] = {kNetVersion, (unsigned)kLayers};
+  bool ok = std::fwrite(kNetMagic, 1, 8, f) == 8 && std::fwrite(hdr, 4, 2, f) == 2;
+  for (int l = 0; l < kLayers && ok; ++l) {
+    const int sh[2] = {kSpec[l].cin, kSpec[l].cout};
+    ok = std::fwrite(sh, 4, 2, f) == 2;
+  }
+  const long long meta[2] = {n, step_};
+  ok = ok && std::fwrite(meta, 8, 2, f) == 2;
+  ok = ok && std::fwrite(w.data(), 4, (size_t)n, f) == (size_t)n;
+  ok = ok && std::fwrite(m.data(), 4, (size_t)n, f) == (size_t)n;
+  ok = ok && std::fwrite(v.data(), 4, (size_t)n, f) == (size_t)n;
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) throw std::runtime_error(std::string("coarse net: write failed: ") + path);
+}
+
+int CoarseNet::file_info(const char* path, long long* nparams, long long* step) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return -1;
+  char mg[8];
+  unsigned hdr[2];
+  int rc = 0;
+  if (std::fread(mg, 1, 8, f) != 8 || std::memcmp(mg, kNetMagic, 8) != 0) rc = -2;
+  if (!rc && std::fread(hdr, 4, 2, f) != 2) rc = -5;
+  if (!rc && hdr[0] != kNetVersion) rc = -3;
+  if (!rc && hdr[1] != (unsigned)kLayers) rc = -4;
+  for (int l = 0; l < kLayers && !rc; ++l) {
+    int sh[2];
+    if (std::fread(sh, 4, 2, f) != 2) rc = -5;
+    else if (sh[0] != kSpec[l].cin || sh[1] != kSpec[l].cout) rc = -4;
+  }
+  long long meta[2] = {0, 0};
+  if (!rc && std::fread(meta, 8, 2, f) != 2) rc = -5;
+  if (!rc && meta[0] != num_params()) rc = -4;
+  if (!rc) {
+    // the three arrays must be present in full
+    const long long need = 3LL * meta[0] * 4;
+    const long pos = std::ftell(f);
+    if (std::fseek(f, 0, SEEK_END) != 0 || std::ftell(f) - pos < need) rc = -5;
+  }
+  std::fclose(f);
+  if (!rc) {
+    if (nparams) *nparams = meta[0];
+    if (step) *step = meta[1];
+  }
+  return rc;
+}
+
+void CoarseNet::load(const char* path) {
+  long long n = 0, st = 0;
+  const int rc = file_info(path, &n, &st);
+  static const char* why[] = {"", "cannot read", "not a coarse-network file", "unsupported version",
+                              "layer shapes differ", "truncated"};
+  if (rc < 0) throw std::runtime_error(std::string("coarse net: ") + path + ": " + why[-rc]);
+  std::vector<float> w((size_t)n), m((size_t)n), v((size_t)n);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) throw std::runtime_error(std::string("coarse net: cannot read ") + path);
+  const long hdr_bytes = 8 + 8 + kLayers * 8 + 16;
+  bool ok = std::fseek(f, hdr_bytes, SEEK_SET) == 0;
+  ok = ok && std::fread(w.data(), 4, (size_t)n, f) == (size_t)n;
+  ok = ok && std::fread(m.data(), 4, (size_t)n, f) == (size_t)n;
+  ok = ok && std::fread(v.data(), 4, (size_t)n, f) == (size_t)n;
+  std::fclose(f);
+  if (!ok) throw std::runtime_error(std::string("coarse net: truncated ") + path);
+  for (long long i = 0; i < n; ++i)
+    if (!std::isfinite(w[(size_t)i]) || !std::isfinite(m[(size_t)i]) || !(v[(size_t)i] >= 0.f))
+      throw std::runtime_error(std::string("coarse net: non-finite weights or state in ") + path);
+  set_weights(w.data());  // resets the moments; restore them below
+  cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
+  upload_unpadded(m.data(), wtotal_, woff_, m_);
+  upload_unpadded(v.data(), wtotal_, woff_, v_);
+  step_ = st;
 }
 
 void CoarseNet::release_acts() {

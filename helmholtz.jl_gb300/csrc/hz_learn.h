@@ -31,6 +31,14 @@ class CoarseNet {
   void get_weights(float* host) const;
   void set_weights(const float* host);
   void get_grad(float* host) const;
+  // versioned binary file: weights and the Adam state (moments, step), so that
+  // training resumes where it stopped; load checks the format and the shapes
+  void save(const char* path) const;
+  void load(const char* path);
+  // header check of a saved file without a GPU: returns 0 and the parameter
+  // count and Adam step, or a negative code (-1 unreadable, -2 not a network
+  // file, -3 other version, -4 other layer shapes, -5 truncated)
+  static int file_info(const char* path, long long* nparams, long long* step);
 
   // forward pass on c.stream; x4 on the device; result in output(); train keeps
   // the activations and allocates their gradients for backward()

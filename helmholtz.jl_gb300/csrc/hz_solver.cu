@@ -1788,6 +1788,38 @@ int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_
   });
 }
 
+int hz_net_save(hz_net* net, const char* path) {
+  if (!net || !path) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    net->net->save(path);
+  });
+}
+
+int hz_net_load(hz_net* net, const char* path) {
+  if (!net || !path) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    long long n = 0, st = 0;
+    const int rc = hz::CoarseNet::file_info(path, &n, &st);
+    if (rc < 0) fail(HZ_ERR_ARG, "%s: not a loadable coarse-network file (code %d)", path, rc);
+    net->net->load(path);
+  });
+}
+
+int hz_net_file_info(const char* path, int64_t* nparams, int64_t* adam_step) {
+  if (!path) return HZ_ERR_ARG;
+  long long n = 0, st = 0;
+  const int rc = hz::CoarseNet::file_info(path, &n, &st);
+  if (rc < 0) {
+    g_thread_error = std::string(path) + ": not a loadable coarse-network file";
+    return HZ_ERR_ARG;
+  }
+  if (nparams) *nparams = n;
+  if (adam_step) *adam_step = st;
+  return HZ_OK;
+}
+
 int hz_net_set_profile(hz_net* net, int32_t on) {
   if (!net) return HZ_ERR_ARG;
   cudaSetDevice(net->dev);

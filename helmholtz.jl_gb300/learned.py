@@ -108,6 +108,14 @@ class CoarseNet:
         L.check(L.load().hz_net_gradient(self._h, px, pt, nx, ny, B, mem, C.byref(loss), g.ctypes.data))
         return loss.value, g
 
+    def save(self, path) -> None:
+        """Weights and Adam state to a versioned binary file (training resumes from it)."""
+        L.check(L.load().hz_net_save(self._h, str(path).encode()))
+
+    def load(self, path) -> None:
+        """Weights and Adam state from a file written by save (format, version and shapes checked)."""
+        L.check(L.load().hz_net_load(self._h, str(path).encode()))
+
     def set_profile(self, on: bool) -> None:
         """Time every kernel launch of the network's own stream with CUDA events."""
         L.check(L.load().hz_net_set_profile(self._h, int(bool(on))))
@@ -140,6 +148,14 @@ class CoarseNet:
         L.check(L.load().hz_net_train(self._h, x.data_ptr(), t.data_ptr(), nx, ny, P, int(batch), int(epochs),
                                       float(lr), int(seed), hist.ctypes.data_as(C.POINTER(C.c_double))))
         return hist
+
+
+def file_info(path) -> tuple[int, int]:
+    """(parameter count, Adam step) of a saved network file; raises for a file
+    that is not loadable (host only, no GPU)."""
+    n, st = C.c_int64(), C.c_int64()
+    L.check(L.load().hz_net_file_info(str(path).encode(), C.byref(n), C.byref(st)))
+    return int(n.value), int(st.value)
 
 
 def level_grid(solver: ShiftedLaplacianMultigridSolver, level: int) -> tuple[int, int]:

@@ -234,6 +234,14 @@ int hz_net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int
  * loss_hist (host, epochs entries, may be NULL) gets the mean loss per epoch. */
 int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t npairs, int32_t batch,
                  int32_t epochs, double lr, int32_t seed, double* loss_hist);
+/* Versioned binary file of the weights and the Adam state ("HZCNET01", version,
+ * layer shapes, parameter count, step, weights, moments): training resumes from a
+ * loaded file.  Load rejects a file of another format, version or shape, a
+ * truncated one, or one with non-finite values (HZ_ERR_ARG, weights unchanged).
+ * hz_net_file_info checks a file on the host only (no GPU). */
+int hz_net_save(hz_net* net, const char* path);
+int hz_net_load(hz_net* net, const char* path);
+int hz_net_file_info(const char* path, int64_t* nparams, int64_t* adam_step);
 /* Launch table of the network's own stream (training, standalone inference),
  * as hz_kernel_times plus the algorithmic flops; profiling on/off and reset. */
 int hz_net_set_profile(hz_net* net, int32_t on);

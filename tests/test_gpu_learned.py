@@ -188,3 +188,34 @@ def test_stagnation_falls_back_to_plain_cycle(hz, O):
     hz.learned.attach(S, None)
     hz.solveLinearSystem(None, B, S)
     assert hz.learned.learned_stats(S)[0] == calls
+
+
+def test_save_load_resume(hz, tmp_path):
+    """Weights and Adam state survive a save/load; a corrupted file is rejected
+    and leaves the weights unchanged; training continues from a loaded file."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn((64, 17, 17, 4), device="cuda", generator=g)
+    t = torch.randn((64, 17, 17, 2), device="cuda", generator=g)
+    a = hz.learned.CoarseNet(seed=4)
+    a.train(x, t, epochs=2, batch=16, lr=1e-3, seed=1)
+    p = tmp_path / "net.hzn"
+    a.save(p)
+    n, step = hz.learned.file_info(p)
+    assert n == CN.num_params() and step == 8
+    b = hz.learned.CoarseNet(seed=9)
+    b.load(p)
+    np.testing.assert_array_equal(b.get_weights(), a.get_weights())
+    # a non-finite weight in the file is rejected, the network keeps its weights
+    raw = bytearray(p.read_bytes())
+    hdr = 8 + 8 + 8 * 8 + 16
+    raw[hdr:hdr + 4] = np.array([np.nan], np.float32).tobytes()
+    q = tmp_path / "bad.hzn"
+    q.write_bytes(bytes(raw))
+    with pytest.raises(hz._lib.HelmgpuError):
+        b.load(q)
+    np.testing.assert_array_equal(b.get_weights(), a.get_weights())
+    # resumed training: the same data and seed on both copies give the same loss (atomics aside)
+    ha = a.train(x, t, epochs=1, batch=16, lr=1e-3, seed=2)
+    hb = b.train(x, t, epochs=1, batch=16, lr=1e-3, seed=2)
+    assert abs(ha[0] - hb[0]) <= 1e-3 * abs(ha[0])

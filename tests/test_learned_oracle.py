@@ -114,3 +114,40 @@ def test_net_entry_points_reject_bad_arguments(hz):
     assert st in (hz._lib.HZ_OK, hz._lib.HZ_ERR_NO_DEVICE)
     if st == hz._lib.HZ_OK:
         lib.hz_net_destroy(out)
+
+
+def _net_file(path, layers=None, version=1, magic=b"HZCNET01", nparams=None, step=7, arrays=3, values=None):
+    import struct
+    layers = layers or CN.LAYERS
+    n = CN.num_params() if nparams is None else nparams
+    with open(path, "wb") as f:
+        f.write(magic)
+        f.write(struct.pack("<II", version, len(layers)))
+        for a, b in layers:
+            f.write(struct.pack("<ii", a, b))
+        f.write(struct.pack("<qq", n, step))
+        v = np.zeros(n, np.float32) if values is None else values
+        for _ in range(arrays):
+            f.write(v.astype(np.float32).tobytes())
+
+
+def test_net_file_format_checks(hz, tmp_path):
+    """The saved-network header check runs on the host: a valid file gives its
+    parameter count and Adam step; another magic, version or layer shape, or a
+    truncated file, is rejected with an error status (no GPU needed)."""
+    good = tmp_path / "good.hzn"
+    _net_file(good)
+    assert hz.learned.file_info(good) == (CN.num_params(), 7)
+    bad = {
+        "magic": dict(magic=b"NOTANETW"),
+        "version": dict(version=2),
+        "shape": dict(layers=[(4, 16)] * 8),
+        "truncated": dict(arrays=2),
+    }
+    for name, kw in bad.items():
+        p = tmp_path / f"{name}.hzn"
+        _net_file(p, **kw)
+        with pytest.raises(hz._lib.HelmgpuError):
+            hz.learned.file_info(p)
+    with pytest.raises(hz._lib.HelmgpuError):
+        hz.learned.file_info(tmp_path / "missing.hzn")
