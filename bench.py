@@ -265,7 +265,7 @@ def run_ours(args, rank, ws, dist):
         prob.neumann_on_top, prob.sommerfeld, prob.order_neumann_bc = 1, 1, 2
         o = L.hz_options()
         lib.hz_default_options(C.byref(o))
-        o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, 200
+        o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, args.max_outer
         o.cycle = ord(args.cycle)
         o.cuda_graph = 0 if args.no_graph else 1
         if args.krylov == "bicgstab":
@@ -523,6 +523,8 @@ def main():
     ap.add_argument("--outer", default="emulated", choices=["fp64", "emulated"],
                     help="outer Krylov arithmetic of the mixed form: native FP64 or FP64 emulated with FP32 pairs")
     ap.add_argument("--no-graph", action="store_true", help="launch the cycles eagerly (no CUDA graphs)")
+    ap.add_argument("--max-outer", type=int, default=200,
+                    help="FGMRES restart cycles (fewer: kernel-rate profiling runs, not a valid RHS/s)")
     ap.add_argument("--cycle", default="V", choices=["V", "W", "K"],
                     help="multigrid cycle (K: two FGMRES steps per coarse level)")
     ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
@@ -608,6 +610,12 @@ def main():
                         share=dom["ms"] / sum(k["ms"] for k in kt),
                         source="CUDA events around every launch on the handle's stream, over the same number of "
                                "solves right after the timed ones")
+    # whole-solve roofline: the algorithmic bytes of every launched kernel of a
+    # solve (from the profiled solves, same workload and iteration counts) over
+    # the unprofiled time of a solve
+    solve_bytes = sum(k["bytes"] for k in head["kernels"]) / max(1, head["steps"])
+    solve_roof = dict(bound="hbm", achieved=solve_bytes / (head["ms_per_step"] / 1e3) / 1e9, peak=peak, unit="GB/s",
+                      frac=solve_bytes / (head["ms_per_step"] / 1e3) / 1e9 / peak, bytes_per_solve=solve_bytes)
     cpu = None
     if not args.no_cpu:
         import __graft_entry__ as ge
@@ -628,7 +636,7 @@ def main():
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
                             l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9)),
                 e2e=head.get("e2e"), gpu_launches=head["launches_per_step"] * args.steps,
-                clocks=head["clocks"], roofline=roofline,
+                clocks=head["clocks"], roofline=roofline, solve_roofline=solve_roof,
                 cpu_baseline=cpu,
                 max_relres=head["max_relres"], check_relres_max=head.get("check_relres_max"),
                 mean_iters=head["mean_iters"],

@@ -192,10 +192,10 @@ void launch_fine_df64(Ctx& ctx, const FineOp& op, const float4* dHd, const float
   const int cpb = (ncols + ch - 1) / ch;
   const double bytes = (double)op.g.N * ncols * (8 + 16) + (double)op.g.N * 16;
   if (op.g.nz > 1)
-    HZ_LAUNCH(ctx, "fine_apply", bytes, (k_fine_df64<true, TO>), dim3((unsigned)nbx, (unsigned)ch), TPB, 0, d, dHd,
+    HZ_LAUNCH(ctx, "outer_apply_df64", bytes, (k_fine_df64<true, TO>), dim3((unsigned)nbx, (unsigned)ch), TPB, 0, d, dHd,
               z, y, ld, cols, ncols, cpb);
   else
-    HZ_LAUNCH(ctx, "fine_apply", bytes, (k_fine_df64<false, TO>), dim3((unsigned)nbx, (unsigned)ch), TPB, 0, d, dHd,
+    HZ_LAUNCH(ctx, "outer_apply_df64", bytes, (k_fine_df64<false, TO>), dim3((unsigned)nbx, (unsigned)ch), TPB, 0, d, dHd,
               z, y, ld, cols, ncols, cpb);
 }
 template void launch_fine_df64<float4>(Ctx&, const FineOp&, const float4*, const float2*, float4*, long long,

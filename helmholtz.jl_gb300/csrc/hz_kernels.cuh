@@ -52,6 +52,7 @@ struct FineOp {
   double o[3];  // 1/h_d^2: interior off-diagonal magnitude per axis
   double b[3];  // BC/h_d^2: boundary-row off-diagonal magnitude per axis
   int adj;      // 1: apply the adjoint (transposed boundary rows, conjugated diagonal)
+  int outer = 0;  // 1: the Krylov method's operator H (launch-table names outer_*), 0: a cycle operator
 };
 
 // y = op(x) on nodes of a fine level, for the columns cols[0..ncols) of the

@@ -837,6 +837,7 @@ void apply_H(hz_handle* h, int adj, int mode, const cplx<TX>* x, const double2* 
              int nc) {
   FineOp fop = h->fop;
   fop.adj = adj;
+  fop.outer = 1;
   launch_fine<double, TX, double>(h->ctx, mode, fop, h->diagH.as<double2>(), nullptr, x, b, y, h->g0.N, cols, nc,
                                   0.0);
 }

@@ -143,6 +143,8 @@ __global__ void __launch_bounds__(256) k_fine(FineOpT<T> op, const cplx<T>* __re
   }
   const int c0 = blockIdx.y * cpb;
   const int c1 = min(ncols, c0 + cpb);
+  // columns are independent: unrolled so that several columns' loads are in flight
+#pragma unroll 4
   for (int ci = c0; ci < c1; ++ci) {
     const long long off = (long long)cols[ci] * ld;
     const cplx<TX>* xc = x + off + p;
@@ -200,12 +202,14 @@ void launch_fine(Ctx& ctx, int mode, const FineOp& op, const cplx<T>* diag, cons
   if (mode == MODE_JACOBI) fbytes += (double)op.g.N * sizeof(cplx<T>);
 #define HZ_FINE_CASE(M, D, NAME) \
   HZ_LAUNCH(ctx, NAME, fbytes, (k_fine<T, TX, TB, M, D>), grid, TPB, 0, o, diag, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
+  const char* nm_apply = op.outer ? "outer_apply" : "fine_apply";
+  const char* nm_resid = op.outer ? "outer_resid" : "fine_resid";
   if (mode == MODE_APPLY) {
-    if (is3d) HZ_FINE_CASE(MODE_APPLY, true, "fine_apply");
-    else HZ_FINE_CASE(MODE_APPLY, false, "fine_apply");
+    if (is3d) HZ_FINE_CASE(MODE_APPLY, true, nm_apply);
+    else HZ_FINE_CASE(MODE_APPLY, false, nm_apply);
   } else if (mode == MODE_RESID) {
-    if (is3d) HZ_FINE_CASE(MODE_RESID, true, "fine_resid");
-    else HZ_FINE_CASE(MODE_RESID, false, "fine_resid");
+    if (is3d) HZ_FINE_CASE(MODE_RESID, true, nm_resid);
+    else HZ_FINE_CASE(MODE_RESID, false, nm_resid);
   } else {
     if (is3d) HZ_FINE_CASE(MODE_JACOBI, true, "fine_jacobi");
     else HZ_FINE_CASE(MODE_JACOBI, false, "fine_jacobi");
@@ -246,6 +250,8 @@ __global__ void __launch_bounds__(128) k_rap(Grid g, const cplx<T>* __restrict__
   if (MODE == MODE_JACOBI) di = dinv[p];
   const int c0 = blockIdx.y * cpb;
   const int c1 = min(ncols, c0 + cpb);
+  // columns are independent: unrolled so that several columns' loads are in flight
+#pragma unroll 2
   for (int ci = c0; ci < c1; ++ci) {
     const long long off = (long long)cols[ci] * ld;
     const cplx<T>* xc = x + off + p;
@@ -317,6 +323,8 @@ __global__ void __launch_bounds__(256) k_jacobi0(long long N, const cplx<T>* __r
   di.y *= w;
   const int c0 = blockIdx.y * cpb;
   const int c1 = min(ncols, c0 + cpb);
+  // columns are independent: unrolled so that several columns' loads are in flight
+#pragma unroll 4
   for (int ci = c0; ci < c1; ++ci) {
     const long long off = (long long)cols[ci] * ld;
     const cplx<TB> bb = b[off + p];
@@ -371,6 +379,8 @@ __global__ void __launch_bounds__(256) k_restrict(Grid gf, Grid gc, const cplx<T
   const T scale = IS3D ? T(0.125) : T(0.25);
   const int c0 = blockIdx.y * cpb;
   const int c1 = min(ncols, c0 + cpb);
+  // columns are independent: unrolled so that several columns' loads are in flight
+#pragma unroll 4
   for (int ci = c0; ci < c1; ++ci) {
     const int col = cols[ci];
     const cplx<T>* r = rf + (long long)col * ldf + pc;
@@ -428,6 +438,8 @@ __global__ void __launch_bounds__(256) k_prolong(Grid gf, Grid gc, const cplx<T>
   const T wgt = IS3D ? T(0.125) : T(0.25);
   const int c0 = blockIdx.y * cpb;
   const int c1 = min(ncols, c0 + cpb);
+  // columns are independent: unrolled so that several columns' loads are in flight
+#pragma unroll 4
   for (int ci = c0; ci < c1; ++ci) {
     const int col = cols[ci];
     const cplx<T>* e = ec + (long long)col * ldc;

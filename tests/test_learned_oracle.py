@@ -151,3 +151,52 @@ def test_net_file_format_checks(hz, tmp_path):
             hz.learned.file_info(p)
     with pytest.raises(hz._lib.HelmgpuError):
         hz.learned.file_info(tmp_path / "missing.hzn")
+
+
+def test_backward_matches_torch_autograd():
+    """The oracle's hand-written backward against PyTorch CPU autograd of the same
+    network (FP64, no rounding): the restriction and prolongation as the same
+    separable linear maps, the convolutions as conv2d cross-correlations."""
+    torch = pytest.importorskip("torch")
+    x, t = _data(11)
+    w = CN.he_init(12).astype(np.float64)
+    _, cache = CN.forward(w, x, emulate=False)
+    L_np, g_np = CN.backward(cache, t)
+
+    ws = [torch.tensor(a, requires_grad=True) for a in CN.split(w)]
+
+    def conv(z, wl):  # z (B, ny, nx, C); wl [cout][9][cin] with tap 3*(dy+1) + (dx+1)
+        k = wl.reshape(wl.shape[0], 3, 3, wl.shape[2]).permute(0, 3, 1, 2)
+        return torch.nn.functional.conv2d(z.permute(0, 3, 1, 2), k, padding=1).permute(0, 2, 3, 1)
+
+    def lin(Ay, Ax, z):
+        return torch.einsum("Jj,Ii,bjic->bJIc", torch.tensor(Ay), torch.tensor(Ax), z)
+
+    def R(z):
+        ny, nx = z.shape[1], z.shape[2]
+        Ry, Rx = CN._fw_1d(ny), CN._fw_1d(nx)
+        return lin(Ry / Ry.sum(1, keepdims=True), Rx / Rx.sum(1, keepdims=True), z)
+
+    def P(z, ny, nx):
+        return lin(CN._p_1d(ny), CN._p_1d(nx), z)
+
+    relu = torch.relu
+    X = torch.tensor(x)
+    ny, nx = X.shape[1], X.shape[2]
+    g1 = (CN.coarse(ny), CN.coarse(nx))
+    g2 = (CN.coarse(g1[0]), CN.coarse(g1[1]))
+    e0 = relu(conv(X, ws[0]))
+    e1 = relu(conv(R(e0), ws[1]))
+    e2 = relu(conv(R(e1), ws[2]))
+    e3 = relu(conv(R(e2), ws[3]))
+    d2 = relu(conv(torch.cat([P(e3, *g2), e2], 3), ws[4]))
+    d1 = relu(conv(torch.cat([P(d2, *g1), e1], 3), ws[5]))
+    d0 = relu(conv(torch.cat([P(d1, ny, nx), e0], 3), ws[6]))
+    y = conv(d0, ws[7])
+    T = torch.tensor(t)
+    B = y.shape[0]
+    loss = (((y - T) ** 2).reshape(B, -1).sum(1) / (T ** 2).reshape(B, -1).sum(1)).mean()
+    loss.backward()
+    g_t = np.concatenate([a.grad.numpy().ravel() for a in ws])
+    assert abs(loss.item() - L_np) <= 1e-12 * abs(L_np)
+    np.testing.assert_allclose(g_np, g_t, rtol=1e-9, atol=1e-12 * np.abs(g_t).max())
