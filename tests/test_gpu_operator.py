@@ -34,10 +34,13 @@ def test_apply_matches_golden_2d_3d(hz):
     assert _rel(H3.H @ g["X3"], g["HadjX3"]) < TOL64
 
 
-@pytest.mark.parametrize("case", ["2d_neumann", "2d_dirichlet_somm", "3d", "2d_bc1"])
+@pytest.mark.parametrize("case", ["2d_neumann", "2d_dirichlet_somm", "3d", "3d_wide", "2d_bc1"])
 def test_apply_matches_oracle_sparse(hz, O, case):
     if case == "3d":
         P = PB.layered((20, 12, 16), seed=4, pad=3, ellipsoid=True)
+    elif case == "3d_wide":
+        # more than a warp of nodes along x, sizes that divide nothing evenly
+        P = PB.layered((40, 18, 20), seed=4, pad=3, ellipsoid=True)
     elif case == "2d_dirichlet_somm":
         P = PB.gradient_2d((40, 24), pad=5, neumann=False, sommerfeld=True)
     else:
