@@ -268,6 +268,7 @@ def run_ours(args, rank, ws, dist):
         o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, args.max_outer
         o.cycle = ord(args.cycle)
         o.cuda_graph = 0 if args.no_graph else 1
+        o.autotune = 0 if args.no_tune else 1
         if args.krylov == "bicgstab":
             o.krylov, o.max_outer = L.HZ_KRYLOV_BICGSTAB, 2000
         o.precision = precision
@@ -523,6 +524,7 @@ def main():
     ap.add_argument("--outer", default="emulated", choices=["fp64", "emulated"],
                     help="outer Krylov arithmetic of the mixed form: native FP64 or FP64 emulated with FP32 pairs")
     ap.add_argument("--no-graph", action="store_true", help="launch the cycles eagerly (no CUDA graphs)")
+    ap.add_argument("--no-tune", action="store_true", help="default stencil launch shapes (no autotuning)")
     ap.add_argument("--max-outer", type=int, default=200,
                     help="FGMRES restart cycles (fewer: kernel-rate profiling runs, not a valid RHS/s)")
     ap.add_argument("--cycle", default="V", choices=["V", "W", "K"],
@@ -631,7 +633,7 @@ def main():
                 data="synthetic (seeded layered model)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
                             krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB", cycle=args.cycle,
-                            cuda_graph=not args.no_graph,
+                            cuda_graph=not args.no_graph, autotune=not args.no_tune,
                             outer_arithmetic=args.outer,
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
                             l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9)),

@@ -71,7 +71,8 @@ class hz_options(C.Structure):
         ("device", C.c_int32),
         ("outer_arith", C.c_int32),
         ("cuda_graph", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("autotune", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -122,6 +123,7 @@ SIGNATURES = {
     "hz_net_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_double,
                                C.c_int32, _dp]),
     "hz_kernel_flops": (C.c_int, [_vp, C.c_int32, _dp]),
+    "hz_tune_info": (C.c_int, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "hz_net_save": (C.c_int, [_vp, C.c_char_p]),
     "hz_net_load": (C.c_int, [_vp, C.c_char_p]),
     "hz_net_file_info": (C.c_int, [C.c_char_p, _i64p, _i64p]),

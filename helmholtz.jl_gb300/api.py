@@ -362,6 +362,7 @@ class MGparam:
     coarseOperator: str = "Galerkin"  # or "Rediscretize" (src/ShiftedLaplacianMultigridSolver.jl:51-62)
     outerArithmetic: str = "fp64"     # or "emulated": FP64 emulated with FP32 pairs (mixed form, FGMRES)
     cudaGraph: bool = True            # replay the FGMRES preconditioner applications from CUDA graphs
+    autotune: bool = True             # time the stencils' launch shapes at the first solve
     doTranspose: int = 0
     _hier: dict = field(default_factory=dict, repr=False)
 
@@ -483,6 +484,7 @@ def _options(s: ShiftedLaplacianMultigridSolver) -> L.hz_options:
     o.coarse_op = L.HZ_COARSE_REDISCRETIZE if MG.coarseOperator == "Rediscretize" else L.HZ_COARSE_GALERKIN
     o.outer_arith = L.HZ_OUTER_EMULATED if MG.outerArithmetic == "emulated" else L.HZ_OUTER_FP64
     o.cuda_graph = int(bool(MG.cudaGraph))
+    o.autotune = int(bool(MG.autotune))
     o.verbose = int(bool(s.verbose))
     return o
 
@@ -496,7 +498,7 @@ def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
     key = (id(s.helmParam), id(s.helmParam.m), id(s.helmParam.gamma), s.MG.levels, s.MG.maxOuterIter,
            s.MG.relativeTol, s.MG.relaxParam, int(s.MG.relaxPre), int(s.MG.relaxPost), s.MG.cycleType,
            s.MG.precision, s.inner, float(s.shift[0]), s.Krylov, s.MG.coarseOperator, s.MG.outerArithmetic,
-           bool(s.MG.cudaGraph))
+           bool(s.MG.cudaGraph), bool(s.MG.autotune))
     if s._handle is not None and s._key == key:
         return s._handle
     _release(s)

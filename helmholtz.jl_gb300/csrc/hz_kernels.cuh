@@ -39,6 +39,10 @@ struct Ctx {
   void resolve();  // after a stream sync: fold pending event pairs into the table
   void add_bytes(const char* name, double bytes) { alg_bytes[name_id(name)] += bytes; }
   void add_flops(const char* name, double flops) { alg_flops[name_id(name)] += flops; }
+  // launch-shape choices of the autotuner: CTAs aimed at per launch of the
+  // fine-level and the Galerkin stencils (0: the default rule), which set how
+  // many right-hand sides a block loops over
+  int tune_fine = 0, tune_rap = 0;
   void release();
 };
 

@@ -18,7 +18,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <sstream>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <tuple>
@@ -177,6 +180,7 @@ struct hz_handle {
   std::map<std::tuple<int, int, int, int>, CycleGraph> graphs;
   long long graph_gen = -1;
   bool graphs_off = false;  // a capture failed: eager launches from then on
+  int tuned_cols = -1;      // column count the stencil launch shapes were tuned for
   // capture of the right-hand sides handed to one level (training pairs)
   bool cap_on = false;
   int cap_level = 0;
@@ -867,6 +871,139 @@ void col_norms(hz_handle* h, const double2* x, const std::vector<int>& cols, dou
   }
 }
 
+// ---- autotuner -----------------------------------------------------------------
+// The launch shape of the fine-level and Galerkin stencils (how many CTAs a
+// launch aims at, hence how many right-hand sides each block loops over) is
+// timed on the handle's own level sizes at its first solve with a given
+// column count, and the fastest kept.  Results are cached per process and,
+// when HELMGPU_TUNE_CACHE names a file, persisted there as "key fine rap" lines.
+std::mutex g_tune_mu;
+std::map<std::string, std::pair<int, int>> g_tune;
+bool g_tune_loaded = false;
+
+std::string tune_key(const hz_handle* h, int ncols) {
+  cudaDeviceProp pr{};
+  cudaGetDeviceProperties(&pr, h->dev);
+  std::string gpu = pr.name;
+  for (char& ch : gpu)
+    if (ch == ' ' || ch == '|') ch = '_';
+  char buf[384];
+  snprintf(buf, sizeof(buf), "%s|sm%d|d%d|%dx%dx%d|c%d|p%d|o%d|L%d|k%d", gpu.c_str(), pr.multiProcessorCount,
+           h->prob.dim, h->g0.nx, h->g0.ny, h->g0.nz, ncols, h->opt.precision, h->opt.outer_arith, h->opt.levels,
+           h->opt.coarse_op);
+  return buf;
+}
+
+void tune_cache_load() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = std::getenv("HELMGPU_TUNE_CACHE");
+  if (!path || !*path) return;
+  std::ifstream f(path);
+  std::string line;
+  while (std::getline(f, line)) {
+    std::istringstream is(line);
+    std::string key;
+    int a = 0, b = 0;
+    if (is >> key >> a >> b && a >= 0 && b >= 0) g_tune[key] = {a, b};
+  }
+}
+
+void tune_cache_store(const std::string& key, int fine, int rap) {
+  g_tune[key] = {fine, rap};
+  const char* path = std::getenv("HELMGPU_TUNE_CACHE");
+  if (!path || !*path) return;
+  std::ofstream f(path, std::ios::app);
+  if (f) f << key << ' ' << fine << ' ' << rap << '\n';
+}
+
+// average milliseconds of one call of f on the handle's stream (1 untimed + 3 timed)
+template <typename F>
+double time_call(hz_handle* h, F&& f) {
+  cudaEvent_t a, b;
+  ck(cudaEventCreate(&a), "event");
+  ck(cudaEventCreate(&b), "event");
+  f();
+  cudaEventRecord(a, h->ctx.stream);
+  for (int r = 0; r < 3; ++r) f();
+  cudaEventRecord(b, h->ctx.stream);
+  ck(cudaEventSynchronize(b), "tune sync");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / 3.0;
+}
+
+template <typename T>
+void autotune(hz_handle* h, Hierarchy& H, int nrhs) {
+  const std::string key = tune_key(h, nrhs);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_cache_load();
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      h->ctx.tune_fine = it->second.first;
+      h->ctx.tune_rap = it->second.second;
+      return;
+    }
+  }
+  Ctx& c = h->ctx;
+  // the tuning launches stay out of the launch table and the statistics
+  const bool prof = c.profile;
+  c.profile = false;
+  const auto counts0 = c.counts;
+  const auto bytes0 = c.alg_bytes;
+  const auto flops0 = c.alg_flops;
+  const long long l0 = c.launches;
+  ensure_level_buffers<T>(h, H, h->rcap);
+  std::vector<int> all(nrhs);
+  for (int q = 0; q < nrhs; ++q) all[q] = q;
+  upload_cols(h, all);
+  const int* dc = h->cols.as<int>();
+  static const int mult[] = {0, 1, 2, 4, 16, 32};  // CTAs per SM aimed at; 0: the default rule (8 per SM)
+  int sms = 0;
+  ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->dev), "SM count");
+  auto pick = [&](int& knob, Level& L, cplx<T>* x, cplx<T>* bb, cplx<T>* y, int level) {
+    const size_t bytes = (size_t)nrhs * L.ld * sizeof(cplx<T>);
+    ck(cudaMemsetAsync(x, 0, bytes, c.stream), "tune zero");
+    ck(cudaMemsetAsync(bb, 0, bytes, c.stream), "tune zero");
+    double best = 1e300;
+    int best_v = 0;
+    for (int m : mult) {
+      knob = m * sms;
+      const double ms = time_call(h, [&] { lev_op<T, T>(h, H, level, MODE_RESID, x, bb, y, dc, nrhs); });
+      if (ms < best * 0.97) {  // a change must win by 3 %
+        best = ms;
+        best_v = knob;
+      }
+    }
+    knob = best_v;
+  };
+  Level& L0 = *H.lv[0];
+  if (H.lv.size() > 1) {
+    // level 0 has two work blocks of its own; the residual goes to the Z workspace
+    pick(c.tune_fine, L0, L0.t.as<cplx<T>>(), L0.r.as<cplx<T>>(), reinterpret_cast<cplx<T>*>(h->Z.p), 0);
+    if (H.lv.size() > 2 && !H.lv[1]->fine) {
+      Level& L1 = *H.lv[1];
+      pick(c.tune_rap, L1, L1.x.as<cplx<T>>(), L1.b.as<cplx<T>>(), L1.r.as<cplx<T>>(), 1);
+    }
+  }
+  sync(h);
+  c.counts = counts0;
+  c.alg_bytes = bytes0;
+  c.alg_flops = flops0;
+  c.counts.resize(c.names.size(), 0);
+  c.alg_bytes.resize(c.names.size(), 0.0);
+  c.alg_flops.resize(c.names.size(), 0.0);
+  c.timed.resize(c.names.size(), 0);
+  c.total_ms.resize(c.names.size(), 0.0);
+  c.launches = l0;
+  c.profile = prof;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_cache_store(key, c.tune_fine, c.tune_rap);
+}
+
 void drop_graphs(hz_handle* h) {
   for (auto& kv : h->graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
@@ -1405,6 +1542,7 @@ void hz_default_options(hz_options* o) {
   o->precision = HZ_PREC_FP64;
   o->coarse_op = HZ_COARSE_GALERKIN;
   o->cuda_graph = 1;
+  o->autotune = 1;
 }
 
 int hz_create(const hz_problem* prob, const hz_options* opt, hz_handle** out) {
@@ -1474,6 +1612,13 @@ int hz_solve(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, 
     auto t0 = clk::now();
     if (!h->hier[transpose].built) build_hierarchy(h, transpose);
     ensure_workspace(h, nrhs);
+    if (h->opt.autotune && h->tuned_cols != nrhs) {
+      if (h->opt.precision == HZ_PREC_MIXED)
+        autotune<float>(h, h->hier[transpose], nrhs);
+      else
+        autotune<double>(h, h->hier[transpose], nrhs);
+      h->tuned_cols = nrhs;
+    }
     auto t1 = clk::now();
     h->setup_time += secs(t0, t1);
     copy_in(h, B, h->Bd.as<double2>(), n, nrhs, mem);
@@ -1654,6 +1799,13 @@ int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int
 int hz_kernel_flops(hz_handle* h, int32_t idx, double* alg_flops) {
   if (!h) return HZ_ERR_ARG;
   return ctx_times(h->ctx, h->dev, idx, nullptr, 0, nullptr, nullptr, nullptr, nullptr, alg_flops);
+}
+
+int hz_tune_info(const hz_handle* h, int32_t* fine_ctas, int32_t* rap_ctas) {
+  if (!h) return HZ_ERR_ARG;
+  if (fine_ctas) *fine_ctas = h->ctx.tune_fine;
+  if (rap_ctas) *rap_ctas = h->ctx.tune_rap;
+  return h->tuned_cols >= 0 ? HZ_OK : HZ_NOT_CONVERGED;
 }
 
 int hz_reset_kernel_times(hz_handle* h) {

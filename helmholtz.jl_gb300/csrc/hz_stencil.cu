@@ -191,7 +191,7 @@ void launch_fine(Ctx& ctx, int mode, const FineOp& op, const cplx<T>* diag, cons
   o.adj = op.adj;
   const int TPB = 256;
   long long nbx = (op.g.N + TPB - 1) / TPB;
-  int ch = chunks_for(nbx, ncols);
+  int ch = ctx.tune_fine > 0 ? chunks_for(nbx, ncols, ctx.tune_fine) : chunks_for(nbx, ncols);
   int cpb = (ncols + ch - 1) / ch;
   dim3 grid((unsigned)nbx, (unsigned)ch);
   const bool is3d = op.g.nz > 1;
@@ -285,7 +285,7 @@ void launch_rap(Ctx& ctx, int mode, const Grid& g, const cplx<T>* coef, long lon
   if (ncols <= 0) return;
   const int TPB = 128;
   long long nbx = (g.N + TPB - 1) / TPB;
-  int ch = chunks_for(nbx, ncols);
+  int ch = ctx.tune_rap > 0 ? chunks_for(nbx, ncols, ctx.tune_rap) : chunks_for(nbx, ncols);
   int cpb = (ncols + ch - 1) / ch;
   dim3 grid((unsigned)nbx, (unsigned)ch);
   const bool is3d = g.nz > 1;

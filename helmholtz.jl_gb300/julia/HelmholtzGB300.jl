@@ -58,9 +58,10 @@ mutable struct HzOptions
     device::Int32
     outer_arith::Int32
     cuda_graph::Int32
-    reserved::NTuple{5,Int32}
+    autotune::Int32
+    reserved::NTuple{4,Int32}
 end
-HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 5))
+HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 4))
 
 mutable struct HzStats
     outer::Int32

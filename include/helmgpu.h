@@ -96,7 +96,8 @@ typedef struct hz_options {
   int32_t device;        /* CUDA device ordinal */
   int32_t outer_arith;   /* FGMRES outer arithmetic: HZ_OUTER_FP64 (native) or HZ_OUTER_EMULATED */
   int32_t cuda_graph;    /* 1 (default): replay each FGMRES preconditioner application from a CUDA graph */
-  int32_t reserved[5];
+  int32_t autotune;      /* 1 (default): time the stencils' launch shapes at the first solve (see hz_tune_info) */
+  int32_t reserved[4];
 } hz_options;
 
 typedef struct hz_stats {
@@ -189,6 +190,12 @@ void* hz_stream(hz_handle* h);
 int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                     int64_t* timed_launches, double* total_ms, double* alg_bytes);
 int hz_reset_kernel_times(hz_handle* h);
+/* Launch shapes chosen by the autotuner for this handle: CTAs aimed at per launch
+ * of the fine-level and the Galerkin stencils (0 = the default rule).  Timed on the
+ * handle's own level sizes at the first solve with a new column count; cached per
+ * process and, when the environment variable HELMGPU_TUNE_CACHE names a file,
+ * persisted there.  Returns HZ_OK once tuned, HZ_NOT_CONVERGED before. */
+int hz_tune_info(const hz_handle* h, int32_t* fine_ctas, int32_t* rap_ctas);
 /* Algorithmic flops of entry idx of the launch table (the tensor-core kernels
  * of the learned correction; 0 for the memory-bound kernels). */
 int hz_kernel_flops(hz_handle* h, int32_t idx, double* alg_flops);
