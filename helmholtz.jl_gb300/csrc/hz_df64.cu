@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(RT, 2) k_update_df(long long N, const float4* 
     }
     re.renorm();
     im.renorm();
-    wc[p] = make_float4(re.hi, im.hi, re.lo, im.lo);
+    __stcs(&wc[p], make_float4(re.hi, im.hi, re.lo, im.lo));
     if (want_norm) {
       nn.mac(re.hi, re.lo, re.hi, re.lo);
       nn.mac(im.hi, im.lo, im.hi, im.lo);
@@ -737,12 +737,14 @@ __global__ void __launch_bounds__(256) k_to_df(long long N, const double2* __res
   const double sc = s[c];
   const double2* xc = x + (long long)c * xld;
   float4* yc = y + (long long)c * yld;
+  // elements are independent (in place: each is read before it is written)
+#pragma unroll 4
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
-    const double2 v = xc[p];
+    const double2 v = __ldcs(&xc[p]);
     float rh, rl, ih, il;
     split(sc * v.x, rh, rl);
     split(sc * v.y, ih, il);
-    yc[p] = make_float4(rh, ih, rl, il);
+    __stcs(&yc[p], make_float4(rh, ih, rl, il));
   }
 }
 
@@ -761,8 +763,10 @@ __global__ void __launch_bounds__(256) k_scale_df(long long N, float4* __restric
   float sh, sl;
   split(s[c], sh, sl);
   float4* wc = w + (long long)c * ld;
+  // elements are independent: unrolled so that several loads are in flight per thread
+#pragma unroll 4
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
-    const float4 v = wc[p];
+    const float4 v = __ldcs(&wc[p]);
     DAcc re, im;
     re.init(0.f, 0.f);
     im.init(0.f, 0.f);
@@ -770,7 +774,7 @@ __global__ void __launch_bounds__(256) k_scale_df(long long N, float4* __restric
     im.mac(v.y, v.w, sh, sl);
     re.renorm();
     im.renorm();
-    wc[p] = make_float4(re.hi, im.hi, re.lo, im.lo);
+    __stcs(&wc[p], make_float4(re.hi, im.hi, re.lo, im.lo));
   }
 }
 

@@ -240,8 +240,8 @@ __global__ void __launch_bounds__(256) k_scale_cols(long long N, const double2* 
   const double2* xc = x + (long long)c * xld;
   double2* yc = y + (long long)c * yld;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
-    const double2 v = xc[p];
-    yc[p] = mk<double>(sc * v.x, sc * v.y);
+    const double2 v = __ldcs(&xc[p]);  // streamed once
+    __stcs(&yc[p], mk<double>(sc * v.x, sc * v.y));
   }
 }
 

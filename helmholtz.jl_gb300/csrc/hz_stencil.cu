@@ -160,16 +160,18 @@ __global__ void __launch_bounds__(256) k_fine(FineOpT<T> op, const cplx<T>* __re
     }
     cplx<T> ax = mk<T>(-sr, -si);
     ax = cfma<T>(d, xp, ax);
+    // b is read once and y written once: streaming hints keep the cache for the
+    // x planes whose neighbours are read again
     if (MODE == MODE_APPLY) {
-      y[off + p] = ax;
+      __stcs(&y[off + p], ax);
     } else {
-      const cplx<TB> bb = b[off + p];
+      const cplx<TB> bb = __ldcs(&b[off + p]);
       const cplx<T> r = mk<T>((T)bb.x - ax.x, (T)bb.y - ax.y);
       if (MODE == MODE_RESID) {
-        y[off + p] = r;
+        __stcs(&y[off + p], r);
       } else {
         const cplx<T> dr = cmul<T>(di, r);
-        y[off + p] = mk<T>(xp.x + w * dr.x, xp.y + w * dr.y);
+        __stcs(&y[off + p], mk<T>(xp.x + w * dr.x, xp.y + w * dr.y));
       }
     }
   }
@@ -452,8 +454,9 @@ __global__ void __launch_bounds__(256) k_prolong(Grid gf, Grid gc, const cplx<T>
       ai += (u0.y + u1.y) + (u2.y + u3.y);
     }
     const long long o = (long long)col * ldf + p;
-    const cplx<T> base = xin ? xin[o] : mk<T>(0, 0);
-    xout[o] = mk<T>(base.x + wgt * ar, base.y + wgt * ai);
+    // the fine vector is read and written once (streaming); the coarse one stays cached
+    const cplx<T> base = xin ? __ldcs(&xin[o]) : mk<T>(0, 0);
+    __stcs(&xout[o], mk<T>(base.x + wgt * ar, base.y + wgt * ai));
   }
 }
 
