@@ -82,8 +82,6 @@ constexpr int kConvStrip = kConvTile + 2;   // rows per strip
 constexpr int kConvCK = 16;                 // channels per staged chunk
 constexpr int kConvSR = kConvCK + 8;        // padded shared row (bf16)
 
-__device__ __forceinline__ unsigned lds32(const bf16* p) { return *reinterpret_cast<const unsigned*>(p); }
-
 // ldmatrix: four (two) 8x8 b16 matrices from shared memory, rows addressed by
 // lanes 0-7, 8-15, 16-23, 24-31 (0-7, 8-15); lane l receives row l/4, columns
 // 2(l%4), 2(l%4)+1 of matrix i in register i -- the m16n8k16 fragment layout.

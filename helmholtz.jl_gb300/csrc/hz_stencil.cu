@@ -266,16 +266,17 @@ __global__ void __launch_bounds__(128) k_rap(Grid g, const cplx<T>* __restrict__
       if (s == NS / 2) xp = v;
       ax = cfma<T>(c[s], v, ax);
     }
+    // b read once, y written once: streaming hints, as in k_fine
     if (MODE == MODE_APPLY) {
-      y[off + p] = ax;
+      __stcs(&y[off + p], ax);
     } else {
-      const cplx<TB> bb = b[off + p];
+      const cplx<TB> bb = __ldcs(&b[off + p]);
       const cplx<T> r = mk<T>((T)bb.x - ax.x, (T)bb.y - ax.y);
       if (MODE == MODE_RESID) {
-        y[off + p] = r;
+        __stcs(&y[off + p], r);
       } else {
         const cplx<T> dr = cmul<T>(di, r);
-        y[off + p] = mk<T>(xp.x + w * dr.x, xp.y + w * dr.y);
+        __stcs(&y[off + p], mk<T>(xp.x + w * dr.x, xp.y + w * dr.y));
       }
     }
   }

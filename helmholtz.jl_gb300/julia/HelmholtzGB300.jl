@@ -22,7 +22,8 @@ using Multigrid: MGparam
 export HelmholtzParam, ShiftedLaplacianMultigridSolver, getShiftedLaplacianMultigridSolver, solveLinearSystem,
        solveLinearSystem!, copySolver, clear!, getMaximalFrequency, getABL, getSommerfeldBC,
        getAcousticPointSource, getHelmholtzFun, HzApply,
-       CoarseNet, netWeights, setNetWeights!, netForward, netGradient, netTrain!, collectPairs!, attachNet!
+       CoarseNet, netWeights, setNetWeights!, netForward, netGradient, netTrain!, collectPairs!, attachNet!,
+       saveNet, loadNet!
 
 const libhelmgpu = get(ENV, "HELMGPU_LIB", joinpath(@__DIR__, "..", "libhelmgpu.so"))
 
@@ -353,6 +354,11 @@ function collectPairs!(s::ShiftedLaplacianMultigridSolver, B::AbstractVecOrMat, 
                 x, t, pe, rr, cnt), h)
     return cnt[], pe[1:cnt[]], X
 end
+# versioned file of the weights and the Adam state; training resumes from a loaded file
+saveNet(net::CoarseNet, path::AbstractString) =
+    check(ccall((:hz_net_save, libhelmgpu), Cint, (Ptr{Cvoid}, Cstring), net.ptr, path))
+loadNet!(net::CoarseNet, path::AbstractString) =
+    check(ccall((:hz_net_load, libhelmgpu), Cint, (Ptr{Cvoid}, Cstring), net.ptr, path))
 # use net for the coarse-grid correction of `level` in the later solves of s (FGMRES only);
 # net = nothing detaches
 function attachNet!(s::ShiftedLaplacianMultigridSolver, net, level::Integer = 2, stagRatio::Float64 = 0.95)
