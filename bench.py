@@ -35,7 +35,7 @@ METRIC = "RHS solved/s to rel. residual 1e-6 on 1 GB300: learned+mixed vs plain 
 # Synthetic seeded workloads (shapes, sizes and value distributions of the
 # measured configurations; no external dataset is needed).
 WORKLOADS = {
-    # configs[0]: 2D 129 x 129 on [0,1]^2, v = 1.5 + 3 z with the v = 4.5 ellipse, one source
+    # 2D 129 x 129 on [0,1]^2, v = 1.5 + 3 z with the v = 4.5 ellipse, one source
     # at (0.5, 2h), absorbing layer 16, 3 levels, FGMRES(10) to 1e-8
     "c1": dict(name="2D 129x129 gradient+ellipse, 1 source, 3 levels, FGMRES(10) tol 1e-8",
                cells=(128, 128), h=1.0 / 128, nrhs=1, levels=3, pad=16, ellipsoid=False, tol=1e-8,

@@ -672,20 +672,22 @@ void launch_inplace_df(Ctx& ctx, long long n, double2* a) {
 }
 
 // ---- solution update x += sum_i y_i Z_i (Z complex FP32, x FP64) -----------------
-__global__ void __launch_bounds__(256) k_update_x_df(long long N, const float2* __restrict__ Z, long long zstride,
+__global__ void __launch_bounds__(256, 4) k_update_x_df(long long N, const float2* __restrict__ Z, long long zstride,
                                                      long long ld, const int* __restrict__ kcol,
                                                      const double2* __restrict__ y, int ystride,
                                                      double2* __restrict__ x, long long xld,
                                                      const int* __restrict__ cols) {
   const int c = cols[blockIdx.y];
   const int k = kcol[c];
-  float yrh[KG], yrl[KG], yih[KG], yil[KG];
-#pragma unroll
-  for (int s = 0; s < KG; ++s) {
-    const double2 v = (s < k) ? y[(long long)c * ystride + s] : mk<double>(0, 0);
-    split(v.x, yrh[s], yrl[s]);
-    split(v.y, yih[s], yil[s]);
+  // the coefficients of this column, split into FP32 pairs once per block and
+  // read from shared memory (broadcast): registers stay free for occupancy
+  __shared__ float sy[4][64];  // Re hi, Re lo, Im hi, Im lo; restart length <= 64
+  for (int s = threadIdx.x; s < k; s += blockDim.x) {
+    const double2 v = y[(long long)c * ystride + s];
+    split(v.x, sy[0][s], sy[1][s]);
+    split(v.y, sy[2][s], sy[3][s]);
   }
+  __syncthreads();
   double2* xc = x + (long long)c * xld;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
     DAcc re, im;
@@ -696,22 +698,18 @@ __global__ void __launch_bounds__(256) k_update_x_df(long long N, const float2* 
       if (s < k) {
         const float2 z = Z[((long long)s * zstride + c) * ld + p];
         // (yr + i yi)(zr + i zi)
-        re.mac1(yrh[s], yrl[s], z.x);
-        re.mac1(-yih[s], -yil[s], z.y);
-        im.mac1(yrh[s], yrl[s], z.y);
-        im.mac1(yih[s], yil[s], z.x);
+        re.mac1(sy[0][s], sy[1][s], z.x);
+        re.mac1(-sy[2][s], -sy[3][s], z.y);
+        im.mac1(sy[0][s], sy[1][s], z.y);
+        im.mac1(sy[2][s], sy[3][s], z.x);
       }
     }
     for (int s = KG; s < k; ++s) {  // restart lengths above KG
-      const double2 v = y[(long long)c * ystride + s];
-      float a, b2, e, f;
-      split(v.x, a, b2);
-      split(v.y, e, f);
       const float2 z = Z[((long long)s * zstride + c) * ld + p];
-      re.mac1(a, b2, z.x);
-      re.mac1(-e, -f, z.y);
-      im.mac1(a, b2, z.y);
-      im.mac1(e, f, z.x);
+      re.mac1(sy[0][s], sy[1][s], z.x);
+      re.mac1(-sy[2][s], -sy[3][s], z.y);
+      im.mac1(sy[0][s], sy[1][s], z.y);
+      im.mac1(sy[2][s], sy[3][s], z.x);
     }
     const double2 xv = xc[p];
     xc[p] = mk<double>(xv.x + re.to_double(), xv.y + im.to_double());
