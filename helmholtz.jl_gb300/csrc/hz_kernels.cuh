@@ -212,6 +212,18 @@ void launch_dgks(Ctx& ctx, const int* cols, int ncols, const double2* before, in
 // out[c*ostride + slot] = sum over blocks of part (slot < K1); accum adds to out.
 void launch_reduce(Ctx& ctx, const double2* part, const int* cols, int ncols, int K1, int nblk, double2* out,
                    int ostride, int accum);
+// Deferred normalisation of the FGMRES basis: stored v_i stands for sig_i v_i
+// (sig[c*sstride + i]).  init: sig_0 = 1; coef_i = sig_i^2 d_i for i < K (the
+// update's coefficients); true: hA_i, hB_i *= sig_i sig_j (i <= j) and the norm
+// slots nr, nr2 *= sig_j^2; next: sig_{j+1} = sig_j * invhn; y_i *= sig_i.
+void launch_sig_init(Ctx& ctx, const int* cols, int ncols, double* sig, int sstride);
+void launch_sig_coef(Ctx& ctx, const int* cols, int ncols, int K, const double* sig, int sstride, const double2* d,
+                     int hstride, double2* coef);
+void launch_sig_true(Ctx& ctx, int j, const int* cols, int ncols, const double* sig, int sstride, double2* hA,
+                     double2* hB, double2* nr, double2* nr2, int hstride);
+void launch_sig_next(Ctx& ctx, int j, const int* cols, int ncols, double* sig, int sstride, const double* invhn);
+void launch_sig_y(Ctx& ctx, const int* cols, int ncols, const int* kcol, const double* sig, int sstride, double2* y,
+                  int ystride);
 // y[:, c] = s[c] * x[:, c]
 void launch_scale_cols(Ctx& ctx, long long N, const double2* x, long long xld, double2* y, long long yld,
                        const double* s, const int* cols, int ncols);

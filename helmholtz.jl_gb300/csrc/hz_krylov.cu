@@ -232,6 +232,94 @@ void launch_reduce(Ctx& ctx, const double2* part, const int* cols, int ncols, in
   HZ_LAUNCH(ctx, "krylov_reduce", (double)ncols * K1 * (nblk + 1) * sizeof(double2), k_reduce, blocks, 256, 0, part, cols, ncols, K1, nblk, out, ostride, accum);
 }
 
+// ---- deferred normalisation of the FGMRES basis --------------------------------
+// The stored basis vector v_i of column c stands for V_i = sig_i v_i with
+// sig_i = sig[c*sstride + i] > 0, so no pass over the vector is spent on
+// normalising it.  From the stored dots d_i = conj(v_i) . w' of the stored
+// candidate w' (= H Z'_j, Z'_j the cycle applied to v_j): the update uses the
+// coefficients sig_i^2 d_i, the Hessenberg entries are sig_i sig_j d_i and
+// h_{j+1,j} = sig_j ||w''||.
+__global__ void k_sig_init(const int* __restrict__ cols, int ncols, double* __restrict__ sig, int sstride) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ncols) sig[(long long)cols[i] * sstride] = 1.0;
+}
+
+__global__ void k_sig_coef(const int* __restrict__ cols, int ncols, int K, const double* __restrict__ sig, int sstride,
+                           const double2* __restrict__ d, int hstride, double2* __restrict__ coef) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncols * K) return;
+  const int c = cols[t / K], i = t % K;
+  const double s = sig[(long long)c * sstride + i];
+  const double2 v = d[(long long)c * hstride + i];
+  coef[(long long)c * hstride + i] = mk<double>(s * s * v.x, s * s * v.y);
+}
+
+__global__ void k_sig_true(int j, const int* __restrict__ cols, int ncols, const double* __restrict__ sig, int sstride,
+                           double2* __restrict__ hA, double2* __restrict__ hB, double2* __restrict__ nr,
+                           double2* __restrict__ nr2, int hstride) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  const double* sc = sig + (long long)c * sstride;
+  const double sj = sc[j];
+  for (int i = 0; i <= j; ++i) {
+    const double f = sc[i] * sj;
+    double2& a = hA[(long long)c * hstride + i];
+    double2& b = hB[(long long)c * hstride + i];
+    a = mk<double>(f * a.x, f * a.y);
+    b = mk<double>(f * b.x, f * b.y);
+  }
+  nr[(long long)c * hstride].x *= sj * sj;
+  nr2[(long long)c * hstride].x *= sj * sj;
+}
+
+__global__ void k_sig_next(int j, const int* __restrict__ cols, int ncols, double* __restrict__ sig, int sstride,
+                           const double* __restrict__ invhn) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  sig[(long long)c * sstride + j + 1] = sig[(long long)c * sstride + j] * invhn[c];
+}
+
+__global__ void k_sig_y(const int* __restrict__ cols, int ncols, const int* __restrict__ kcol,
+                        const double* __restrict__ sig, int sstride, double2* __restrict__ y, int ystride) {
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ncols) return;
+  const int c = cols[pos];
+  for (int i = 0; i < kcol[c]; ++i) {
+    const double s = sig[(long long)c * sstride + i];
+    double2& v = y[(long long)c * ystride + i];
+    v = mk<double>(s * v.x, s * v.y);
+  }
+}
+
+void launch_sig_init(Ctx& ctx, const int* cols, int ncols, double* sig, int sstride) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "basis_scale", 0.0, k_sig_init, (ncols + 127) / 128, 128, 0, cols, ncols, sig, sstride);
+}
+void launch_sig_coef(Ctx& ctx, const int* cols, int ncols, int K, const double* sig, int sstride, const double2* d,
+                     int hstride, double2* coef) {
+  if (ncols <= 0 || K <= 0) return;
+  HZ_LAUNCH(ctx, "basis_scale", 0.0, k_sig_coef, (ncols * K + 127) / 128, 128, 0, cols, ncols, K, sig, sstride, d,
+            hstride, coef);
+}
+void launch_sig_true(Ctx& ctx, int j, const int* cols, int ncols, const double* sig, int sstride, double2* hA,
+                     double2* hB, double2* nr, double2* nr2, int hstride) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "basis_scale", 0.0, k_sig_true, (ncols + 127) / 128, 128, 0, j, cols, ncols, sig, sstride, hA, hB, nr,
+            nr2, hstride);
+}
+void launch_sig_next(Ctx& ctx, int j, const int* cols, int ncols, double* sig, int sstride, const double* invhn) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "basis_scale", 0.0, k_sig_next, (ncols + 127) / 128, 128, 0, j, cols, ncols, sig, sstride, invhn);
+}
+void launch_sig_y(Ctx& ctx, const int* cols, int ncols, const int* kcol, const double* sig, int sstride, double2* y,
+                  int ystride) {
+  if (ncols <= 0) return;
+  HZ_LAUNCH(ctx, "basis_scale", 0.0, k_sig_y, (ncols + 127) / 128, 128, 0, cols, ncols, kcol, sig, sstride, y,
+            ystride);
+}
+
 __global__ void __launch_bounds__(256) k_scale_cols(long long N, const double2* __restrict__ x, long long xld,
                                                     double2* __restrict__ y, long long yld,
                                                     const double* __restrict__ s, const int* __restrict__ cols) {

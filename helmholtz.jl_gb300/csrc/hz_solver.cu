@@ -147,6 +147,7 @@ struct hz_handle {
   DBuf Bd, Xd, V, Z, part, hA, hB, nr, nr2, flag, Hh, cs, sn, gv, yv, est, invhn, bnorm, bnorm_inv, beta, beta_inv,
       cols, kcol;
   DBuf bsc;         // BiCGSTAB per-column scalars
+  DBuf sig, hC;     // FGMRES basis scales (stored v_i stands for sig_i v_i) and update coefficients
   DBuf tmpA, tmpB;  // hz_apply staging
   double* h_est = nullptr;  // pinned
   double* h_nrm = nullptr;  // pinned
@@ -565,6 +566,8 @@ void ensure_workspace(hz_handle* h, int nrhs) {
   h->V.alloc((size_t)std::max(m + 1, 6) * R * N * 16);  // BiCGSTAB uses 6 FP64 blocks
   h->Z.alloc((size_t)std::max(m, 2) * R * N * zb);
   h->bsc.alloc((size_t)R * 8 * 16);
+  h->sig.alloc((size_t)R * (m + 1) * sizeof(double));
+  h->hC.alloc((size_t)R * (m + 2) * 16);
   const int nblk = krylov_nblk(N, 1);
   h->part.alloc((size_t)R * 18 * nblk * 16);
   const int HS = m + 2;
@@ -1141,6 +1144,11 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
   else
     launch_scale_cols(h->ctx, N, B, N, Vj(0), N, h->bnorm_inv.as<double>(), dc, (int)act.size());
   launch_cycle_init(h->ctx, m, dc, (int)act.size(), h->bnorm.as<double>(), h->gv.as<double2>());
+  // the basis is normalised lazily: stored v_i stands for sig_i v_i (V_0 is normalised)
+  double* sig = h->sig.as<double>();
+  double2* hC = h->hC.as<double2>();
+  const int SS = m + 1;
+  launch_sig_init(h->ctx, dc, (int)act.size(), sig, SS);
   std::vector<int> kcol(h->rcap, 0);
   int outer = 0;
   for (outer = 1; outer <= std::max(1, h->opt.max_outer); ++outer) {
@@ -1184,24 +1192,26 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
             launch_dots(h->ctx, N, V, vstride, N, i0, k, w, N, dc, nl, nblk, wn, part, mask);
           launch_reduce(h->ctx, part, dc, nl, k + wn, nblk, hh + i0, HS, 0);
         }
+        // update coefficients for the stored vectors: sig_i^2 d_i
+        launch_sig_coef(h->ctx, dc, nl, K, sig, SS, hh, HS, hC);
         for (int i0 = 0; i0 < K; i0 += 16) {
           const int k = std::min(16, K - i0);
           const int wn = (i0 + 16 >= K) ? 1 : 0;
           if (df)
-            launch_update_df(h->ctx, N, Vd, vstride, N, i0, k, hh, HS, Vdj(j + 1), N, dc, nl, nblk, wn, part, mask);
+            launch_update_df(h->ctx, N, Vd, vstride, N, i0, k, hC, HS, Vdj(j + 1), N, dc, nl, nblk, wn, part, mask);
           else
-            launch_update(h->ctx, N, V, vstride, N, i0, k, hh, HS, w, N, dc, nl, nblk, wn, part, mask);
+            launch_update(h->ctx, N, V, vstride, N, i0, k, hC, HS, w, N, dc, nl, nblk, wn, part, mask);
           if (wn) launch_reduce(h->ctx, part, dc, nl, 1, nblk, nrm, HS, 0);
         }
         if (pass == 0) launch_dgks(h->ctx, dc, nl, hA, HS, K, h->nr.as<double2>(), HS, flag);
       }
+      // Hessenberg entries of the normalised basis: sig_i sig_j d_i, h_{j+1,j} = sig_j ||w''||
+      launch_sig_true(h->ctx, j, dc, nl, sig, SS, hA, hB, h->nr.as<double2>(), h->nr2.as<double2>(), HS);
       launch_arnoldi_step(h->ctx, j, m, dc, nl, hA, hB, h->nr.as<double2>(), h->nr2.as<double2>(), flag, HS,
                           h->Hh.as<double2>(), h->cs.as<double2>(), h->sn.as<double2>(), h->gv.as<double2>(),
                           h->est.as<double>(), h->invhn.as<double>());
-      if (df)
-        launch_scale_df(h->ctx, N, Vdj(j + 1), N, h->invhn.as<double>(), dc, nl);
-      else
-        launch_scale_cols(h->ctx, N, w, N, w, N, h->invhn.as<double>(), dc, nl);
+      // v_{j+1} = w'' stays unnormalised: sig_{j+1} = sig_j / h_{j+1,j}
+      launch_sig_next(h->ctx, j, dc, nl, sig, SS, h->invhn.as<double>());
       ck(cudaMemcpyAsync(h->h_est, h->est.p, (size_t)h->rcap * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "est");
       ck(cudaMemcpyAsync(h->h_flag, h->flag.p, (size_t)h->rcap * sizeof(int), cudaMemcpyDeviceToHost, h->ctx.stream),
          "flags");
@@ -1231,6 +1241,8 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
        "kcol");
     launch_lsq(h->ctx, m, dc, (int)act.size(), h->kcol.as<int>(), h->Hh.as<double2>(), h->gv.as<double2>(),
                h->yv.as<double2>());
+    // Z_i = sig_i Z'_i (the cycles scale with their input): fold sig_i into y_i
+    launch_sig_y(h->ctx, dc, (int)act.size(), h->kcol.as<int>(), sig, SS, h->yv.as<double2>(), m);
     long long zcols = 0;
     for (int c : act) zcols += kcol[c];
     if (df)
@@ -1270,6 +1282,7 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
     else
       launch_scale_cols(h->ctx, N, Vj(0), N, Vj(0), N, h->beta_inv.as<double>(), dc, (int)act.size());
     launch_cycle_init(h->ctx, m, dc, (int)act.size(), h->beta.as<double>(), h->gv.as<double2>());
+    launch_sig_init(h->ctx, dc, (int)act.size(), sig, SS);
   }
   return std::min(outer, std::max(1, h->opt.max_outer));
 }
