@@ -754,34 +754,6 @@ void launch_to_df(Ctx& ctx, long long N, const double2* x, long long xld, float4
             cols);
 }
 
-// w[:, c] *= s[c] in df64 (normalisation of a new basis vector)
-__global__ void __launch_bounds__(256) k_scale_df(long long N, float4* __restrict__ w, long long ld,
-                                                  const double* __restrict__ s, const int* __restrict__ cols) {
-  const int c = cols[blockIdx.y];
-  float sh, sl;
-  split(s[c], sh, sl);
-  float4* wc = w + (long long)c * ld;
-  // elements are independent: unrolled so that several loads are in flight per thread
-#pragma unroll 4
-  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {
-    const float4 v = __ldcs(&wc[p]);
-    DAcc re, im;
-    re.init(0.f, 0.f);
-    im.init(0.f, 0.f);
-    re.mac(v.x, v.z, sh, sl);
-    im.mac(v.y, v.w, sh, sl);
-    re.renorm();
-    im.renorm();
-    __stcs(&wc[p], make_float4(re.hi, im.hi, re.lo, im.lo));
-  }
-}
-
-void launch_scale_df(Ctx& ctx, long long N, float4* w, long long ld, const double* s, const int* cols, int ncols) {
-  if (ncols <= 0) return;
-  const int nb = std::max(1, std::min((int)((N + 255) / 256), 8 * kSMs / std::max(ncols, 1) + 1));
-  HZ_LAUNCH(ctx, "scale_cols", (double)N * ncols * 32.0, k_scale_df, dim3(nb, ncols), 256, 0, N, w, ld, s, cols);
-}
-
 // df64 diag(H) from the FP64 array (once per handle)
 __global__ void k_diag_to_df(long long N, const double2* __restrict__ d, float4* __restrict__ out) {
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x) {

@@ -124,7 +124,6 @@ void launch_update_df(Ctx& ctx, long long N, const float4* V, long long vstride,
 // y = s[c] x (FP64 x into df64 y; may run in place on the same memory)
 void launch_to_df(Ctx& ctx, long long N, const double2* x, long long xld, float4* y, long long yld, const double* s,
                   const int* cols, int ncols);
-void launch_scale_df(Ctx& ctx, long long N, float4* w, long long ld, const double* s, const int* cols, int ncols);
 void launch_diag_to_df(Ctx& ctx, long long N, const double2* d, float4* out);
 // x += sum_{i<kcol[c]} y_i Z_i with the products and their sum in df64, x FP64.
 void launch_update_x_df(Ctx& ctx, long long N, const float2* Z, long long zstride, long long ld, const int* kcol,
