@@ -199,8 +199,85 @@ int slmg_threads(void) {
 
 typedef struct {
   double w;
-  int pre, post, wcycle;
+  int pre, post, wcycle; /* wcycle: 0 V, 1 W, 2 K */
 } cyc_t;
+
+static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, const cyc_t* cp);
+
+/* K-cycle coarse correction on level l (Multigrid.jl cycleType 'K' of
+   test/ShiftedLaplacianTest.jl:137-140, restated): two steps of FGMRES on the
+   level's operator from a zero guess, right-preconditioned by the level's own
+   cycle, per column (3x2 least squares by two complex Givens rotations). */
+static void kcycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, const cyc_t* cp) {
+  const csr_t* A = &S->A[l];
+  const int64_t n = A->nrows;
+  const size_t bytes = sizeof(cplx) * (size_t)n * nrhs;
+  cplx* V0 = (cplx*)malloc(bytes);
+  cplx* V1 = (cplx*)malloc(bytes);
+  cplx* Z0 = (cplx*)malloc(bytes);
+  cplx* Z1 = (cplx*)malloc(bytes);
+  cplx* W = (cplx*)malloc(bytes);
+  double* beta = (double*)calloc((size_t)nrhs, sizeof(double));
+  cplx* hs = (cplx*)calloc((size_t)nrhs * 6, sizeof(cplx)); /* h00 h10 h01 h11 h21 per column */
+  for (int c = 0; c < nrhs; ++c) {
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i) s += creal(b[c * n + i]) * creal(b[c * n + i]) + cimag(b[c * n + i]) * cimag(b[c * n + i]);
+    beta[c] = sqrt(s);
+    const double inv = beta[c] > 0 ? 1.0 / beta[c] : 0.0;
+    for (int64_t i = 0; i < n; ++i) V0[c * n + i] = inv * b[c * n + i];
+  }
+  mg_cycle(S, l, V0, Z0, nrhs, cp);
+  spmm(A, Z0, n, W, n, nrhs, 0, 1.0);
+  for (int c = 0; c < nrhs; ++c) {
+    cplx h00 = 0;
+    for (int64_t i = 0; i < n; ++i) h00 += conj(V0[c * n + i]) * W[c * n + i];
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      W[c * n + i] -= h00 * V0[c * n + i];
+      s += creal(W[c * n + i]) * creal(W[c * n + i]) + cimag(W[c * n + i]) * cimag(W[c * n + i]);
+    }
+    const double h10 = sqrt(s), inv = h10 > 0 ? 1.0 / h10 : 0.0;
+    for (int64_t i = 0; i < n; ++i) V1[c * n + i] = inv * W[c * n + i];
+    hs[c * 6 + 0] = h00;
+    hs[c * 6 + 1] = h10;
+  }
+  mg_cycle(S, l, V1, Z1, nrhs, cp);
+  spmm(A, Z1, n, W, n, nrhs, 0, 1.0);
+  for (int c = 0; c < nrhs; ++c) {
+    cplx h01 = 0, h11 = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      h01 += conj(V0[c * n + i]) * W[c * n + i];
+      h11 += conj(V1[c * n + i]) * W[c * n + i];
+    }
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      const cplx v = W[c * n + i] - h01 * V0[c * n + i] - h11 * V1[c * n + i];
+      s += creal(v) * creal(v) + cimag(v) * cimag(v);
+    }
+    const cplx a = hs[c * 6 + 0], bb = h01, d = h11;
+    const double c10 = creal(hs[c * 6 + 1]), e = sqrt(s);
+    cplx y0 = 0, y1 = 0;
+    const double r1 = sqrt(creal(a) * creal(a) + cimag(a) * cimag(a) + c10 * c10);
+    if (beta[c] > 0 && r1 > 0) {
+      const cplx cs = a / r1;
+      const double sn = c10 / r1;
+      const cplx bp = conj(cs) * bb + sn * d, dp = -sn * bb + cs * d;
+      const cplx g0 = conj(cs) * beta[c];
+      const double g1 = -sn * beta[c];
+      const double r2 = sqrt(creal(dp) * creal(dp) + cimag(dp) * cimag(dp) + e * e);
+      if (r2 > 0) y1 = conj(dp) * g1 / (r2 * r2);
+      y0 = (g0 - bp * y1) / r1;
+    }
+    for (int64_t i = 0; i < n; ++i) x[c * n + i] = y0 * Z0[c * n + i] + y1 * Z1[c * n + i];
+  }
+  free(V0);
+  free(V1);
+  free(Z0);
+  free(Z1);
+  free(W);
+  free(beta);
+  free(hs);
+}
 
 /* x = cycle(b) on level l, zero initial guess, nrhs columns (ld = level size). */
 static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, const cyc_t* cp) {
@@ -223,13 +300,16 @@ static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, c
     for (int64_t i = 0; i < n; ++i)
       for (int c = 0; c < nrhs; ++c) x[c * n + i] += cp->w * di[i] * (b[c * n + i] - r[c * n + i]);
   }
-  int ncalls = (cp->wcycle && l < S->nlev - 2) ? 2 : 1;
+  int ncalls = (cp->wcycle == 1 && l < S->nlev - 2) ? 2 : 1;
   for (int call = 0; call < ncalls; ++call) {
     spmm(A, x, n, r, n, nrhs, 0, 1.0);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n * nrhs; ++i) r[i] = b[i] - r[i];
     spmm(&S->R[l], r, n, bc, nc, nrhs, 0, 1.0);
-    mg_cycle(S, l + 1, bc, xc, nrhs, cp);
+    if (cp->wcycle == 2 && l + 1 < S->nlev - 1)
+      kcycle(S, l + 1, bc, xc, nrhs, cp);
+    else
+      mg_cycle(S, l + 1, bc, xc, nrhs, cp);
     spmm(&S->P[l], xc, nc, x, n, nrhs, 1, 1.0);
   }
   for (int s = 0; s < cp->post; ++s) {

@@ -97,7 +97,7 @@ class CpuSLMG:
         hp, hi, hd, _ = self.H
         t0 = time.perf_counter()
         outer = lib().slmg_solve(self.h, n, hp.ctypes.data, hi.ctypes.data, hd.ctypes.data, B2.ctypes.data,
-                                 X.ctypes.data, nrhs, restart, tol, max_outer, w, pre, post, int(cycle == "W"),
+                                 X.ctypes.data, nrhs, restart, tol, max_outer, w, pre, post, {"V": 0, "W": 1, "K": 2}[cycle],
                                  it.ctypes.data, rr.ctypes.data)
         dt = time.perf_counter() - t0
         return CpuSolveResult(X=X, iters=it, relres=rr, outer=outer, setup_s=self.setup_s, solve_s=dt,

@@ -145,3 +145,17 @@ def test_oracle_kcycle_converges_faster_than_v(O):
         assert np.all(r <= 1e-8 * 1.0001)
         it[cyc] = int(sol.result.iters.max())
     assert it["K"] < it["V"], it
+
+
+@pytest.mark.parametrize("cycle", ["W", "K"])
+def test_c_oracle_cycles_match_numpy_oracle(O, cpu_slmg, cycle):
+    """The two restatements of the solve (NumPy and threaded C) take the same
+    iterations per column with the W- and the K-cycle and agree on the solution."""
+    P = PB.layered((64, 64), seed=3, pad=8)
+    B = PB.rhs(P["m"].size, 3, seed=1)
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    r = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 4).solve(B, tol=1e-8, max_outer=60, cycle=cycle)
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=4, tol=1e-8, max_outer=60,
+                       cycle=cycle)
+    np.testing.assert_array_equal(r.iters, sol.result.iters)
+    assert np.abs(r.X - sol.result.X).max() <= 1e-12 * np.abs(sol.result.X).max()
