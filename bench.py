@@ -484,7 +484,7 @@ def run_learned(args, rank, ws, dist):
     return res, info, wl
 
 
-def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4):
+def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: str = "V"):
     """C oracle (threaded CSR SLMG, plain FP64) on a bounded sample of the
     workload: the full grid and operator, a few of its right-hand sides."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -497,14 +497,15 @@ def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4):
     cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"])
     B = sources(P, wl["nrhs"], seed=0)
     ncols = 1
-    r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200)
+    r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200, cycle=cycle)
     t1 = r.solve_s
     ncols = int(max(1, min(ncols_max, budget_s // max(t1, 1e-3))))
     if ncols > 1:
-        r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200)
+        r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200, cycle=cycle)
     return dict(value=ncols / r.solve_s, unit="RHS/s", cores=r.threads, kind="port",
                 sample=f"{ncols} of the {wl['nrhs']} right-hand sides of the same workload (full grid, "
-                       f"same operator, plain FP64 SLMG in threaded C, {int(r.iters.mean())} iterations per RHS)",
+                       f"same operator, plain FP64 SLMG ({cycle}-cycle) in threaded C, "
+                       f"{int(r.iters.mean())} iterations per RHS)",
                 seconds=r.solve_s, setup_s=r.setup_s, max_relres=float(r.relres.max()))
 
 
@@ -553,7 +554,7 @@ def main():
         vals = []
         cs = None
         for i in range(args.warmup + args.steps):
-            cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps))
+            cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps), cycle=args.cycle)
             if i >= args.warmup:
                 vals.append(cs["value"])
         v = float(np.mean(vals))
@@ -623,7 +624,7 @@ def main():
         import __graft_entry__ as ge
         hz = ge.load_package()
         gam = gamma_of(P, wl["pad"], None, hz)
-        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget)
+        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget, cycle=args.cycle)
     plain = results.get("fp64")
     line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
