@@ -499,7 +499,7 @@ def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: st
     ncols = 1
     r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200, cycle=cycle)
     t1 = r.solve_s
-    ncols = int(max(1, min(ncols_max, budget_s // max(t1, 1e-3))))
+    ncols = int(max(1, min(ncols_max, B.shape[1], budget_s // max(t1, 1e-3))))
     if ncols > 1:
         r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200, cycle=cycle)
     return dict(value=ncols / r.solve_s, unit="RHS/s", cores=r.threads, kind="port",

@@ -21,3 +21,5 @@ def test_reference_arm_json_line():
     assert line["impl"] == "reference" and line["unit"] == "RHS/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    # the sample never counts more columns than the workload has
+    assert line["cpu_baseline"]["sample"].startswith("1 of the 1 ")
