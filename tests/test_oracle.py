@@ -65,6 +65,57 @@ def test_oracle_matches_golden(O):
                                       g[f"abl3_neu{neu}"])
 
 
+def _attenuated_point_source(O, nn, pad, src0, complex_omega):
+    """test/AttenuationTest.jl restated: unit slowness on [0,10]^2 with nn x nn nodes,
+    f = 2.5 (w = 5 pi), attenuation alpha = pi, absorbing layer getABL(n, false,
+    [pad, pad], getMaximalFrequency), no Sommerfeld, q = 1/h^2 at node src0 (0-based).
+    Either the attenuation joins gamma at real w (s1 of the test) or the frequency
+    becomes w - i alpha/2 (s2).  Returns (u, r, k): the direct solution, the distance
+    of every node from the source, and the wavenumber of the free-space problem."""
+    n = np.array([nn, nn])
+    M = O.getRegularMesh([0.0, 10.0, 0.0, 10.0], n - 1)
+    m = np.ones(nn * nn)
+    w, alpha = 2 * np.pi * 2.5, 0.5 * 2 * np.pi
+    gamma = O.getABL(n, False, [pad, pad], O.getMaximalFrequency(m, M)).ravel(order="F")
+    q = np.zeros((nn * nn, 1), dtype=complex)
+    q[O.loc2cs(n, [src0 + 1, src0 + 1]) - 1] = 1.0 / M.h[0] ** 2
+    if complex_omega:
+        H = O.GetHelmholtzOperator(M, m, w - 0.5j * alpha, gamma, False, False)
+        k = w - 0.5j * alpha                         # k^2 = w'^2 exactly (gamma = 0 inside)
+    else:
+        H = O.GetHelmholtzOperator(M, m, w, gamma + alpha, False, False)
+        k = np.sqrt(w * w - 1j * alpha * w)          # k^2 = w^2 (1 - i alpha / w)
+        k = k if k.imag < 0 else -k
+    xn = O.getNodalGrid(M)
+    r = np.hypot(xn[:, 0] - src0 * M.h[0], xn[:, 1] - src0 * M.h[1])
+    return O.direct_solve(H, q)[:, 0], r, k
+
+
+def _green_error(u, r, k, r0=0.3, r1=2.5):
+    """Relative L2 distance to the decaying free-space Green's function of
+    -Laplace - k^2, (-i/4) H0^(2)(k r), over r0 <= r <= r1 (inside the layer)."""
+    from scipy.special import hankel2
+    sel = (r >= r0) & (r <= r1)
+    g = -0.25j * hankel2(0, k * r[sel])
+    return float(np.linalg.norm(u[sel] - g) / np.linalg.norm(g))
+
+
+@pytest.mark.parametrize("complex_omega", [False, True])
+def test_attenuation_matches_greens_function(O, complex_omega):
+    """The reference's attenuation example (512^2 nodes, source at div(n, 2)) only
+    plots its two solutions beside an analytic ray solution; here each is held to
+    the exact damped Green's function of its own continuous problem."""
+    u, r, k = _attenuated_point_source(O, 512, 35, 255, complex_omega)
+    assert _green_error(u, r, k) < 0.05
+
+
+def test_attenuated_green_error_is_second_order(O):
+    """Halving h (257^2 -> 513^2 nodes, same physical layer width, source at the
+    centre node) divides the distance to the Green's function by about 4."""
+    e = [_green_error(*_attenuated_point_source(O, nn, pad, (nn - 1) // 2, True)) for nn, pad in ((257, 18), (513, 35))]
+    assert 3.5 < e[0] / e[1] < 4.6, e
+
+
 def test_laplacian_rows_follow_reference_boundary_rule(O):
     """(2u_0 - 2u_1)/h^2 boundary rows (orderNeumannBC = 2), interior [-1 2 -1]/h^2."""
     D = O.dxxMat(5, 0.5).toarray()
