@@ -116,6 +116,38 @@ def test_attenuated_green_error_is_second_order(O):
     assert 3.5 < e[0] / e[1] < 4.6, e
 
 
+@pytest.mark.parametrize("shifted", [False, True])
+def test_surface_source_matches_half_space_greens_function(O, shifted):
+    """test/HelmholtzTest.jl restated (it only plots): 257x129 nodes on
+    [0,13.5]x[0,4.2], unit slowness, f = 1, gamma = 0.01, Neumann top with the
+    absorbing layer (pad 25, getMaximalFrequency) and Sommerfeld rows elsewhere,
+    the top point source q = 1/||h||^2, solved with H and with SH = H + shift 0.1.
+    The Neumann rows mirror the half-space, so away from the layer the solution is
+    the full-space damped Green's function with strength q hx hy.  This holds the
+    source scaling, the mirror rows of the Neumann top and the sign of the shift
+    (the Sommerfeld rows matter little here: the layer already absorbs)."""
+    from scipy.special import hankel2
+    M = O.getRegularMesh([0.0, 13.5, 0.0, 4.2], [256, 128])
+    m = np.ones(257 * 129)
+    w = 2 * np.pi
+    H, _ = O.GetHelmholtzOperatorABL(M, m, w, 0.01 * np.ones(m.size), True, [25, 25],
+                                     O.getMaximalFrequency(m, M), True)
+    k2 = w * w - 1j * 0.01 * w
+    if shifted:
+        H = (H + O.GetHelmholtzShiftOP(m, w, 0.1)).tocsr()
+        k2 -= 0.1j * w * w
+    k = np.sqrt(k2)
+    k = k if k.imag < 0 else -k
+    q, src = O.getAcousticPointSource(M, np.complex128)
+    assert src == [128, 1] and q.max() == pytest.approx(1.0 / (M.h[0] ** 2 + M.h[1] ** 2))
+    u = O.direct_solve(H, q[:, None])[:, 0]
+    xn = O.getNodalGrid(M)
+    r = np.hypot(xn[:, 0] - (src[0] - 1) * M.h[0], xn[:, 1] - (src[1] - 1) * M.h[1])
+    sel = (r >= 0.5) & (r <= 2.5)
+    g = -0.25j * hankel2(0, k * r[sel]) * q.max() * M.h[0] * M.h[1]
+    assert np.linalg.norm(u[sel] - g) / np.linalg.norm(g) < 0.05
+
+
 def test_laplacian_rows_follow_reference_boundary_rule(O):
     """(2u_0 - 2u_1)/h^2 boundary rows (orderNeumannBC = 2), interior [-1 2 -1]/h^2."""
     D = O.dxxMat(5, 0.5).toarray()
