@@ -148,6 +148,46 @@ def test_surface_source_matches_half_space_greens_function(O, shifted):
     assert np.linalg.norm(u[sel] - g) / np.linalg.norm(g) < 0.05
 
 
+@pytest.fixture(scope="module")
+def shifted_laplacian_example(O):
+    """test/ShiftedLaplacianTest.jl:14-83 restated: v = 1.5 on 257x129 nodes of
+    [0,13.5]x[0,4.2], f = 2.5, gamma = 0.01 w plus the absorbing layer (pad 16,
+    getMaximalFrequency), Neumann top, Sommerfeld; q = 1/h1^2 at (div(n1, 2), 1)."""
+    M = O.getRegularMesh([0.0, 13.5, 0.0, 4.2], [256, 128])
+    m = np.full(257 * 129, 1 / 1.5**2)
+    w = 2 * np.pi * 2.5
+    H, gamma = O.GetHelmholtzOperatorABL(M, m, w, w * 0.01 * np.ones(m.size), True, [16, 16],
+                                         O.getMaximalFrequency(m, M), True)
+    n = M.n + 1
+    q = np.zeros(int(np.prod(n)), dtype=complex)
+    q[O.loc2cs(n, [n[0] // 2, 1]) - 1] = 1.0 / M.h[0] ** 2
+    rng = np.random.default_rng(0)
+    B2 = rng.random((q.size, 2)) + 1j * rng.random((q.size, 2))  # rand(ComplexF64, n, 2)
+    return M, m, np.ravel(gamma, order="F"), w, H, q, B2
+
+
+@pytest.mark.parametrize("krylov,cycle,restart,rhs", [
+    ("GMRES", "W", 20, "point"),     # :63-73  getMGparam(levels 2, Jac 0.75, 2/2, 'W'), GMRES(20)
+    ("BiCGSTAB", "W", 0, "point"),   # :75-78
+    ("BiCGSTAB", "W", 0, "random"),  # :121-135 two random right-hand sides
+    ("GMRES", "K", 5, "random"),     # :137-142 K-cycle, GMRES(5) (damped Jacobi relaxation)
+])
+def test_shifted_laplacian_example(O, shifted_laplacian_example, krylov, cycle, restart, rhs):
+    """Each solve of the reference's shifted-Laplacian example (shift 0.2/10 on every
+    level, maxIter 30, tolerance 1e-6) reaches the residual the example prints and
+    the direct solution."""
+    M, m, gamma, w, H, q, B2 = shifted_laplacian_example
+    B = q if rhs == "point" else B2
+    sol = O.slmg_solve(M, m, gamma, w, True, True, B, levels=2, shift=0.02, relax_w=0.75, pre=2, post=2,
+                       restart=max(restart, 1), tol=1e-6, max_outer=30, cycle=cycle, krylov=krylov)
+    assert np.all(sol.result.converged)
+    X = sol.X.reshape(q.size, -1)
+    Bm = B.reshape(q.size, -1)
+    assert np.all(np.linalg.norm(H @ X - Bm, axis=0) <= 1e-6 * np.linalg.norm(Bm, axis=0))
+    Xd = O.direct_solve(H, Bm)
+    assert np.linalg.norm(X - Xd) / np.linalg.norm(Xd) < 1e-4
+
+
 def test_laplacian_rows_follow_reference_boundary_rule(O):
     """(2u_0 - 2u_1)/h^2 boundary rows (orderNeumannBC = 2), interior [-1 2 -1]/h^2."""
     D = O.dxxMat(5, 0.5).toarray()
