@@ -59,6 +59,16 @@ WORKLOADS = {
 }
 
 
+def workload(args) -> dict:
+    """The chosen workload with the command line's overrides (RHS count, level count)."""
+    wl = dict(WORKLOADS[args.workload])
+    if args.nrhs > 0:
+        wl["nrhs"] = args.nrhs
+    if args.levels > 0:
+        wl["levels"] = args.levels
+    return wl
+
+
 def make_problem(wl: dict, seed: int):
     """Seeded layered (+ ellipsoid) velocity model, 10 points per wavelength,
     attenuation 0.01 w plus a quadratic absorbing layer of amplitude 0.95 w."""
@@ -243,9 +253,7 @@ def run_ours(args, rank, ws, dist):
     hz = ge.load_package()
     L = hz._lib
     lib = L.load()
-    wl = dict(WORKLOADS[args.workload])
-    if args.nrhs > 0:
-        wl["nrhs"] = args.nrhs
+    wl = workload(args)
     P = make_problem(wl, seed=1234)
     gam = gamma_of(P, wl["pad"], lib, hz)
     nrhs = wl["nrhs"]
@@ -267,6 +275,7 @@ def run_ours(args, rank, ws, dist):
         lib.hz_default_options(C.byref(o))
         o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, args.max_outer
         o.cycle = ord(args.cycle)
+        o.coarse_op = L.HZ_COARSE_REDISCRETIZE if args.coarse == "rediscretize" else L.HZ_COARSE_GALERKIN
         o.cuda_graph = 0 if args.no_graph else 1
         o.autotune = 0 if args.no_tune else 1
         if args.krylov == "bicgstab":
@@ -390,9 +399,7 @@ def run_learned(args, rank, ws, dist):
     hz = ge.load_package()
     L = hz._lib
     lib = L.load()
-    wl = dict(WORKLOADS[args.workload])
-    if args.nrhs > 0:
-        wl["nrhs"] = args.nrhs
+    wl = workload(args)
     level = args.net_level if args.net_level > 0 else wl["net_level"]
 
     def solver(P, precision, outer="fp64", max_outer=60):
@@ -400,7 +407,8 @@ def run_learned(args, rank, ws, dist):
         gam = gamma_of(P, wl["pad"], lib, hz)
         param = hz.HelmholtzParam(M, gam, P["m"], P["w"], True, True)
         MG = hz.getMGparam(complex, int, wl["levels"], 1, max_outer, wl["tol"], "Jac", 0.8, 1, 1, args.cycle,
-                           "Julia", 0.5, 0.0, precision=precision, outerArithmetic=outer)
+                           "Julia", 0.5, 0.0, precision=precision, outerArithmetic=outer,
+                           coarseOperator="Rediscretize" if args.coarse == "rediscretize" else "Galerkin")
         return hz.getShiftedLaplacianMultigridSolver(param, MG, 0.5, "GMRES", 10)
 
     # 1. training pairs from the FP64 solver on seeded training models
@@ -484,9 +492,11 @@ def run_learned(args, rank, ws, dist):
     return res, info, wl
 
 
-def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: str = "V"):
+def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: str = "V",
+                   coarse: str = "galerkin"):
     """C oracle (threaded CSR SLMG, plain FP64) on a bounded sample of the
-    workload: the full grid and operator, a few of its right-hand sides."""
+    workload: the full grid and operator, a few of its right-hand sides, with
+    the GPU arm's cycle and coarse operators (Galerkin or re-discretised)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import helmholtz_oracle as O
     import slmg_cpu
@@ -494,7 +504,10 @@ def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: st
     gam = gam_fn()
     H = O.GetHelmholtzOperator(M, P["m"], P["w"], gam, True, True)
     SH = (H + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
-    cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"])
+    hier = None
+    if coarse == "rediscretize":
+        hier = O.build_hierarchy_rediscretized(M, P["m"], gam, P["w"], 0.5, True, True, wl["levels"])
+    cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"], hier=hier)
     B = sources(P, wl["nrhs"], seed=0)
     ncols = 1
     r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200, cycle=cycle)
@@ -504,7 +517,7 @@ def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: st
         r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200, cycle=cycle)
     return dict(value=ncols / r.solve_s, unit="RHS/s", cores=r.threads, kind="port",
                 sample=f"{ncols} of the {wl['nrhs']} right-hand sides of the same workload (full grid, "
-                       f"same operator, plain FP64 SLMG ({cycle}-cycle) in threaded C, "
+                       f"same operator, plain FP64 SLMG ({cycle}-cycle, {coarse} coarse levels) in threaded C, "
                        f"{int(r.iters.mean())} iterations per RHS)",
                 seconds=r.solve_s, setup_s=r.setup_s, max_relres=float(r.relres.max()))
 
@@ -530,6 +543,9 @@ def main():
                     help="FGMRES restart cycles (fewer: kernel-rate profiling runs, not a valid RHS/s)")
     ap.add_argument("--cycle", default="V", choices=["V", "W", "K"],
                     help="multigrid cycle (K: two FGMRES steps per coarse level)")
+    ap.add_argument("--coarse", default="galerkin", choices=["galerkin", "rediscretize"],
+                    help="coarse-level operators: Galerkin R A P, or the operator re-discretised on each coarse mesh")
+    ap.add_argument("--levels", type=int, default=0, help="multigrid levels (0: the workload's)")
     ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
     ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
     ap.add_argument("--pairs-per-model", type=int, default=200)
@@ -546,7 +562,7 @@ def main():
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:
             return
-        wl = WORKLOADS[args.workload]
+        wl = workload(args)
         P = make_problem(wl, seed=1234)
         import __graft_entry__ as ge
         hz = ge.load_package()
@@ -554,13 +570,15 @@ def main():
         vals = []
         cs = None
         for i in range(args.warmup + args.steps):
-            cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps), cycle=args.cycle)
+            cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps), cycle=args.cycle,
+                                coarse=args.coarse)
             if i >= args.warmup:
                 vals.append(cs["value"])
         v = float(np.mean(vals))
         line = dict(metric=METRIC, value=v, unit="RHS/s", impl="reference", n_gpus=args.gpus, steps=args.steps,
                     warmup=args.warmup, higher_is_better=True, dtype="c128",
-                    config=dict(workload=wl["name"], nrhs=wl["nrhs"]),
+                    config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], cycle=args.cycle,
+                                coarse=args.coarse),
                     cpu_baseline=dict(value=v, unit="RHS/s", cores=cs["cores"], kind="port", sample=cs["sample"]),
                     e2e=dict(value=v, unit="RHS/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
                     note="reference path = the C oracle port of the Julia SLMG (Julia and Multigrid.jl are absent)")
@@ -580,7 +598,8 @@ def main():
                     vs_baseline=None, dtype="c64 V-cycle + bf16 network / c128 outer",
                     data="synthetic (seeded layered+inclusion models, random source positions)",
                     config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
-                                krylov="FGMRES(10)", cycle=args.cycle, outer_arithmetic=args.outer, learned=True,
+                                krylov="FGMRES(10)", cycle=args.cycle, coarse=args.coarse,
+                                outer_arithmetic=args.outer, learned=True,
                                 net_level=args.net_level if args.net_level > 0 else wl["net_level"],
                                 stag_ratio=args.stag_ratio,
                                 step="solver setup + solve of one held-out model's right-hand sides",
@@ -624,7 +643,7 @@ def main():
         import __graft_entry__ as ge
         hz = ge.load_package()
         gam = gamma_of(P, wl["pad"], None, hz)
-        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget, cycle=args.cycle)
+        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget, cycle=args.cycle, coarse=args.coarse)
     plain = results.get("fp64")
     line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
@@ -634,6 +653,7 @@ def main():
                 data="synthetic (seeded layered model)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
                             krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB", cycle=args.cycle,
+                            coarse=args.coarse,
                             cuda_graph=not args.no_graph, autotune=not args.no_tune,
                             outer_arithmetic=args.outer,
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,

@@ -58,9 +58,12 @@ class CpuSolveResult:
 class CpuSLMG:
     """Plain FP64 SLMG on the CPU: hierarchy from SciPy, solve in threaded C."""
 
-    def __init__(self, H, SH, M, levels: int):
+    def __init__(self, H, SH, M, levels: int, hier=None):
+        """hier: a prebuilt hierarchy (e.g. O.build_hierarchy_rediscretized);
+        by default the Galerkin hierarchy of SH."""
         t0 = time.perf_counter()
-        self.hier = O.build_hierarchy(SH, M, levels)
+        self.hier = O.build_hierarchy(SH, M, levels) if hier is None else hier
+        levels = len(self.hier.levels)
         self.H = _csr(H)
         mats = []
         for l, L in enumerate(self.hier.levels):

@@ -282,3 +282,41 @@ def test_c_oracle_cycles_match_numpy_oracle(O, cpu_slmg, cycle):
                        cycle=cycle)
     np.testing.assert_array_equal(r.iters, sol.result.iters)
     assert np.abs(r.X - sol.result.X).max() <= 1e-12 * np.abs(sol.result.X).max()
+
+
+@pytest.mark.parametrize("cycle", ["V", "K"])
+def test_c_oracle_rediscretized_matches_numpy_oracle(O, cpu_slmg, cycle):
+    """The C solve on a prebuilt re-discretised hierarchy takes the NumPy
+    oracle's iterations (coarse_op = re-discretise, the CPU baseline of that option)."""
+    P = PB.layered((64, 64), seed=4, pad=8)
+    B = PB.rhs(P["m"].size, 2, seed=2)
+    hier = O.build_hierarchy_rediscretized(P["M"], P["m"], P["gamma"], P["w"], 0.5, True, True, 4)
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    r = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 4, hier=hier).solve(B, tol=1e-8, max_outer=60, cycle=cycle)
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=4, tol=1e-8, max_outer=60,
+                       cycle=cycle, coarse="rediscretize")
+    np.testing.assert_array_equal(r.iters, sol.result.iters)
+    assert np.abs(r.X - sol.result.X).max() <= 1e-12 * np.abs(sol.result.X).max()
+
+
+def test_kcycle_depth_galerkin_vs_rediscretized_3d(O, cpu_slmg):
+    """3D layered+ellipsoid at 10 points per wavelength: with four levels the
+    Galerkin K-cycle converges, but a fifth level (0.625 points per wavelength)
+    stalls it; the re-discretised K-cycle is unaffected by the extra level.
+    This is why the 257^3 solve needs re-discretised coarse levels (or four
+    Galerkin levels) with its five-level hierarchy."""
+    P = PB.layered((64, 64, 64), seed=7, pad=8, ellipsoid=True)
+    B = np.zeros((P["m"].size, 1), dtype=complex)
+    B[32 + 65 * (32 + 65 * 1), 0] = 1.0
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    it = {}
+    for coarse in ("galerkin", "rediscretize"):
+        for levels in (4, 5):
+            hier = None
+            if coarse == "rediscretize":
+                hier = O.build_hierarchy_rediscretized(P["M"], P["m"], P["gamma"], P["w"], 0.5, True, True, levels)
+            r = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], levels, hier=hier).solve(B, tol=1e-6, max_outer=15, cycle="K")
+            it[coarse, levels] = (int(r.iters[0]), float(r.relres[0]))
+    assert it["galerkin", 4][0] < 60 and it["galerkin", 4][1] <= 1e-6, it
+    assert it["galerkin", 5][1] > 1e-6, it          # not converged in 15 restarts of 10
+    assert it["rediscretize", 5][0] <= 1.2 * it["rediscretize", 4][0] and it["rediscretize", 5][1] <= 1e-6, it
