@@ -1,6 +1,7 @@
 """Static checks of the Julia ccall shim (Julia is not installed here, so the
 shim cannot run): its C struct mirrors have the header's fields in the header's
-order with matching types, and every symbol it ccalls is declared by the header."""
+order with matching types, every symbol it ccalls is declared by the header, and
+every ccall's return type and argument types agree with the C prototype."""
 import re
 from pathlib import Path
 
@@ -54,3 +55,99 @@ def test_option_constants_match_header():
     for name, val in re.findall(r"const (HZ_\w+) = Int32\((-?\d+)\)", SHIM):
         m = re.search(r"#define %s \(?(-?\d+)\)?" % name, HEADER)
         assert m and int(m.group(1)) == int(val), name
+
+
+# C parameter / return types and the Julia ccall types that pass them correctly
+# (complex arrays travel as interleaved double pairs: Ptr{ComplexF64} for double*).
+C2CCALL = {
+    "void": {"Cvoid"},
+    "int": {"Cint", "Int32"},
+    "int32_t": {"Int32", "Cint"},
+    "int64_t": {"Int64"},
+    "double": {"Float64", "Cdouble"},
+    "const char*": {"Cstring", "Ptr{UInt8}"},
+    "char*": {"Ptr{UInt8}"},
+    "double*": {"Ptr{Float64}", "Ptr{ComplexF64}", "Ref{Float64}"},
+    "const double*": {"Ptr{Float64}", "Ptr{ComplexF64}"},
+    "float*": {"Ptr{Float32}"},
+    "const float*": {"Ptr{Float32}"},
+    "int32_t*": {"Ptr{Int32}", "Ref{Int32}"},
+    "int64_t*": {"Ptr{Int64}", "Ref{Int64}"},
+    "const int64_t*": {"Ptr{Int64}"},
+    "void*": {"Ptr{Cvoid}"},
+    "hz_handle*": {"Ptr{Cvoid}"},
+    "const hz_handle*": {"Ptr{Cvoid}"},
+    "hz_net*": {"Ptr{Cvoid}"},
+    "hz_handle**": {"Ref{Ptr{Cvoid}}"},
+    "hz_net**": {"Ref{Ptr{Cvoid}}"},
+    "const hz_problem*": {"Ref{HzProblem}"},
+    "hz_options*": {"Ref{HzOptions}"},
+    "const hz_options*": {"Ref{HzOptions}"},
+    "hz_stats*": {"Ref{HzStats}"},
+}
+
+
+def _c_prototypes():
+    text = re.sub(r"/\*.*?\*/", "", HEADER, flags=re.S)
+    text = "\n".join(ln for ln in text.splitlines() if not ln.lstrip().startswith("#"))
+    protos = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(hz_\w+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+        ret = " ".join(m.group(1).replace("*", " * ").split()).replace(" *", "*")
+        params = " ".join(m.group(3).split())
+        types = []
+        for p in ([] if params in ("", "void") else params.split(",")):
+            p = " ".join(p.replace("*", " * ").split()).replace(" *", "*")
+            types.append(p if p.endswith("*") else p.rsplit(" ", 1)[0])
+        protos[m.group(2)] = (ret, types)
+    return protos
+
+
+def _split_top(s):
+    parts, depth, cur = [], 0, ""
+    for ch in s:
+        depth += ch in "({["
+        depth -= ch in ")}]"
+        if ch == "," and depth == 0:
+            parts.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    return parts + ([cur.strip()] if cur.strip() else [])
+
+
+def _ccalls():
+    calls = []
+    for m in re.finditer(r"ccall\(\(:(\w+),\s*libhelmgpu\),", SHIM):
+        i, depth = m.end(), 0
+        for k in range(i, len(SHIM)):
+            depth += SHIM[k] in "({["
+            depth -= SHIM[k] in ")}]"
+            if SHIM[k] == "," and depth == 0:
+                break
+        ret = SHIM[i:k].strip()
+        j = k + 1
+        while SHIM[j].isspace():
+            j += 1
+        assert SHIM[j] == "(", m.group(1)
+        depth = 0
+        for e in range(j, len(SHIM)):
+            depth += SHIM[e] in "({["
+            depth -= SHIM[e] in ")}]"
+            if depth == 0:
+                break
+        calls.append((m.group(1), ret, _split_top(SHIM[j + 1:e])))
+    return calls
+
+
+def test_ccall_signatures_match_prototypes():
+    """Every ccall passes as many arguments as the C prototype takes, each with a
+    Julia type that has the C type's size and meaning, and reads the right return type."""
+    protos = _c_prototypes()
+    calls = _ccalls()
+    assert len(calls) >= 20
+    for name, ret, args in calls:
+        cret, cargs = protos[name]
+        assert ret in C2CCALL[cret], (name, ret, cret)
+        assert len(args) == len(cargs), (name, args, cargs)
+        for a, c in zip(args, cargs):
+            assert a in C2CCALL[c], (name, a, c)
