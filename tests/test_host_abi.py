@@ -133,3 +133,38 @@ def test_api_validation(hz):
     assert X.shape == (81,) and not np.any(X)
     S3 = hz.copySolver(S2)
     assert S3.MG is not S2.MG and S3.inner == 10
+
+
+def _ctypes_kind(t):
+    if t is None:
+        return "void"
+    if t is C.c_char_p:
+        return "charp"
+    if t is C.c_void_p or (isinstance(t, type) and issubclass(t, C._Pointer)):
+        return "ptr"
+    if t is C.c_double:
+        return "double"
+    return ("int", C.sizeof(t))
+
+
+def _c_kind(t):
+    if t in ("char*", "const char*"):
+        return "charp"
+    if t.endswith("*"):
+        return "ptr"
+    if t == "double":
+        return "double"
+    if t == "void":
+        return "void"
+    return ("int", {"int": 4, "int32_t": 4, "int64_t": 8}[t])
+
+
+def test_ctypes_signatures_match_prototypes(hz):
+    """Every ctypes binding has the C prototype's arity, integer widths, floating
+    and pointer kinds, and return type (no silent truncation of an int64 size)."""
+    import cheader
+    protos = cheader.prototypes()
+    for name, (res, args) in hz._lib.SIGNATURES.items():
+        cres, cargs = protos[name]
+        assert _ctypes_kind(res) == _c_kind(cres), (name, res, cres)
+        assert [_ctypes_kind(a) for a in args] == [_c_kind(c) for c in cargs], (name, args, cargs)

@@ -5,6 +5,8 @@ every ccall's return type and argument types agree with the C prototype."""
 import re
 from pathlib import Path
 
+import cheader
+
 ROOT = Path(__file__).resolve().parent.parent
 HEADER = (ROOT / "include" / "helmgpu.h").read_text()
 SHIM = (ROOT / "helmholtz.jl_gb300" / "julia" / "HelmholtzGB300.jl").read_text()
@@ -87,21 +89,6 @@ C2CCALL = {
 }
 
 
-def _c_prototypes():
-    text = re.sub(r"/\*.*?\*/", "", HEADER, flags=re.S)
-    text = "\n".join(ln for ln in text.splitlines() if not ln.lstrip().startswith("#"))
-    protos = {}
-    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(hz_\w+)\s*\(([^;{]*?)\)\s*;", text, re.S):
-        ret = " ".join(m.group(1).replace("*", " * ").split()).replace(" *", "*")
-        params = " ".join(m.group(3).split())
-        types = []
-        for p in ([] if params in ("", "void") else params.split(",")):
-            p = " ".join(p.replace("*", " * ").split()).replace(" *", "*")
-            types.append(p if p.endswith("*") else p.rsplit(" ", 1)[0])
-        protos[m.group(2)] = (ret, types)
-    return protos
-
-
 def _split_top(s):
     parts, depth, cur = [], 0, ""
     for ch in s:
@@ -142,7 +129,7 @@ def _ccalls():
 def test_ccall_signatures_match_prototypes():
     """Every ccall passes as many arguments as the C prototype takes, each with a
     Julia type that has the C type's size and meaning, and reads the right return type."""
-    protos = _c_prototypes()
+    protos = cheader.prototypes()
     calls = _ccalls()
     assert len(calls) >= 20
     for name, ret, args in calls:
