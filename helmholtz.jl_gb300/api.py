@@ -541,11 +541,12 @@ def solveLinearSystem(ShiftedHT, B, param: ShiftedLaplacianMultigridSolver, doTr
         raise ValueError("ShiftedHT has the wrong size")
     if param.doClear == 1:
         clear_(param)
-    if on_device:
-        if float(torch.linalg.vector_norm(Bt)) == 0.0:
-            return torch.zeros_like(B), param
-    elif np.linalg.norm(B2) == 0.0:
-        return np.zeros_like(Bc), param
+    zero = float(torch.linalg.vector_norm(Bt)) == 0.0 if on_device else np.linalg.norm(B2) == 0.0
+    if zero:
+        # zero solution, zero residual: the per-column results describe this call, not an earlier one
+        param.last_relres = np.zeros(nrhs)
+        param.last_iters = np.zeros(nrhs, dtype=np.int32)
+        return (torch.zeros_like(B) if on_device else np.zeros_like(Bc)), param
     h = _ensure_handle(param)
     st = L.hz_stats()
     if on_device:
