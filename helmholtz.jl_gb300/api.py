@@ -24,6 +24,7 @@ compiled library or a GPU every compute call raises.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -182,9 +183,20 @@ class _Device:
             self.handle = None
 
 
+def current_device() -> int:
+    """The CUDA device new handles are built on: the one this process selected
+    with torch.cuda.set_device (one process per GPU under torchrun), or device 0
+    when torch is not loaded or sees no GPU."""
+    torch = sys.modules.get("torch")
+    if torch is not None and torch.cuda.is_available():
+        return int(torch.cuda.current_device())
+    return 0
+
+
 def _default_options() -> L.hz_options:
     o = L.hz_options()
     L.load().hz_default_options(C.byref(o))
+    o.device = current_device()
     return o
 
 
@@ -426,6 +438,7 @@ class ShiftedLaplacianMultigridSolver:
     solveTime: float = 0.0
     _handle: object = field(default=None, repr=False)
     _key: tuple = field(default=(), repr=False)
+    _device: int = field(default=0, repr=False)  # CUDA device of _handle
     last_stats: object = field(default=None, repr=False)
     last_relres: np.ndarray | None = field(default=None, repr=False)
     last_iters: np.ndarray | None = field(default=None, repr=False)
@@ -495,7 +508,8 @@ def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
         raise NotImplementedError(f"Krylov {s.Krylov!r}: FGMRES ('GMRES') and 'BiCGSTAB' are built")
     if not np.all(s.shift == s.shift[0]):
         raise NotImplementedError("level-dependent shifts are not built")
-    key = (id(s.helmParam), id(s.helmParam.m), id(s.helmParam.gamma), s.MG.levels, s.MG.maxOuterIter,
+    dev = current_device()
+    key = (dev, id(s.helmParam), id(s.helmParam.m), id(s.helmParam.gamma), s.MG.levels, s.MG.maxOuterIter,
            s.MG.relativeTol, s.MG.relaxParam, int(s.MG.relaxPre), int(s.MG.relaxPost), s.MG.cycleType,
            s.MG.precision, s.inner, float(s.shift[0]), s.Krylov, s.MG.coarseOperator, s.MG.outerArithmetic,
            bool(s.MG.cudaGraph), bool(s.MG.autotune))
@@ -508,6 +522,7 @@ def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
     L.check(L.load().hz_create(C.byref(p), C.byref(o), C.byref(h)))
     s._handle = h
     s._key = key
+    s._device = int(o.device)
     if s.learned is not None:
         from .learned import _apply
         _apply(s)

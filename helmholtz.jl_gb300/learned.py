@@ -23,7 +23,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib as L
-from .api import ShiftedLaplacianMultigridSolver, _ensure_handle, _is_device_array, _nodes
+from .api import ShiftedLaplacianMultigridSolver, _ensure_handle, _is_device_array, _nodes, current_device
 
 
 def num_params() -> int:
@@ -54,10 +54,12 @@ def _ptr(a):
 class CoarseNet:
     """The network on one CUDA device (seeded He-normal initial weights)."""
 
-    def __init__(self, seed: int = 0, device: int = 0):
+    def __init__(self, seed: int = 0, device: int | None = None):
+        """device: CUDA device index (None: the process's current device, as for solver handles)."""
+        device = current_device() if device is None else int(device)
         self._h = C.c_void_p()
-        L.check(L.load().hz_net_create(int(seed), int(device), C.byref(self._h)))
-        self.device = int(device)
+        L.check(L.load().hz_net_create(int(seed), device, C.byref(self._h)))
+        self.device = device
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -188,7 +190,7 @@ def collect_pairs(solver: ShiftedLaplacianMultigridSolver, B, level: int = 2, sw
     if max_pairs is None:
         max_pairs = nrhs * solver.MG.maxOuterIter * max(1, solver.inner)
     h = _ensure_handle(solver)
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", solver._device)
     x = torch.empty((max_pairs, ny, nx, 4), dtype=torch.float32, device=dev)
     t = torch.empty((max_pairs, ny, nx, 2), dtype=torch.float32, device=dev)
     pe = np.zeros(max_pairs)

@@ -168,3 +168,19 @@ def test_ctypes_signatures_match_prototypes(hz):
         cres, cargs = protos[name]
         assert _ctypes_kind(res) == _c_kind(cres), (name, res, cres)
         assert [_ctypes_kind(a) for a in args] == [_c_kind(c) for c in cargs], (name, args, cargs)
+
+
+def test_handles_follow_the_selected_device(hz, monkeypatch):
+    """New handles (solver, operator products, networks) are built on the device the
+    process selected with torch.cuda.set_device, device 0 without torch or a GPU."""
+    import sys
+    import types
+    from helmholtz_jl_gb300 import api
+    fake = types.SimpleNamespace(cuda=types.SimpleNamespace(is_available=lambda: True, current_device=lambda: 3))
+    monkeypatch.setitem(sys.modules, "torch", fake)
+    assert api.current_device() == 3
+    assert api._default_options().device == 3
+    fake.cuda.is_available = lambda: False
+    assert api.current_device() == 0
+    monkeypatch.delitem(sys.modules, "torch")
+    assert api.current_device() == 0 and api._default_options().device == 0
