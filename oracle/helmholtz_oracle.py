@@ -370,7 +370,54 @@ def jacobi(L: Level, x: np.ndarray, b: np.ndarray, w: float, sweeps: int) -> np.
     return x
 
 
-def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int) -> np.ndarray:
+def gmres_relax(L: Level, x: np.ndarray, b: np.ndarray, w: float, steps: int) -> np.ndarray:
+    """relaxType "Jac-GMRES" (set by test/ShiftedLaplacianTest.jl:138 for its
+    K-cycle; Multigrid.jl v0.8.0, not vendored, restated from the published
+    method): `steps` Arnoldi steps of GMRES on the level's operator, started
+    from the current iterate and right-preconditioned by one damped-Jacobi sweep
+    (M^-1 = w D^-1), classical Gram-Schmidt, then the least-squares update
+    x += Z y per column.  A column with zero residual is left unchanged."""
+    if steps <= 0:
+        return x
+    b = b.reshape(b.shape[0], -1)
+    x = np.array(x, dtype=np.complex128).reshape(b.shape)
+    r = b - L.A @ x
+    beta = np.linalg.norm(r, axis=0)
+    V = [r / np.where(beta > 0, beta, 1.0)]
+    Z = []
+    Hm = np.zeros((steps + 1, steps, b.shape[1]), dtype=np.complex128)
+    for j in range(steps):
+        Z.append(w * (L.dinv[:, None] * V[j]))
+        u = L.A @ Z[j]
+        h = [np.sum(np.conj(V[i]) * u, axis=0) for i in range(j + 1)]
+        for i in range(j + 1):
+            Hm[i, j] = h[i]
+            u = u - h[i] * V[i]
+        hn = np.linalg.norm(u, axis=0)
+        Hm[j + 1, j] = hn
+        V.append(u / np.where(hn > 0, hn, 1.0) * (hn > 0))
+    for c in range(b.shape[1]):
+        if beta[c] == 0:
+            continue
+        e = np.zeros(steps + 1, dtype=np.complex128)
+        e[0] = beta[c]
+        y = np.linalg.lstsq(Hm[:, :, c], e, rcond=None)[0]
+        for j in range(steps):
+            x[:, c] += y[j] * Z[j][:, c]
+    return x
+
+
+def relax(L: Level, x: np.ndarray, b: np.ndarray, w: float, sweeps: int, relax_type: str = "Jac") -> np.ndarray:
+    """The smoother of relaxType: damped Jacobi ("Jac") or "Jac-GMRES"."""
+    if relax_type == "Jac-GMRES":
+        return gmres_relax(L, x, b, w, sweeps)
+    if relax_type != "Jac":
+        raise ValueError(f"relaxType {relax_type!r}")
+    return jacobi(L, x, b, w, sweeps)
+
+
+def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int,
+           relax_type: str = "Jac") -> np.ndarray:
     """K-cycle coarse correction on level ``lev`` (Multigrid.jl cycleType 'K',
     used by test/ShiftedLaplacianTest.jl:137-140, restated): two steps of FGMRES
     on that level's operator from a zero guess, right-preconditioned by the
@@ -380,13 +427,13 @@ def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: i
     out = np.zeros_like(b)
     beta = np.linalg.norm(b, axis=0)
     V0 = b / np.where(beta > 0, beta, 1.0)
-    Z0 = mg_cycle(hier, lev, V0, w, pre, post, "K")
+    Z0 = mg_cycle(hier, lev, V0, w, pre, post, "K", relax_type)
     W = A @ Z0
     h00 = np.sum(np.conj(V0) * W, axis=0)
     W = W - h00 * V0
     h10 = np.linalg.norm(W, axis=0)
     V1 = W / np.where(h10 > 0, h10, 1.0) * (h10 > 0)
-    Z1 = mg_cycle(hier, lev, V1, w, pre, post, "K")
+    Z1 = mg_cycle(hier, lev, V1, w, pre, post, "K", relax_type)
     W = A @ Z1
     h01 = np.sum(np.conj(V0) * W, axis=0)
     h11 = np.sum(np.conj(V1) * W, axis=0)
@@ -401,23 +448,24 @@ def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: i
     return out
 
 
-def mg_cycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int, cycle: str = "V") -> np.ndarray:
+def mg_cycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int, cycle: str = "V",
+             relax_type: str = "Jac") -> np.ndarray:
     """One V, W or K cycle with zero initial guess on level ``lev``."""
     L = hier.levels[lev]
     if lev == len(hier.levels) - 1:
         return hier.lu.solve(b)
     x = np.zeros_like(b)
-    x = jacobi(L, x, b, w, pre)
+    x = relax(L, x, b, w, pre, relax_type)
     ncalls = 2 if cycle == "W" and lev < len(hier.levels) - 2 else 1
     for _ in range(ncalls):
         r = b - L.A @ x
         bc = L.R @ r
         if cycle == "K" and lev + 1 < len(hier.levels) - 1:
-            xc = kcycle(hier, lev + 1, bc, w, pre, post).reshape(bc.shape)
+            xc = kcycle(hier, lev + 1, bc, w, pre, post, relax_type).reshape(bc.shape)
         else:
-            xc = mg_cycle(hier, lev + 1, bc, w, pre, post, cycle)
+            xc = mg_cycle(hier, lev + 1, bc, w, pre, post, cycle, relax_type)
         x = x + L.P @ xc
-    x = jacobi(L, x, b, w, post)
+    x = relax(L, x, b, w, post, relax_type)
     return x
 
 
@@ -585,7 +633,8 @@ class SLMGSolution:
 def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Sommerfeld: bool, B: np.ndarray,
                levels: int, shift: float = 0.5, relax_w: float = 0.8, pre: int = 1, post: int = 1,
                restart: int = 10, tol: float = 1e-8, max_outer: int = 100, cycle: str = "V",
-               transpose: bool = False, krylov: str = "GMRES", coarse: str = "galerkin") -> SLMGSolution:
+               transpose: bool = False, krylov: str = "GMRES", coarse: str = "galerkin",
+               relax_type: str = "Jac") -> SLMGSolution:
     """Plain FP64 SLMG: FGMRES(restart) on H (or H^H when ``transpose``),
     right-preconditioned by one multigrid cycle on SH = H + i*s*w^2*diag(m)
     (or SH^H), src/ShiftedLaplacianMultigridSolver.jl:33-102."""
@@ -603,10 +652,11 @@ def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Somme
     if vec:
         B2 = B2[:, None]
     if krylov == "BiCGSTAB":
-        res = bicgstab(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle), B2, tol, max_outer)
+        res = bicgstab(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle, relax_type), B2,
+                       tol, max_outer)
     else:
-        res = fgmres(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle), B2, restart, tol,
-                     max_outer)
+        res = fgmres(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle, relax_type), B2,
+                     restart, tol, max_outer)
     X = res.X[:, 0] if vec else res.X
     return SLMGSolution(X=X, result=res, hier=hier)
 

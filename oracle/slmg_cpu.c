@@ -9,7 +9,7 @@
  * It restates the solve phase of the reference path:
  *   - SpMatMul / ParSpMatVec threaded CSR products (src/GetHelmholtz.jl:90-91;
  *     ParSpMatVec v0.1.1, C/OpenMP, pinned in Manifest.toml:106-110),
- *   - the Multigrid.jl V/W cycle with damped Jacobi, full-weighting
+ *   - the Multigrid.jl V/W/K cycle with damped Jacobi or Jac-GMRES, full-weighting
  *     restriction and linear prolongation given as CSR matrices, and a
  *     direct (banded LU, partial pivoting) coarsest solve,
  *   - FGMRES(restart) per column with classical Gram-Schmidt and the DGKS
@@ -200,9 +200,107 @@ int slmg_threads(void) {
 typedef struct {
   double w;
   int pre, post, wcycle; /* wcycle: 0 V, 1 W, 2 K */
+  int relax;             /* 0 damped Jacobi ("Jac"), 1 "Jac-GMRES" */
 } cyc_t;
 
 static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, const cyc_t* cp);
+
+/* relaxType "Jac-GMRES" (set by test/ShiftedLaplacianTest.jl:138; Multigrid.jl
+   v0.8.0 is not vendored, so the published method is restated, as in
+   oracle/helmholtz_oracle.py:gmres_relax): `steps` Arnoldi steps of GMRES on
+   level l's operator from the current x, right-preconditioned by one damped
+   Jacobi sweep (w D^-1), classical Gram-Schmidt, the (steps+1) x steps least
+   squares by complex Givens rotations, then x += Z y per column. */
+static void gmres_relax(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, double w, int steps) {
+  if (steps <= 0) return;
+  const csr_t* A = &S->A[l];
+  const int64_t n = A->nrows;
+  const cplx* di = S->dinv[l];
+  const int64_t blk = n * (int64_t)nrhs;
+  cplx* V = (cplx*)malloc(sizeof(cplx) * (size_t)(steps + 1) * (size_t)blk);
+  cplx* Z = (cplx*)malloc(sizeof(cplx) * (size_t)steps * (size_t)blk);
+  cplx* u = (cplx*)malloc(sizeof(cplx) * (size_t)blk);
+  cplx* Hm = (cplx*)calloc((size_t)(steps + 1) * steps * nrhs, sizeof(cplx)); /* Hm[(c*(steps+1)+i)*steps+j] */
+  double* beta = (double*)calloc((size_t)nrhs, sizeof(double));
+  spmm(A, x, n, u, n, nrhs, 0, 1.0);
+  for (int c = 0; c < nrhs; ++c) {
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      const cplx r = b[c * n + i] - u[c * n + i];
+      V[c * n + i] = r;
+      s += creal(r) * creal(r) + cimag(r) * cimag(r);
+    }
+    beta[c] = sqrt(s);
+    const double inv = beta[c] > 0 ? 1.0 / beta[c] : 1.0;
+    for (int64_t i = 0; i < n; ++i) V[c * n + i] *= inv;
+  }
+  for (int j = 0; j < steps; ++j) {
+    cplx* Vj = V + (int64_t)j * blk;
+    cplx* Zj = Z + (int64_t)j * blk;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i)
+      for (int c = 0; c < nrhs; ++c) Zj[c * n + i] = w * di[i] * Vj[c * n + i];
+    spmm(A, Zj, n, u, n, nrhs, 0, 1.0);
+    for (int c = 0; c < nrhs; ++c) {
+      cplx* uc = u + (int64_t)c * n;
+      cplx h[64];
+      for (int i = 0; i <= j; ++i) {
+        const cplx* Vi = V + (int64_t)i * blk + (int64_t)c * n;
+        cplx d = 0;
+        for (int64_t k = 0; k < n; ++k) d += conj(Vi[k]) * uc[k];
+        h[i] = d;
+      }
+      double s = 0;
+      for (int64_t k = 0; k < n; ++k) {
+        cplx v = uc[k];
+        for (int i = 0; i <= j; ++i) v -= h[i] * V[(int64_t)i * blk + (int64_t)c * n + k];
+        uc[k] = v;
+        s += creal(v) * creal(v) + cimag(v) * cimag(v);
+      }
+      const double hn = sqrt(s), inv = hn > 0 ? 1.0 / hn : 0.0;
+      for (int i = 0; i <= j; ++i) Hm[((int64_t)c * (steps + 1) + i) * steps + j] = h[i];
+      Hm[((int64_t)c * (steps + 1) + j + 1) * steps + j] = hn;
+      cplx* Vn = V + (int64_t)(j + 1) * blk + (int64_t)c * n;
+      for (int64_t k = 0; k < n; ++k) Vn[k] = inv * uc[k];
+    }
+  }
+  for (int c = 0; c < nrhs; ++c) {
+    if (beta[c] == 0) continue;
+    cplx R[65][64], g[65], y[64];
+    for (int i = 0; i <= steps; ++i) {
+      g[i] = i == 0 ? beta[c] : 0;
+      for (int j = 0; j < steps; ++j) R[i][j] = Hm[((int64_t)c * (steps + 1) + i) * steps + j];
+    }
+    for (int j = 0; j < steps; ++j) { /* rotate rows j, j+1 to zero R[j+1][j] */
+      const cplx a = R[j][j], e = R[j + 1][j];
+      const double r = sqrt(creal(a) * creal(a) + cimag(a) * cimag(a) + creal(e) * creal(e) + cimag(e) * cimag(e));
+      if (r == 0) continue;
+      const cplx cs = a / r, sn = e / r;
+      for (int k = j; k < steps; ++k) {
+        const cplx top = R[j][k], bot = R[j + 1][k];
+        R[j][k] = conj(cs) * top + conj(sn) * bot;
+        R[j + 1][k] = -sn * top + cs * bot;
+      }
+      const cplx gt = g[j], gb = g[j + 1];
+      g[j] = conj(cs) * gt + conj(sn) * gb;
+      g[j + 1] = -sn * gt + cs * gb;
+    }
+    for (int j = steps - 1; j >= 0; --j) {
+      cplx v = g[j];
+      for (int k = j + 1; k < steps; ++k) v -= R[j][k] * y[k];
+      y[j] = R[j][j] != 0 ? v / R[j][j] : 0;
+    }
+    for (int j = 0; j < steps; ++j) {
+      const cplx* Zj = Z + (int64_t)j * blk + (int64_t)c * n;
+      for (int64_t k = 0; k < n; ++k) x[c * n + k] += y[j] * Zj[k];
+    }
+  }
+  free(V);
+  free(Z);
+  free(u);
+  free(Hm);
+  free(beta);
+}
 
 /* K-cycle coarse correction on level l (Multigrid.jl cycleType 'K' of
    test/ShiftedLaplacianTest.jl:137-140, restated): two steps of FGMRES on the
@@ -294,7 +392,8 @@ static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, c
   cplx* xc = (cplx*)malloc(sizeof(cplx) * (size_t)nc * nrhs);
   memset(x, 0, bytes);
   const cplx* di = S->dinv[l];
-  for (int s = 0; s < cp->pre; ++s) {
+  if (cp->relax == 1) gmres_relax(S, l, b, x, nrhs, cp->w, cp->pre);
+  for (int s = 0; s < (cp->relax == 1 ? 0 : cp->pre); ++s) {
     spmm(A, x, n, r, n, nrhs, 0, 1.0);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i)
@@ -312,7 +411,8 @@ static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, c
       mg_cycle(S, l + 1, bc, xc, nrhs, cp);
     spmm(&S->P[l], xc, nc, x, n, nrhs, 1, 1.0);
   }
-  for (int s = 0; s < cp->post; ++s) {
+  if (cp->relax == 1) gmres_relax(S, l, b, x, nrhs, cp->w, cp->post);
+  for (int s = 0; s < (cp->relax == 1 ? 0 : cp->post); ++s) {
     spmm(A, x, n, r, n, nrhs, 0, 1.0);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i)
@@ -334,14 +434,15 @@ static double col_norm(const cplx* x, int64_t n) {
    batched, each with its own Arnoldi process.  Returns restart cycles run. */
 int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const double* hd, const double* Bd,
                double* Xd, int nrhs, int restart, double tol, int max_outer, double w, int pre, int post, int wcycle,
-               int32_t* iters_out, double* relres_out) {
+               int relax, int32_t* iters_out, double* relres_out) {
   slmg_t* S = (slmg_t*)h;
   const csr_t Hop = {hn, hn, hp, hi, (const cplx*)hd};
   const int64_t n = hn;
   const int m = restart;
   const cplx* B = (const cplx*)Bd;
   cplx* X = (cplx*)Xd;
-  const cyc_t cp = {w, pre, post, wcycle};
+  if (relax == 1 && (pre > 64 || post > 64)) return -1;
+  const cyc_t cp = {w, pre, post, wcycle, relax};
   memset(X, 0, sizeof(cplx) * (size_t)n * nrhs);
   double* bn = (double*)calloc((size_t)nrhs, sizeof(double));
   int* conv = (int*)calloc((size_t)nrhs, sizeof(int));

@@ -33,7 +33,7 @@ def lib():
         _lib.slmg_solve.restype = C.c_int
         _lib.slmg_solve.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
-                                    C.c_int, C.c_void_p, C.c_void_p]
+                                    C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -91,7 +91,9 @@ class CpuSLMG:
             raise RuntimeError("C oracle setup failed")
         self.setup_s = time.perf_counter() - t0
 
-    def solve(self, B, restart=10, tol=1e-8, max_outer=50, w=0.8, pre=1, post=1, cycle="V") -> CpuSolveResult:
+    def solve(self, B, restart=10, tol=1e-8, max_outer=50, w=0.8, pre=1, post=1, cycle="V",
+              relax="Jac") -> CpuSolveResult:
+        """relax: "Jac" (damped Jacobi sweeps) or "Jac-GMRES" (pre / post GMRES steps, at most 64)."""
         B2 = np.asfortranarray(np.asarray(B, dtype=np.complex128).reshape(B.shape[0], -1))
         n, nrhs = B2.shape
         X = np.zeros((n, nrhs), dtype=np.complex128, order="F")
@@ -101,7 +103,9 @@ class CpuSLMG:
         t0 = time.perf_counter()
         outer = lib().slmg_solve(self.h, n, hp.ctypes.data, hi.ctypes.data, hd.ctypes.data, B2.ctypes.data,
                                  X.ctypes.data, nrhs, restart, tol, max_outer, w, pre, post, {"V": 0, "W": 1, "K": 2}[cycle],
-                                 it.ctypes.data, rr.ctypes.data)
+                                 {"Jac": 0, "Jac-GMRES": 1}[relax], it.ctypes.data, rr.ctypes.data)
+        if outer < 0:
+            raise ValueError("Jac-GMRES takes at most 64 steps per smoothing")
         dt = time.perf_counter() - t0
         return CpuSolveResult(X=X, iters=it, relres=rr, outer=outer, setup_s=self.setup_s, solve_s=dt,
                               threads=lib().slmg_threads())

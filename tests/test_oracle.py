@@ -166,20 +166,22 @@ def shifted_laplacian_example(O):
     return M, m, np.ravel(gamma, order="F"), w, H, q, B2
 
 
-@pytest.mark.parametrize("krylov,cycle,restart,rhs", [
-    ("GMRES", "W", 20, "point"),     # :63-73  getMGparam(levels 2, Jac 0.75, 2/2, 'W'), GMRES(20)
-    ("BiCGSTAB", "W", 0, "point"),   # :75-78
-    ("BiCGSTAB", "W", 0, "random"),  # :121-135 two random right-hand sides
-    ("GMRES", "K", 5, "random"),     # :137-142 K-cycle, GMRES(5) (damped Jacobi relaxation)
+@pytest.mark.parametrize("krylov,cycle,restart,rhs,relax", [
+    ("GMRES", "W", 20, "point", "Jac"),      # :63-73  getMGparam(levels 2, Jac 0.75, 2/2, 'W'), GMRES(20)
+    ("BiCGSTAB", "W", 0, "point", "Jac"),    # :75-78
+    ("BiCGSTAB", "W", 0, "random", "Jac"),   # :121-135 two random right-hand sides
+    ("GMRES", "K", 5, "random", "Jac-GMRES"),  # :137-142 relaxType "Jac-GMRES", K-cycle, GMRES(5)
+    ("GMRES", "K", 5, "random", "Jac"),      # the same with damped Jacobi (the relaxation the GPU path builds)
 ])
-def test_shifted_laplacian_example(O, shifted_laplacian_example, krylov, cycle, restart, rhs):
+def test_shifted_laplacian_example(O, shifted_laplacian_example, krylov, cycle, restart, rhs, relax):
     """Each solve of the reference's shifted-Laplacian example (shift 0.2/10 on every
     level, maxIter 30, tolerance 1e-6) reaches the residual the example prints and
     the direct solution."""
     M, m, gamma, w, H, q, B2 = shifted_laplacian_example
     B = q if rhs == "point" else B2
     sol = O.slmg_solve(M, m, gamma, w, True, True, B, levels=2, shift=0.02, relax_w=0.75, pre=2, post=2,
-                       restart=max(restart, 1), tol=1e-6, max_outer=30, cycle=cycle, krylov=krylov)
+                       restart=max(restart, 1), tol=1e-6, max_outer=30, cycle=cycle, krylov=krylov,
+                       relax_type=relax)
     assert np.all(sol.result.converged)
     X = sol.X.reshape(q.size, -1)
     Bm = B.reshape(q.size, -1)
@@ -320,3 +322,56 @@ def test_kcycle_depth_galerkin_vs_rediscretized_3d(O, cpu_slmg):
     assert it["galerkin", 4][0] < 60 and it["galerkin", 4][1] <= 1e-6, it
     assert it["galerkin", 5][1] > 1e-6, it          # not converged in 15 restarts of 10
     assert it["rediscretize", 5][0] <= 1.2 * it["rediscretize", 4][0] and it["rediscretize", 5][1] <= 1e-6, it
+
+
+@pytest.mark.parametrize("cycle,pre,post", [("V", 1, 1), ("V", 2, 2), ("K", 3, 1), ("W", 2, 2)])
+def test_c_oracle_jac_gmres_matches_numpy_oracle(O, cpu_slmg, cycle, pre, post):
+    """relaxType "Jac-GMRES": the NumPy and the threaded C restatements take the
+    same iterations per column and agree on the solution."""
+    P = PB.layered((64, 64), seed=3, pad=8)
+    B = PB.rhs(P["m"].size, 3, seed=1)
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    r = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 4).solve(B, tol=1e-8, max_outer=60, cycle=cycle, pre=pre, post=post,
+                                                       relax="Jac-GMRES")
+    sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=4, tol=1e-8, max_outer=60,
+                       cycle=cycle, pre=pre, post=post, relax_type="Jac-GMRES")
+    np.testing.assert_array_equal(r.iters, sol.result.iters)
+    assert np.abs(r.X - sol.result.X).max() <= 1e-12 * np.abs(sol.result.X).max()
+
+
+def test_jac_gmres_step_properties(O):
+    """One Jac-GMRES smoothing never raises a column's residual (GMRES minimises it
+    over a space that contains the old iterate); as many steps as unknowns solve
+    the level exactly; a zero-residual column is left as it is."""
+    P = PB.gradient_2d((8, 8))
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    L = O.build_hierarchy(SH, P["M"], 1).levels[0]
+    rng = np.random.default_rng(0)
+    n = SH.shape[0]
+    b = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+    x = rng.standard_normal((n, 3)) + 0j
+    r0 = np.linalg.norm(b - SH @ x, axis=0)
+    for steps in (1, 2, 5):
+        x1 = O.gmres_relax(L, x.copy(), b, 0.8, steps)
+        assert np.all(np.linalg.norm(b - SH @ x1, axis=0) <= r0 * (1 + 1e-12))
+    xs = O.gmres_relax(L, np.zeros((n, 1), complex), b[:, :1], 0.8, n)
+    assert np.linalg.norm(b[:, :1] - SH @ xs) <= 1e-8 * np.linalg.norm(b[:, :1])
+    xe = np.linalg.solve(SH.toarray(), b[:, :1])
+    be = SH @ xe  # the residual b - A x is exactly zero for this pair
+    np.testing.assert_array_equal(O.gmres_relax(L, xe.copy(), be, 0.8, 2), xe)
+
+
+def test_jac_gmres_rescues_deep_galerkin_3d(O, cpu_slmg):
+    """3D layered+ellipsoid at 10 points per wavelength, five Galerkin levels (the
+    fifth at 0.625 points per wavelength): the K-cycle with damped Jacobi does not
+    converge in 15 restarts of 10, with one Jac-GMRES step per smoothing it does,
+    well within them."""
+    P = PB.layered((64, 64, 64), seed=7, pad=8, ellipsoid=True)
+    B = np.zeros((P["m"].size, 1), dtype=complex)
+    B[32 + 65 * (32 + 65 * 1), 0] = 1.0
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    S = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 5)
+    jac = S.solve(B, tol=1e-6, max_outer=15, cycle="K")
+    jg = S.solve(B, tol=1e-6, max_outer=15, cycle="K", relax="Jac-GMRES")
+    assert jac.relres[0] > 1e-6, jac.relres
+    assert jg.relres[0] <= 1e-6 and jg.iters[0] <= 60, (jg.iters, jg.relres)
