@@ -407,17 +407,22 @@ def gmres_relax(L: Level, x: np.ndarray, b: np.ndarray, w: float, steps: int) ->
     return x
 
 
-def relax(L: Level, x: np.ndarray, b: np.ndarray, w: float, sweeps: int, relax_type: str = "Jac") -> np.ndarray:
-    """The smoother of relaxType: damped Jacobi ("Jac") or "Jac-GMRES"."""
-    if relax_type == "Jac-GMRES":
+def relax(L: Level, x: np.ndarray, b: np.ndarray, w: float, sweeps: int, relax_type: str = "Jac",
+          lev: int = 0, gmres_from: int = 0) -> np.ndarray:
+    """The smoother of relaxType on level ``lev``: damped Jacobi ("Jac") or
+    "Jac-GMRES"; with "Jac-GMRES", levels above ``gmres_from`` keep damped Jacobi
+    (gmres_from = 0, every level, is the reference's option)."""
+    if relax_type == "Jac-GMRES" and lev >= gmres_from:
         return gmres_relax(L, x, b, w, sweeps)
+    if relax_type == "Jac-GMRES":
+        return jacobi(L, x, b, w, sweeps)
     if relax_type != "Jac":
         raise ValueError(f"relaxType {relax_type!r}")
     return jacobi(L, x, b, w, sweeps)
 
 
 def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int,
-           relax_type: str = "Jac") -> np.ndarray:
+           relax_type: str = "Jac", gmres_from: int = 0) -> np.ndarray:
     """K-cycle coarse correction on level ``lev`` (Multigrid.jl cycleType 'K',
     used by test/ShiftedLaplacianTest.jl:137-140, restated): two steps of FGMRES
     on that level's operator from a zero guess, right-preconditioned by the
@@ -427,13 +432,13 @@ def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: i
     out = np.zeros_like(b)
     beta = np.linalg.norm(b, axis=0)
     V0 = b / np.where(beta > 0, beta, 1.0)
-    Z0 = mg_cycle(hier, lev, V0, w, pre, post, "K", relax_type)
+    Z0 = mg_cycle(hier, lev, V0, w, pre, post, "K", relax_type, gmres_from)
     W = A @ Z0
     h00 = np.sum(np.conj(V0) * W, axis=0)
     W = W - h00 * V0
     h10 = np.linalg.norm(W, axis=0)
     V1 = W / np.where(h10 > 0, h10, 1.0) * (h10 > 0)
-    Z1 = mg_cycle(hier, lev, V1, w, pre, post, "K", relax_type)
+    Z1 = mg_cycle(hier, lev, V1, w, pre, post, "K", relax_type, gmres_from)
     W = A @ Z1
     h01 = np.sum(np.conj(V0) * W, axis=0)
     h11 = np.sum(np.conj(V1) * W, axis=0)
@@ -449,23 +454,23 @@ def kcycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: i
 
 
 def mg_cycle(hier: Hierarchy, lev: int, b: np.ndarray, w: float, pre: int, post: int, cycle: str = "V",
-             relax_type: str = "Jac") -> np.ndarray:
+             relax_type: str = "Jac", gmres_from: int = 0) -> np.ndarray:
     """One V, W or K cycle with zero initial guess on level ``lev``."""
     L = hier.levels[lev]
     if lev == len(hier.levels) - 1:
         return hier.lu.solve(b)
     x = np.zeros_like(b)
-    x = relax(L, x, b, w, pre, relax_type)
+    x = relax(L, x, b, w, pre, relax_type, lev, gmres_from)
     ncalls = 2 if cycle == "W" and lev < len(hier.levels) - 2 else 1
     for _ in range(ncalls):
         r = b - L.A @ x
         bc = L.R @ r
         if cycle == "K" and lev + 1 < len(hier.levels) - 1:
-            xc = kcycle(hier, lev + 1, bc, w, pre, post, relax_type).reshape(bc.shape)
+            xc = kcycle(hier, lev + 1, bc, w, pre, post, relax_type, gmres_from).reshape(bc.shape)
         else:
-            xc = mg_cycle(hier, lev + 1, bc, w, pre, post, cycle, relax_type)
+            xc = mg_cycle(hier, lev + 1, bc, w, pre, post, cycle, relax_type, gmres_from)
         x = x + L.P @ xc
-    x = relax(L, x, b, w, post, relax_type)
+    x = relax(L, x, b, w, post, relax_type, lev, gmres_from)
     return x
 
 
@@ -634,10 +639,11 @@ def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Somme
                levels: int, shift: float = 0.5, relax_w: float = 0.8, pre: int = 1, post: int = 1,
                restart: int = 10, tol: float = 1e-8, max_outer: int = 100, cycle: str = "V",
                transpose: bool = False, krylov: str = "GMRES", coarse: str = "galerkin",
-               relax_type: str = "Jac") -> SLMGSolution:
+               relax_type: str = "Jac", gmres_from: int = 0) -> SLMGSolution:
     """Plain FP64 SLMG: FGMRES(restart) on H (or H^H when ``transpose``),
     right-preconditioned by one multigrid cycle on SH = H + i*s*w^2*diag(m)
-    (or SH^H), src/ShiftedLaplacianMultigridSolver.jl:33-102."""
+    (or SH^H), src/ShiftedLaplacianMultigridSolver.jl:33-102.  relax_type
+    "Jac-GMRES" smooths levels >= gmres_from by GMRES steps (gmres_relax)."""
     H = GetHelmholtzOperator(M, m, omega, gamma, NeumannOnTop, Sommerfeld)
     SH = (H + GetHelmholtzShiftOP(m, omega, shift)).tocsr()
     if transpose:
@@ -652,11 +658,11 @@ def slmg_solve(M: RegularMesh, m, gamma, omega: float, NeumannOnTop: bool, Somme
     if vec:
         B2 = B2[:, None]
     if krylov == "BiCGSTAB":
-        res = bicgstab(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle, relax_type), B2,
-                       tol, max_outer)
+        res = bicgstab(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle, relax_type,
+                                                           gmres_from), B2, tol, max_outer)
     else:
-        res = fgmres(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle, relax_type), B2,
-                     restart, tol, max_outer)
+        res = fgmres(lambda X: H @ X, lambda V: mg_cycle(hier, 0, V, relax_w, pre, post, cycle, relax_type,
+                                                         gmres_from), B2, restart, tol, max_outer)
     X = res.X[:, 0] if vec else res.X
     return SLMGSolution(X=X, result=res, hier=hier)
 

@@ -201,6 +201,7 @@ typedef struct {
   double w;
   int pre, post, wcycle; /* wcycle: 0 V, 1 W, 2 K */
   int relax;             /* 0 damped Jacobi ("Jac"), 1 "Jac-GMRES" */
+  int gmres_from;        /* Jac-GMRES: first level smoothed by GMRES (finer levels: Jacobi) */
 } cyc_t;
 
 static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, const cyc_t* cp);
@@ -392,8 +393,9 @@ static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, c
   cplx* xc = (cplx*)malloc(sizeof(cplx) * (size_t)nc * nrhs);
   memset(x, 0, bytes);
   const cplx* di = S->dinv[l];
-  if (cp->relax == 1) gmres_relax(S, l, b, x, nrhs, cp->w, cp->pre);
-  for (int s = 0; s < (cp->relax == 1 ? 0 : cp->pre); ++s) {
+  const int use_gmres = cp->relax == 1 && l >= cp->gmres_from;
+  if (use_gmres) gmres_relax(S, l, b, x, nrhs, cp->w, cp->pre);
+  for (int s = 0; s < (use_gmres ? 0 : cp->pre); ++s) {
     spmm(A, x, n, r, n, nrhs, 0, 1.0);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i)
@@ -411,8 +413,8 @@ static void mg_cycle(const slmg_t* S, int l, const cplx* b, cplx* x, int nrhs, c
       mg_cycle(S, l + 1, bc, xc, nrhs, cp);
     spmm(&S->P[l], xc, nc, x, n, nrhs, 1, 1.0);
   }
-  if (cp->relax == 1) gmres_relax(S, l, b, x, nrhs, cp->w, cp->post);
-  for (int s = 0; s < (cp->relax == 1 ? 0 : cp->post); ++s) {
+  if (use_gmres) gmres_relax(S, l, b, x, nrhs, cp->w, cp->post);
+  for (int s = 0; s < (use_gmres ? 0 : cp->post); ++s) {
     spmm(A, x, n, r, n, nrhs, 0, 1.0);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i)
@@ -434,7 +436,7 @@ static double col_norm(const cplx* x, int64_t n) {
    batched, each with its own Arnoldi process.  Returns restart cycles run. */
 int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const double* hd, const double* Bd,
                double* Xd, int nrhs, int restart, double tol, int max_outer, double w, int pre, int post, int wcycle,
-               int relax, int32_t* iters_out, double* relres_out) {
+               int relax, int gmres_from, int32_t* iters_out, double* relres_out) {
   slmg_t* S = (slmg_t*)h;
   const csr_t Hop = {hn, hn, hp, hi, (const cplx*)hd};
   const int64_t n = hn;
@@ -442,7 +444,7 @@ int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const 
   const cplx* B = (const cplx*)Bd;
   cplx* X = (cplx*)Xd;
   if (relax == 1 && (pre > 64 || post > 64)) return -1;
-  const cyc_t cp = {w, pre, post, wcycle, relax};
+  const cyc_t cp = {w, pre, post, wcycle, relax, gmres_from};
   memset(X, 0, sizeof(cplx) * (size_t)n * nrhs);
   double* bn = (double*)calloc((size_t)nrhs, sizeof(double));
   int* conv = (int*)calloc((size_t)nrhs, sizeof(int));

@@ -33,7 +33,7 @@ def lib():
         _lib.slmg_solve.restype = C.c_int
         _lib.slmg_solve.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
-                                    C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+                                    C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -92,8 +92,9 @@ class CpuSLMG:
         self.setup_s = time.perf_counter() - t0
 
     def solve(self, B, restart=10, tol=1e-8, max_outer=50, w=0.8, pre=1, post=1, cycle="V",
-              relax="Jac") -> CpuSolveResult:
-        """relax: "Jac" (damped Jacobi sweeps) or "Jac-GMRES" (pre / post GMRES steps, at most 64)."""
+              relax="Jac", gmres_from=0) -> CpuSolveResult:
+        """relax: "Jac" (damped Jacobi sweeps) or "Jac-GMRES" (pre / post GMRES steps, at most 64,
+        on the levels >= gmres_from; finer levels keep damped Jacobi)."""
         B2 = np.asfortranarray(np.asarray(B, dtype=np.complex128).reshape(B.shape[0], -1))
         n, nrhs = B2.shape
         X = np.zeros((n, nrhs), dtype=np.complex128, order="F")
@@ -103,7 +104,8 @@ class CpuSLMG:
         t0 = time.perf_counter()
         outer = lib().slmg_solve(self.h, n, hp.ctypes.data, hi.ctypes.data, hd.ctypes.data, B2.ctypes.data,
                                  X.ctypes.data, nrhs, restart, tol, max_outer, w, pre, post, {"V": 0, "W": 1, "K": 2}[cycle],
-                                 {"Jac": 0, "Jac-GMRES": 1}[relax], it.ctypes.data, rr.ctypes.data)
+                                 {"Jac": 0, "Jac-GMRES": 1}[relax], int(gmres_from), it.ctypes.data,
+                                 rr.ctypes.data)
         if outer < 0:
             raise ValueError("Jac-GMRES takes at most 64 steps per smoothing")
         dt = time.perf_counter() - t0

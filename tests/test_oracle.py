@@ -324,17 +324,19 @@ def test_kcycle_depth_galerkin_vs_rediscretized_3d(O, cpu_slmg):
     assert it["rediscretize", 5][0] <= 1.2 * it["rediscretize", 4][0] and it["rediscretize", 5][1] <= 1e-6, it
 
 
-@pytest.mark.parametrize("cycle,pre,post", [("V", 1, 1), ("V", 2, 2), ("K", 3, 1), ("W", 2, 2)])
-def test_c_oracle_jac_gmres_matches_numpy_oracle(O, cpu_slmg, cycle, pre, post):
-    """relaxType "Jac-GMRES": the NumPy and the threaded C restatements take the
-    same iterations per column and agree on the solution."""
+@pytest.mark.parametrize("cycle,pre,post,gmres_from", [("V", 1, 1, 0), ("V", 2, 2, 0), ("K", 3, 1, 0), ("W", 2, 2, 0),
+                                                         ("K", 1, 1, 1), ("V", 2, 1, 2)])
+def test_c_oracle_jac_gmres_matches_numpy_oracle(O, cpu_slmg, cycle, pre, post, gmres_from):
+    """relaxType "Jac-GMRES" (on every level, or from a coarse level down): the
+    NumPy and the threaded C restatements take the same iterations per column and
+    agree on the solution."""
     P = PB.layered((64, 64), seed=3, pad=8)
     B = PB.rhs(P["m"].size, 3, seed=1)
     SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
     r = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 4).solve(B, tol=1e-8, max_outer=60, cycle=cycle, pre=pre, post=post,
-                                                       relax="Jac-GMRES")
+                                                       relax="Jac-GMRES", gmres_from=gmres_from)
     sol = O.slmg_solve(P["M"], P["m"], P["gamma"], P["w"], True, True, B, levels=4, tol=1e-8, max_outer=60,
-                       cycle=cycle, pre=pre, post=post, relax_type="Jac-GMRES")
+                       cycle=cycle, pre=pre, post=post, relax_type="Jac-GMRES", gmres_from=gmres_from)
     np.testing.assert_array_equal(r.iters, sol.result.iters)
     assert np.abs(r.X - sol.result.X).max() <= 1e-12 * np.abs(sol.result.X).max()
 
@@ -365,7 +367,8 @@ def test_jac_gmres_rescues_deep_galerkin_3d(O, cpu_slmg):
     """3D layered+ellipsoid at 10 points per wavelength, five Galerkin levels (the
     fifth at 0.625 points per wavelength): the K-cycle with damped Jacobi does not
     converge in 15 restarts of 10, with one Jac-GMRES step per smoothing it does,
-    well within them."""
+    well within them, and as well with GMRES smoothing on the coarse levels only
+    (damped Jacobi kept on the fine level, where the smoothing costs the most)."""
     P = PB.layered((64, 64, 64), seed=7, pad=8, ellipsoid=True)
     B = np.zeros((P["m"].size, 1), dtype=complex)
     B[32 + 65 * (32 + 65 * 1), 0] = 1.0
@@ -375,3 +378,5 @@ def test_jac_gmres_rescues_deep_galerkin_3d(O, cpu_slmg):
     jg = S.solve(B, tol=1e-6, max_outer=15, cycle="K", relax="Jac-GMRES")
     assert jac.relres[0] > 1e-6, jac.relres
     assert jg.relres[0] <= 1e-6 and jg.iters[0] <= 60, (jg.iters, jg.relres)
+    jc = S.solve(B, tol=1e-6, max_outer=15, cycle="K", relax="Jac-GMRES", gmres_from=1)
+    assert jc.relres[0] <= 1e-6 and jc.iters[0] <= 1.1 * jg.iters[0], (jc.iters, jg.iters)
