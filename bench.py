@@ -276,6 +276,8 @@ def run_ours(args, rank, ws, dist):
         o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, args.max_outer
         o.cycle = ord(args.cycle)
         o.coarse_op = L.HZ_COARSE_REDISCRETIZE if args.coarse == "rediscretize" else L.HZ_COARSE_GALERKIN
+        o.relax_type = L.HZ_RELAX_JAC_GMRES if args.relax == "jac-gmres" else L.HZ_RELAX_JAC
+        o.relax_from = args.relax_from
         o.cuda_graph = 0 if args.no_graph else 1
         o.autotune = 0 if args.no_tune else 1
         if args.krylov == "bicgstab":
@@ -406,9 +408,11 @@ def run_learned(args, rank, ws, dist):
         M = hz.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
         gam = gamma_of(P, wl["pad"], lib, hz)
         param = hz.HelmholtzParam(M, gam, P["m"], P["w"], True, True)
-        MG = hz.getMGparam(complex, int, wl["levels"], 1, max_outer, wl["tol"], "Jac", 0.8, 1, 1, args.cycle,
+        MG = hz.getMGparam(complex, int, wl["levels"], 1, max_outer, wl["tol"],
+                           "Jac-GMRES" if args.relax == "jac-gmres" else "Jac", 0.8, 1, 1, args.cycle,
                            "Julia", 0.5, 0.0, precision=precision, outerArithmetic=outer,
-                           coarseOperator="Rediscretize" if args.coarse == "rediscretize" else "Galerkin")
+                           coarseOperator="Rediscretize" if args.coarse == "rediscretize" else "Galerkin",
+                           relaxFrom=args.relax_from)
         return hz.getShiftedLaplacianMultigridSolver(param, MG, 0.5, "GMRES", 10)
 
     # 1. training pairs from the FP64 solver on seeded training models
@@ -493,10 +497,12 @@ def run_learned(args, rank, ws, dist):
 
 
 def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: str = "V",
-                   coarse: str = "galerkin"):
+                   coarse: str = "galerkin", relax: str = "jac", relax_from: int = 0):
     """C oracle (threaded CSR SLMG, plain FP64) on a bounded sample of the
     workload: the full grid and operator, a few of its right-hand sides, with
-    the GPU arm's cycle and coarse operators (Galerkin or re-discretised)."""
+    the GPU arm's cycle, coarse operators (Galerkin or re-discretised) and
+    smoother (damped Jacobi, or Jac-GMRES from level relax_from down)."""
+    rkw = dict(relax="Jac-GMRES" if relax == "jac-gmres" else "Jac", gmres_from=relax_from)
     sys.path.insert(0, str(ROOT / "oracle"))
     import helmholtz_oracle as O
     import slmg_cpu
@@ -510,14 +516,15 @@ def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: st
     cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"], hier=hier)
     B = sources(P, wl["nrhs"], seed=0)
     ncols = 1
-    r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200, cycle=cycle)
+    r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200, cycle=cycle, **rkw)
     t1 = r.solve_s
     ncols = int(max(1, min(ncols_max, B.shape[1], budget_s // max(t1, 1e-3))))
     if ncols > 1:
-        r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200, cycle=cycle)
+        r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200, cycle=cycle, **rkw)
     return dict(value=ncols / r.solve_s, unit="RHS/s", cores=r.threads, kind="port",
                 sample=f"{ncols} of the {wl['nrhs']} right-hand sides of the same workload (full grid, "
-                       f"same operator, plain FP64 SLMG ({cycle}-cycle, {coarse} coarse levels) in threaded C, "
+                       f"same operator, plain FP64 SLMG ({cycle}-cycle, {coarse} coarse levels, {rkw['relax']} "
+                       f"smoothing{f' from level {relax_from}' if relax == 'jac-gmres' else ''}) in threaded C, "
                        f"{int(r.iters.mean())} iterations per RHS)",
                 seconds=r.solve_s, setup_s=r.setup_s, max_relres=float(r.relres.max()))
 
@@ -546,6 +553,10 @@ def main():
     ap.add_argument("--coarse", default="galerkin", choices=["galerkin", "rediscretize"],
                     help="coarse-level operators: Galerkin R A P, or the operator re-discretised on each coarse mesh")
     ap.add_argument("--levels", type=int, default=0, help="multigrid levels (0: the workload's)")
+    ap.add_argument("--relax", default="jac", choices=["jac", "jac-gmres"],
+                    help="smoother: damped Jacobi, or GMRES steps preconditioned by a Jacobi sweep (relaxType "
+                         "'Jac-GMRES'; on the GPU it needs HELMGPU_ENABLE_JAC_GMRES=1 until its parity test has run)")
+    ap.add_argument("--relax-from", type=int, default=0, help="jac-gmres: first level smoothed by GMRES steps")
     ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
     ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
     ap.add_argument("--pairs-per-model", type=int, default=200)
@@ -571,14 +582,14 @@ def main():
         cs = None
         for i in range(args.warmup + args.steps):
             cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps), cycle=args.cycle,
-                                coarse=args.coarse)
+                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from)
             if i >= args.warmup:
                 vals.append(cs["value"])
         v = float(np.mean(vals))
         line = dict(metric=METRIC, value=v, unit="RHS/s", impl="reference", n_gpus=args.gpus, steps=args.steps,
                     warmup=args.warmup, higher_is_better=True, dtype="c128",
                     config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], cycle=args.cycle,
-                                coarse=args.coarse),
+                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from),
                     cpu_baseline=dict(value=v, unit="RHS/s", cores=cs["cores"], kind="port", sample=cs["sample"]),
                     e2e=dict(value=v, unit="RHS/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
                     note="reference path = the C oracle port of the Julia SLMG (Julia and Multigrid.jl are absent)")
@@ -598,8 +609,8 @@ def main():
                     vs_baseline=None, dtype="c64 V-cycle + bf16 network / c128 outer",
                     data="synthetic (seeded layered+inclusion models, random source positions)",
                     config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
-                                krylov="FGMRES(10)", cycle=args.cycle, coarse=args.coarse,
-                                outer_arithmetic=args.outer, learned=True,
+                                krylov="FGMRES(10)", cycle=args.cycle, coarse=args.coarse, relax=args.relax,
+                                relax_from=args.relax_from, outer_arithmetic=args.outer, learned=True,
                                 net_level=args.net_level if args.net_level > 0 else wl["net_level"],
                                 stag_ratio=args.stag_ratio,
                                 step="solver setup + solve of one held-out model's right-hand sides",
@@ -643,7 +654,8 @@ def main():
         import __graft_entry__ as ge
         hz = ge.load_package()
         gam = gamma_of(P, wl["pad"], None, hz)
-        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget, cycle=args.cycle, coarse=args.coarse)
+        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget, cycle=args.cycle, coarse=args.coarse,
+                             relax=args.relax, relax_from=args.relax_from)
     plain = results.get("fp64")
     line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
@@ -653,7 +665,7 @@ def main():
                 data="synthetic (seeded layered model)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
                             krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB", cycle=args.cycle,
-                            coarse=args.coarse,
+                            coarse=args.coarse, relax=args.relax, relax_from=args.relax_from,
                             cuda_graph=not args.no_graph, autotune=not args.no_tune,
                             outer_arithmetic=args.outer,
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,

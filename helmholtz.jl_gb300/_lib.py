@@ -32,6 +32,8 @@ HZ_KRYLOV_FGMRES = 0
 HZ_KRYLOV_BICGSTAB = 1
 HZ_COARSE_GALERKIN = 0
 HZ_COARSE_REDISCRETIZE = 1
+HZ_RELAX_JAC = 0
+HZ_RELAX_JAC_GMRES = 1
 HZ_OP_H = 0
 HZ_OP_SH = 1
 HZ_NOALLOC_MAX_COLS = 4096
@@ -72,7 +74,9 @@ class hz_options(C.Structure):
         ("outer_arith", C.c_int32),
         ("cuda_graph", C.c_int32),
         ("autotune", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("relax_type", C.c_int32),
+        ("relax_from", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 

@@ -24,6 +24,7 @@ compiled library or a GPU every compute call raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import sys
 from dataclasses import dataclass, field
 
@@ -375,6 +376,7 @@ class MGparam:
     outerArithmetic: str = "fp64"     # or "emulated": FP64 emulated with FP32 pairs (mixed form, FGMRES)
     cudaGraph: bool = True            # replay the FGMRES preconditioner applications from CUDA graphs
     autotune: bool = True             # time the stencils' launch shapes at the first solve
+    relaxFrom: int = 0                # "Jac-GMRES": first level smoothed by GMRES steps (finer: "Jac")
     doTranspose: int = 0
     _hier: dict = field(default_factory=dict, repr=False)
 
@@ -383,7 +385,7 @@ _SUPPORTED_COARSE = {"Julia", "MUMPS", "NoMUMPS", "BandLU"}
 
 
 def getMGparam(*args, transferType: str | None = None, precision: str = "fp64",
-               coarseOperator: str = "Galerkin", outerArithmetic: str = "fp64") -> MGparam:
+               coarseOperator: str = "Galerkin", outerArithmetic: str = "fp64", relaxFrom: int = 0) -> MGparam:
     """Positional forms of Multigrid.jl getMGparam:
     (TYPE, ITYPE, levels, numCores, maxIter, relativeTol, relaxType, relaxParam,
      relaxPre, relaxPost, cycleType, coarseSolveType[, low, high[, transferType]])
@@ -401,12 +403,16 @@ def getMGparam(*args, transferType: str | None = None, precision: str = "fp64",
     mg = MGparam(int(levels), int(numCores), int(maxIter), float(tol), str(relaxType), float(relaxParam), pre, post,
                  str(cycle), str(coarse), float(low), float(high), str(tt), precision, coarseOperator,
                  outerArithmetic)
+    mg.relaxFrom = int(relaxFrom)
     return mg
 
 
 def _validate_mg(MG: MGparam):
-    if MG.relaxType != "Jac":
-        raise NotImplementedError(f"relaxType {MG.relaxType!r}: only damped Jacobi ('Jac') is built")
+    if MG.relaxType not in ("Jac", "Jac-GMRES"):
+        raise NotImplementedError(f"relaxType {MG.relaxType!r}: damped Jacobi ('Jac') and 'Jac-GMRES' are built")
+    if MG.relaxType == "Jac-GMRES" and os.environ.get("HELMGPU_ENABLE_JAC_GMRES") != "1":
+        raise NotImplementedError("relaxType 'Jac-GMRES' awaits its GPU parity test "
+                                  "(set HELMGPU_ENABLE_JAC_GMRES=1 to run it)")
     if MG.cycleType not in ("V", "W", "K"):
         raise NotImplementedError(f"cycleType {MG.cycleType!r}: only 'V', 'W' and 'K' cycles are built")
     if MG.coarseSolveType not in _SUPPORTED_COARSE:
@@ -498,6 +504,8 @@ def _options(s: ShiftedLaplacianMultigridSolver) -> L.hz_options:
     o.outer_arith = L.HZ_OUTER_EMULATED if MG.outerArithmetic == "emulated" else L.HZ_OUTER_FP64
     o.cuda_graph = int(bool(MG.cudaGraph))
     o.autotune = int(bool(MG.autotune))
+    o.relax_type = L.HZ_RELAX_JAC_GMRES if MG.relaxType == "Jac-GMRES" else L.HZ_RELAX_JAC
+    o.relax_from = int(MG.relaxFrom)
     o.verbose = int(bool(s.verbose))
     return o
 
@@ -512,7 +520,7 @@ def _ensure_handle(s: ShiftedLaplacianMultigridSolver):
     key = (dev, id(s.helmParam), id(s.helmParam.m), id(s.helmParam.gamma), s.MG.levels, s.MG.maxOuterIter,
            s.MG.relativeTol, s.MG.relaxParam, int(s.MG.relaxPre), int(s.MG.relaxPost), s.MG.cycleType,
            s.MG.precision, s.inner, float(s.shift[0]), s.Krylov, s.MG.coarseOperator, s.MG.outerArithmetic,
-           bool(s.MG.cudaGraph), bool(s.MG.autotune))
+           bool(s.MG.cudaGraph), bool(s.MG.autotune), s.MG.relaxType, int(s.MG.relaxFrom))
     if s._handle is not None and s._key == key:
         return s._handle
     _release(s)

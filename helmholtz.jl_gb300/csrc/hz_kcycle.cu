@@ -1,7 +1,9 @@
 // K-cycle coarse-grid correction: two steps of FGMRES on a coarse level's
 // operator, right-preconditioned by that level's own cycle, for a block of
 // columns at once (the Krylov-accelerated cycle Multigrid.jl offers as
-// cycleType 'K', used by test/ShiftedLaplacianTest.jl:137-140).
+// cycleType 'K', used by test/ShiftedLaplacianTest.jl:137-140).  The same
+// kernels run the "Jac-GMRES" smoother (relaxType of that test, :138): one or
+// two GMRES steps preconditioned by a damped-Jacobi sweep, added to the iterate.
 //
 // Per column c the scalars live on the device in ks[c*8 + slot]:
 //   0 beta^2 (real), 1 h00, 2 h10^2 (real), 3 h01, 4 h11, 5 h21^2 (real), 6 y0, 7 y1.
@@ -105,6 +107,20 @@ __global__ void __launch_bounds__(256) k_kc_scale(long long N, long long ld, con
     Y[off + p] = cscale<T>(s, X[off + p]);
 }
 
+// X += y0 Z0 + y1 Z1 (the GMRES smoothing update of the current iterate)
+template <typename T>
+__global__ void __launch_bounds__(256) k_kc_combine_add(long long N, long long ld, const int* __restrict__ cols,
+                                                        const double2* __restrict__ ks,
+                                                        const cplx<T>* __restrict__ Z0,
+                                                        const cplx<T>* __restrict__ Z1, cplx<T>* __restrict__ X) {
+  const int c = cols[blockIdx.y];
+  const double2 y0d = ks[c * 8 + 6], y1d = ks[c * 8 + 7];
+  const cplx<T> y0 = mk<T>((T)y0d.x, (T)y0d.y), y1 = mk<T>((T)y1d.x, (T)y1d.y);
+  const long long off = (long long)c * ld;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (long long)gridDim.x * blockDim.x)
+    X[off + p] = cfma<T>(y1, Z1[off + p], cfma<T>(y0, Z0[off + p], X[off + p]));
+}
+
 // X = y0 Z0 + y1 Z1
 template <typename T>
 __global__ void __launch_bounds__(256) k_kc_combine(long long N, long long ld, const int* __restrict__ cols,
@@ -148,6 +164,20 @@ __global__ void k_kc_lsq(const int* __restrict__ cols, int nc, double2* __restri
   }
   s[6] = y0;
   s[7] = y1;
+}
+
+// One GMRES step: min || beta e0 - [h00; h10] y0 || = conj(h00) beta / (|h00|^2 + h10^2); y1 = 0.
+__global__ void k_kc_lsq1(const int* __restrict__ cols, int nc, double2* __restrict__ ks) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  double2* s = ks + cols[i] * 8;
+  const double beta = sqrt(fmax(s[0].x, 0.0));
+  const double2 a = s[1];
+  const double den = a.x * a.x + a.y * a.y + fmax(s[2].x, 0.0);
+  double2 y0 = make_double2(0.0, 0.0);
+  if (beta > 0.0 && den > 0.0) y0 = make_double2(a.x * beta / den, -a.y * beta / den);
+  s[6] = y0;
+  s[7] = make_double2(0.0, 0.0);
 }
 
 static int kc_nblk(long long N) {
@@ -194,6 +224,18 @@ void launch_kc_lsq(Ctx& ctx, const int* cols, int nc, double2* ks) {
   HZ_LAUNCH(ctx, "kcycle_lsq", (double)nc * 8 * 16, k_kc_lsq, (nc + 127) / 128, 128, 0, cols, nc, ks);
 }
 
+void launch_kc_lsq1(Ctx& ctx, const int* cols, int nc, double2* ks) {
+  HZ_LAUNCH(ctx, "smooth_lsq", (double)nc * 8 * 16, k_kc_lsq1, (nc + 127) / 128, 128, 0, cols, nc, ks);
+}
+
+template <typename T>
+void launch_kc_combine_add(Ctx& ctx, long long N, long long ld, const int* cols, int nc, const double2* ks,
+                           const cplx<T>* Z0, const cplx<T>* Z1, cplx<T>* X) {
+  const int nblk = kc_nblk(N);
+  HZ_LAUNCH(ctx, "smooth_update", (double)N * nc * 4 * sizeof(cplx<T>), k_kc_combine_add<T>, dim3(nblk, nc), 256, 0,
+            N, ld, cols, ks, Z0, Z1, X);
+}
+
 int kcycle_nblk(long long N) { return kc_nblk(N); }
 
 #define HZ_KC_INST(T)                                                                                                \
@@ -204,7 +246,9 @@ int kcycle_nblk(long long N) { return kc_nblk(N); }
   template void launch_kc_scale<T>(Ctx&, long long, long long, const int*, int, const double2*, int, const cplx<T>*, \
                                    cplx<T>*);                                                                        \
   template void launch_kc_combine<T>(Ctx&, long long, long long, const int*, int, const double2*, const cplx<T>*,    \
-                                     const cplx<T>*, cplx<T>*);
+                                     const cplx<T>*, cplx<T>*);                                                      \
+  template void launch_kc_combine_add<T>(Ctx&, long long, long long, const int*, int, const double2*,                \
+                                         const cplx<T>*, const cplx<T>*, cplx<T>*);
 HZ_KC_INST(float)
 HZ_KC_INST(double)
 #undef HZ_KC_INST

@@ -165,6 +165,11 @@ void launch_kc_combine(Ctx& ctx, long long N, long long ld, const int* cols, int
                        const cplx<T>* Z0, const cplx<T>* Z1, cplx<T>* X);
 // the 3x2 least-squares problem of each column -> y0, y1
 void launch_kc_lsq(Ctx& ctx, const int* cols, int nc, double2* ks);
+// one-step least squares (y0 from slots 0-2, y1 = 0) and X += y0 Z0 + y1 Z1 (GMRES smoothing)
+void launch_kc_lsq1(Ctx& ctx, const int* cols, int nc, double2* ks);
+template <typename T>
+void launch_kc_combine_add(Ctx& ctx, long long N, long long ld, const int* cols, int nc, const double2* ks,
+                           const cplx<T>* Z0, const cplx<T>* Z1, cplx<T>* X);
 
 // ---- setup kernels ---------------------------------------------------------
 // Fine-level diagonals on the device from nodal m and gamma (device arrays):

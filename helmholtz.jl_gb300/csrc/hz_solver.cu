@@ -17,6 +17,7 @@
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -111,6 +112,9 @@ struct Level {
   DBuf x, t, r, b;
   // K-cycle on this level: V0, V1, Z0, Z1, W blocks, per-column scalars, partial sums
   DBuf kv, ks, kp;
+  // GMRES smoothing ("Jac-GMRES") on this level: the same layout, own storage (the
+  // smoother runs inside the K-cycle's cycles on the same level)
+  DBuf gv, gs, gp;
 };
 
 struct Hierarchy {
@@ -622,6 +626,11 @@ void ensure_level_buffers(hz_handle* h, Hierarchy& H, int R) {
       L.ks.alloc((size_t)R * 8 * 16);
       L.kp.alloc((size_t)R * 3 * kcycle_nblk(L.g.N) * 16);
     }
+    if (h->opt.relax_type == HZ_RELAX_JAC_GMRES && (int)l >= h->opt.relax_from && l + 1 < H.lv.size()) {
+      L.gv.alloc(5 * bytes);
+      L.gs.alloc((size_t)R * 8 * 16);
+      L.gp.alloc((size_t)R * 3 * kcycle_nblk(L.g.N) * 16);
+    }
   }
   // band work: 3 vectors per column; the dense product's split-K partials need
   // splits(ncols) * ncols vectors, largest over the active column counts
@@ -753,6 +762,62 @@ void capture_rhs(hz_handle* h, Level& L, const cplx<TB>* b, const int* cols, int
   }
 }
 
+// x += the relaxType "Jac-GMRES" smoothing step on level l: `steps` (1 or 2)
+// Arnoldi steps of GMRES on the level's operator from the current x,
+// right-preconditioned by one damped-Jacobi sweep (Z_j = w D^-1 V_j), and the
+// least-squares update x += sum_j y_j Z_j per column.  The K-cycle's kernels
+// with the smoother's own buffers; a column with zero residual is unchanged.
+template <typename T, typename TB>
+void gmres_smooth(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* x, const int* cols, int nc,
+                  int steps) {
+  Level& L = *H.lv[l];
+  Ctx& c = h->ctx;
+  const long long N = L.g.N, ld = L.ld, vs = (long long)h->rcap * ld;
+  cplx<T>* base = L.gv.as<cplx<T>>();
+  if (!base || !L.gs.p || !L.gp.p) fail(HZ_ERR_STATE, "internal: GMRES smoothing buffers missing on level %d", l);
+  cplx<T>* V0 = base;
+  cplx<T>* V1 = base + vs;
+  cplx<T>* Z0 = base + 2 * vs;
+  cplx<T>* Z1 = base + 3 * vs;
+  cplx<T>* W = base + 4 * vs;
+  double2* ks = L.gs.as<double2>();
+  double2* part = L.gp.as<double2>();
+  const cplx<T>* none = nullptr;
+  lev_op<T, TB>(h, H, l, MODE_RESID, x, b, W, cols, nc);                    // W = b - A x
+  launch_kc_sums<T>(c, N, ld, cols, nc, 0, 1, none, none, W, part, ks, 0);  // beta^2
+  launch_kc_scale<T>(c, N, ld, cols, nc, ks, 0, W, V0);
+  lev_jacobi0<T, T>(h, H, l, V0, Z0, cols, nc);                              // Z0 = w D^-1 V0
+  lev_op<T, T>(h, H, l, MODE_APPLY, Z0, none, W, cols, nc);
+  launch_kc_sums<T>(c, N, ld, cols, nc, 1, 0, V0, none, W, part, ks, 1);     // h00
+  launch_kc_update<T>(c, N, ld, cols, nc, 1, 1, ks, V0, none, W, part, 2);   // W -= h00 V0, h10^2
+  if (steps == 1) {
+    launch_kc_lsq1(c, cols, nc, ks);
+    launch_kc_combine_add<T>(c, N, ld, cols, nc, ks, Z0, Z0, x);  // y1 = 0
+    return;
+  }
+  launch_kc_scale<T>(c, N, ld, cols, nc, ks, 2, W, V1);
+  lev_jacobi0<T, T>(h, H, l, V1, Z1, cols, nc);                              // Z1 = w D^-1 V1
+  lev_op<T, T>(h, H, l, MODE_APPLY, Z1, none, W, cols, nc);
+  launch_kc_sums<T>(c, N, ld, cols, nc, 2, 0, V0, V1, W, part, ks, 3);       // h01, h11
+  launch_kc_update<T>(c, N, ld, cols, nc, 2, 3, ks, V0, V1, W, part, 5);     // h21^2
+  launch_kc_lsq(c, cols, nc, ks);
+  launch_kc_combine_add<T>(c, N, ld, cols, nc, ks, Z0, Z1, x);
+}
+
+// C.x = the coarse-grid correction of level l + 1 for the right-hand sides in C.b:
+// the network, a K-cycle step or a recursive cycle.
+template <typename T>
+void coarse_correction(hz_handle* h, Hierarchy& H, int l, const int* cols, int nc) {
+  Level& C = *H.lv[l + 1];
+  const int last = (int)H.lv.size() - 1;
+  if (h->net_active && l + 1 == h->net_level)
+    learned_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+  else if (h->opt.cycle == 'K' && l + 1 < last)
+    kcycle_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+  else
+    mg_cycle<T, T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+}
+
 // x_out = cycle(b) on level l with zero initial guess.
 template <typename T, typename TB>
 void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out, const int* cols, int nc) {
@@ -787,6 +852,19 @@ void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out
     oth = (cur == out) ? tb : out;
   }
   const int ncalls = (h->opt.cycle == 'W' && l + 1 < last) ? 2 : 1;
+  if (h->opt.relax_type == HZ_RELAX_JAC_GMRES && l >= h->opt.relax_from) {
+    // relaxType "Jac-GMRES": smoothing steps update `out` in place
+    launch_zero_cols<T>(h->ctx, L.g.N, out, L.ld, cols, nc);
+    if (pre > 0) gmres_smooth<T, TB>(h, H, l, b, out, cols, nc, pre);
+    for (int call = 0; call < ncalls; ++call) {
+      lev_op<T, TB>(h, H, l, MODE_RESID, out, b, rb, cols, nc);
+      launch_restrict<T>(h->ctx, L.g, C.g, rb, L.ld, C.b.as<cplx<T>>(), C.ld, cols, nc);
+      coarse_correction<T>(h, H, l, cols, nc);
+      launch_prolong<T>(h->ctx, L.g, C.g, C.x.as<cplx<T>>(), C.ld, out, out, L.ld, cols, nc);
+    }
+    if (post > 0) gmres_smooth<T, TB>(h, H, l, b, out, cols, nc, post);
+    return;
+  }
   bool zero_guess = true;
   if (pre > 0) {
     lev_jacobi0<T, TB>(h, H, l, b, cur, cols, nc);
@@ -809,12 +887,7 @@ void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out
       lev_op<T, TB>(h, H, l, MODE_RESID, cur, b, rb, cols, nc);
       launch_restrict<T>(h->ctx, L.g, C.g, rb, L.ld, C.b.as<cplx<T>>(), C.ld, cols, nc);
     }
-    if (h->net_active && l + 1 == h->net_level)
-      learned_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
-    else if (h->opt.cycle == 'K' && l + 1 < last)
-      kcycle_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
-    else
-      mg_cycle<T, T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
+    coarse_correction<T>(h, H, l, cols, nc);
     launch_prolong<T>(h->ctx, L.g, C.g, C.x.as<cplx<T>>(), C.ld, zero_guess ? nullptr : cur, cur, L.ld, cols, nc);
     zero_guess = false;
   }
@@ -1468,6 +1541,20 @@ void validate(const hz_problem* p, const hz_options* o) {
   if (o->outer_arith == HZ_OUTER_EMULATED && o->precision != HZ_PREC_MIXED)
     fail(HZ_ERR_ARG, "emulated-FP64 outer arithmetic is part of the mixed form (precision = HZ_PREC_MIXED)");
   if (!(o->rel_tol > 0)) fail(HZ_ERR_ARG, "rel_tol must be > 0");
+  if (o->relax_type != HZ_RELAX_JAC && o->relax_type != HZ_RELAX_JAC_GMRES)
+    fail(HZ_ERR_ARG, "relax_type must be HZ_RELAX_JAC or HZ_RELAX_JAC_GMRES");
+  if (o->relax_type == HZ_RELAX_JAC_GMRES) {
+    if (o->krylov != HZ_KRYLOV_FGMRES)
+      fail(HZ_ERR_ARG, "the Jac-GMRES smoother makes the cycle nonlinear: it needs FGMRES");
+    if (o->relax_pre < 0 || o->relax_pre > 2 || o->relax_post < 0 || o->relax_post > 2)
+      fail(HZ_ERR_ARG, "Jac-GMRES takes 0, 1 or 2 GMRES steps per smoothing (relax_pre, relax_post)");
+    if (o->relax_from < 0 || o->relax_from >= o->levels) fail(HZ_ERR_ARG, "relax_from must be in [0, levels - 1]");
+    // built and compiled, switched on once its GPU parity test has run
+    const char* on = std::getenv("HELMGPU_ENABLE_JAC_GMRES");
+    if (!on || std::strcmp(on, "1") != 0)
+      fail(HZ_ERR_ARG, "relax_type HZ_RELAX_JAC_GMRES awaits its GPU parity test "
+                       "(set HELMGPU_ENABLE_JAC_GMRES=1 to run it)");
+  }
 }
 
 void copy_in(hz_handle* h, const double* src, double2* dst, long long N, int nrhs, int mem) {

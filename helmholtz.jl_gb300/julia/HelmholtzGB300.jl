@@ -60,9 +60,11 @@ mutable struct HzOptions
     outer_arith::Int32
     cuda_graph::Int32
     autotune::Int32
-    reserved::NTuple{4,Int32}
+    relax_type::Int32
+    relax_from::Int32
+    reserved::NTuple{2,Int32}
 end
-HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 4))
+HzOptions() = HzOptions(0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, ntuple(_ -> Int32(0), 2))
 
 mutable struct HzStats
     outer::Int32

@@ -55,6 +55,11 @@ extern "C" {
 #define HZ_COARSE_GALERKIN 0     /* A_{l+1} = R A_l P (reference default RAP path) */
 #define HZ_COARSE_REDISCRETIZE 1 /* re-assembled 5/7-point operator from restricted m, gamma */
 
+/* smoother (Multigrid.jl relaxType) */
+#define HZ_RELAX_JAC 0       /* "Jac": relax_pre / relax_post damped-Jacobi sweeps */
+#define HZ_RELAX_JAC_GMRES 1 /* "Jac-GMRES": relax_pre / relax_post (1 or 2) GMRES steps preconditioned by one
+                                damped-Jacobi sweep, on the levels >= relax_from (finer levels: "Jac") */
+
 #define HZ_OP_H 0  /* Helmholtz operator H */
 #define HZ_OP_SH 1 /* shifted operator SH = H + i*shift*w^2*diag(m) */
 
@@ -97,7 +102,9 @@ typedef struct hz_options {
   int32_t outer_arith;   /* FGMRES outer arithmetic: HZ_OUTER_FP64 (native) or HZ_OUTER_EMULATED */
   int32_t cuda_graph;    /* 1 (default): replay each FGMRES preconditioner application from a CUDA graph */
   int32_t autotune;      /* 1 (default): time the stencils' launch shapes at the first solve (see hz_tune_info) */
-  int32_t reserved[4];
+  int32_t relax_type;    /* HZ_RELAX_* (default HZ_RELAX_JAC) */
+  int32_t relax_from;    /* HZ_RELAX_JAC_GMRES: first level smoothed by GMRES steps (0: every level) */
+  int32_t reserved[2];
 } hz_options;
 
 typedef struct hz_stats {

@@ -184,3 +184,50 @@ def test_handles_follow_the_selected_device(hz, monkeypatch):
     assert api.current_device() == 0
     monkeypatch.delitem(sys.modules, "torch")
     assert api.current_device() == 0 and api._default_options().device == 0
+
+
+def test_jac_gmres_option_checks_and_gate(hz, monkeypatch):
+    """relax_type HZ_RELAX_JAC_GMRES: its argument checks run before any device
+    work, and until its GPU parity test has run the option is refused unless
+    HELMGPU_ENABLE_JAC_GMRES=1 (then creation proceeds to the device check)."""
+    L = hz._lib
+    lib = L.load()
+    m = np.ones(81)
+    g = np.zeros(81)
+    p = L.hz_problem()
+    p.dim, p.n[0], p.n[1], p.h[0], p.h[1], p.omega_re = 2, 8, 8, 0.125, 0.125, 2.0
+    p.m = m.ctypes.data_as(C.POINTER(C.c_double))
+    p.gamma = g.ctypes.data_as(C.POINTER(C.c_double))
+    p.order_neumann_bc = 2
+
+    def create(**kw):
+        o = L.hz_options()
+        lib.hz_default_options(C.byref(o))
+        o.relax_type, o.cycle = L.HZ_RELAX_JAC_GMRES, ord("K")
+        for k, v in kw.items():
+            setattr(o, k, v)
+        h = C.c_void_p()
+        st = lib.hz_create(C.byref(p), C.byref(o), C.byref(h))
+        if st == L.HZ_OK:
+            lib.hz_destroy(h)
+        return st, (lib.hz_last_error(None) or b"").decode()
+
+    monkeypatch.delenv("HELMGPU_ENABLE_JAC_GMRES", raising=False)
+    st, msg = create()
+    assert st == L.HZ_ERR_ARG and "parity test" in msg
+    monkeypatch.setenv("HELMGPU_ENABLE_JAC_GMRES", "1")
+    assert create()[0] in (L.HZ_OK, L.HZ_ERR_NO_DEVICE)
+    assert create(relax_from=1)[0] in (L.HZ_OK, L.HZ_ERR_NO_DEVICE)
+    for bad in (dict(krylov=L.HZ_KRYLOV_BICGSTAB, cycle=ord("V")), dict(relax_pre=3), dict(relax_post=-1),
+                dict(relax_from=3), dict(relax_from=-1), dict(relax_type=2)):
+        assert create(**bad)[0] == L.HZ_ERR_ARG, bad
+    # the Python layer maps the option and keeps the same gate
+    MG = hz.getMGparam(complex, int, 3, 1, 50, 1e-8, "Jac-GMRES", 0.8, 2, 2, "K", "Julia", relaxFrom=1)
+    S = hz.getShiftedLaplacianMultigridSolver(hz.HelmholtzParam(hz.getRegularMesh([0.0, 1.0, 0.0, 1.0], [8, 8]),
+                                                                g, m, 2.0, True, True), MG, 0.5, "GMRES", 10)
+    o = hz.api._options(S)
+    assert (o.relax_type, o.relax_from, o.relax_pre) == (L.HZ_RELAX_JAC_GMRES, 1, 2)
+    assert hz.copySolver(S).MG.relaxFrom == 1
+    monkeypatch.delenv("HELMGPU_ENABLE_JAC_GMRES")
+    with pytest.raises(NotImplementedError):
+        hz.solveLinearSystem(None, np.ones(81), S)
