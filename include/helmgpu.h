@@ -87,8 +87,8 @@ typedef struct hz_options {
   int32_t levels;        /* multigrid levels (>= 1) */
   int32_t max_outer;     /* MGparam.maxOuterIter: FGMRES restart cycles */
   double rel_tol;        /* relative residual ||b - H x|| / ||b|| per column */
-  int32_t relax_pre;     /* Jacobi sweeps before the coarse correction */
-  int32_t relax_post;    /* Jacobi sweeps after the coarse correction */
+  int32_t relax_pre;     /* Jacobi sweeps (HZ_RELAX_JAC_GMRES: GMRES steps) before the coarse correction */
+  int32_t relax_post;    /* Jacobi sweeps (HZ_RELAX_JAC_GMRES: GMRES steps) after the coarse correction */
   double relax_param;    /* Jacobi damping w */
   int32_t cycle;         /* 'V', 'W' or 'K' (K: two FGMRES steps per coarse level; FGMRES outer only) */
   int32_t krylov;        /* HZ_KRYLOV_* */
