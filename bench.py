@@ -278,6 +278,7 @@ def run_ours(args, rank, ws, dist):
         o.coarse_op = L.HZ_COARSE_REDISCRETIZE if args.coarse == "rediscretize" else L.HZ_COARSE_GALERKIN
         o.relax_type = L.HZ_RELAX_JAC_GMRES if args.relax == "jac-gmres" else L.HZ_RELAX_JAC
         o.relax_from = args.relax_from
+        o.shift = args.shift
         o.cuda_graph = 0 if args.no_graph else 1
         o.autotune = 0 if args.no_tune else 1
         if args.krylov == "bicgstab":
@@ -413,7 +414,7 @@ def run_learned(args, rank, ws, dist):
                            "Julia", 0.5, 0.0, precision=precision, outerArithmetic=outer,
                            coarseOperator="Rediscretize" if args.coarse == "rediscretize" else "Galerkin",
                            relaxFrom=args.relax_from)
-        return hz.getShiftedLaplacianMultigridSolver(param, MG, 0.5, "GMRES", 10)
+        return hz.getShiftedLaplacianMultigridSolver(param, MG, args.shift, "GMRES", 10)
 
     # 1. training pairs from the FP64 solver on seeded training models
     t0 = time.perf_counter()
@@ -497,7 +498,7 @@ def run_learned(args, rank, ws, dist):
 
 
 def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: str = "V",
-                   coarse: str = "galerkin", relax: str = "jac", relax_from: int = 0):
+                   coarse: str = "galerkin", relax: str = "jac", relax_from: int = 0, shift: float = 0.5):
     """C oracle (threaded CSR SLMG, plain FP64) on a bounded sample of the
     workload: the full grid and operator, a few of its right-hand sides, with
     the GPU arm's cycle, coarse operators (Galerkin or re-discretised) and
@@ -509,10 +510,10 @@ def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: st
     M = O.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
     gam = gam_fn()
     H = O.GetHelmholtzOperator(M, P["m"], P["w"], gam, True, True)
-    SH = (H + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    SH = (H + O.GetHelmholtzShiftOP(P["m"], P["w"], shift)).tocsr()
     hier = None
     if coarse == "rediscretize":
-        hier = O.build_hierarchy_rediscretized(M, P["m"], gam, P["w"], 0.5, True, True, wl["levels"])
+        hier = O.build_hierarchy_rediscretized(M, P["m"], gam, P["w"], shift, True, True, wl["levels"])
     cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"], hier=hier)
     B = sources(P, wl["nrhs"], seed=0)
     ncols = 1
@@ -557,6 +558,7 @@ def main():
                     help="smoother: damped Jacobi, or GMRES steps preconditioned by a Jacobi sweep (relaxType "
                          "'Jac-GMRES'; on the GPU it needs HELMGPU_ENABLE_JAC_GMRES=1 until its parity test has run)")
     ap.add_argument("--relax-from", type=int, default=0, help="jac-gmres: first level smoothed by GMRES steps")
+    ap.add_argument("--shift", type=float, default=0.5, help="s of the shifted operator SH = H + i s w^2 diag(m)")
     ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
     ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
     ap.add_argument("--pairs-per-model", type=int, default=200)
@@ -582,14 +584,16 @@ def main():
         cs = None
         for i in range(args.warmup + args.steps):
             cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps), cycle=args.cycle,
-                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from)
+                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from,
+                                shift=args.shift)
             if i >= args.warmup:
                 vals.append(cs["value"])
         v = float(np.mean(vals))
         line = dict(metric=METRIC, value=v, unit="RHS/s", impl="reference", n_gpus=args.gpus, steps=args.steps,
                     warmup=args.warmup, higher_is_better=True, dtype="c128",
                     config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], cycle=args.cycle,
-                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from),
+                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from,
+                                shift=args.shift),
                     cpu_baseline=dict(value=v, unit="RHS/s", cores=cs["cores"], kind="port", sample=cs["sample"]),
                     e2e=dict(value=v, unit="RHS/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
                     note="reference path = the C oracle port of the Julia SLMG (Julia and Multigrid.jl are absent)")
@@ -610,7 +614,8 @@ def main():
                     data="synthetic (seeded layered+inclusion models, random source positions)",
                     config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
                                 krylov="FGMRES(10)", cycle=args.cycle, coarse=args.coarse, relax=args.relax,
-                                relax_from=args.relax_from, outer_arithmetic=args.outer, learned=True,
+                                relax_from=args.relax_from, shift=args.shift, outer_arithmetic=args.outer,
+                                learned=True,
                                 net_level=args.net_level if args.net_level > 0 else wl["net_level"],
                                 stag_ratio=args.stag_ratio,
                                 step="solver setup + solve of one held-out model's right-hand sides",
@@ -655,7 +660,7 @@ def main():
         hz = ge.load_package()
         gam = gamma_of(P, wl["pad"], None, hz)
         cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget, cycle=args.cycle, coarse=args.coarse,
-                             relax=args.relax, relax_from=args.relax_from)
+                             relax=args.relax, relax_from=args.relax_from, shift=args.shift)
     plain = results.get("fp64")
     line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
@@ -665,7 +670,7 @@ def main():
                 data="synthetic (seeded layered model)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
                             krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB", cycle=args.cycle,
-                            coarse=args.coarse, relax=args.relax, relax_from=args.relax_from,
+                            coarse=args.coarse, relax=args.relax, relax_from=args.relax_from, shift=args.shift,
                             cuda_graph=not args.no_graph, autotune=not args.no_tune,
                             outer_arithmetic=args.outer,
                             precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
