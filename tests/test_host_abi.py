@@ -231,3 +231,20 @@ def test_jac_gmres_option_checks_and_gate(hz, monkeypatch):
     monkeypatch.delenv("HELMGPU_ENABLE_JAC_GMRES")
     with pytest.raises(NotImplementedError):
         hz.solveLinearSystem(None, np.ones(81), S)
+
+
+def test_3d_sommerfeld_and_mass_match_oracle(hz, O):
+    """3D: the library's Sommerfeld rows (both top-face rules) against the golden
+    vectors, and its mass term with the absorbing layer against the oracle."""
+    g = np.load(GOLD)
+    M3 = hz.getRegularMesh([0.0, 1.5, 0.0, 1.0, 0.0, 2.0], [6, 4, 8])
+    Mo = O.getRegularMesh([0.0, 1.5, 0.0, 1.0, 0.0, 2.0], [6, 4, 8])
+    m3, w3 = g["m3"], float(g["w3"])
+    for neu in (0, 1):
+        s = hz.getSommerfeldBC(M3, m3, w3, bool(neu)).ravel(order="F")
+        np.testing.assert_allclose(s, g[f"somm3_neu{neu}"], rtol=1e-15, atol=0)
+        np.testing.assert_array_equal(O.getSommerfeldBC(Mo, m3, w3, bool(neu)).ravel(order="F"), g[f"somm3_neu{neu}"])
+    for neu, somm in ((False, True), (True, True), (True, False)):
+        p = hz.HelmholtzParam(M3, g["gamma3"], m3, w3, neu, somm)
+        np.testing.assert_allclose(hz.helmholtz_mass(p), O.helmholtz_mass(Mo, m3, w3, g["gamma3"], neu, somm),
+                                   rtol=1e-14, atol=0)
