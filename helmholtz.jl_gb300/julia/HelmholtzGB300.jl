@@ -91,6 +91,8 @@ const HZ_KRYLOV_FGMRES = Int32(0)
 const HZ_KRYLOV_BICGSTAB = Int32(1)
 const HZ_COARSE_GALERKIN = Int32(0)
 const HZ_COARSE_REDISCRETIZE = Int32(1)
+const HZ_RELAX_JAC = Int32(0)
+const HZ_RELAX_JAC_GMRES = Int32(1)
 
 lasterror(h::Ptr{Cvoid}) = unsafe_string(ccall((:hz_last_error, libhelmgpu), Cstring, (Ptr{Cvoid},), h))
 function check(st::Integer, h::Ptr{Cvoid} = C_NULL)
@@ -163,6 +165,7 @@ mutable struct ShiftedLaplacianMultigridSolver <: AbstractSolver   # src/Shifted
     precision::Int32            # HZ_PREC_FP64 (plain) or HZ_PREC_MIXED
     outerArith::Int32           # HZ_OUTER_FP64 or HZ_OUTER_EMULATED (mixed form only)
     coarseOp::Int32             # HZ_COARSE_GALERKIN or HZ_COARSE_REDISCRETIZE
+    relaxFrom::Int32            # relaxType "Jac-GMRES": first level smoothed by GMRES steps
     handle::Ptr{Cvoid}
     net::Any                    # attached CoarseNet (or nothing), its level and stagnation ratio
     netLevel::Int32
@@ -172,9 +175,9 @@ end
 function getShiftedLaplacianMultigridSolver(helmParam::HelmholtzParam, MG::MGparam, shift::Array{Float64},
                                             Krylov::String = "BiCGSTAB", inner::Int64 = 5, verbose::Bool = false;
                                             precision::Int32 = HZ_PREC_FP64, outerArith::Int32 = HZ_OUTER_FP64,
-                                            coarseOp::Int32 = HZ_COARSE_GALERKIN)
+                                            coarseOp::Int32 = HZ_COARSE_GALERKIN, relaxFrom::Int32 = Int32(0))
     s = ShiftedLaplacianMultigridSolver(helmParam, MG, shift, Krylov, inner, 0, verbose, 0.0, 0, 0.0, precision,
-                                        outerArith, coarseOp, C_NULL, nothing, Int32(0), 0.95)
+                                        outerArith, coarseOp, relaxFrom, C_NULL, nothing, Int32(0), 0.95)
     finalizer(release!, s)
     return s
 end
@@ -190,7 +193,8 @@ end
 
 function options(s::ShiftedLaplacianMultigridSolver)
     MG = s.MG
-    MG.relaxType == "Jac" || throw(ArgumentError("relaxType $(MG.relaxType): only \"Jac\" is built"))
+    MG.relaxType in ("Jac", "Jac-GMRES") ||
+        throw(ArgumentError("relaxType $(MG.relaxType): \"Jac\" and \"Jac-GMRES\" are built"))
     MG.cycleType in ('V', 'W', 'K') ||
         throw(ArgumentError("cycleType $(MG.cycleType): only 'V', 'W' and 'K' are built"))
     s.Krylov in ("GMRES", "BiCGSTAB") ||
@@ -209,6 +213,8 @@ function options(s::ShiftedLaplacianMultigridSolver)
     o.precision = s.precision
     o.outer_arith = s.outerArith
     o.coarse_op = s.coarseOp
+    o.relax_type = MG.relaxType == "Jac-GMRES" ? HZ_RELAX_JAC_GMRES : HZ_RELAX_JAC
+    o.relax_from = s.relaxFrom
     o.krylov = s.Krylov == "BiCGSTAB" ? HZ_KRYLOV_BICGSTAB : HZ_KRYLOV_FGMRES
     o.verbose = Int32(s.verbose)
     return o
@@ -264,7 +270,7 @@ end
 function copySolver(s::ShiftedLaplacianMultigridSolver)   # src/ShiftedLaplacianMultigridSolver.jl:18-22
     return getShiftedLaplacianMultigridSolver(s.helmParam, s.MG, s.shift, s.Krylov, s.inner, s.verbose;
                                               precision = s.precision, outerArith = s.outerArith,
-                                              coarseOp = s.coarseOp)
+                                              coarseOp = s.coarseOp, relaxFrom = s.relaxFrom)
 end
 
 function clear!(s::ShiftedLaplacianMultigridSolver)        # src/ShiftedLaplacianMultigridSolver.jl:105-109
