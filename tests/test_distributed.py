@@ -25,7 +25,7 @@ def _free_port():
     return port
 
 
-def _worker(rank, world, port, q):
+def _worker(rank, world, port, q, ncols=7):
     import sys
     from pathlib import Path
     root = Path(__file__).resolve().parent.parent
@@ -38,7 +38,7 @@ def _worker(rank, world, port, q):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     rng = np.random.default_rng(5)
-    B = rng.standard_normal((50, 7)) + 1j * rng.standard_normal((50, 7))
+    B = rng.standard_normal((50, ncols)) + 1j * rng.standard_normal((50, ncols))
     seen = []
 
     def fake_solve(Bs):  # stands in for the per-rank GPU solve; records its slice
@@ -48,7 +48,7 @@ def _worker(rank, world, port, q):
     X = solve_sharded(fake_solve, B, dist)
     if rank == 0:
         q.put(("x", np.abs(X - (2.0 - 1.0j) * B).max()))
-    q.put(("cols", rank, seen[0]))
+    q.put(("cols", rank, seen[0] if seen else 0))
     dist.barrier()
     dist.destroy_process_group()
 
@@ -69,3 +69,23 @@ def test_solve_sharded_gloo_world2(hz):
     assert xs and xs[0][1] == 0.0
     cols = sorted((m[1], m[2]) for m in msgs if m[0] == "cols")
     assert cols == [(0, 4), (1, 3)]
+
+
+def test_solve_sharded_gloo_world3_empty_slice(hz):
+    """Fewer columns than ranks: the rank with an empty slice does not call the
+    solve, sends nothing that lands in X, and rank 0 still assembles every column."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 3, port, q, 2)) for r in range(3)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    msgs = [q.get(timeout=10) for _ in range(4)]
+    xs = [m for m in msgs if m[0] == "x"]
+    assert xs and xs[0][1] == 0.0
+    cols = sorted((m[1], m[2]) for m in msgs if m[0] == "cols")
+    assert cols == [(0, 1), (1, 1), (2, 0)]
