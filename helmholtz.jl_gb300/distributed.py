@@ -1,9 +1,11 @@
 """Right-hand-side sharding across GPUs (one process per GPU).
 
 The columns of B are independent, so N ranks each solve a contiguous slice
-of the columns with their own replica of the operator and hierarchy; the only
-communication is the host-side gather of X (no collective on the data path).
-Works with any torch.distributed backend (NCCL between GPUs, gloo on CPU).
+of the columns with their own replica of the operator and hierarchy.  The
+only communication is one status flag per solve (so that a failed rank stops
+the others instead of leaving them in the gather) and the host-side gather of
+X; no collective touches the data path.  Works with any torch.distributed
+backend (NCCL between GPUs, gloo on CPU).
 """
 from __future__ import annotations
 
@@ -49,13 +51,36 @@ def gather_columns(X_local: np.ndarray, ncols: int, dist, group=None) -> np.ndar
     return X
 
 
+class ShardFailed(RuntimeError):
+    """Another rank's solve failed; this rank's slice was solved but not gathered."""
+
+
 def solve_sharded(solve, B: np.ndarray, dist, group=None) -> np.ndarray | None:
     """Solve the columns of B across the ranks of `group`: each rank calls
     solve(B[:, its slice]) (normally solveLinearSystem on its own GPU) and
-    rank 0 returns the gathered solution."""
+    rank 0 returns the gathered solution.
+
+    Before the gather every rank reports whether its solve succeeded (one
+    all-reduce of a status flag), so a failed rank does not leave the others
+    waiting in the gather: it re-raises its own exception and every other rank
+    raises ShardFailed."""
+    import torch
     world = dist.get_world_size(group)
     rank = dist.get_rank(group)
     a, b = partition_columns(B.shape[1], world)[rank]
-    X_local = solve(B[:, a:b]) if b > a else np.zeros((B.shape[0], 0), dtype=np.complex128)
-    X_local = np.asarray(X_local, dtype=np.complex128).reshape(B.shape[0], b - a)
+    err = None
+    try:
+        X_local = solve(B[:, a:b]) if b > a else np.zeros((B.shape[0], 0), dtype=np.complex128)
+        X_local = np.asarray(X_local, dtype=np.complex128).reshape(B.shape[0], b - a)
+    except Exception as e:  # reported to every rank below, then re-raised here
+        err = e
+        X_local = None
+    flag = torch.tensor([0.0 if err is None else 1.0], dtype=torch.float64)
+    if dist.get_backend(group) == "nccl":
+        flag = flag.cuda()
+    dist.all_reduce(flag, op=dist.ReduceOp.MAX, group=group)
+    if err is not None:
+        raise err
+    if float(flag.item()) > 0.0:
+        raise ShardFailed("column sharding: another rank's solve failed")
     return gather_columns(X_local, B.shape[1], dist, group)

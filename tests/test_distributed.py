@@ -89,3 +89,49 @@ def test_solve_sharded_gloo_world3_empty_slice(hz):
     assert xs and xs[0][1] == 0.0
     cols = sorted((m[1], m[2]) for m in msgs if m[0] == "cols")
     assert cols == [(0, 1), (1, 1), (2, 0)]
+
+
+def _failing_worker(rank, world, port, q):
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    sys.path.insert(0, str(root))
+    import torch.distributed as dist
+    import __graft_entry__ as ge
+    ge.load_package()
+    from helmholtz_jl_gb300.distributed import ShardFailed, solve_sharded
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    B = np.ones((20, 4), dtype=np.complex128)
+
+    def solve(Bs):  # rank 1's solve fails on the host (no GPU fault involved)
+        if rank == 1:
+            raise ValueError("injected failure")
+        return Bs
+
+    try:
+        solve_sharded(solve, B, dist)
+        q.put((rank, "returned"))
+    except ShardFailed:
+        q.put((rank, "ShardFailed"))
+    except ValueError as e:
+        q.put((rank, f"ValueError: {e}"))
+    dist.destroy_process_group()
+
+
+def test_failed_rank_does_not_hang_the_others(hz):
+    """A rank whose solve raises re-raises it; the others learn of it through the
+    status all-reduce before the gather and raise ShardFailed instead of waiting."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_failing_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    assert got == [(0, "ShardFailed"), (1, "ValueError: injected failure")]
