@@ -135,9 +135,10 @@ extern "C" int hz_helmholtz_mass(const hz_problem* pr, double* mass_out) {
   for (int64_t p = 0; p < N; ++p)
     M[p] = -w2 * pr->m[p] * cd(1.0, -pr->gamma[p] / pr->omega_re);
   if (pr->sommerfeld) {
+    // src/GetHelmholtz.jl:45 calls getSommerfeldBC without orderNeumannBC, so the
+    // boundary factor is its default BC = 2 (:222) whatever order the Laplacian uses
     std::vector<double> s((size_t)(2 * N));
-    int st = hz_sommerfeld(pr->dim, pr->n, pr->h, pr->m, pr->omega_re, pr->neumann_on_top,
-                           pr->order_neumann_bc == 1 ? 1 : 2, s.data());
+    int st = hz_sommerfeld(pr->dim, pr->n, pr->h, pr->m, pr->omega_re, pr->neumann_on_top, 2, s.data());
     if (st != HZ_OK) return st;
     const cd* S = reinterpret_cast<const cd*>(s.data());
     for (int64_t p = 0; p < N; ++p) M[p] -= S[p];

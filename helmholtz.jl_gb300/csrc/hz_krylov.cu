@@ -598,7 +598,10 @@ template void launch_bicg_xr<float>(Ctx&, long long, double2*, const float2*, co
 // Per node: Sommerfeld term summed over the boundary faces the node lies on
 // (top face skipped when NeumannOnTop; same face order as the host helper),
 // mass = -w^2 m (1 - i gamma / Re w) - Somm, diag(H) = Laplacian diagonal + mass,
-// diag(SH) = diag(H) + i s (Re w)^2 m, and 1/diag(SH).
+// diag(SH) = diag(H) + i s (Re w)^2 m, and 1/diag(SH).  BC is the Laplacian's
+// boundary-row factor (orderNeumannBC); the Sommerfeld term always takes the
+// factor 2, because src/GetHelmholtz.jl:45 calls getSommerfeldBC without the
+// order and its default is 2 (:222).
 __global__ void k_fine_setup(Grid g, int dim, double h0, double h1, double h2, double wr, double wi, double s,
                              double BC, int neumann_on_top, int sommerfeld, const double* __restrict__ m,
                              const double* __restrict__ gamma, double2* __restrict__ dH, double2* __restrict__ dSH,
@@ -616,22 +619,23 @@ __global__ void k_fine_setup(Grid g, int dim, double h0, double h1, double h2, d
   double mr = -(w2r * a - w2i * b) * mp;
   double mi = -(w2r * b + w2i * a) * mp;
   if (sommerfeld) {
-    // Somm += -i w (BC/h_d) sqrt(m) on each face; host order: 2D top, bottom, x-high, x-low;
-    // 3D top, bottom, y-low, y-high, x-low, x-high
+    // Somm += -i w (SB/h_d) sqrt(m) on each face, SB = 2; host order: 2D top, bottom,
+    // x-high, x-low; 3D top, bottom, y-low, y-high, x-low, x-high
+    const double SB = 2.0;
     const double sq = sqrt(mp);
     double si = 0.0;
     if (dim == 2) {
-      if (!neumann_on_top && j == 0) si += -wr * (BC / h1) * sq;
-      if (j == g.ny - 1) si += -wr * (BC / h1) * sq;
-      if (i == g.nx - 1) si += -wr * (BC / h0) * sq;
-      if (i == 0) si += -wr * (BC / h0) * sq;
+      if (!neumann_on_top && j == 0) si += -wr * (SB / h1) * sq;
+      if (j == g.ny - 1) si += -wr * (SB / h1) * sq;
+      if (i == g.nx - 1) si += -wr * (SB / h0) * sq;
+      if (i == 0) si += -wr * (SB / h0) * sq;
     } else {
-      if (!neumann_on_top && k == 0) si += -wr * (BC / h2) * sq;
-      if (k == g.nz - 1) si += -wr * (BC / h2) * sq;
-      if (j == 0) si += -wr * (BC / h1) * sq;
-      if (j == g.ny - 1) si += -wr * (BC / h1) * sq;
-      if (i == 0) si += -wr * (BC / h0) * sq;
-      if (i == g.nx - 1) si += -wr * (BC / h0) * sq;
+      if (!neumann_on_top && k == 0) si += -wr * (SB / h2) * sq;
+      if (k == g.nz - 1) si += -wr * (SB / h2) * sq;
+      if (j == 0) si += -wr * (SB / h1) * sq;
+      if (j == g.ny - 1) si += -wr * (SB / h1) * sq;
+      if (i == 0) si += -wr * (SB / h0) * sq;
+      if (i == g.nx - 1) si += -wr * (SB / h0) * sq;
     }
     mi -= si;
   }

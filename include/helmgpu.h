@@ -299,7 +299,9 @@ int hz_abl(int32_t dim, const int64_t* nodes, int32_t neumann_at_first_dim, cons
 int hz_sommerfeld(int32_t dim, const int64_t* n, const double* h, const double* m, double omega,
                   int32_t neumann_on_top, int32_t order_neumann_bc, double* somm_out);
 
-/* Diagonal of H (src/GetHelmholtz.jl:41-47): -w^2 m (1 - i gamma / Re w) - Somm. */
+/* Diagonal of H (src/GetHelmholtz.jl:41-47): -w^2 m (1 - i gamma / Re w) - Somm.
+ * Somm is getSommerfeldBC with its default order 2 whatever order_neumann_bc is:
+ * the reference calls it without the order (src/GetHelmholtz.jl:45). */
 int hz_helmholtz_mass(const hz_problem* prob, double* mass_out);
 
 /* getAcousticPointSource with getTopPointSrc / loc2cs (src/getPointSource.jl:63-111):

@@ -206,13 +206,17 @@ def getSommerfeldBC(M: RegularMesh, mNodal, omega: float, NeumannOnTop: bool, or
 
 def helmholtz_mass(M: RegularMesh, mNodal, omega, gamma, NeumannOnTop: bool, Sommerfeld: bool,
                    orderNeumannBC: int = 2) -> np.ndarray:
-    """Diagonal (mass) part of H, src/GetHelmholtz.jl:41-47, flattened column-major."""
+    """Diagonal (mass) part of H, src/GetHelmholtz.jl:41-47, flattened column-major.
+
+    orderNeumannBC does not reach the Sommerfeld term: src/GetHelmholtz.jl:45 calls
+    getSommerfeldBC(Msh, mNodal, real(omega), NeumannAtFirstDim) without it, so the
+    term takes getSommerfeldBC's default order 2 (:222) for either Laplacian."""
     m = np.asarray(mNodal, dtype=np.float64).ravel(order="F")
     g = np.asarray(gamma, dtype=np.float64).ravel(order="F")
     w = complex(omega)
     mass = -(w**2) * m * (1.0 - 1j * g / w.real)
     if Sommerfeld:
-        mass = mass - getSommerfeldBC(M, m, w.real, NeumannOnTop, orderNeumannBC).ravel(order="F")
+        mass = mass - getSommerfeldBC(M, m, w.real, NeumannOnTop).ravel(order="F")
     return mass
 
 

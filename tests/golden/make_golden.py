@@ -12,6 +12,7 @@ import sys
 from pathlib import Path
 
 import numpy as np
+import scipy.sparse as sp
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent / "oracle"))
@@ -42,6 +43,13 @@ def main():
     out["SHX2"] = SH @ X
     out["HadjX2"] = H.conj().T @ X
     out["Xsol2"] = O.direct_solve(H, X)
+    # orderNeumannBC = 1 with Sommerfeld on: first-order Laplacian rows, and the
+    # Sommerfeld term that src/GetHelmholtz.jl:45 builds with getSommerfeldBC's
+    # default order 2 (:222), assembled term by term here
+    L1 = O.getNodalLaplacianMatrix(M, 1).astype(np.complex128)
+    mass1 = -(w**2) * m * (1.0 - 1j * out["gamma2"] / w) - O.getSommerfeldBC(M, m, w, True, 2).ravel(order="F")
+    H1 = (L1 + sp.diags(mass1)).tocsr()
+    out["HX2_bc1"] = H1 @ X
     q, _ = O.getAcousticPointSource(M, np.complex128)
     out["q2"] = q
     # 3D: 6 x 4 x 8 cells on [0,1.5]x[0,1]x[0,2]

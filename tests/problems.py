@@ -36,6 +36,20 @@ def layered(nc, seed=1, pad=6, neumann=True, sommerfeld=True, ellipsoid=False, l
     return dict(M=M, m=m, w=w, gamma=np.ravel(g, order="F"), H=H, neumann=neumann, sommerfeld=sommerfeld)
 
 
+def operator_from_parts(P, order):
+    """H assembled term by term as src/GetHelmholtz.jl:36-49 writes it, without
+    the oracle's helmholtz_mass: the order-`order` nodal Laplacian, the mass
+    -w^2 m (1 - i gamma / Re w), and the Sommerfeld term of getSommerfeldBC called
+    with no order argument (:45), i.e. its default order 2 (:222)."""
+    import scipy.sparse as sp
+    M, m, w = P["M"], P["m"], P["w"]
+    L = O.getNodalLaplacianMatrix(M, order).astype(np.complex128)
+    mass = -(w**2) * m * (1.0 - 1j * P["gamma"] / np.real(w))
+    if P["sommerfeld"]:
+        mass = mass - O.getSommerfeldBC(M, m, np.real(w), P["neumann"], 2).ravel(order="F")
+    return (L + sp.diags(mass)).tocsr()
+
+
 def rhs(n, nrhs, seed=0):
     rng = np.random.default_rng(seed)
     return rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs))

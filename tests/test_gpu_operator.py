@@ -27,6 +27,9 @@ def test_apply_matches_golden_2d_3d(hz):
     assert _rel(H.H @ g["X2"], g["HadjX2"]) < TOL64
     SH = H + hz.GetHelmholtzShiftOP(g["m2"], w, 0.5)
     assert _rel(SH @ g["X2"], g["SHX2"]) < TOL64
+    # orderNeumannBC = 1 with Sommerfeld on (order-2 Sommerfeld term, src/GetHelmholtz.jl:45)
+    H1 = hz.GetHelmholtzOperator(hz.HelmholtzParam(M, gam, g["m2"], w, True, True), 1)
+    assert _rel(H1 @ g["X2"], g["HX2_bc1"]) < TOL64
     M3 = hz.getRegularMesh([0.0, 1.5, 0.0, 1.0, 0.0, 2.0], [6, 4, 8])
     w3 = float(g["w3"])
     H3, _ = hz.GetHelmholtzOperator(M3, g["m3"], w3, [], False, [2, 2, 3], 0.9 * w3, True)
@@ -34,20 +37,27 @@ def test_apply_matches_golden_2d_3d(hz):
     assert _rel(H3.H @ g["X3"], g["HadjX3"]) < TOL64
 
 
-@pytest.mark.parametrize("case", ["2d_neumann", "2d_dirichlet_somm", "3d", "3d_wide", "2d_bc1"])
+@pytest.mark.parametrize("case", ["2d_neumann", "2d_dirichlet_somm", "3d", "3d_wide", "2d_bc1", "2d_bc1_somm",
+                                  "3d_bc1_somm"])
 def test_apply_matches_oracle_sparse(hz, O, case):
     if case == "3d":
         P = PB.layered((20, 12, 16), seed=4, pad=3, ellipsoid=True)
     elif case == "3d_wide":
         # more than a warp of nodes along x, sizes that divide nothing evenly
         P = PB.layered((40, 18, 20), seed=4, pad=3, ellipsoid=True)
-    elif case == "2d_dirichlet_somm":
+    elif case == "3d_bc1_somm":
+        P = PB.layered((20, 12, 16), seed=6, pad=3, neumann=False, ellipsoid=True)
+    elif case in ("2d_dirichlet_somm", "2d_bc1_somm"):
         P = PB.gradient_2d((40, 24), pad=5, neumann=False, sommerfeld=True)
     else:
         P = PB.gradient_2d((40, 24), pad=5, neumann=True, sommerfeld=(case == "2d_neumann"))
-    order = 1 if case == "2d_bc1" else 2
+    order = 1 if "bc1" in case else 2
     Mo = P["M"]
     Ho = O.GetHelmholtzOperator(Mo, P["m"], P["w"], P["gamma"], P["neumann"], P["sommerfeld"], order)
+    if "bc1_somm" in case:
+        # the operator assembled term by term, not through the oracle's mass helper:
+        # first-order Laplacian rows, order-2 Sommerfeld term (src/GetHelmholtz.jl:45)
+        Ho = PB.operator_from_parts(P, order)
     p = PB.hz_param(hz, P)
     H = hz.GetHelmholtzOperator(p, order)
     X = PB.rhs(Ho.shape[0], 5, seed=11)

@@ -233,6 +233,19 @@ def test_jac_gmres_option_checks_and_gate(hz, monkeypatch):
         hz.solveLinearSystem(None, np.ones(81), S)
 
 
+@pytest.mark.parametrize("nc", [(24, 16), (8, 6, 10)])
+def test_mass_with_first_order_laplacian_keeps_order_two_sommerfeld(hz, O, nc):
+    """hz_helmholtz_mass for orderNeumannBC = 1: the Sommerfeld term is the BC = 2
+    one of src/GetHelmholtz.jl:45, the same as for orderNeumannBC = 2."""
+    import problems as PB
+    P = PB.layered(nc, seed=2, pad=2, neumann=False, ellipsoid=len(nc) == 3)
+    p = PB.hz_param(hz, P)
+    m1 = hz.helmholtz_mass(p, 1)
+    np.testing.assert_array_equal(m1, hz.helmholtz_mass(p, 2))
+    ref = PB.operator_from_parts(P, 1).diagonal() - O.getNodalLaplacianMatrix(P["M"], 1).diagonal()
+    np.testing.assert_allclose(m1, ref, rtol=1e-13, atol=0)
+
+
 def test_3d_sommerfeld_and_mass_match_oracle(hz, O):
     """3D: the library's Sommerfeld rows (both top-face rules) against the golden
     vectors, and its mass term with the absorbing layer against the oracle."""

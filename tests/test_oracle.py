@@ -59,6 +59,8 @@ def test_oracle_matches_golden(O):
     H, gam = O.GetHelmholtzOperatorABL(M, m, w, 0.01 * w * np.ones(m.size), True, [3, 2], 0.9 * w, True)
     np.testing.assert_array_equal(np.ravel(gam, order="F"), g["gamma2"])
     np.testing.assert_allclose(H @ g["X2"], g["HX2"], rtol=0, atol=1e-12 * np.abs(g["HX2"]).max())
+    H1 = O.GetHelmholtzOperator(M, m, w, gam, True, True, 1)
+    np.testing.assert_allclose(H1 @ g["X2"], g["HX2_bc1"], rtol=0, atol=1e-12 * np.abs(g["HX2_bc1"]).max())
     M3 = O.getRegularMesh([0.0, 1.5, 0.0, 1.0, 0.0, 2.0], [6, 4, 8])
     for neu in (0, 1):
         np.testing.assert_array_equal(O.getABL(M3.n + 1, bool(neu), [2, 2, 3], 0.9 * float(g["w3"])).ravel(order="F"),
@@ -199,6 +201,22 @@ def test_laplacian_rows_follow_reference_boundary_rule(O):
     np.testing.assert_allclose(D[2, 1:4] * h2, [-1, 2, -1])
     D1 = O.dxxMat(5, 0.5, 1).toarray()
     np.testing.assert_allclose(D1[0, :2] * h2, [1, -1])
+
+
+@pytest.mark.parametrize("nc", [(24, 16), (8, 6, 10)])
+def test_sommerfeld_term_keeps_order_two_with_first_order_laplacian(O, nc):
+    """GetHelmholtzOperator(..., orderNeumannBC = 1) with Sommerfeld on: the
+    Laplacian's boundary rows take BC = 1, the Sommerfeld term keeps BC = 2
+    (src/GetHelmholtz.jl:45 passes no order to getSommerfeldBC)."""
+    import problems as PB
+    P = PB.layered(nc, seed=2, pad=2, neumann=False, ellipsoid=len(nc) == 3)
+    H1 = O.GetHelmholtzOperator(P["M"], P["m"], P["w"], P["gamma"], False, True, 1)
+    ref = PB.operator_from_parts(P, 1)
+    assert abs(H1 - ref).max() <= 1e-14 * abs(ref).max()
+    # and it differs from the operator a BC = 1 Sommerfeld term would give
+    somm1 = O.getSommerfeldBC(P["M"], P["m"], P["w"], False, 1).ravel(order="F")
+    somm2 = O.getSommerfeldBC(P["M"], P["m"], P["w"], False, 2).ravel(order="F")
+    assert np.abs(somm2 - somm1).max() > 0.1 * np.abs(somm2).max()
 
 
 def test_abl_corner_rule_2d(O):
