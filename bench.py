@@ -556,7 +556,7 @@ def main():
     ap.add_argument("--levels", type=int, default=0, help="multigrid levels (0: the workload's)")
     ap.add_argument("--relax", default="jac", choices=["jac", "jac-gmres"],
                     help="smoother: damped Jacobi, or GMRES steps preconditioned by a Jacobi sweep (relaxType "
-                         "'Jac-GMRES'; on the GPU it needs HELMGPU_ENABLE_JAC_GMRES=1 until its parity test has run)")
+                         "'Jac-GMRES')")
     ap.add_argument("--relax-from", type=int, default=0, help="jac-gmres: first level smoothed by GMRES steps")
     ap.add_argument("--shift", type=float, default=0.5, help="s of the shifted operator SH = H + i s w^2 diag(m)")
     ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")

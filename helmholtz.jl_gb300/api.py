@@ -24,7 +24,6 @@ compiled library or a GPU every compute call raises.
 from __future__ import annotations
 
 import ctypes as C
-import os
 import sys
 from dataclasses import dataclass, field
 
@@ -205,6 +204,17 @@ def _is_device_array(x) -> bool:
     return hasattr(x, "data_ptr") and getattr(getattr(x, "device", None), "type", "cpu") == "cuda"
 
 
+def _device_inputs_ready() -> None:
+    """Make the work queued for the tensors handed to the library complete
+    before the library reads them.  The library orders its own stream after the
+    legacy default stream (torch's default stream); work queued on another
+    current torch stream is waited for here."""
+    import torch
+    cur = torch.cuda.current_stream()
+    if cur.cuda_stream != 0:
+        cur.synchronize()
+
+
 def _apply(dev: _Device, op: int, adj: bool, X):
     lib = L.load()
     if _is_device_array(X):
@@ -215,6 +225,7 @@ def _apply(dev: _Device, op: int, adj: bool, X):
         # column-major n x nrhs: a (nrhs, n) row-major tensor has that layout
         Xc = Xt.t().contiguous()
         Yc = torch.empty_like(Xc)
+        _device_inputs_ready()
         L.check(lib.hz_apply(dev.handle, op, int(adj), Xc.data_ptr(), Yc.data_ptr(), Xc.shape[1], Xc.shape[0],
                              L.HZ_MEM_DEVICE), dev.handle)
         Y = Yc.t()
@@ -410,9 +421,6 @@ def getMGparam(*args, transferType: str | None = None, precision: str = "fp64",
 def _validate_mg(MG: MGparam):
     if MG.relaxType not in ("Jac", "Jac-GMRES"):
         raise NotImplementedError(f"relaxType {MG.relaxType!r}: damped Jacobi ('Jac') and 'Jac-GMRES' are built")
-    if MG.relaxType == "Jac-GMRES" and os.environ.get("HELMGPU_ENABLE_JAC_GMRES") != "1":
-        raise NotImplementedError("relaxType 'Jac-GMRES' awaits its GPU parity test "
-                                  "(set HELMGPU_ENABLE_JAC_GMRES=1 to run it)")
     if MG.cycleType not in ("V", "W", "K"):
         raise NotImplementedError(f"cycleType {MG.cycleType!r}: only 'V', 'W' and 'K' cycles are built")
     if MG.coarseSolveType not in _SUPPORTED_COARSE:
@@ -575,6 +583,7 @@ def solveLinearSystem(ShiftedHT, B, param: ShiftedLaplacianMultigridSolver, doTr
     if on_device:
         Bc_ = Bt.t().contiguous()
         Xc_ = torch.empty_like(Bc_)
+        _device_inputs_ready()
         code = lib.hz_solve(h, Bc_.data_ptr(), Xc_.data_ptr(), n, nrhs, int(doTranspose), L.HZ_MEM_DEVICE,
                             C.byref(st))
         L.check(code, h)

@@ -153,6 +153,9 @@ struct hz_handle {
   DBuf bsc;         // BiCGSTAB per-column scalars
   DBuf sig, hC;     // FGMRES basis scales (stored v_i stands for sig_i v_i) and update coefficients
   DBuf tmpA, tmpB;  // hz_apply staging
+  DBuf apply_cols;  // hz_apply's column list 0..nrhs-1, grown only when nrhs grows
+  int apply_ncols = 0;
+  cudaEvent_t order_ev = nullptr;  // orders the handle's stream after the legacy default stream
   double* h_est = nullptr;  // pinned
   double* h_nrm = nullptr;  // pinned
   int* h_flag = nullptr;    // pinned copy of the second-pass flags
@@ -234,6 +237,25 @@ void set_device(hz_handle* h) { ck(cudaSetDevice(h->dev), "cudaSetDevice"); }
 void sync(hz_handle* h) {
   ck(cudaStreamSynchronize(h->ctx.stream), "stream sync");
   h->ctx.resolve();
+}
+
+// The handle's stream does not synchronise with the legacy default stream by
+// itself (it is non-blocking).  Calls that read or write caller-owned device
+// memory first make it wait for the work already issued to the legacy default
+// stream, where a caller that names no stream puts its copies and kernels.
+void order_after_default_stream(hz_handle* h) {
+  ck(cudaEventRecord(h->order_ev, cudaStreamLegacy), "record ordering event");
+  ck(cudaStreamWaitEvent(h->ctx.stream, h->order_ev, 0), "order after the default stream");
+}
+
+// Device X and Y of an operator apply must not overlap: the stencil reads the
+// neighbours of a node in X while it writes Y.
+void check_no_overlap(const double* X, const double* Y, long long n, int nrhs) {
+  const unsigned char* a = reinterpret_cast<const unsigned char*>(X);
+  const unsigned char* b = reinterpret_cast<const unsigned char*>(Y);
+  const size_t bytes = (size_t)n * (size_t)nrhs * 16;
+  if (a < b + bytes && b < a + bytes)
+    fail(HZ_ERR_ARG, "X and Y overlap: the operator apply does not work in place");
 }
 
 // Diagonals of H and SH on the node grid of problem p (5/7-point Laplacian
@@ -1549,11 +1571,6 @@ void validate(const hz_problem* p, const hz_options* o) {
     if (o->relax_pre < 0 || o->relax_pre > 2 || o->relax_post < 0 || o->relax_post > 2)
       fail(HZ_ERR_ARG, "Jac-GMRES takes 0, 1 or 2 GMRES steps per smoothing (relax_pre, relax_post)");
     if (o->relax_from < 0 || o->relax_from >= o->levels) fail(HZ_ERR_ARG, "relax_from must be in [0, levels - 1]");
-    // built and compiled, switched on once its GPU parity test has run
-    const char* on = std::getenv("HELMGPU_ENABLE_JAC_GMRES");
-    if (!on || std::strcmp(on, "1") != 0)
-      fail(HZ_ERR_ARG, "relax_type HZ_RELAX_JAC_GMRES awaits its GPU parity test "
-                       "(set HELMGPU_ENABLE_JAC_GMRES=1 to run it)");
   }
 }
 
@@ -1599,7 +1616,19 @@ int guarded(hz_handle* h, F&& f) {
 struct hz_net {
   int dev = 0;
   std::unique_ptr<hz::CoarseNet> net;
+  cudaEvent_t order_ev = nullptr;  // orders the network's stream after the legacy default stream
+  ~hz_net() {
+    if (order_ev) cudaEventDestroy(order_ev);
+  }
 };
+
+namespace {
+// As order_after_default_stream, for the network's own stream.
+void net_order_after_default_stream(hz_net* net) {
+  ck(cudaEventRecord(net->order_ev, cudaStreamLegacy), "record ordering event");
+  ck(cudaStreamWaitEvent(net->net->ctx.stream, net->order_ev, 0), "order after the default stream");
+}
+}  // namespace
 
 namespace {
 
@@ -1668,12 +1697,14 @@ int hz_create(const hz_problem* prob, const hz_options* opt, hz_handle** out) {
     h->dev = opt->device;
     set_device(h.get());
     ck(cudaStreamCreateWithFlags(&h->ctx.stream, cudaStreamNonBlocking), "stream");
+    ck(cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming), "ordering event");
     h->ctx.profile = opt->profile != 0;
     auto t0 = clk::now();
     init_fine(h.get());
     h->setup_time += secs(t0, clk::now());
   });
   if (st != HZ_OK) {
+    if (h->order_ev) cudaEventDestroy(h->order_ev);
     if (h->ctx.stream) cudaStreamDestroy(h->ctx.stream);
     return st;
   }
@@ -1690,6 +1721,7 @@ int hz_destroy(hz_handle* h) {
   if (h->h_est) cudaFreeHost(h->h_est);
   if (h->h_nrm) cudaFreeHost(h->h_nrm);
   if (h->h_flag) cudaFreeHost(h->h_flag);
+  if (h->order_ev) cudaEventDestroy(h->order_ev);
   if (h->ctx.stream) cudaStreamDestroy(h->ctx.stream);
   delete h;
   return HZ_OK;
@@ -1709,6 +1741,7 @@ int hz_solve(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, 
     set_device(h);
     const long long l0 = h->ctx.launches;
     h->h2d = h->d2h = 0;
+    if (mem == HZ_MEM_DEVICE) order_after_default_stream(h);
     auto t0 = clk::now();
     if (!h->hier[transpose].built) build_hierarchy(h, transpose);
     ensure_workspace(h, nrhs);
@@ -1776,9 +1809,11 @@ int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, doubl
     if (nrhs < 1) fail(HZ_ERR_ARG, "nrhs must be >= 1");
     if (op != HZ_OP_H && op != HZ_OP_SH) fail(HZ_ERR_ARG, "op must be HZ_OP_H or HZ_OP_SH");
     if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "bad mem");
+    if (transpose != 0 && transpose != 1) fail(HZ_ERR_ARG, "transpose must be 0 or 1");
+    if (mem == HZ_MEM_DEVICE) check_no_overlap(X, Y, n, nrhs);
     set_device(h);
-    const long long l0 = h->ctx.launches;
     h->h2d = h->d2h = 0;
+    if (mem == HZ_MEM_DEVICE) order_after_default_stream(h);
     const double2* xd;
     double2* yd;
     const size_t bytes = (size_t)n * nrhs * 16;
@@ -1792,19 +1827,24 @@ int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, doubl
       xd = reinterpret_cast<const double2*>(X);
       yd = reinterpret_cast<double2*>(Y);
     }
-    std::vector<int> all(nrhs);
-    for (int c = 0; c < nrhs; ++c) all[c] = c;
-    DBuf dc;
-    dc.alloc(all.size() * sizeof(int));
-    ck(cudaMemcpyAsync(dc.p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, h->ctx.stream), "cols");
+    if (nrhs > h->apply_ncols) {
+      // the list 0..nrhs-1 only grows: later calls with as many columns or fewer
+      // reuse it and leave the allocation generation (and the solver's graphs) alone
+      std::vector<int> all(nrhs);
+      for (int c = 0; c < nrhs; ++c) all[c] = c;
+      h->apply_cols.alloc(all.size() * sizeof(int));
+      ck(cudaMemcpyAsync(h->apply_cols.p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice,
+                         h->ctx.stream),
+         "cols");
+      h->apply_ncols = nrhs;
+    }
     FineOp fop = h->fop;
     fop.adj = transpose ? 1 : 0;
     const double2* diag = (op == HZ_OP_H) ? h->diagH.as<double2>() : h->diagSH.as<double2>();
     launch_fine<double, double, double>(h->ctx, MODE_APPLY, fop, diag, nullptr, xd, (const double2*)nullptr, yd, n,
-                                        dc.as<int>(), nrhs, 0.0);
+                                        h->apply_cols.as<int>(), nrhs, 0.0);
     if (mem == HZ_MEM_HOST) copy_out(h, yd, Y, n, nrhs, HZ_MEM_HOST);
     sync(h);
-    (void)l0;
   });
 }
 
@@ -1818,7 +1858,9 @@ int hz_apply_noalloc(hz_handle* h, int32_t op, int32_t transpose, const double* 
       fail(HZ_ERR_ARG, "hz_apply_noalloc takes 1 to %d columns (got %d)", HZ_NOALLOC_MAX_COLS, (int)nrhs);
     if (op != HZ_OP_H && op != HZ_OP_SH) fail(HZ_ERR_ARG, "op must be HZ_OP_H or HZ_OP_SH");
     if (transpose != 0 && transpose != 1) fail(HZ_ERR_ARG, "transpose must be 0 or 1");
+    check_no_overlap(X, Y, n, nrhs);
     set_device(h);
+    order_after_default_stream(h);
     FineOp fop = h->fop;
     fop.adj = transpose;
     const double2* diag = (op == HZ_OP_H) ? h->diagH.as<double2>() : h->diagSH.as<double2>();
@@ -1939,6 +1981,7 @@ int hz_net_create(int32_t seed, int32_t device, hz_net** out) {
     ck(cudaSetDevice(device), "cudaSetDevice");
     n->dev = device;
     n->net = std::make_unique<hz::CoarseNet>((unsigned)seed);
+    ck(cudaEventCreateWithFlags(&n->order_ev, cudaEventDisableTiming), "ordering event");
   });
   if (st == HZ_OK) *out = n.release();
   return st;
@@ -1987,6 +2030,7 @@ int hz_net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny
     hz::CoarseNet& c = *net->net;
     const long long N = nx * ny;
     const float* dx = x;
+    if (mem == HZ_MEM_DEVICE) net_order_after_default_stream(net);
     if (mem == HZ_MEM_HOST) {
       float* st = c.input_staging((int)nx, (int)ny, batch);
       ck(cudaMemcpyAsync(st, x, (size_t)batch * N * 16, cudaMemcpyHostToDevice, c.ctx.stream), "copy x");
@@ -2013,6 +2057,7 @@ int hz_net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int
     DBuf bx, bt;
     const float* dx = x;
     const float* dt = t;
+    if (mem == HZ_MEM_DEVICE) net_order_after_default_stream(net);
     if (mem == HZ_MEM_HOST) {
       bx.alloc((size_t)batch * N * 16);
       bt.alloc((size_t)batch * N * 8);
@@ -2037,6 +2082,7 @@ int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_
     if (!(lr > 0)) fail(HZ_ERR_ARG, "lr must be > 0");
     ck(cudaSetDevice(net->dev), "cudaSetDevice");
     hz::CoarseNet& c = *net->net;
+    net_order_after_default_stream(net);
     c.train(c.ctx, x, t, (int)nx, (int)ny, npairs, batch, epochs, lr, (unsigned)seed, loss_hist);
   });
 }

@@ -23,7 +23,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib as L
-from .api import ShiftedLaplacianMultigridSolver, _ensure_handle, _is_device_array, _nodes, current_device
+from .api import (ShiftedLaplacianMultigridSolver, _device_inputs_ready, _ensure_handle, _is_device_array, _nodes,
+                  current_device)
 
 
 def num_params() -> int:
@@ -45,6 +46,7 @@ def _ptr(a):
     if _is_device_array(a):
         if not a.is_contiguous():
             raise ValueError("device arrays must be contiguous")
+        _device_inputs_ready()
         return a.data_ptr(), L.HZ_MEM_DEVICE
     if a.dtype != np.float32 or not a.flags.c_contiguous:
         raise ValueError("host arrays must be C-contiguous float32")
@@ -147,6 +149,7 @@ class CoarseNet:
             raise ValueError("training pairs must be CUDA tensors")
         P, ny, nx, _ = x.shape
         hist = np.zeros(int(epochs))
+        _device_inputs_ready()
         L.check(L.load().hz_net_train(self._h, x.data_ptr(), t.data_ptr(), nx, ny, P, int(batch), int(epochs),
                                       float(lr), int(seed), hist.ctypes.data_as(C.POINTER(C.c_double))))
         return hist

@@ -8,6 +8,13 @@
  * column-major with axis 1 fastest, exactly the vec() ordering of the
  * reference (src/PlainNodalLaplacian.jl:32-46, src/getPointSource.jl:82-100).
  *
+ * Device memory and streams: a call that reads caller-owned device memory
+ * (mem = HZ_MEM_DEVICE, hz_apply_noalloc, the network's device inputs) first
+ * makes its own stream wait for the work already issued to the legacy default
+ * stream.  Work the caller queued on any other stream must be complete before
+ * the call: synchronise that stream, or make hz_stream(h) wait on an event
+ * recorded on it.  Every call returns after its outputs are complete.
+ *
  * Status convention: 0 = ok, > 0 = finished but not converged (X is still
  * valid, the reference prints a warning: src/ShiftedLaplacianMultigridSolver.jl:97-99),
  * < 0 = error (the message is available from hz_last_error).  No exception
@@ -157,7 +164,9 @@ int hz_column_stats(const hz_handle* h, double* relres, int32_t* iters, int32_t 
 
 /* Y = op X with op = H or SH (transpose = 1: the adjoint): the matrix-free
  * replacement of getHelmholtzFun's closure (src/GetHelmholtz.jl:85-95) and of
- * the sparse products H*x the reference tests take. */
+ * the sparse products H*x the reference tests take.  The apply does not work in
+ * place: device X and Y that overlap are rejected with HZ_ERR_ARG.  The column
+ * list the kernel reads is kept in the handle and grows only with nrhs. */
 int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, double* Y, int64_t n, int32_t nrhs,
              int32_t mem);
 
@@ -174,7 +183,9 @@ int hz_apply(hz_handle* h, int32_t op, int32_t transpose, const double* X, doubl
  * device address (cudaGetSymbolAddress) with the device current; make that
  * first call before any stream capture.  All calls on a device share the
  * array: calls that overlap on the GPU (different handles or streams) race.
- * Returns after the result is complete, like hz_apply. */
+ * X must be complete before the call (see "Device memory and streams" above)
+ * and must not overlap Y (HZ_ERR_ARG).  Returns after the result is complete,
+ * like hz_apply. */
 #define HZ_NOALLOC_MAX_COLS 4096
 int hz_apply_noalloc(hz_handle* h, int32_t op, int32_t transpose, const double* X, double* Y, int64_t n,
                      int32_t nrhs);

@@ -53,17 +53,35 @@ def _worker(rank, world, port, q, ncols=7):
     dist.destroy_process_group()
 
 
+def _run_all(procs, timeout=120.0):
+    """Start the rank processes and wait for them; a rank still alive after the
+    timeout is terminated (then killed) before the test fails, so no hung rank
+    keeps its port or outlives the test."""
+    import time
+    for p in procs:
+        p.start()
+    deadline = time.monotonic() + timeout
+    for p in procs:
+        p.join(max(0.0, deadline - time.monotonic()))
+    hung = [p for p in procs if p.is_alive()]
+    for p in hung:
+        p.terminate()
+    for p in hung:
+        p.join(5)
+        if p.is_alive():
+            p.kill()
+            p.join(5)
+    assert not hung, f"{len(hung)} rank(s) did not finish within {timeout} s"
+    assert [p.exitcode for p in procs] == [0] * len(procs)
+
+
 def test_solve_sharded_gloo_world2(hz):
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
     procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
-    for p in procs:
-        p.start()
-    for p in procs:
-        p.join(120)
-        assert p.exitcode == 0
+    _run_all(procs)
     msgs = [q.get(timeout=10) for _ in range(3)]
     xs = [m for m in msgs if m[0] == "x"]
     assert xs and xs[0][1] == 0.0
@@ -79,11 +97,7 @@ def test_solve_sharded_gloo_world3_empty_slice(hz):
     q = ctx.Queue()
     port = _free_port()
     procs = [ctx.Process(target=_worker, args=(r, 3, port, q, 2)) for r in range(3)]
-    for p in procs:
-        p.start()
-    for p in procs:
-        p.join(120)
-        assert p.exitcode == 0
+    _run_all(procs)
     msgs = [q.get(timeout=10) for _ in range(4)]
     xs = [m for m in msgs if m[0] == "x"]
     assert xs and xs[0][1] == 0.0
@@ -128,10 +142,6 @@ def test_failed_rank_does_not_hang_the_others(hz):
     q = ctx.Queue()
     port = _free_port()
     procs = [ctx.Process(target=_failing_worker, args=(r, 2, port, q)) for r in range(2)]
-    for p in procs:
-        p.start()
-    for p in procs:
-        p.join(120)
-        assert p.exitcode == 0
+    _run_all(procs)
     got = sorted(q.get(timeout=10) for _ in range(2))
     assert got == [(0, "ShardFailed"), (1, "ValueError: injected failure")]

@@ -3,20 +3,13 @@ test/ShiftedLaplacianTest.jl:138): one or two GMRES steps per smoothing,
 right-preconditioned by a damped-Jacobi sweep, on every level or from a coarse
 level down.  Plain FP64: solution within 1e-6 of the direct solve at residual
 1e-8 and iteration counts within one of the NumPy oracle's; mixed form within
-1e-4 at residual 1e-6; CUDA-graph replays identical to eager launches.
-
-The option is switched on by HELMGPU_ENABLE_JAC_GMRES=1 until these tests have
-passed on a GPU; without it the module is skipped."""
-import os
-
+1e-4 at residual 1e-6; CUDA-graph replays identical to eager launches."""
 import numpy as np
 import pytest
 
 import problems as PB
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("HELMGPU_ENABLE_JAC_GMRES") != "1",
-                                 reason="Jac-GMRES is switched on by HELMGPU_ENABLE_JAC_GMRES=1")]
+pytestmark = pytest.mark.gpu
 
 
 def _solver(hz, P, levels, tol, cycle="K", pre=1, post=1, relax_from=0, precision="fp64", outer="fp64",

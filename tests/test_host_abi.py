@@ -124,8 +124,11 @@ def test_api_validation(hz):
     p = hz.HelmholtzParam(M, np.zeros(81), np.ones(81), 2.0, True, True)
     S = hz.getShiftedLaplacianMultigridSolver(p, MG, 0.5, "GMRES", 10)
     assert np.all(S.shift == 0.5) and S.shift.size == 3
+    # an option outside the built subset is refused before any device work
+    MGs = hz.getMGparam(complex, int, 3, 1, 50, 1e-8, "SPAI", 0.8, 1, 1, "V", "Julia")
+    Ss = hz.getShiftedLaplacianMultigridSolver(p, MGs, 0.5, "GMRES", 10)
     with pytest.raises(NotImplementedError):
-        hz.solveLinearSystem(None, np.ones(81), S)
+        hz.solveLinearSystem(None, np.ones(81), Ss)
     # zero right-hand side: zeros, without touching the device (src/ShiftedLaplacianMultigridSolver.jl:40-43)
     MG2 = hz.getMGparam(complex, int, 3, 1, 50, 1e-8, "Jac", 0.8, 1, 1, "V", "Julia")
     S2 = hz.getShiftedLaplacianMultigridSolver(p, MG2, 0.5, "GMRES", 10)
@@ -186,10 +189,9 @@ def test_handles_follow_the_selected_device(hz, monkeypatch):
     assert api.current_device() == 0 and api._default_options().device == 0
 
 
-def test_jac_gmres_option_checks_and_gate(hz, monkeypatch):
+def test_jac_gmres_option_checks(hz):
     """relax_type HZ_RELAX_JAC_GMRES: its argument checks run before any device
-    work, and until its GPU parity test has run the option is refused unless
-    HELMGPU_ENABLE_JAC_GMRES=1 (then creation proceeds to the device check)."""
+    work; valid options proceed to the device check."""
     L = hz._lib
     lib = L.load()
     m = np.ones(81)
@@ -212,25 +214,18 @@ def test_jac_gmres_option_checks_and_gate(hz, monkeypatch):
             lib.hz_destroy(h)
         return st, (lib.hz_last_error(None) or b"").decode()
 
-    monkeypatch.delenv("HELMGPU_ENABLE_JAC_GMRES", raising=False)
-    st, msg = create()
-    assert st == L.HZ_ERR_ARG and "parity test" in msg
-    monkeypatch.setenv("HELMGPU_ENABLE_JAC_GMRES", "1")
     assert create()[0] in (L.HZ_OK, L.HZ_ERR_NO_DEVICE)
     assert create(relax_from=1)[0] in (L.HZ_OK, L.HZ_ERR_NO_DEVICE)
     for bad in (dict(krylov=L.HZ_KRYLOV_BICGSTAB, cycle=ord("V")), dict(relax_pre=3), dict(relax_post=-1),
                 dict(relax_from=3), dict(relax_from=-1), dict(relax_type=2)):
         assert create(**bad)[0] == L.HZ_ERR_ARG, bad
-    # the Python layer maps the option and keeps the same gate
+    # the Python layer maps the option
     MG = hz.getMGparam(complex, int, 3, 1, 50, 1e-8, "Jac-GMRES", 0.8, 2, 2, "K", "Julia", relaxFrom=1)
     S = hz.getShiftedLaplacianMultigridSolver(hz.HelmholtzParam(hz.getRegularMesh([0.0, 1.0, 0.0, 1.0], [8, 8]),
                                                                 g, m, 2.0, True, True), MG, 0.5, "GMRES", 10)
     o = hz.api._options(S)
     assert (o.relax_type, o.relax_from, o.relax_pre) == (L.HZ_RELAX_JAC_GMRES, 1, 2)
     assert hz.copySolver(S).MG.relaxFrom == 1
-    monkeypatch.delenv("HELMGPU_ENABLE_JAC_GMRES")
-    with pytest.raises(NotImplementedError):
-        hz.solveLinearSystem(None, np.ones(81), S)
 
 
 @pytest.mark.parametrize("nc", [(24, 16), (8, 6, 10)])

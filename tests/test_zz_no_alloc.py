@@ -46,6 +46,8 @@ def test_apply_noalloc_matches_apply(hz, case):
             ref = Yref.cpu().numpy()
             for _ in range(2):  # two calls in a row share the static scratch
                 Y = torch.full_like(X, complex(float("nan"), float("nan")))
+                # X and Y must be complete before the call (the fill runs on torch's stream)
+                torch.cuda.synchronize()
                 rc = lib.hz_apply_noalloc(h, op, adj, X.data_ptr(), Y.data_ptr(), n, nrhs)
                 assert rc == L.HZ_OK, lib.hz_last_error(h)
                 got = Y.cpu().numpy()
@@ -53,8 +55,14 @@ def test_apply_noalloc_matches_apply(hz, case):
                 assert np.linalg.norm(got - ref) <= TOL64 * np.linalg.norm(ref)
         # more columns than the static scratch holds: a clear error, nothing launched
         big = L.HZ_NOALLOC_MAX_COLS + 1
-        rc = lib.hz_apply_noalloc(h, L.HZ_OP_H, 0, X.data_ptr(), X.data_ptr(), n, big)
+        Y = torch.empty_like(X)
+        rc = lib.hz_apply_noalloc(h, L.HZ_OP_H, 0, X.data_ptr(), Y.data_ptr(), n, big)
         assert rc == L.HZ_ERR_ARG
         assert b"columns" in lib.hz_last_error(h)
+        # in place (X and Y overlapping) is refused by both entry points
+        rc = lib.hz_apply_noalloc(h, L.HZ_OP_H, 0, X.data_ptr(), X.data_ptr(), n, nrhs)
+        assert rc == L.HZ_ERR_ARG and b"overlap" in lib.hz_last_error(h)
+        rc = lib.hz_apply(h, L.HZ_OP_H, 0, X.data_ptr(), X.data_ptr() + 16, n, nrhs, L.HZ_MEM_DEVICE)
+        assert rc == L.HZ_ERR_ARG and b"overlap" in lib.hz_last_error(h)
     finally:
         lib.hz_destroy(h)
