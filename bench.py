@@ -1,10 +1,19 @@
 """Throughput benchmark: right-hand sides solved per second to relative
 residual 1e-6 by the shifted-Laplacian multigrid FGMRES solve on one GB300.
 
-One step = one hz_solve of the whole right-hand-side block of the workload
-(every column to rel. residual <= tol).  The headline arm runs the
-complex-FP32 V-cycle inside the FP64 FGMRES ("mixed"); the plain FP64 form of
-the same solver is timed in the same process for the ratio the metric names.
+One step = one hz_solve of the workload's whole right-hand-side block (every
+column to rel. residual <= tol).  Default workload: 3D 257^3 nodes x 32
+surface sources, five Galerkin levels, K-cycle with "Jac-GMRES" smoothing from
+level 1 down, FGMRES(10) to 1e-6.  Three forms of the same solver run in one
+process on the same GPU:
+
+  mixed           complex-FP32 cycle, FP64 coarsest LU, native-FP64 outer FGMRES (headline)
+  mixed_emulated  the same cycle, outer FGMRES in FP64 emulated by FP32 pairs (labelled arm)
+  fp64            plain complex FP64 throughout (the metric's denominator)
+
+Every arm states its relative residual and its error against an FP64 oracle
+(2D: sparse direct solve of sampled columns; 3D: the C oracle's FP64 SLMG
+solve of a sampled column to 1e-10).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c1|c2|c3|c4|c5]
   python bench.py --impl reference ...   # CPU reference path (C oracle, all host threads)
@@ -32,6 +41,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "RHS solved/s to rel. residual 1e-6 on 1 GB300: learned+mixed vs plain FP64 SLMG"
 
+# solver options a workload does not set
+SOLVER_DEFAULTS = dict(cycle="V", relax="jac", relax_from=0, shift=0.5, coarse="galerkin")
+
 # Synthetic seeded workloads (shapes, sizes and value distributions of the
 # measured configurations; no external dataset is needed).
 WORKLOADS = {
@@ -39,24 +51,27 @@ WORKLOADS = {
     # at (0.5, 2h), absorbing layer 16, 3 levels, FGMRES(10) to 1e-8
     "c1": dict(name="2D 129x129 gradient+ellipse, 1 source, 3 levels, FGMRES(10) tol 1e-8",
                cells=(128, 128), h=1.0 / 128, nrhs=1, levels=3, pad=16, ellipsoid=False, tol=1e-8,
-               model="gradient_ellipse"),
+               model="gradient_ellipse", err_cols=1),
     # 2D 1025 x 513 nodes, h = 10 m, 12 seeded layers in [1.5, 4.5] km/s,
     # absorbing layer 32 cells, 64 sources along the surface row, 5 levels
     "c2": dict(name="2D 1025x513 layered, 64 surface sources, 5 levels, FGMRES(10) tol 1e-6",
-               cells=(1024, 512), h=0.010, nrhs=64, levels=5, pad=32, ellipsoid=False, tol=1e-6),
+               cells=(1024, 512), h=0.010, nrhs=64, levels=5, pad=32, ellipsoid=False, tol=1e-6, err_cols=4),
     # 3D 129^3 nodes layered + ellipsoid, absorbing layer 12, 4x4 surface sources, 4 levels
     "c3": dict(name="3D 129^3 layered+ellipsoid, 16 surface sources, 4 levels, FGMRES(10) tol 1e-6",
-               cells=(128, 128, 128), h=0.010, nrhs=16, levels=4, pad=12, ellipsoid=True, tol=1e-6),
+               cells=(128, 128, 128), h=0.010, nrhs=16, levels=4, pad=12, ellipsoid=True, tol=1e-6, err_cols=1),
     # 2D 513 x 513 layered + inclusion models, learned coarse correction below level 2: trained on
     # pairs from seeded training models, evaluated on held-out seeds x 32 random-position sources
     "c4": dict(name="2D 513x513 layered+inclusion, learned coarse correction below level 2, 32 random sources, "
                     "5 levels, FGMRES(10) tol 1e-6",
                cells=(512, 512), h=0.010, nrhs=32, levels=5, pad=32, ellipsoid=True, tol=1e-6, learned=True,
                net_level=2),
-    # 3D 257^3 nodes (16,974,593 unknowns per RHS), absorbing layer 16, 32 surface sources
+    # 3D 257^3 nodes (16,974,593 unknowns per RHS), absorbing layer 16, 32 surface sources; the
+    # five-level Galerkin hierarchy converges with the K-cycle and GMRES smoothing from level 1
     "c5": dict(name="3D 257^3 layered+ellipsoid, 32 surface sources, 5 levels, FGMRES(10) tol 1e-6",
-               cells=(256, 256, 256), h=0.010, nrhs=32, levels=5, pad=16, ellipsoid=True, tol=1e-6),
+               cells=(256, 256, 256), h=0.010, nrhs=32, levels=5, pad=16, ellipsoid=True, tol=1e-6, err_cols=1,
+               cycle="K", relax="jac-gmres", relax_from=1, shift=0.3),
 }
+DEFAULT_WORKLOAD = "c5"
 
 
 def workload(args) -> dict:
@@ -67,6 +82,14 @@ def workload(args) -> dict:
     if args.levels > 0:
         wl["levels"] = args.levels
     return wl
+
+
+def resolve_solver_args(args) -> None:
+    """Fill the solver options the command line left unset from the workload."""
+    wl = WORKLOADS[args.workload]
+    for k, v in SOLVER_DEFAULTS.items():
+        if getattr(args, k) is None:
+            setattr(args, k, wl.get(k, v))
 
 
 def make_problem(wl: dict, seed: int):
@@ -131,8 +154,27 @@ def sources(P: dict, nrhs: int, seed: int) -> np.ndarray:
 
 
 def gamma_of(P: dict, pad: int, lib, hz) -> np.ndarray:
+    """Total attenuation through the library's getABL (the GPU arms)."""
     abl = hz.getABL(P["nodes"], True, [pad] * P["dim"], 0.95 * P["w"]).ravel(order="F")
     return abl + 0.01 * P["w"]
+
+
+def gamma_oracle(P: dict, pad: int) -> np.ndarray:
+    """The same attenuation through the oracle's getABL (the CPU reference and
+    checker legs, which use nothing of the product)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import helmholtz_oracle as O
+    abl = O.getABL(np.array(P["nodes"]), True, [pad] * P["dim"], 0.95 * P["w"]).ravel(order="F")
+    return abl + 0.01 * P["w"]
+
+
+def run_config(args, wl: dict, P: dict) -> dict:
+    """The `config` object both arms print (the same keys and values)."""
+    return dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
+                krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB", cycle=args.cycle,
+                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from, shift=args.shift,
+                seed=1234, learned=False,
+                l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9))
 
 
 class ClockSampler:
@@ -246,6 +288,19 @@ def traffic_ratio_from_profiles(kernel: str, workload: str):
         return None
 
 
+# ---------------------------------------------------------------------------
+# GPU arms
+# ---------------------------------------------------------------------------
+ARMS = {
+    # name: (precision, outer arithmetic)
+    "mixed": ("mixed", "fp64"),
+    "mixed_emulated": ("mixed", "emulated"),
+    "fp64": ("fp64", "fp64"),
+}
+ARM_SETS = {"all": ["mixed", "mixed_emulated", "fp64"], "both": ["mixed", "fp64"], "mixed": ["mixed"],
+            "emulated": ["mixed_emulated"], "fp64": ["fp64"]}
+
+
 def run_ours(args, rank, ws, dist):
     import torch
     import __graft_entry__ as ge
@@ -259,8 +314,9 @@ def run_ours(args, rank, ws, dist):
     nrhs = wl["nrhs"]
     B = sources(P, nrhs, seed=rank)
     n = B.shape[0]
+    err_cols = list(range(min(nrhs, wl.get("err_cols", 1))))
 
-    def make_handle(precision):
+    def make_handle(precision, outer):
         prob = L.hz_problem()
         prob.dim = P["dim"]
         for d in range(P["dim"]):
@@ -283,9 +339,8 @@ def run_ours(args, rank, ws, dist):
         o.autotune = 0 if args.no_tune else 1
         if args.krylov == "bicgstab":
             o.krylov, o.max_outer = L.HZ_KRYLOV_BICGSTAB, 2000
-        o.precision = precision
-        if precision == L.HZ_PREC_MIXED and args.outer == "emulated":
-            o.outer_arith = L.HZ_OUTER_EMULATED
+        o.precision = L.HZ_PREC_MIXED if precision == "mixed" else L.HZ_PREC_FP64
+        o.outer_arith = L.HZ_OUTER_EMULATED if outer == "emulated" else L.HZ_OUTER_FP64
         o.device = torch.cuda.current_device()
         hh = C.c_void_p()
         L.check(lib.hz_create(C.byref(prob), C.byref(o), C.byref(hh)))
@@ -317,37 +372,43 @@ def run_ours(args, rank, ws, dist):
         return e0.elapsed_time(e1) / 1000.0, last
 
     results = {}
-    order = ["mixed", "fp64"] if args.precision == "both" else [args.precision]
-    for prec in order:
-        hh = make_handle(L.HZ_PREC_MIXED if prec == "mixed" else L.HZ_PREC_FP64)
+    names = ARM_SETS[args.precision]
+    for ai, name in enumerate(names):
+        prec, outer = ARMS[name]
+        head = ai == 0
+        hh = make_handle(prec, outer)
+        warm = args.warmup if head else max(1, args.arm_warmup)
+        steps = args.steps if head else max(1, args.plain_steps if name == "fp64" else args.arm_steps)
         t_setup0 = time.perf_counter()
-        for _ in range(args.warmup):
+        for _ in range(warm):
             solve_device(hh)
         setup_and_warm = time.perf_counter() - t_setup0
-        steps = args.steps if prec == order[0] else max(1, args.plain_steps)
         lib.hz_reset_kernel_times(hh)
         lib.hz_set_profile(hh, 0)
         with ClockSampler(torch.cuda.current_device()) as clocks:
             t, (st, code) = timed(hh, steps, solve_device)
         t = max_over_ranks(dist, t)
-        if prec == order[0]:
-            # per-kernel CUDA events on the handle's stream over the same number of
-            # solves right after (event records around every launch would slow the
-            # timed solves themselves, most on small workloads)
-            lib.hz_reset_kernel_times(hh)
-            lib.hz_set_profile(hh, 1)
-            timed(hh, steps, solve_device)
-            lib.hz_set_profile(hh, 0)
+        launches = int(st.kernel_launches)
         rr = np.zeros(nrhs)
         it = np.zeros(nrhs, dtype=np.int32)
         lib.hz_column_stats(hh, rr.ctypes.data_as(C.POINTER(C.c_double)), it.ctypes.data_as(C.POINTER(C.c_int32)),
                             nrhs)
-        kt = kernel_table(lib, hh)
-        res = dict(seconds=t, steps=steps, rhs_per_s=nrhs * ws * steps / t, ms_per_step=1000.0 * t / steps,
-                   max_relres=float(rr.max()), mean_iters=float(it.mean()), max_iters=int(it.max()),
-                   outer=int(st.outer), launches_per_step=int(st.kernel_launches), kernels=kt,
-                   clocks=clocks.summary(), setup_warm_s=setup_and_warm, code=int(code))
-        if prec == order[0]:
+        res = dict(precision=prec, outer_arithmetic=outer, seconds=t, steps=steps, warmup=warm,
+                   rhs_per_s=nrhs * ws * steps / t, ms_per_step=1000.0 * t / steps, max_relres=float(rr.max()),
+                   converged_cols=int(np.sum(rr <= wl["tol"])), mean_iters=float(it.mean()), max_iters=int(it.max()),
+                   outer=int(st.outer), launches_per_step=launches, clocks=clocks.summary(),
+                   setup_warm_s=setup_and_warm, code=int(code),
+                   x_err_cols=Xd[err_cols].cpu().numpy())
+        if head:
+            # per-kernel CUDA events on the handle's stream over one solve right after the timed
+            # ones, with the cycle launched eagerly so that every kernel of it is timed by itself
+            lib.hz_reset_kernel_times(hh)
+            lib.hz_set_cuda_graph(hh, 0)
+            lib.hz_set_profile(hh, 1)
+            timed(hh, 1, solve_device)
+            lib.hz_set_profile(hh, 0)
+            lib.hz_set_cuda_graph(hh, 0 if args.no_graph else 1)
+            res["kernels"] = kernel_table(lib, hh)
             # end to end through the public call with host buffers (pinned), copies inside the timed region
             Bh = torch.from_numpy(np.ascontiguousarray(B.T)).pin_memory()
             Xh = torch.empty_like(Bh).pin_memory()
@@ -358,27 +419,287 @@ def run_ours(args, rank, ws, dist):
                         hh_)
                 return st_
 
-            lib.hz_set_profile(hh, 0)
+            e2e_steps = max(1, min(steps, args.e2e_steps))
             solve_host(hh)
-            t0 = time.perf_counter()
             barrier(dist)
-            for _ in range(steps):
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
                 st_h = solve_host(hh)
             barrier(dist)
             te = max_over_ranks(dist, time.perf_counter() - t0)
-            res["e2e"] = dict(value=nrhs * ws * steps / te, unit="RHS/s", h2d_bytes_per_step=int(st_h.h2d_bytes),
-                              d2h_bytes_per_step=int(st_h.d2h_bytes))
-            # accuracy check of the last device solve against the FP64 operator
+            res["e2e"] = dict(value=nrhs * ws * e2e_steps / te, unit="RHS/s", steps=e2e_steps,
+                              h2d_bytes_per_step=int(st_h.h2d_bytes), d2h_bytes_per_step=int(st_h.d2h_bytes))
+            # residual check of the last device solve with the FP64 operator
             Y = torch.empty_like(Xd)
             L.check(lib.hz_apply(hh, L.HZ_OP_H, 0, Xd.data_ptr(), Y.data_ptr(), n, nrhs, L.HZ_MEM_DEVICE), hh)
             rel = torch.linalg.vector_norm(Y - Bd, dim=1) / torch.linalg.vector_norm(Bd, dim=1)
             res["check_relres_max"] = float(rel.max())
+            del Bh, Xh, Y
         lib.hz_destroy(hh)
-        results[prec] = res
+        results[name] = res
         torch.cuda.empty_cache()
-    return results, wl, P
+    del Bd, Xd
+    torch.cuda.empty_cache()
+    return results, wl, P, B, err_cols
 
 
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle): checker and baseline
+# ---------------------------------------------------------------------------
+class OracleSolver:
+    """The C oracle (threaded CSR SLMG, plain FP64) on the workload's full grid
+    with the GPU arms' cycle, coarse operators and smoother."""
+
+    def __init__(self, wl, P, args):
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import helmholtz_oracle as O
+        import slmg_cpu
+        t0 = time.perf_counter()
+        M = O.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
+        gam = gamma_oracle(P, wl["pad"])
+        H = O.GetHelmholtzOperator(M, P["m"], P["w"], gam, True, True)
+        SH = (H + O.GetHelmholtzShiftOP(P["m"], P["w"], args.shift)).tocsr()
+        hier = None
+        if args.coarse == "rediscretize":
+            hier = O.build_hierarchy_rediscretized(M, P["m"], gam, P["w"], args.shift, True, True, wl["levels"])
+        self.cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"], hier=hier)
+        self.kw = dict(cycle=args.cycle, relax="Jac-GMRES" if args.relax == "jac-gmres" else "Jac",
+                       gmres_from=args.relax_from)
+        self.desc = (f"plain FP64 SLMG ({args.cycle}-cycle, {args.coarse} coarse levels, {self.kw['relax']} smoothing"
+                     f"{f' from level {args.relax_from}' if args.relax == 'jac-gmres' else ''}) in threaded C")
+        self.setup_s = time.perf_counter() - t0
+
+    def cycles(self, b, tol, max_cycles, X0=None):
+        """Restart cycles of one column, one call per cycle, from X0 (default
+        zero) until rel. residual <= tol: returns (X, iterations, seconds per
+        cycle, relres, threads)."""
+        X = np.zeros((b.shape[0], 1), dtype=np.complex128) if X0 is None else X0
+        its, secs, rr, thr = 0, [], np.inf, 1
+        for _ in range(max_cycles):
+            r = self.cpu.solve(b, tol=tol, max_outer=1, X0=X, **self.kw)
+            X = r.X
+            its += int(r.iters.sum())
+            secs.append(r.solve_s)
+            rr = float(r.relres.max())
+            thr = r.threads
+            if rr <= tol:
+                break
+        return X, its, secs, rr, thr
+
+
+def direct_errors(wl, P, B, err_cols, arms):
+    """2D: relative error of each arm's sampled columns against a sparse direct
+    solve (SuperLU) of the same operator, assembled by the oracle."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import helmholtz_oracle as O
+    M = O.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
+    H = O.GetHelmholtzOperator(M, P["m"], P["w"], gamma_oracle(P, wl["pad"]), True, True)
+    Xref = O.direct_solve(H, B[:, err_cols])
+    out = {}
+    for name, res in arms.items():
+        Xg = res["x_err_cols"].T
+        out[name] = float(max(np.linalg.norm(Xg[:, k] - Xref[:, k]) / np.linalg.norm(Xref[:, k])
+                              for k in range(len(err_cols))))
+    return out, dict(kind="sparse direct solve (SciPy SuperLU) of the oracle's FP64 operator",
+                     columns=list(err_cols))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("HZ_BENCH_WORKLOAD", DEFAULT_WORKLOAD),
+                    choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="all", choices=sorted(ARM_SETS),
+                    help="arms: all = mixed (headline) + mixed_emulated + fp64; both = mixed + fp64")
+    ap.add_argument("--plain-steps", type=int, default=3, help="timed solves of the plain FP64 arm")
+    ap.add_argument("--arm-steps", type=int, default=3, help="timed solves of the emulated-outer arm")
+    ap.add_argument("--arm-warmup", type=int, default=1, help="untimed solves before the other arms' timed ones")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="end-to-end solves (host buffers), at most --steps")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the 3D oracle error")
+    ap.add_argument("--nrhs", type=int, default=0, help="override the workload's RHS count (small profiling cases)")
+    ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
+    ap.add_argument("--no-graph", action="store_true", help="launch the cycles eagerly (no CUDA graphs)")
+    ap.add_argument("--no-tune", action="store_true", help="default stencil launch shapes (no autotuning)")
+    ap.add_argument("--max-outer", type=int, default=200,
+                    help="FGMRES restart cycles (fewer: kernel-rate profiling runs, not a valid RHS/s)")
+    ap.add_argument("--cycle", default=None, choices=["V", "W", "K"],
+                    help="multigrid cycle (K: two FGMRES steps per coarse level; default: the workload's)")
+    ap.add_argument("--coarse", default=None, choices=["galerkin", "rediscretize"],
+                    help="coarse-level operators: Galerkin R A P, or the operator re-discretised on each coarse mesh")
+    ap.add_argument("--levels", type=int, default=0, help="multigrid levels (0: the workload's)")
+    ap.add_argument("--relax", default=None, choices=["jac", "jac-gmres"],
+                    help="smoother: damped Jacobi, or GMRES steps preconditioned by a Jacobi sweep (relaxType "
+                         "'Jac-GMRES')")
+    ap.add_argument("--relax-from", type=int, default=None, help="jac-gmres: first level smoothed by GMRES steps")
+    ap.add_argument("--shift", type=float, default=None, help="s of the shifted operator SH = H + i s w^2 diag(m)")
+    ap.add_argument("--outer", default="fp64", choices=["fp64", "emulated"],
+                    help="learned workload: outer arithmetic of its mixed arms")
+    ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
+    ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
+    ap.add_argument("--pairs-per-model", type=int, default=200)
+    ap.add_argument("--train-epochs", type=int, default=20)
+    ap.add_argument("--net-level", type=int, default=0, help="learned workload: multigrid level of the network "
+                    "(0: the workload's)")
+    ap.add_argument("--stag-ratio", type=float, default=0.95,
+                    help="learned workload: a restart cycle reducing a residual by less than this hands over "
+                         "to the plain cycle")
+    args = ap.parse_args()
+    resolve_solver_args(args)
+    peak, peak_kind = load_peaks()
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    rank, ws, dist = dist_setup()
+    if WORKLOADS[args.workload].get("learned"):
+        run_learned_main(args, rank, ws, dist)
+        return
+    results, wl, P, B, err_cols = run_ours(args, rank, ws, dist)
+    if rank != 0:
+        return
+    names = ARM_SETS[args.precision]
+    head = results[names[0]]
+    # per-kernel rates of the eager profiled solve; the dominant kernel names the roofline
+    kt = [k for k in head["kernels"] if k["timed"] > 0]
+    tot_ms = sum(k["ms"] for k in kt) or 1.0
+    dom = max(kt, key=lambda k: k["ms"]) if kt else None
+    roofline = None
+    if dom:
+        achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
+        ratio = traffic_ratio_from_profiles(dom["name"], args.workload) if args.nrhs == 0 else None
+        tr = None if ratio is None else ratio * dom["bytes"] / dom["launches"]
+        roofline = dict(bound="hbm", kernel=dom["name"], achieved=achieved, peak=peak, unit="GB/s",
+                        frac=achieved / peak, peak_source=f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                        traffic=tr, avg_launch_ms=dom["ms"] / dom["timed"], share=dom["ms"] / tot_ms,
+                        source="CUDA events around every launch on the handle's stream, over one eager solve "
+                               "right after the timed ones")
+    # whole-solve roofline: the algorithmic bytes of every launched kernel of a solve over
+    # the unprofiled time of a solve
+    solve_bytes = sum(k["bytes"] for k in head["kernels"])
+    solve_roof = dict(bound="hbm", achieved=solve_bytes / (head["ms_per_step"] / 1e3) / 1e9, peak=peak, unit="GB/s",
+                      frac=solve_bytes / (head["ms_per_step"] / 1e3) / 1e9 / peak, bytes_per_solve=solve_bytes)
+    # error against an FP64 oracle, and the CPU baseline
+    errs, err_info, cpu = {}, None, None
+    if P["dim"] == 2:
+        errs, err_info = direct_errors(wl, P, B, err_cols, results)
+    if not args.no_cpu:
+        orc = OracleSolver(wl, P, args)
+        b0 = B[:, :1]
+        X1, its, secs, rr1, thr = orc.cycles(b0, wl["tol"], 400)
+        t1 = float(sum(secs))
+        cpu = dict(value=1.0 / t1, unit="RHS/s", cores=thr, kind="port",
+                   sample=f"column 0 of the {wl['nrhs']} right-hand sides of the same workload solved to "
+                          f"{wl['tol']:g} ({its} iterations, {len(secs)} restart cycles timed one by one), full grid, "
+                          f"same operator, {orc.desc}",
+                   seconds=t1, setup_s=orc.setup_s, max_relres=rr1, iterations=its)
+        if P["dim"] == 3:
+            # continue column 0 to 1e-10: the FP64 oracle solution the arms' errors are taken against
+            Xr, its2, secs2, rr2, _ = orc.cycles(b0, 1e-10, 400, X0=X1)
+            xr = Xr[:, 0]
+            for name, res in results.items():
+                xg = res["x_err_cols"][0]
+                errs[name] = float(np.linalg.norm(xg - xr) / np.linalg.norm(xr))
+            err_info = dict(kind="C oracle FP64 FGMRES-SLMG solve (same cycle) to rel. residual 1e-10",
+                            columns=[0], oracle_relres=rr2, oracle_iterations=its + its2)
+    plain = results.get("fp64")
+    emu = results.get("mixed_emulated")
+
+    def arm_summary(r, name):
+        return dict(precision=r["precision"], outer_arithmetic=r["outer_arithmetic"], rhs_per_s=r["rhs_per_s"],
+                    ms_per_step=r["ms_per_step"], steps=r["steps"], warmup=r["warmup"], mean_iters=r["mean_iters"],
+                    max_iters=r["max_iters"], max_relres=r["max_relres"], converged_cols=r["converged_cols"],
+                    max_err_vs_oracle=errs.get(name), clocks=r["clocks"])
+
+    line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
+                warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
+                vs_baseline=None,
+                dtype=("c64 cycle / c128 outer" + (" (emulated by FP32 pairs)" if head["outer_arithmetic"] == "emulated"
+                                                   else "") if head["precision"] == "mixed" else "c128"),
+                data="synthetic (seeded layered+ellipsoid model)" if P["dim"] == 3 else "synthetic (seeded model)",
+                config=dict(run_config(args, wl, P), precision=head["precision"],
+                            outer_arithmetic=head["outer_arithmetic"], cuda_graph=not args.no_graph,
+                            autotune=not args.no_tune),
+                e2e=head.get("e2e"), gpu_launches=head["launches_per_step"] * args.steps,
+                clocks=head["clocks"], roofline=roofline, solve_roofline=solve_roof,
+                cpu_baseline=cpu,
+                max_relres=head["max_relres"], check_relres_max=head.get("check_relres_max"),
+                converged_cols=head["converged_cols"], mean_iters=head["mean_iters"],
+                max_err_vs_oracle=errs.get(names[0]), err_oracle=err_info,
+                plain_fp64=None if plain is None else arm_summary(plain, "fp64"),
+                mixed_over_plain=None if plain is None else head["rhs_per_s"] / plain["rhs_per_s"],
+                emulated_outer=None if emu is None else arm_summary(emu, "mixed_emulated"),
+                emulated_over_plain=(None if (emu is None or plain is None)
+                                     else emu["rhs_per_s"] / plain["rhs_per_s"]),
+                kernels=[dict(name=k["name"], launches=k["launches"], ms=round(k["ms"], 3),
+                              gbs=(k["bytes"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None,
+                              frac=(k["bytes"] / (k["ms"] / 1e3) / 1e9 / peak) if k["ms"] > 0 else None,
+                              share=k["ms"] / tot_ms)
+                         for k in sorted(kt, key=lambda k: -k["ms"])[:24]],
+                kernels_source="one eager solve (cycle kernels launched one by one) after the timed solves")
+    print(json.dumps(line))
+
+
+def run_reference(args):
+    """The reference arm: the C oracle port of the reference's SLMG path (Julia
+    and Multigrid.jl are absent), plain FP64 on all host threads, on the same
+    workload and config.  One step = one restart cycle (10 FGMRES iterations)
+    of the current column of the workload; a column that converges hands over
+    to the next one.  RHS/s = (iterations per second over the timed cycles) /
+    (iterations per right-hand side of the columns solved)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = workload(args)
+    P = make_problem(wl, seed=1234)
+    B = sources(P, wl["nrhs"], seed=0)
+    orc = OracleSolver(wl, P, args)
+    col, X = 0, None
+    solved_iters, cur_iters = [], 0
+    t_steps, it_steps = [], []
+    thr = 1
+    for step in range(args.warmup + args.steps):
+        b = B[:, col:col + 1]
+        X, its, secs, rr, thr = orc.cycles(b, wl["tol"], 1, X0=X)
+        cur_iters += its
+        if step >= args.warmup:
+            t_steps.append(secs[0])
+            it_steps.append(its)
+        if rr <= wl["tol"]:
+            solved_iters.append(cur_iters)
+            col, X, cur_iters = (col + 1) % wl["nrhs"], None, 0
+    if not solved_iters:
+        # no column finished within the steps: finish the current one (untimed) for its iteration count
+        b = B[:, col:col + 1]
+        X, its, _, rr, _ = orc.cycles(b, wl["tol"], 400, X0=X)
+        solved_iters.append(cur_iters + its)
+    ips = sum(it_steps) / sum(t_steps)
+    per_rhs = float(np.mean(solved_iters))
+    v = ips / per_rhs
+    line = dict(metric=METRIC, value=v, unit="RHS/s", impl="reference", n_gpus=args.gpus, steps=args.steps,
+                warmup=args.warmup, ms_per_step=1000.0 * sum(t_steps) / len(t_steps), higher_is_better=True,
+                scaling="weak", vs_baseline=None, dtype="c128",
+                data="synthetic (seeded layered+ellipsoid model)" if P["dim"] == 3 else "synthetic (seeded model)",
+                config=dict(run_config(args, wl, P), precision="fp64", outer_arithmetic="fp64", cuda_graph=False,
+                            autotune=False),
+                cpu_baseline=dict(value=v, unit="RHS/s", cores=thr, kind="port",
+                                  sample=f"one restart cycle (10 FGMRES iterations) of one column per step, full "
+                                         f"grid, {orc.desc}; {per_rhs:.0f} iterations per right-hand side "
+                                         f"({len(solved_iters)} column(s) solved to {wl['tol']:g})",
+                                  setup_s=orc.setup_s),
+                e2e=dict(value=v, unit="RHS/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                iterations_per_s=ips, iterations_per_rhs=per_rhs,
+                note="reference path = the C oracle port of the Julia SLMG (Julia and Multigrid.jl are absent); "
+                     "it imports nothing of the product")
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# Learned coarse correction workload (2D)
+# ---------------------------------------------------------------------------
 def random_sources(P: dict, nrhs: int, seed: int, pad: int) -> np.ndarray:
     """Delta sources q = 1/||h||^2 at seeded random nodes outside the absorbing layer (2D)."""
     rng = np.random.default_rng(seed)
@@ -497,197 +818,33 @@ def run_learned(args, rank, ws, dist):
     return res, info, wl
 
 
-def run_cpu_sample(wl, P, gam_fn, budget_s: float, ncols_max: int = 4, cycle: str = "V",
-                   coarse: str = "galerkin", relax: str = "jac", relax_from: int = 0, shift: float = 0.5):
-    """C oracle (threaded CSR SLMG, plain FP64) on a bounded sample of the
-    workload: the full grid and operator, a few of its right-hand sides, with
-    the GPU arm's cycle, coarse operators (Galerkin or re-discretised) and
-    smoother (damped Jacobi, or Jac-GMRES from level relax_from down)."""
-    rkw = dict(relax="Jac-GMRES" if relax == "jac-gmres" else "Jac", gmres_from=relax_from)
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import helmholtz_oracle as O
-    import slmg_cpu
-    M = O.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
-    gam = gam_fn()
-    H = O.GetHelmholtzOperator(M, P["m"], P["w"], gam, True, True)
-    SH = (H + O.GetHelmholtzShiftOP(P["m"], P["w"], shift)).tocsr()
-    hier = None
-    if coarse == "rediscretize":
-        hier = O.build_hierarchy_rediscretized(M, P["m"], gam, P["w"], shift, True, True, wl["levels"])
-    cpu = slmg_cpu.CpuSLMG(H, SH, M, wl["levels"], hier=hier)
-    B = sources(P, wl["nrhs"], seed=0)
-    ncols = 1
-    r = cpu.solve(B[:, :1], tol=wl["tol"], max_outer=200, cycle=cycle, **rkw)
-    t1 = r.solve_s
-    ncols = int(max(1, min(ncols_max, B.shape[1], budget_s // max(t1, 1e-3))))
-    if ncols > 1:
-        r = cpu.solve(B[:, :ncols], tol=wl["tol"], max_outer=200, cycle=cycle, **rkw)
-    return dict(value=ncols / r.solve_s, unit="RHS/s", cores=r.threads, kind="port",
-                sample=f"{ncols} of the {wl['nrhs']} right-hand sides of the same workload (full grid, "
-                       f"same operator, plain FP64 SLMG ({cycle}-cycle, {coarse} coarse levels, {rkw['relax']} "
-                       f"smoothing{f' from level {relax_from}' if relax == 'jac-gmres' else ''}) in threaded C, "
-                       f"{int(r.iters.mean())} iterations per RHS)",
-                seconds=r.solve_s, setup_s=r.setup_s, max_relres=float(r.relres.max()))
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=os.environ.get("HZ_BENCH_WORKLOAD", "c2"), choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="both", choices=["both", "mixed", "fp64"])
-    ap.add_argument("--plain-steps", type=int, default=1)
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--nrhs", type=int, default=0, help="override the workload's RHS count (small profiling cases)")
-    ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
-    ap.add_argument("--outer", default="emulated", choices=["fp64", "emulated"],
-                    help="outer Krylov arithmetic of the mixed form: native FP64 or FP64 emulated with FP32 pairs")
-    ap.add_argument("--no-graph", action="store_true", help="launch the cycles eagerly (no CUDA graphs)")
-    ap.add_argument("--no-tune", action="store_true", help="default stencil launch shapes (no autotuning)")
-    ap.add_argument("--max-outer", type=int, default=200,
-                    help="FGMRES restart cycles (fewer: kernel-rate profiling runs, not a valid RHS/s)")
-    ap.add_argument("--cycle", default="V", choices=["V", "W", "K"],
-                    help="multigrid cycle (K: two FGMRES steps per coarse level)")
-    ap.add_argument("--coarse", default="galerkin", choices=["galerkin", "rediscretize"],
-                    help="coarse-level operators: Galerkin R A P, or the operator re-discretised on each coarse mesh")
-    ap.add_argument("--levels", type=int, default=0, help="multigrid levels (0: the workload's)")
-    ap.add_argument("--relax", default="jac", choices=["jac", "jac-gmres"],
-                    help="smoother: damped Jacobi, or GMRES steps preconditioned by a Jacobi sweep (relaxType "
-                         "'Jac-GMRES')")
-    ap.add_argument("--relax-from", type=int, default=0, help="jac-gmres: first level smoothed by GMRES steps")
-    ap.add_argument("--shift", type=float, default=0.5, help="s of the shifted operator SH = H + i s w^2 diag(m)")
-    ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
-    ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
-    ap.add_argument("--pairs-per-model", type=int, default=200)
-    ap.add_argument("--train-epochs", type=int, default=20)
-    ap.add_argument("--net-level", type=int, default=0, help="learned workload: multigrid level of the network "
-                    "(0: the workload's)")
-    ap.add_argument("--stag-ratio", type=float, default=0.95,
-                    help="learned workload: a restart cycle reducing a residual by less than this hands over "
-                         "to the plain cycle")
-    args = ap.parse_args()
-    peak, peak_kind = load_peaks()
-
-    if args.impl == "reference":
-        rank = int(os.environ.get("RANK", "0"))
-        if rank != 0:
-            return
-        wl = workload(args)
-        P = make_problem(wl, seed=1234)
-        import __graft_entry__ as ge
-        hz = ge.load_package()
-        gam = gamma_of(P, wl["pad"], None, hz)
-        vals = []
-        cs = None
-        for i in range(args.warmup + args.steps):
-            cs = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget / max(1, args.steps), cycle=args.cycle,
-                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from,
-                                shift=args.shift)
-            if i >= args.warmup:
-                vals.append(cs["value"])
-        v = float(np.mean(vals))
-        line = dict(metric=METRIC, value=v, unit="RHS/s", impl="reference", n_gpus=args.gpus, steps=args.steps,
-                    warmup=args.warmup, higher_is_better=True, dtype="c128",
-                    config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], cycle=args.cycle,
-                                coarse=args.coarse, relax=args.relax, relax_from=args.relax_from,
-                                shift=args.shift),
-                    cpu_baseline=dict(value=v, unit="RHS/s", cores=cs["cores"], kind="port", sample=cs["sample"]),
-                    e2e=dict(value=v, unit="RHS/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
-                    note="reference path = the C oracle port of the Julia SLMG (Julia and Multigrid.jl are absent)")
-        print(json.dumps(line))
-        return
-
-    rank, ws, dist = dist_setup()
-    if WORKLOADS[args.workload].get("learned"):
-        res, info, wl = run_learned(args, rank, ws, dist)
-        if rank != 0:
-            return
-        head = res["learned_mixed"]
-        # the metric counts right-hand sides solved to the tolerance: columns that
-        # did not converge within the restart limit count as time spent, not as solved
-        line = dict(metric=METRIC, value=head["converged_rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
-                    warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
-                    vs_baseline=None, dtype="c64 V-cycle + bf16 network / c128 outer",
-                    data="synthetic (seeded layered+inclusion models, random source positions)",
-                    config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
-                                krylov="FGMRES(10)", cycle=args.cycle, coarse=args.coarse, relax=args.relax,
-                                relax_from=args.relax_from, shift=args.shift, outer_arithmetic=args.outer,
-                                learned=True,
-                                net_level=args.net_level if args.net_level > 0 else wl["net_level"],
-                                stag_ratio=args.stag_ratio,
-                                step="solver setup + solve of one held-out model's right-hand sides",
-                                l2="inputs larger than L2 (one step touches > 1 GB)"),
-                    gpu_launches=head["launches_per_step"] * args.steps, clocks=head["clocks"],
-                    learned_over_plain_fp64=(head["converged_rhs_per_s"] / res["fp64"]["converged_rhs_per_s"]
-                                             if res["fp64"]["converged_rhs_per_s"] > 0 else None),
-                    learned_over_mixed=(head["converged_rhs_per_s"] / res["mixed"]["converged_rhs_per_s"]
-                                        if res["mixed"]["converged_rhs_per_s"] > 0 else None),
-                    arms=res, training=info)
-        print(json.dumps(line))
-        return
-    results, wl, P = run_ours(args, rank, ws, dist)
+def run_learned_main(args, rank, ws, dist):
+    res, info, wl = run_learned(args, rank, ws, dist)
     if rank != 0:
         return
-    head = results[args.precision if args.precision != "both" else "mixed"]
-    # dominant kernel of the timed region (event-timed per launch on the handle's stream)
-    kt = [k for k in head["kernels"] if k["timed"] > 0]
-    # the graph entry aggregates the cycle's kernels: the roofline names a kernel
-    kk = [k for k in kt if k["name"] != "vcycle_graph"]
-    dom = max(kk, key=lambda k: k["ms"]) if kk else None
-    roofline = None
-    if dom:
-        achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
-        ratio = traffic_ratio_from_profiles(dom["name"], args.workload) if args.nrhs == 0 else None
-        tr = None if ratio is None else ratio * dom["bytes"] / dom["launches"]
-        roofline = dict(bound="hbm", kernel=dom["name"], achieved=achieved, peak=peak, unit="GB/s",
-                        frac=achieved / peak, peak_source=f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                        traffic=tr, avg_launch_ms=dom["ms"] / dom["timed"],
-                        share=dom["ms"] / sum(k["ms"] for k in kt),
-                        source="CUDA events around every launch on the handle's stream, over the same number of "
-                               "solves right after the timed ones")
-    # whole-solve roofline: the algorithmic bytes of every launched kernel of a
-    # solve (from the profiled solves, same workload and iteration counts) over
-    # the unprofiled time of a solve
-    solve_bytes = sum(k["bytes"] for k in head["kernels"]) / max(1, head["steps"])
-    solve_roof = dict(bound="hbm", achieved=solve_bytes / (head["ms_per_step"] / 1e3) / 1e9, peak=peak, unit="GB/s",
-                      frac=solve_bytes / (head["ms_per_step"] / 1e3) / 1e9 / peak, bytes_per_solve=solve_bytes)
-    cpu = None
-    if not args.no_cpu:
-        import __graft_entry__ as ge
-        hz = ge.load_package()
-        gam = gamma_of(P, wl["pad"], None, hz)
-        cpu = run_cpu_sample(wl, P, lambda: gam, args.cpu_budget, cycle=args.cycle, coarse=args.coarse,
-                             relax=args.relax, relax_from=args.relax_from, shift=args.shift)
-    plain = results.get("fp64")
-    line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
+    head = res["learned_mixed"]
+    # the metric counts right-hand sides solved to the tolerance: columns that
+    # did not converge within the restart limit count as time spent, not as solved
+    line = dict(metric=METRIC, value=head["converged_rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
-                vs_baseline=None,
-                dtype=("c64 V-cycle / c128 outer" + (" (emulated by FP32 pairs)" if args.outer == "emulated" else "")
-                       if args.precision != "fp64" else "c128"),
-                data="synthetic (seeded layered model)",
+                vs_baseline=None, dtype="c64 cycle + bf16 network / c128 outer",
+                data="synthetic (seeded layered+inclusion models, random source positions)",
                 config=dict(workload=wl["name"], nrhs=wl["nrhs"], levels=wl["levels"], tol=wl["tol"],
-                            krylov="FGMRES(10)" if args.krylov == "fgmres" else "BiCGSTAB", cycle=args.cycle,
-                            coarse=args.coarse, relax=args.relax, relax_from=args.relax_from, shift=args.shift,
-                            cuda_graph=not args.no_graph, autotune=not args.no_tune,
-                            outer_arithmetic=args.outer,
-                            precision="mixed" if args.precision != "fp64" else "fp64", learned=False,
-                            l2="inputs larger than L2 (RHS block %.2f GB)" % (P["m"].size * wl["nrhs"] * 16 / 1e9)),
-                e2e=head.get("e2e"), gpu_launches=head["launches_per_step"] * args.steps,
-                clocks=head["clocks"], roofline=roofline, solve_roofline=solve_roof,
-                cpu_baseline=cpu,
-                max_relres=head["max_relres"], check_relres_max=head.get("check_relres_max"),
-                mean_iters=head["mean_iters"],
-                plain_fp64=None if plain is None else dict(rhs_per_s=plain["rhs_per_s"],
-                                                           ms_per_step=plain["ms_per_step"],
-                                                           mean_iters=plain["mean_iters"],
-                                                           max_relres=plain["max_relres"]),
-                mixed_over_plain=None if plain is None else head["rhs_per_s"] / plain["rhs_per_s"],
-                kernels=[dict(name=k["name"], launches=k["launches"], ms=round(k["ms"], 3),
-                              gbs=(k["bytes"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None)
-                         for k in sorted(kt, key=lambda k: -k["ms"])[:12]])
+                            krylov="FGMRES(10)", cycle=args.cycle, coarse=args.coarse, relax=args.relax,
+                            relax_from=args.relax_from, shift=args.shift, outer_arithmetic=args.outer,
+                            learned=True,
+                            net_level=args.net_level if args.net_level > 0 else wl["net_level"],
+                            stag_ratio=args.stag_ratio,
+                            step="solver setup + solve of one held-out model's right-hand sides",
+                            l2="inputs larger than L2 (one step touches > 1 GB)"),
+                gpu_launches=head["launches_per_step"] * args.steps, clocks=head["clocks"],
+                learned_over_plain_fp64=(head["converged_rhs_per_s"] / res["fp64"]["converged_rhs_per_s"]
+                                         if res["fp64"]["converged_rhs_per_s"] > 0 else None),
+                learned_over_mixed=(head["converged_rhs_per_s"] / res["mixed"]["converged_rhs_per_s"]
+                                    if res["mixed"]["converged_rhs_per_s"] > 0 else None),
+                arms=res, training=info)
     print(json.dumps(line))
 
 

@@ -116,6 +116,7 @@ SIGNATURES = {
     "hz_kernel_times": (C.c_int, [_vp, C.c_int32, C.c_char_p, C.c_int32, _i64p, _i64p, _dp, _dp]),
     "hz_reset_kernel_times": (C.c_int, [_vp]),
     "hz_set_profile": (C.c_int, [_vp, C.c_int32]),
+    "hz_set_cuda_graph": (C.c_int, [_vp, C.c_int32]),
     "hz_net_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(_vp)]),
     "hz_net_destroy": (C.c_int, [_vp]),
     "hz_net_num_params": (C.c_int64, []),

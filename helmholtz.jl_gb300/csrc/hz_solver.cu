@@ -1956,6 +1956,12 @@ int hz_reset_kernel_times(hz_handle* h) {
   return HZ_OK;
 }
 
+int hz_set_cuda_graph(hz_handle* h, int32_t on) {
+  if (!h) return HZ_ERR_ARG;
+  h->opt.cuda_graph = on != 0;
+  return HZ_OK;
+}
+
 int hz_set_profile(hz_handle* h, int32_t on) {
   if (!h) return HZ_ERR_ARG;
   cudaSetDevice(h->dev);

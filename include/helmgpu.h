@@ -217,6 +217,11 @@ int hz_tune_info(const hz_handle* h, int32_t* fine_ctas, int32_t* rap_ctas);
 /* Algorithmic flops of entry idx of the launch table (the tensor-core kernels
  * of the learned correction; 0 for the memory-bound kernels). */
 int hz_kernel_flops(hz_handle* h, int32_t idx, double* alg_flops);
+/* Replay the preconditioner applications from CUDA graphs (1) or launch them
+ * eagerly (0) from the next application on (options.cuda_graph at create time);
+ * graphs already captured are kept for when replay is switched back on.  Eager
+ * launches let per-launch profiling time each kernel of the cycle. */
+int hz_set_cuda_graph(hz_handle* h, int32_t on);
 /* Turn per-launch CUDA-event timing on (1) or off (0) (options.profile at create time). */
 int hz_set_profile(hz_handle* h, int32_t on);
 

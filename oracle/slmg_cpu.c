@@ -433,10 +433,12 @@ static double col_norm(const cplx* x, int64_t n) {
 }
 
 /* FGMRES(restart) on Hop right-preconditioned by the cycle; all columns
-   batched, each with its own Arnoldi process.  Returns restart cycles run. */
+   batched, each with its own Arnoldi process.  use_x0 != 0 starts from the
+   X passed in (a restarted solve continued over several calls takes the same
+   iterates as one call), else from zero.  Returns restart cycles run. */
 int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const double* hd, const double* Bd,
                double* Xd, int nrhs, int restart, double tol, int max_outer, double w, int pre, int post, int wcycle,
-               int relax, int gmres_from, int32_t* iters_out, double* relres_out) {
+               int relax, int gmres_from, int32_t* iters_out, double* relres_out, int use_x0) {
   slmg_t* S = (slmg_t*)h;
   const csr_t Hop = {hn, hn, hp, hi, (const cplx*)hd};
   const int64_t n = hn;
@@ -445,7 +447,7 @@ int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const 
   cplx* X = (cplx*)Xd;
   if (relax == 1 && (pre > 64 || post > 64)) return -1;
   const cyc_t cp = {w, pre, post, wcycle, relax, gmres_from};
-  memset(X, 0, sizeof(cplx) * (size_t)n * nrhs);
+  if (!use_x0) memset(X, 0, sizeof(cplx) * (size_t)n * nrhs);
   double* bn = (double*)calloc((size_t)nrhs, sizeof(double));
   int* conv = (int*)calloc((size_t)nrhs, sizeof(int));
   for (int c = 0; c < nrhs; ++c) {
@@ -456,6 +458,18 @@ int slmg_solve(void* h, int64_t hn, const int64_t* hp, const int64_t* hi, const 
   }
   cplx* Rr = (cplx*)malloc(sizeof(cplx) * (size_t)n * nrhs);
   memcpy(Rr, B, sizeof(cplx) * (size_t)n * nrhs);
+  if (use_x0) {
+    for (int c = 0; c < nrhs; ++c) {
+      if (conv[c]) continue;
+      cplx* r = Rr + (int64_t)c * n;
+      const cplx* b = B + (int64_t)c * n;
+      spmm(&Hop, X + (int64_t)c * n, n, r, n, 1, 0, 1.0);
+#pragma omp parallel for schedule(static)
+      for (int64_t p = 0; p < n; ++p) r[p] = b[p] - r[p];
+      relres_out[c] = col_norm(r, n) / bn[c];
+      if (relres_out[c] <= tol) conv[c] = 1;
+    }
+  }
   int* cols = (int*)malloc(sizeof(int) * (size_t)nrhs);
   cplx* V = (cplx*)malloc(sizeof(cplx) * (size_t)(m + 1) * n * nrhs);
   cplx* Z = (cplx*)malloc(sizeof(cplx) * (size_t)m * n * nrhs);

@@ -33,7 +33,7 @@ def lib():
         _lib.slmg_solve.restype = C.c_int
         _lib.slmg_solve.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
-                                    C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+                                    C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
     return _lib
 
 
@@ -92,12 +92,17 @@ class CpuSLMG:
         self.setup_s = time.perf_counter() - t0
 
     def solve(self, B, restart=10, tol=1e-8, max_outer=50, w=0.8, pre=1, post=1, cycle="V",
-              relax="Jac", gmres_from=0) -> CpuSolveResult:
+              relax="Jac", gmres_from=0, X0=None) -> CpuSolveResult:
         """relax: "Jac" (damped Jacobi sweeps) or "Jac-GMRES" (pre / post GMRES steps, at most 64,
-        on the levels >= gmres_from; finer levels keep damped Jacobi)."""
+        on the levels >= gmres_from; finer levels keep damped Jacobi).  X0: initial guess
+        (default zero); continuing a restarted solve from its last X over several calls
+        takes the same iterates as one call with the summed max_outer."""
         B2 = np.asfortranarray(np.asarray(B, dtype=np.complex128).reshape(B.shape[0], -1))
         n, nrhs = B2.shape
-        X = np.zeros((n, nrhs), dtype=np.complex128, order="F")
+        if X0 is None:
+            X = np.zeros((n, nrhs), dtype=np.complex128, order="F")
+        else:
+            X = np.array(np.asarray(X0, dtype=np.complex128).reshape(n, nrhs), order="F", copy=True)
         it = np.zeros(nrhs, dtype=np.int32)
         rr = np.zeros(nrhs, dtype=np.float64)
         hp, hi, hd, _ = self.H
@@ -105,7 +110,7 @@ class CpuSLMG:
         outer = lib().slmg_solve(self.h, n, hp.ctypes.data, hi.ctypes.data, hd.ctypes.data, B2.ctypes.data,
                                  X.ctypes.data, nrhs, restart, tol, max_outer, w, pre, post, {"V": 0, "W": 1, "K": 2}[cycle],
                                  {"Jac": 0, "Jac-GMRES": 1}[relax], int(gmres_from), it.ctypes.data,
-                                 rr.ctypes.data)
+                                 rr.ctypes.data, int(X0 is not None))
         if outer < 0:
             raise ValueError("Jac-GMRES takes at most 64 steps per smoothing")
         dt = time.perf_counter() - t0

@@ -248,6 +248,26 @@ def test_oracle_transpose_solve(O):
     assert np.linalg.norm(sol.X - X) / np.linalg.norm(X) < 1e-7
 
 
+def test_c_oracle_restart_cycles_continue_one_solve(O, cpu_slmg):
+    """A restarted FGMRES solve continued one restart cycle per call from the last
+    X takes the same iterates as one call (the CPU baseline times such cycles)."""
+    P = PB.gradient_2d((64, 64))
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    B = PB.rhs(P["H"].shape[0], 2, seed=9)
+    cpu = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 3)
+    whole = cpu.solve(B, tol=1e-8, max_outer=60, cycle="K")
+    X = np.zeros_like(B)
+    iters = np.zeros(2, dtype=np.int64)
+    for _ in range(60):
+        r = cpu.solve(B, tol=1e-8, max_outer=1, cycle="K", X0=X)
+        X = r.X
+        iters += r.iters
+        if np.all(r.relres <= 1e-8):
+            break
+    np.testing.assert_array_equal(iters, whole.iters)
+    assert np.linalg.norm(X - whole.X) <= 1e-12 * np.linalg.norm(whole.X)
+
+
 def test_c_oracle_matches_numpy_oracle(O, cpu_slmg):
     P = PB.gradient_2d((64, 64))
     SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
