@@ -64,8 +64,38 @@ template <typename T> __host__ __device__ __forceinline__ cplx<T> cscale(T s, cp
 }
 template <typename T> __host__ __device__ __forceinline__ cplx<T> cconj(cplx<T> a) { return mk<T>(a.x, -a.y); }
 
+// FP32 -> FP64 widening from the IEEE-754 bit layouts, exact: for a normal
+// number the 8-bit exponent is re-biased (127 -> 1023) and the 23-bit fraction
+// moves to the top of the 52-bit fraction, with integer operations only.
+// Returns false for zero, subnormal, infinite and NaN inputs (the caller uses
+// the hardware conversion for those).  GB300's FP64 pipe also executes the
+// hardware conversion, so FP64 kernels that widen FP32 data (H z with z from
+// the complex-FP32 cycle, x += Z y) use this to keep the conversions off it.
+__host__ __device__ __forceinline__ bool widen_f32_bits(uint32_t u, uint32_t& hi, uint32_t& lo) {
+  const uint32_t a = u & 0x7fffffffu;
+  if (a - 0x00800000u >= 0x7f000000u) return false;
+  hi = ((a >> 3) + 0x38000000u) | (u & 0x80000000u);
+  lo = u << 29;
+  return true;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ double widen_f32(float f) {
+  uint32_t hi, lo;
+  if (!widen_f32_bits(__float_as_uint(f), hi, lo)) return (double)f;
+  return __hiloint2double((int)hi, (int)lo);
+}
+#endif
+
 template <typename To, typename From> __host__ __device__ __forceinline__ cplx<To> ccast(cplx<From> a) {
   return mk<To>((To)a.x, (To)a.y);
+}
+template <> __host__ __device__ __forceinline__ cplx<double> ccast<double, float>(cplx<float> a) {
+#ifdef __CUDA_ARCH__
+  return mk<double>(widen_f32(a.x), widen_f32(a.y));
+#else
+  return mk<double>((double)a.x, (double)a.y);
+#endif
 }
 
 // Node grid of one multigrid level.  2D grids have nz == 1.

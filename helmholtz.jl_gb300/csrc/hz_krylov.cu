@@ -358,12 +358,12 @@ __global__ void __launch_bounds__(256) k_update_x(long long N, const cplx<TZ>* _
     for (int s = 0; s < KG; ++s) {
       if (s < k) {
         const cplx<TZ> z = Z[((long long)s * zstride + c) * ld + p];
-        acc = cfma<double>(yv[s], mk<double>((double)z.x, (double)z.y), acc);
+        acc = cfma<double>(yv[s], ccast<double, TZ>(z), acc);
       }
     }
     for (int s = KG; s < k; ++s) {  // restart lengths above KG
       const cplx<TZ> z = Z[((long long)s * zstride + c) * ld + p];
-      acc = cfma<double>(y[(long long)c * ystride + s], mk<double>((double)z.x, (double)z.y), acc);
+      acc = cfma<double>(y[(long long)c * ystride + s], ccast<double, TZ>(z), acc);
     }
     xc[p] = acc;
   }
