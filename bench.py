@@ -69,7 +69,10 @@ WORKLOADS = {
     # five-level Galerkin hierarchy converges with the K-cycle and GMRES smoothing from level 1
     "c5": dict(name="3D 257^3 layered+ellipsoid, 32 surface sources, 5 levels, FGMRES(10) tol 1e-6",
                cells=(256, 256, 256), h=0.010, nrhs=32, levels=5, pad=16, ellipsoid=True, tol=1e-6, err_cols=1,
-               cycle="K", relax="jac-gmres", relax_from=1, shift=0.3),
+               cycle="K", relax="jac-gmres", relax_from=1, shift=0.3,
+               # 3D learned correction below level 2 (65^3): pairs from seeded training models
+               learned3d=True, net_level=2, train_models=6, train_rhs=4, pairs_per_model=160, train_outer=2,
+               pair_sweeps=12, train_epochs=30, train_batch=8),
 }
 DEFAULT_WORKLOAD = "c5"
 
@@ -292,13 +295,87 @@ def traffic_ratio_from_profiles(kernel: str, workload: str):
 # GPU arms
 # ---------------------------------------------------------------------------
 ARMS = {
-    # name: (precision, outer arithmetic)
-    "mixed": ("mixed", "fp64"),
-    "mixed_emulated": ("mixed", "emulated"),
-    "fp64": ("fp64", "fp64"),
+    # name: (precision, outer arithmetic, learned correction)
+    "learned_mixed": ("mixed", "fp64", True),
+    "mixed": ("mixed", "fp64", False),
+    "mixed_emulated": ("mixed", "emulated", False),
+    "learned_emulated": ("mixed", "emulated", True),
+    "fp64": ("fp64", "fp64", False),
 }
 ARM_SETS = {"all": ["mixed", "mixed_emulated", "fp64"], "both": ["mixed", "fp64"], "mixed": ["mixed"],
             "emulated": ["mixed_emulated"], "fp64": ["fp64"]}
+# with the learned correction the headline is the metric's own learned+mixed form
+ARM_SETS_LEARNED = {"all": ["learned_mixed", "mixed", "mixed_emulated", "learned_emulated", "fp64"],
+                    "both": ["learned_mixed", "fp64"], "mixed": ["learned_mixed"], "emulated": ["learned_emulated"],
+                    "fp64": ["fp64"]}
+
+
+def arm_names(args, wl) -> list:
+    learned = wl.get("learned3d") and not args.no_learned
+    return (ARM_SETS_LEARNED if learned else ARM_SETS)[args.precision]
+
+
+def sources_random3(P: dict, nrhs: int, seed: int, pad: int) -> np.ndarray:
+    """Delta sources q = 1/||h||^2 at seeded random nodes of a 3D grid outside the absorbing layer."""
+    rng = np.random.default_rng(seed)
+    nn = P["nodes"]
+    B = np.zeros((int(np.prod(nn)), nrhs), dtype=np.complex128, order="F")
+    amp = 1.0 / float(np.linalg.norm(P["h"])) ** 2
+    for c in range(nrhs):
+        i = int(rng.integers(pad, nn[0] - pad))
+        j = int(rng.integers(pad, nn[1] - pad))
+        k = int(rng.integers(1, nn[2] - pad))
+        B[i + nn[0] * (j + nn[1] * k), c] = amp
+    return B
+
+
+def train_network3d(args, wl, hz, lib):
+    """Training pairs on the network's level from the FP64 solver on seeded
+    training models (the first restart cycles of solves with random sources),
+    then GPU training of the 3D network by the library's kernels."""
+    import torch
+    level = wl["net_level"]
+    xs, ts, pes, worst = [], [], [], 0.0
+    t0 = time.perf_counter()
+    for s in range(wl["train_models"]):
+        P = make_problem(wl, seed=10_000 + s)
+        gam = gamma_of(P, wl["pad"], lib, hz)
+        M = hz.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
+        param = hz.HelmholtzParam(M, gam, P["m"], P["w"], True, True)
+        MG = hz.getMGparam(complex, int, wl["levels"], 1, wl["train_outer"], wl["tol"],
+                           "Jac-GMRES" if args.relax == "jac-gmres" else "Jac", 0.8, 1, 1, args.cycle, "Julia",
+                           args.shift, 0.0, precision="fp64", relaxFrom=args.relax_from)
+        S = hz.getShiftedLaplacianMultigridSolver(param, MG, args.shift, "GMRES", 10)
+        B = sources_random3(P, wl["train_rhs"], seed=20_000 + s, pad=wl["pad"])
+        d = hz.learned.collect_pairs(S, B, level=level, sweeps=wl["pair_sweeps"], max_pairs=wl["pairs_per_model"])
+        xs.append(d["x"].clone())
+        ts.append(d["t"].clone())
+        pes.append(d["plain_err"])
+        worst = max(worst, float(d["target_relres"]))
+        del S, d
+        torch.cuda.empty_cache()
+    x = torch.cat(xs).contiguous()
+    t = torch.cat(ts).contiguous()
+    del xs, ts
+    collect_s = time.perf_counter() - t0
+    net = hz.learned.CoarseNet3D(seed=1)
+    t0 = time.perf_counter()
+    hist = net.train(x, t, epochs=wl["train_epochs"], batch=wl["train_batch"], lr=2e-3, seed=3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    err = hz.learned.pair_errors(net, x[:256], t[:256], batch=8)
+    pe = np.concatenate(pes)
+    info = dict(train_models=wl["train_models"], train_pairs=int(x.shape[0]), grid=list(x.shape[1:4][::-1]),
+                level=level, epochs=wl["train_epochs"], batch=wl["train_batch"], loss_first=float(hist[0]),
+                loss_last=float(hist[-1]), collect_s=collect_s, train_s=train_s,
+                target_relres_max=worst, pair_error_median_network=float(np.median(err)),
+                pair_error_median_plain_correction=float(np.median(pe)),
+                pairs="level-2 right-hand sides of the first %d restart cycles of FP64 solves of %d random sources "
+                      "per training model; targets from %d restarted plain corrections on that level"
+                      % (wl["train_outer"], wl["train_rhs"], wl["pair_sweeps"]))
+    del x, t
+    torch.cuda.empty_cache()
+    return net, info
 
 
 def run_ours(args, rank, ws, dist):
@@ -372,11 +449,16 @@ def run_ours(args, rank, ws, dist):
         return e0.elapsed_time(e1) / 1000.0, last
 
     results = {}
-    names = ARM_SETS[args.precision]
+    names = arm_names(args, wl)
+    net, train_info = None, None
+    if any(ARMS[nm][2] for nm in names):
+        net, train_info = train_network3d(args, wl, hz, lib)
     for ai, name in enumerate(names):
-        prec, outer = ARMS[name]
+        prec, outer, use_net = ARMS[name]
         head = ai == 0
         hh = make_handle(prec, outer)
+        if use_net:
+            L.check(lib.hz_attach_net(hh, net._h, wl["net_level"], args.stag_ratio), hh)
         warm = args.warmup if head else max(1, args.arm_warmup)
         steps = args.steps if head else max(1, args.plain_steps if name == "fp64" else args.arm_steps)
         t_setup0 = time.perf_counter()
@@ -393,7 +475,11 @@ def run_ours(args, rank, ws, dist):
         it = np.zeros(nrhs, dtype=np.int32)
         lib.hz_column_stats(hh, rr.ctypes.data_as(C.POINTER(C.c_double)), it.ctypes.data_as(C.POINTER(C.c_int32)),
                             nrhs)
-        res = dict(precision=prec, outer_arithmetic=outer, seconds=t, steps=steps, warmup=warm,
+        calls, fbs = C.c_int64(0), C.c_int32(0)
+        if use_net:
+            lib.hz_learned_stats(hh, C.byref(calls), C.byref(fbs))
+        res = dict(precision=prec, outer_arithmetic=outer, learned=use_net, net_calls=int(calls.value),
+                   net_fallbacks=int(fbs.value), seconds=t, steps=steps, warmup=warm,
                    rhs_per_s=nrhs * ws * steps / t, ms_per_step=1000.0 * t / steps, max_relres=float(rr.max()),
                    converged_cols=int(np.sum(rr <= wl["tol"])), mean_iters=float(it.mean()), max_iters=int(it.max()),
                    outer=int(st.outer), launches_per_step=launches, clocks=clocks.summary(),
@@ -440,7 +526,7 @@ def run_ours(args, rank, ws, dist):
         torch.cuda.empty_cache()
     del Bd, Xd
     torch.cuda.empty_cache()
-    return results, wl, P, B, err_cols
+    return results, wl, P, B, err_cols, train_info
 
 
 # ---------------------------------------------------------------------------
@@ -519,6 +605,8 @@ def main():
     ap.add_argument("--arm-warmup", type=int, default=1, help="untimed solves before the other arms' timed ones")
     ap.add_argument("--e2e-steps", type=int, default=3, help="end-to-end solves (host buffers), at most --steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the 3D oracle error")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="3D 257^3 workload: skip the learned correction (no training, no learned arms)")
     ap.add_argument("--nrhs", type=int, default=0, help="override the workload's RHS count (small profiling cases)")
     ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
     ap.add_argument("--no-graph", action="store_true", help="launch the cycles eagerly (no CUDA graphs)")
@@ -558,10 +646,10 @@ def main():
     if WORKLOADS[args.workload].get("learned"):
         run_learned_main(args, rank, ws, dist)
         return
-    results, wl, P, B, err_cols = run_ours(args, rank, ws, dist)
+    results, wl, P, B, err_cols, train_info = run_ours(args, rank, ws, dist)
     if rank != 0:
         return
-    names = ARM_SETS[args.precision]
+    names = arm_names(args, wl)
     head = results[names[0]]
     # per-kernel rates of the eager profiled solve; the dominant kernel names the roofline
     kt = [k for k in head["kernels"] if k["timed"] > 0]
@@ -609,31 +697,42 @@ def main():
     emu = results.get("mixed_emulated")
 
     def arm_summary(r, name):
-        return dict(precision=r["precision"], outer_arithmetic=r["outer_arithmetic"], rhs_per_s=r["rhs_per_s"],
-                    ms_per_step=r["ms_per_step"], steps=r["steps"], warmup=r["warmup"], mean_iters=r["mean_iters"],
-                    max_iters=r["max_iters"], max_relres=r["max_relres"], converged_cols=r["converged_cols"],
-                    max_err_vs_oracle=errs.get(name), clocks=r["clocks"])
+        return dict(precision=r["precision"], outer_arithmetic=r["outer_arithmetic"], learned=r["learned"],
+                    rhs_per_s=r["rhs_per_s"], ms_per_step=r["ms_per_step"], steps=r["steps"], warmup=r["warmup"],
+                    mean_iters=r["mean_iters"], max_iters=r["max_iters"], max_relres=r["max_relres"],
+                    converged_cols=r["converged_cols"], max_err_vs_oracle=errs.get(name),
+                    net_calls=r["net_calls"], net_fallbacks=r["net_fallbacks"], clocks=r["clocks"])
+
+    def over_plain(name):
+        r = results.get(name)
+        return None if (r is None or plain is None) else r["rhs_per_s"] / plain["rhs_per_s"]
 
     line = dict(metric=METRIC, value=head["rhs_per_s"], unit="RHS/s", n_gpus=ws, steps=args.steps,
                 warmup=args.warmup, ms_per_step=head["ms_per_step"], higher_is_better=True, scaling="weak",
                 vs_baseline=None,
-                dtype=("c64 cycle / c128 outer" + (" (emulated by FP32 pairs)" if head["outer_arithmetic"] == "emulated"
-                                                   else "") if head["precision"] == "mixed" else "c128"),
+                dtype=("c64 cycle" + (" + bf16 network" if head["learned"] else "") + " / c128 outer" +
+                       (" (emulated by FP32 pairs)" if head["outer_arithmetic"] == "emulated" else "")
+                       if head["precision"] == "mixed" else "c128"),
                 data="synthetic (seeded layered+ellipsoid model)" if P["dim"] == 3 else "synthetic (seeded model)",
                 config=dict(run_config(args, wl, P), precision=head["precision"],
                             outer_arithmetic=head["outer_arithmetic"], cuda_graph=not args.no_graph,
-                            autotune=not args.no_tune),
+                            autotune=not args.no_tune, learned=bool(head["learned"]),
+                            net_level=wl.get("net_level") if head["learned"] else None),
                 e2e=head.get("e2e"), gpu_launches=head["launches_per_step"] * args.steps,
                 clocks=head["clocks"], roofline=roofline, solve_roofline=solve_roof,
                 cpu_baseline=cpu,
                 max_relres=head["max_relres"], check_relres_max=head.get("check_relres_max"),
                 converged_cols=head["converged_cols"], mean_iters=head["mean_iters"],
                 max_err_vs_oracle=errs.get(names[0]), err_oracle=err_info,
+                arms={nm: arm_summary(r, nm) for nm, r in results.items()},
                 plain_fp64=None if plain is None else arm_summary(plain, "fp64"),
-                mixed_over_plain=None if plain is None else head["rhs_per_s"] / plain["rhs_per_s"],
+                headline_over_plain=over_plain(names[0]),
+                learned_over_plain_fp64=over_plain("learned_mixed"),
+                mixed_over_plain=over_plain("mixed"),
                 emulated_outer=None if emu is None else arm_summary(emu, "mixed_emulated"),
-                emulated_over_plain=(None if (emu is None or plain is None)
-                                     else emu["rhs_per_s"] / plain["rhs_per_s"]),
+                emulated_over_plain=over_plain("mixed_emulated"),
+                learned_emulated_over_plain=over_plain("learned_emulated"),
+                training=train_info,
                 kernels=[dict(name=k["name"], launches=k["launches"], ms=round(k["ms"], 3),
                               gbs=(k["bytes"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None,
                               frac=(k["bytes"] / (k["ms"] / 1e3) / 1e9 / peak) if k["ms"] > 0 else None,
@@ -684,7 +783,7 @@ def run_reference(args):
                 scaling="weak", vs_baseline=None, dtype="c128",
                 data="synthetic (seeded layered+ellipsoid model)" if P["dim"] == 3 else "synthetic (seeded model)",
                 config=dict(run_config(args, wl, P), precision="fp64", outer_arithmetic="fp64", cuda_graph=False,
-                            autotune=False),
+                            autotune=False, learned=False, net_level=None),
                 cpu_baseline=dict(value=v, unit="RHS/s", cores=thr, kind="port",
                                   sample=f"one restart cycle (10 FGMRES iterations) of one column per step, full "
                                          f"grid, {orc.desc}; {per_rhs:.0f} iterations per right-hand side "

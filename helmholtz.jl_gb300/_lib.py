@@ -127,6 +127,15 @@ SIGNATURES = {
     "hz_net_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _dp, _vp]),
     "hz_net_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_double,
                                C.c_int32, _dp]),
+    "hz_net3d_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(_vp)]),
+    "hz_net3d_num_params": (C.c_int64, []),
+    "hz_net3d_layer_shape": (C.c_int, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "hz_net_dim": (C.c_int, [_vp]),
+    "hz_net3d_forward": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32]),
+    "hz_net3d_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _dp,
+                                    _vp]),
+    "hz_net3d_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
+                                 C.c_double, C.c_int32, _dp]),
     "hz_kernel_flops": (C.c_int, [_vp, C.c_int32, _dp]),
     "hz_tune_info": (C.c_int, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "hz_net_save": (C.c_int, [_vp, C.c_char_p]),

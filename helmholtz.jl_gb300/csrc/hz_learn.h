@@ -93,6 +93,89 @@ class CoarseNet {
   long long bcap_ = 0;
 };
 
+// 3D convolutional encoder-decoder of the same kind (three grid levels, 8-16-32
+// channels, 3x3x3 convolutions; the layers and their order are in hz_learn3d.cu):
+//   input  x [B][N][4] FP32 and output y [B][N][8] FP32 as for the 2D network,
+//   N = nx * ny * nz, axis 1 fastest; n - 1 divisible by 4 on every axis.
+// Weights exchanged with the host: layer after layer, each [cout][27][cin] with
+// tap t = 9 (dz + 1) + 3 (dy + 1) + (dx + 1).
+class CoarseNet3 {
+ public:
+  static constexpr int kLayers = 6;
+  explicit CoarseNet3(unsigned seed);
+  ~CoarseNet3();
+  CoarseNet3(const CoarseNet3&) = delete;
+  CoarseNet3& operator=(const CoarseNet3&) = delete;
+
+  static long long num_params();
+  static bool supports(long long nx, long long ny, long long nz);
+  static void layer_shape(int l, int* cin, int* cout);
+
+  void get_weights(float* host) const;
+  void set_weights(const float* host);
+  void get_grad(float* host) const;
+  void save(const char* path) const;
+  void load(const char* path);
+  static int file_info(const char* path, long long* nparams, long long* step);
+
+  void forward(Ctx& c, const float* x4, int nx, int ny, int nz, int B, bool train = false);
+  const float* output() const { return y32_; }
+  float* input_staging(int nx, int ny, int nz, int B);
+  float* scale_staging(int B);
+  double backward(Ctx& c, const float* t, int nx, int ny, int nz, int B);
+  void adam(Ctx& c, double lr);
+  void train(Ctx& c, const float* x, const float* t, int nx, int ny, int nz, long long nsamples, int batch,
+             int epochs, double lr, unsigned seed, double* loss_hist);
+
+  Ctx ctx;
+
+ private:
+  void ensure(int nx, int ny, int nz, int B, bool grads);
+  void release_acts();
+  void conv_fwd(Ctx& c, int l, int B, const __nv_bfloat16* in, int ldi, int i_off, __nv_bfloat16* out, int ldo,
+                int o_off, int relu, float* out32);
+  void conv_bwd(Ctx& c, int l, int B, const __nv_bfloat16* in, int ldi, const __nv_bfloat16* dout, int ldd,
+                int d_off, __nv_bfloat16* din, int ldn, int n_off, const __nv_bfloat16* mask, int ldm, int mask_lo);
+
+  long long woff_[kLayers] = {};
+  long long wtotal_ = 0;
+  float* w32_ = nullptr;
+  __nv_bfloat16* wbf_ = nullptr;
+  __nv_bfloat16* wt_ = nullptr;
+  float* g32_ = nullptr;
+  float* m_ = nullptr;
+  float* v_ = nullptr;
+  long long step_ = 0;
+  int g_[3][3] = {};  // node counts (x, y, z) of the network's three grids
+  int B_ = 0;
+  bool grads_ = false;
+  __nv_bfloat16* act_[8] = {};
+  __nv_bfloat16* grd_[8] = {};
+  float* y32_ = nullptr;
+  float* x4_ = nullptr;
+  long long x4cap_ = 0;
+  float* scale_ = nullptr;
+  int scalecap_ = 0;
+  double* loss_ = nullptr;
+  float* bx_ = nullptr;
+  float* bt_ = nullptr;
+  int* perm_ = nullptr;
+  long long bcap_ = 0;
+};
+
+// Kernels the 2D and 3D networks share (hz_learn.cu): input assembly into
+// 16-channel rows, the loss and its gradient, Adam, FP32 -> BF16, and the
+// mini-batch gather of training pairs.
+__global__ void k_pack_in(long long BN, const float4* __restrict__ x4, __nv_bfloat16* __restrict__ x16);
+__global__ void __launch_bounds__(256) k_loss(int N, int B, const float* __restrict__ y, const float* __restrict__ t,
+                                              __nv_bfloat16* __restrict__ dy, double* __restrict__ loss);
+__global__ void k_adam(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, __nv_bfloat16* __restrict__ wb, float lr, float b1, float b2, float eps,
+                       float c1, float c2);
+__global__ void k_f2bf(long long n, const float* __restrict__ a, __nv_bfloat16* __restrict__ b);
+__global__ void k_gather_pairs(int B, long long N, const int* __restrict__ perm, const float4* __restrict__ x,
+                               const float2* __restrict__ t, float4* __restrict__ bx, float2* __restrict__ bt);
+
 // Column RMS s_k of the active columns of b (one level, ld-strided), then the
 // network input x[k][p] = (b/s, feat[p]) (conj: the adjoint solve feeds conj(b)).
 template <typename T>

@@ -167,7 +167,8 @@ struct hz_handle {
   std::vector<int> col_iters;
   long long h2d = 0, d2h = 0;
   // learned coarse-grid correction (the network is owned by the caller)
-  hz::CoarseNet* net = nullptr;
+  hz::CoarseNet* net = nullptr;    // 2D network, or
+  hz::CoarseNet3* net3 = nullptr;  // 3D network (at most one of the two is attached)
   int net_level = 0;         // level whose correction the network computes
   double net_stag = 0.5;     // restart-cycle residual ratio above which the plain cycle takes over
   bool net_active = false;   // network in use by the running solve
@@ -698,16 +699,19 @@ void lev_jacobi0(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* 
 }
 
 // Network input features on level l: the medium restricted l times by nodal
-// full weighting, as w^2 m hx hy and gamma / w (w = Re omega).
+// full weighting, as w^2 m hx hy and gamma / w (w = Re omega); hx hy (the
+// square of the cell size for the cubic cells of the 3D grids) scales the
+// network's output back to an error.
 const float2* net_features(hz_handle* h, int l) {
   if (h->net_feat_level == l) return h->net_feat.as<float2>();
+  const int dim = h->prob.dim;
   Grid g = h->g0;
   std::vector<double> m = h->m, gm = h->gamma;
   double hx = h->prob.h[0], hy = h->prob.h[1];
   for (int k = 0; k < l; ++k) {
-    const Grid c = coarsen(g, 2);
-    m = restrict_nodal(m, g, c, 2);
-    gm = restrict_nodal(gm, g, c, 2);
+    const Grid c = coarsen(g, dim);
+    m = restrict_nodal(m, g, c, dim);
+    gm = restrict_nodal(gm, g, c, dim);
     g = c;
     hx *= 2.0;
     hy *= 2.0;
@@ -728,13 +732,26 @@ const float2* net_features(hz_handle* h, int l) {
 template <typename T>
 void learned_correction(hz_handle* h, Hierarchy& H, int l, const cplx<T>* b, cplx<T>* out, const int* cols, int nc) {
   Level& L = *H.lv[l];
-  hz::CoarseNet* net = h->net;
   const float2* feat = net_features(h, l);
-  float* x4 = net->input_staging(L.g.nx, L.g.ny, nc);
-  float* sc = net->scale_staging(nc);
-  launch_net_pack<T>(h->ctx, L.g.N, b, L.ld, cols, nc, feat, H.adj, sc, x4);
-  net->forward(h->ctx, x4, L.g.nx, L.g.ny, nc);
-  launch_net_unpack<T>(h->ctx, L.g.N, net->output(), sc, h->net_h2, H.adj, out, L.ld, cols, nc);
+  float* x4;
+  float* sc;
+  const float* y;
+  if (h->net3) {
+    hz::CoarseNet3* net = h->net3;
+    x4 = net->input_staging(L.g.nx, L.g.ny, L.g.nz, nc);
+    sc = net->scale_staging(nc);
+    launch_net_pack<T>(h->ctx, L.g.N, b, L.ld, cols, nc, feat, H.adj, sc, x4);
+    net->forward(h->ctx, x4, L.g.nx, L.g.ny, L.g.nz, nc);
+    y = net->output();
+  } else {
+    hz::CoarseNet* net = h->net;
+    x4 = net->input_staging(L.g.nx, L.g.ny, nc);
+    sc = net->scale_staging(nc);
+    launch_net_pack<T>(h->ctx, L.g.N, b, L.ld, cols, nc, feat, H.adj, sc, x4);
+    net->forward(h->ctx, x4, L.g.nx, L.g.ny, nc);
+    y = net->output();
+  }
+  launch_net_unpack<T>(h->ctx, L.g.N, y, sc, h->net_h2, H.adj, out, L.ld, cols, nc);
   h->net_calls += 1;
 }
 
@@ -1221,7 +1238,7 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
     hz_handle* h;
     ~NetScope() { h->net_active = false; }
   } net_scope{h};
-  h->net_active = h->net != nullptr;
+  h->net_active = h->net != nullptr || h->net3 != nullptr;
   std::vector<double> prev = bn;
   if (mixed)
     ensure_level_buffers<float>(h, H, h->rcap);
@@ -1615,8 +1632,11 @@ int guarded(hz_handle* h, F&& f) {
 // A trained or training coarse-correction network on one device.
 struct hz_net {
   int dev = 0;
-  std::unique_ptr<hz::CoarseNet> net;
+  std::unique_ptr<hz::CoarseNet> net;    // the 2D network, or
+  std::unique_ptr<hz::CoarseNet3> net3;  // the 3D network
   cudaEvent_t order_ev = nullptr;  // orders the network's stream after the legacy default stream
+  int dim() const { return net3 ? 3 : 2; }
+  hz::Ctx& ctx() { return net3 ? net3->ctx : net->ctx; }
   ~hz_net() {
     if (order_ev) cudaEventDestroy(order_ev);
   }
@@ -1626,7 +1646,7 @@ namespace {
 // As order_after_default_stream, for the network's own stream.
 void net_order_after_default_stream(hz_net* net) {
   ck(cudaEventRecord(net->order_ev, cudaStreamLegacy), "record ordering event");
-  ck(cudaStreamWaitEvent(net->net->ctx.stream, net->order_ev, 0), "order after the default stream");
+  ck(cudaStreamWaitEvent(net->ctx().stream, net->order_ev, 0), "order after the default stream");
 }
 }  // namespace
 
@@ -1973,7 +1993,9 @@ int hz_set_profile(hz_handle* h, int32_t on) {
 
 // ---- learned coarse-grid correction -------------------------------------------
 
-int hz_net_create(int32_t seed, int32_t device, hz_net** out) {
+namespace {
+// A network on a device: the 2D encoder-decoder (dim 2) or the 3D one (dim 3).
+int net_create(int32_t seed, int32_t device, int dim, hz_net** out) {
   if (!out) return HZ_ERR_ARG;
   *out = nullptr;
   auto n = std::make_unique<hz_net>();
@@ -1986,12 +2008,32 @@ int hz_net_create(int32_t seed, int32_t device, hz_net** out) {
     if (device < 0 || device >= cnt) fail(HZ_ERR_ARG, "device %d out of range", device);
     ck(cudaSetDevice(device), "cudaSetDevice");
     n->dev = device;
-    n->net = std::make_unique<hz::CoarseNet>((unsigned)seed);
+    if (dim == 3)
+      n->net3 = std::make_unique<hz::CoarseNet3>((unsigned)seed);
+    else
+      n->net = std::make_unique<hz::CoarseNet>((unsigned)seed);
     ck(cudaEventCreateWithFlags(&n->order_ev, cudaEventDisableTiming), "ordering event");
   });
   if (st == HZ_OK) *out = n.release();
   return st;
 }
+
+void check_net3_grid(long long nx, long long ny, long long nz, int batch) {
+  if (!hz::CoarseNet3::supports(nx, ny, nz))
+    fail(HZ_ERR_ARG, "network grid %lldx%lldx%lld: node counts must be 4k+1 (k >= 1)", nx, ny, nz);
+  if (batch < 1) fail(HZ_ERR_ARG, "batch must be >= 1");
+}
+
+void need_dim(const hz_net* net, int dim, const char* what) {
+  if (net->dim() != dim) fail(HZ_ERR_ARG, "%s takes a %dD network (this one is %dD)", what, dim, net->dim());
+}
+}  // namespace
+
+int hz_net_create(int32_t seed, int32_t device, hz_net** out) { return net_create(seed, device, 2, out); }
+
+int hz_net3d_create(int32_t seed, int32_t device, hz_net** out) { return net_create(seed, device, 3, out); }
+
+int hz_net_dim(const hz_net* net) { return net ? net->dim() : HZ_ERR_ARG; }
 
 int hz_net_destroy(hz_net* net) {
   if (!net) return HZ_OK;
@@ -2002,6 +2044,8 @@ int hz_net_destroy(hz_net* net) {
 
 int64_t hz_net_num_params(void) { return hz::CoarseNet::num_params(); }
 
+int64_t hz_net3d_num_params(void) { return hz::CoarseNet3::num_params(); }
+
 int hz_net_layer_shape(int32_t layer, int32_t* cin, int32_t* cout) {
   if (layer < 0 || layer >= hz::CoarseNet::kLayers || !cin || !cout) return HZ_ERR_ARG;
   int a = 0, b = 0;
@@ -2011,11 +2055,23 @@ int hz_net_layer_shape(int32_t layer, int32_t* cin, int32_t* cout) {
   return HZ_OK;
 }
 
+int hz_net3d_layer_shape(int32_t layer, int32_t* cin, int32_t* cout) {
+  if (layer < 0 || layer >= hz::CoarseNet3::kLayers || !cin || !cout) return HZ_ERR_ARG;
+  int a = 0, b = 0;
+  hz::CoarseNet3::layer_shape(layer, &a, &b);
+  *cin = a;
+  *cout = b;
+  return HZ_OK;
+}
+
 int hz_net_get_weights(hz_net* net, float* w) {
   if (!net || !w) return HZ_ERR_ARG;
   return guarded(nullptr, [&] {
     ck(cudaSetDevice(net->dev), "cudaSetDevice");
-    net->net->get_weights(w);
+    if (net->net3)
+      net->net3->get_weights(w);
+    else
+      net->net->get_weights(w);
   });
 }
 
@@ -2023,31 +2079,92 @@ int hz_net_set_weights(hz_net* net, const float* w) {
   if (!net || !w) return HZ_ERR_ARG;
   return guarded(nullptr, [&] {
     ck(cudaSetDevice(net->dev), "cudaSetDevice");
-    net->net->set_weights(w);
+    if (net->net3)
+      net->net3->set_weights(w);
+    else
+      net->net->set_weights(w);
   });
 }
+
+namespace {
+// y = net(x) for a batch on a grid of nz = 1 (2D) or nz > 1 (3D) planes
+void net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, int64_t nz, int32_t batch,
+                 int32_t mem) {
+  if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "mem must be HZ_MEM_HOST or HZ_MEM_DEVICE");
+  ck(cudaSetDevice(net->dev), "cudaSetDevice");
+  hz::Ctx& cx = net->ctx();
+  const long long N = nx * ny * nz;
+  const float* dx = x;
+  if (mem == HZ_MEM_DEVICE) net_order_after_default_stream(net);
+  if (mem == HZ_MEM_HOST) {
+    float* st = net->net3 ? net->net3->input_staging((int)nx, (int)ny, (int)nz, batch)
+                          : net->net->input_staging((int)nx, (int)ny, batch);
+    ck(cudaMemcpyAsync(st, x, (size_t)batch * N * 16, cudaMemcpyHostToDevice, cx.stream), "copy x");
+    dx = st;
+  }
+  const float* out;
+  if (net->net3) {
+    net->net3->forward(cx, dx, (int)nx, (int)ny, (int)nz, batch);
+    out = net->net3->output();
+  } else {
+    net->net->forward(cx, dx, (int)nx, (int)ny, batch);
+    out = net->net->output();
+  }
+  ck(cudaMemcpy2DAsync(y, 8, out, 32, 8, (size_t)batch * N,
+                       mem == HZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, cx.stream),
+     "copy y");
+  ck(cudaStreamSynchronize(cx.stream), "sync");
+  cx.resolve();
+}
+
+void net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int32_t batch,
+                  int32_t mem, double* loss, float* grad) {
+  if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "mem must be HZ_MEM_HOST or HZ_MEM_DEVICE");
+  ck(cudaSetDevice(net->dev), "cudaSetDevice");
+  hz::Ctx& cx = net->ctx();
+  const long long N = nx * ny * nz;
+  DBuf bx, bt;
+  const float* dx = x;
+  const float* dt = t;
+  if (mem == HZ_MEM_DEVICE) net_order_after_default_stream(net);
+  if (mem == HZ_MEM_HOST) {
+    bx.alloc((size_t)batch * N * 16);
+    bt.alloc((size_t)batch * N * 8);
+    ck(cudaMemcpyAsync(bx.p, x, (size_t)batch * N * 16, cudaMemcpyHostToDevice, cx.stream), "copy x");
+    ck(cudaMemcpyAsync(bt.p, t, (size_t)batch * N * 8, cudaMemcpyHostToDevice, cx.stream), "copy t");
+    dx = bx.as<float>();
+    dt = bt.as<float>();
+  }
+  double l;
+  if (net->net3) {
+    net->net3->forward(cx, dx, (int)nx, (int)ny, (int)nz, batch, true);
+    l = net->net3->backward(cx, dt, (int)nx, (int)ny, (int)nz, batch);
+    if (grad) net->net3->get_grad(grad);
+  } else {
+    net->net->forward(cx, dx, (int)nx, (int)ny, batch, true);
+    l = net->net->backward(cx, dt, (int)nx, (int)ny, batch);
+    if (grad) net->net->get_grad(grad);
+  }
+  if (loss) *loss = l;
+}
+}  // namespace
 
 int hz_net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, int32_t batch, int32_t mem) {
   if (!net || !x || !y) return HZ_ERR_ARG;
   return guarded(nullptr, [&] {
+    need_dim(net, 2, "hz_net_forward");
     check_net_grid(nx, ny, batch);
-    if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "mem must be HZ_MEM_HOST or HZ_MEM_DEVICE");
-    ck(cudaSetDevice(net->dev), "cudaSetDevice");
-    hz::CoarseNet& c = *net->net;
-    const long long N = nx * ny;
-    const float* dx = x;
-    if (mem == HZ_MEM_DEVICE) net_order_after_default_stream(net);
-    if (mem == HZ_MEM_HOST) {
-      float* st = c.input_staging((int)nx, (int)ny, batch);
-      ck(cudaMemcpyAsync(st, x, (size_t)batch * N * 16, cudaMemcpyHostToDevice, c.ctx.stream), "copy x");
-      dx = st;
-    }
-    c.forward(c.ctx, dx, (int)nx, (int)ny, batch);
-    ck(cudaMemcpy2DAsync(y, 8, c.output(), 32, 8, (size_t)batch * N,
-                         mem == HZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c.ctx.stream),
-       "copy y");
-    ck(cudaStreamSynchronize(c.ctx.stream), "sync");
-    c.ctx.resolve();
+    net_forward(net, x, y, nx, ny, 1, batch, mem);
+  });
+}
+
+int hz_net3d_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, int64_t nz, int32_t batch,
+                     int32_t mem) {
+  if (!net || !x || !y) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    need_dim(net, 3, "hz_net3d_forward");
+    check_net3_grid(nx, ny, nz, batch);
+    net_forward(net, x, y, nx, ny, nz, batch, mem);
   });
 }
 
@@ -2055,27 +2172,19 @@ int hz_net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int
                     double* loss, float* grad) {
   if (!net || !x || !t) return HZ_ERR_ARG;
   return guarded(nullptr, [&] {
+    need_dim(net, 2, "hz_net_gradient");
     check_net_grid(nx, ny, batch);
-    if (mem != HZ_MEM_HOST && mem != HZ_MEM_DEVICE) fail(HZ_ERR_ARG, "mem must be HZ_MEM_HOST or HZ_MEM_DEVICE");
-    ck(cudaSetDevice(net->dev), "cudaSetDevice");
-    hz::CoarseNet& c = *net->net;
-    const long long N = nx * ny;
-    DBuf bx, bt;
-    const float* dx = x;
-    const float* dt = t;
-    if (mem == HZ_MEM_DEVICE) net_order_after_default_stream(net);
-    if (mem == HZ_MEM_HOST) {
-      bx.alloc((size_t)batch * N * 16);
-      bt.alloc((size_t)batch * N * 8);
-      ck(cudaMemcpyAsync(bx.p, x, (size_t)batch * N * 16, cudaMemcpyHostToDevice, c.ctx.stream), "copy x");
-      ck(cudaMemcpyAsync(bt.p, t, (size_t)batch * N * 8, cudaMemcpyHostToDevice, c.ctx.stream), "copy t");
-      dx = bx.as<float>();
-      dt = bt.as<float>();
-    }
-    c.forward(c.ctx, dx, (int)nx, (int)ny, batch, true);
-    const double l = c.backward(c.ctx, dt, (int)nx, (int)ny, batch);
-    if (loss) *loss = l;
-    if (grad) c.get_grad(grad);
+    net_gradient(net, x, t, nx, ny, 1, batch, mem, loss, grad);
+  });
+}
+
+int hz_net3d_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int32_t batch,
+                      int32_t mem, double* loss, float* grad) {
+  if (!net || !x || !t) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    need_dim(net, 3, "hz_net3d_gradient");
+    check_net3_grid(nx, ny, nz, batch);
+    net_gradient(net, x, t, nx, ny, nz, batch, mem, loss, grad);
   });
 }
 
@@ -2083,6 +2192,7 @@ int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_
                  int32_t epochs, double lr, int32_t seed, double* loss_hist) {
   if (!net || !x || !t) return HZ_ERR_ARG;
   return guarded(nullptr, [&] {
+    need_dim(net, 2, "hz_net_train");
     check_net_grid(nx, ny, batch);
     if (npairs < 1 || epochs < 1) fail(HZ_ERR_ARG, "npairs and epochs must be >= 1");
     if (!(lr > 0)) fail(HZ_ERR_ARG, "lr must be > 0");
@@ -2093,11 +2203,29 @@ int hz_net_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_
   });
 }
 
+int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int64_t npairs,
+                   int32_t batch, int32_t epochs, double lr, int32_t seed, double* loss_hist) {
+  if (!net || !x || !t) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    need_dim(net, 3, "hz_net3d_train");
+    check_net3_grid(nx, ny, nz, batch);
+    if (npairs < 1 || epochs < 1) fail(HZ_ERR_ARG, "npairs and epochs must be >= 1");
+    if (!(lr > 0)) fail(HZ_ERR_ARG, "lr must be > 0");
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    hz::CoarseNet3& c = *net->net3;
+    net_order_after_default_stream(net);
+    c.train(c.ctx, x, t, (int)nx, (int)ny, (int)nz, npairs, batch, epochs, lr, (unsigned)seed, loss_hist);
+  });
+}
+
 int hz_net_save(hz_net* net, const char* path) {
   if (!net || !path) return HZ_ERR_ARG;
   return guarded(nullptr, [&] {
     ck(cudaSetDevice(net->dev), "cudaSetDevice");
-    net->net->save(path);
+    if (net->net3)
+      net->net3->save(path);
+    else
+      net->net->save(path);
   });
 }
 
@@ -2106,16 +2234,20 @@ int hz_net_load(hz_net* net, const char* path) {
   return guarded(nullptr, [&] {
     ck(cudaSetDevice(net->dev), "cudaSetDevice");
     long long n = 0, st = 0;
-    const int rc = hz::CoarseNet::file_info(path, &n, &st);
-    if (rc < 0) fail(HZ_ERR_ARG, "%s: not a loadable coarse-network file (code %d)", path, rc);
-    net->net->load(path);
+    const int rc = net->net3 ? hz::CoarseNet3::file_info(path, &n, &st) : hz::CoarseNet::file_info(path, &n, &st);
+    if (rc < 0) fail(HZ_ERR_ARG, "%s: not a loadable %dD coarse-network file (code %d)", path, net->dim(), rc);
+    if (net->net3)
+      net->net3->load(path);
+    else
+      net->net->load(path);
   });
 }
 
 int hz_net_file_info(const char* path, int64_t* nparams, int64_t* adam_step) {
   if (!path) return HZ_ERR_ARG;
   long long n = 0, st = 0;
-  const int rc = hz::CoarseNet::file_info(path, &n, &st);
+  int rc = hz::CoarseNet::file_info(path, &n, &st);
+  if (rc == -2) rc = hz::CoarseNet3::file_info(path, &n, &st);  // not a 2D file: a 3D one?
   if (rc < 0) {
     g_thread_error = std::string(path) + ": not a loadable coarse-network file";
     return HZ_ERR_ARG;
@@ -2128,7 +2260,7 @@ int hz_net_file_info(const char* path, int64_t* nparams, int64_t* adam_step) {
 int hz_net_set_profile(hz_net* net, int32_t on) {
   if (!net) return HZ_ERR_ARG;
   cudaSetDevice(net->dev);
-  Ctx& c = net->net->ctx;
+  Ctx& c = net->ctx();
   cudaStreamSynchronize(c.stream);
   c.resolve();
   c.profile = on != 0;
@@ -2138,13 +2270,13 @@ int hz_net_set_profile(hz_net* net, int32_t on) {
 int hz_net_kernel_times(hz_net* net, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                         int64_t* timed_launches, double* total_ms, double* alg_bytes, double* alg_flops) {
   if (!net) return HZ_ERR_ARG;
-  return ctx_times(net->net->ctx, net->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes,
+  return ctx_times(net->ctx(), net->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes,
                    alg_flops);
 }
 
 int hz_net_reset_kernel_times(hz_net* net) {
   if (!net) return HZ_ERR_ARG;
-  ctx_reset(net->net->ctx, net->dev);
+  ctx_reset(net->ctx(), net->dev);
   return HZ_OK;
 }
 
@@ -2153,18 +2285,24 @@ int hz_attach_net(hz_handle* h, hz_net* net, int32_t level, double stag_ratio) {
   return guarded(h, [&] {
     if (!net) {
       h->net = nullptr;
+      h->net3 = nullptr;
       h->net_level = 0;
       return;
     }
-    if (h->prob.dim != 2) fail(HZ_ERR_ARG, "the learned correction is 2D only");
+    if (net->dim() != h->prob.dim)
+      fail(HZ_ERR_ARG, "a %dD network cannot correct a %dD problem", net->dim(), h->prob.dim);
     if (h->opt.krylov != HZ_KRYLOV_FGMRES)
       fail(HZ_ERR_ARG, "the learned correction is a nonlinear preconditioner: it needs FGMRES");
     if (level < 1 || level >= h->opt.levels) fail(HZ_ERR_ARG, "level must be in [1, levels - 1]");
     if (!(stag_ratio > 0)) fail(HZ_ERR_ARG, "stag_ratio must be > 0");
     if (net->dev != h->dev) fail(HZ_ERR_ARG, "network and solver live on different devices");
     const Grid g = level_grid(h, level);
-    check_net_grid(g.nx, g.ny, 1);
+    if (h->prob.dim == 2)
+      check_net_grid(g.nx, g.ny, 1);
+    else
+      check_net3_grid(g.nx, g.ny, g.nz, 1);
     h->net = net->net.get();
+    h->net3 = net->net3.get();
     h->net_level = level;
     h->net_stag = stag_ratio;
   });
@@ -2177,6 +2315,78 @@ int hz_learned_stats(const hz_handle* h, int64_t* net_calls, int32_t* fallbacks)
   return HZ_OK;
 }
 
+namespace {
+// 3D training targets for the right-hand sides captured on `level`: a band LU of
+// a 3D coarse level is out of reach (65^3 nodes, bandwidth 4225), so the target
+// e = A^{-1} r starts from the coarse-grid correction the plain solver applies
+// on that level (what the network replaces: two FGMRES steps preconditioned by
+// the level's cycle for the K-cycle, one cycle otherwise) and takes sweeps - 1
+// restarted two-step FGMRES corrections e += K(r - A e) preconditioned by the
+// level's cycle, in FP64.  Each minimises the residual over its space, so the
+// residual never grows, whatever the cycle.
+void collect_targets_iterative(hz_handle* h, Hierarchy& H, int level, int sweeps, long long cnt, float* x_out,
+                               float* t_out, double* plain_err, double* target_relres) {
+  const Grid g = level_grid(h, level);
+  const long long N = g.N;
+  const int R = h->rcap;
+  const int last = (int)H.lv.size() - 1;
+  if (level >= last) fail(HZ_ERR_ARG, "pairs need a level above the coarsest");
+  const bool kstep = h->opt.cycle == 'K';
+  Level& Lv = *H.lv[level];
+  if (!Lv.kv.p) {  // the two-step corrections' vectors (allocated by the K-cycle itself otherwise)
+    Lv.kv.alloc((size_t)5 * R * Lv.ld * sizeof(double2));
+    Lv.ks.alloc((size_t)R * 8 * 16);
+    Lv.kp.alloc((size_t)R * 3 * kcycle_nblk(Lv.g.N) * 16);
+  }
+  DBuf xe, res, ev, x1, idc, sc, nrm;
+  xe.alloc((size_t)R * N * 16);
+  res.alloc((size_t)R * N * 16);
+  ev.alloc((size_t)R * N * 16);
+  x1.alloc((size_t)R * N * 16);
+  sc.alloc((size_t)R * 4);
+  nrm.alloc((size_t)R * 6 * 8);
+  idc.alloc((size_t)R * sizeof(int));
+  std::vector<int> seq(R);
+  for (int c = 0; c < R; ++c) seq[c] = c;
+  ck(cudaMemcpy(idc.p, seq.data(), R * sizeof(int), cudaMemcpyHostToDevice), "upload cols");
+  const int* dc = idc.as<int>();
+  const float2* feat = net_features(h, level);
+  auto plain = [&](const double2* b, double2* out, int k) {
+    if (kstep)
+      kcycle_correction<double>(h, H, level, b, out, dc, k);
+    else
+      mg_cycle<double, double>(h, H, level, b, out, dc, k);
+  };
+  std::vector<double> hn((size_t)R * 6);
+  double worst = 0.0;
+  for (long long i0 = 0; i0 < cnt; i0 += R) {
+    const int k = (int)std::min<long long>(R, cnt - i0);
+    const double2* r = h->cap_buf.as<double2>() + i0 * N;
+    double2* xd = xe.as<double2>();
+    plain(r, x1.as<double2>(), k);  // what the network replaces
+    ck(cudaMemcpyAsync(xd, x1.p, (size_t)k * N * 16, cudaMemcpyDeviceToDevice, h->ctx.stream), "first sweep");
+    for (int s = 1; s < sweeps; ++s) {
+      lev_op<double, double>(h, H, level, MODE_RESID, xd, r, res.as<double2>(), dc, k);
+      kcycle_correction<double>(h, H, level, res.as<double2>(), ev.as<double2>(), dc, k);
+      launch_axpy_compact(h->ctx, N, k, ev.as<double2>(), xd);
+    }
+    lev_op<double, double>(h, H, level, MODE_RESID, xd, r, res.as<double2>(), dc, k);
+    launch_diff_norms(h->ctx, N, k, res.as<double2>(), r, nrm.as<double>());
+    launch_diff_norms(h->ctx, N, k, x1.as<double2>(), xd, nrm.as<double>() + 3 * R);
+    launch_pair_pack(h->ctx, N, r, xd, k, feat, h->net_h2, sc.as<float>(), x_out + i0 * N * 4, t_out + i0 * N * 2);
+    ck(cudaMemcpyAsync(hn.data(), nrm.p, (size_t)R * 6 * 8, cudaMemcpyDeviceToHost, h->ctx.stream), "norms");
+    sync(h);
+    for (int c = 0; c < k; ++c) {
+      const double rr = hn[3 * c + 2] > 0 ? std::sqrt(hn[3 * c + 1] / hn[3 * c + 2]) : 0.0;
+      worst = std::max(worst, rr);
+      const double* q = hn.data() + 3 * R + 3 * c;
+      if (plain_err) plain_err[i0 + c] = q[2] > 0 ? std::sqrt(q[0] / q[2]) : 0.0;
+    }
+  }
+  if (target_relres) *target_relres = worst;
+}
+}  // namespace
+
 int hz_collect_pairs(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, int32_t mem, int32_t level,
                      int32_t sweeps, int64_t max_pairs, float* x_out, float* t_out, double* plain_err,
                      double* target_relres, int64_t* count) {
@@ -2184,16 +2394,20 @@ int hz_collect_pairs(hz_handle* h, const double* B, double* X, int64_t n, int32_
   return guarded(h, [&] {
     if (!x_out || !t_out || !count) fail(HZ_ERR_ARG, "null output");
     if (h->opt.precision != HZ_PREC_FP64) fail(HZ_ERR_ARG, "training pairs come from the FP64 solver");
-    if (h->prob.dim != 2) fail(HZ_ERR_ARG, "the learned correction is 2D only");
     if (level < 1 || level >= h->opt.levels) fail(HZ_ERR_ARG, "level must be in [1, levels - 1]");
     if (sweeps < 1 || max_pairs < 1) fail(HZ_ERR_ARG, "sweeps and max_pairs must be >= 1");
     const Grid g = level_grid(h, level);
-    check_net_grid(g.nx, g.ny, 1);
+    if (h->prob.dim == 2)
+      check_net_grid(g.nx, g.ny, 1);
+    else
+      check_net3_grid(g.nx, g.ny, g.nz, 1);
     set_device(h);
     const long long N = g.N;
     h->cap_buf.alloc((size_t)max_pairs * N * 16);
     hz::CoarseNet* saved = h->net;
+    hz::CoarseNet3* saved3 = h->net3;
     h->net = nullptr;
+    h->net3 = nullptr;
     h->cap_on = true;
     h->cap_level = level;
     h->cap_count = 0;
@@ -2201,10 +2415,16 @@ int hz_collect_pairs(hz_handle* h, const double* B, double* X, int64_t n, int32_
     const int rc = hz_solve(h, B, X, n, nrhs, 0, mem, nullptr);
     h->cap_on = false;
     h->net = saved;
+    h->net3 = saved3;
     if (rc < 0) fail(rc, "%s", h->err.c_str());
     Hierarchy& H = h->hier[0];
     const long long cnt = h->cap_count;
     const int R = h->rcap;
+    if (h->prob.dim == 3) {
+      collect_targets_iterative(h, H, level, sweeps, cnt, x_out, t_out, plain_err, target_relres);
+      *count = cnt;
+      return;
+    }
     // targets: exact solves with a banded LU of the capture level's operator
     // (plain cycles as a stationary iteration need not converge on coarse levels)
     Level& Lv = *H.lv[level];

@@ -362,6 +362,51 @@ function collectPairs!(s::ShiftedLaplacianMultigridSolver, B::AbstractVecOrMat, 
                 x, t, pe, rr, cnt), h)
     return cnt[], pe[1:cnt[]], X
 end
+# The 3D network (three grid levels, 8-16-32 channels, 3x3x3 convolutions): arrays
+# (4, nx, ny, nz, batch) and (2, nx, ny, nz, batch); node counts 4k+1.  Weights,
+# files, profiling and attachNet! take it like the 2D one.
+function CoarseNet3D(seed::Integer = 0, device::Integer = 0)
+    p = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hz_net3d_create, libhelmgpu), Cint, (Int32, Int32, Ref{Ptr{Cvoid}}), seed, device, p))
+    net = CoarseNet(p[])
+    finalizer(n -> (n.ptr != C_NULL && ccall((:hz_net_destroy, libhelmgpu), Cint, (Ptr{Cvoid},), n.ptr);
+                    n.ptr = C_NULL), net)
+    return net
+end
+netDim(net::CoarseNet) = Int(ccall((:hz_net_dim, libhelmgpu), Cint, (Ptr{Cvoid},), net.ptr))
+function netWeights3D(net::CoarseNet)
+    w = Vector{Float32}(undef, ccall((:hz_net3d_num_params, libhelmgpu), Int64, ()))
+    check(ccall((:hz_net_get_weights, libhelmgpu), Cint, (Ptr{Cvoid}, Ptr{Float32}), net.ptr, w))
+    return w
+end
+function netForward(net::CoarseNet, x::Array{Float32,5})
+    _, nx, ny, nz, b = size(x)
+    y = Array{Float32}(undef, 2, nx, ny, nz, b)
+    check(ccall((:hz_net3d_forward, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Int64, Int64, Int64, Int32, Int32),
+                net.ptr, x, y, nx, ny, nz, Int32(b), HZ_MEM_HOST))
+    return y
+end
+function netGradient(net::CoarseNet, x::Array{Float32,5}, t::Array{Float32,5})
+    _, nx, ny, nz, b = size(x)
+    g = netWeights3D(net)
+    loss = Ref{Float64}(0.0)
+    check(ccall((:hz_net3d_gradient, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Int64, Int64, Int64, Int32, Int32, Ref{Float64},
+                 Ptr{Float32}),
+                net.ptr, x, t, nx, ny, nz, Int32(b), HZ_MEM_HOST, loss, g))
+    return loss[], g
+end
+function netTrain3D!(net::CoarseNet, x::Ptr{Float32}, t::Ptr{Float32}, nx::Integer, ny::Integer, nz::Integer,
+                     npairs::Integer; batch::Integer = 8, epochs::Integer = 20, lr::Float64 = 2e-3,
+                     seed::Integer = 0)
+    hist = zeros(Float64, epochs)
+    check(ccall((:hz_net3d_train, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Int64, Int64, Int64, Int64, Int32, Int32, Float64, Int32,
+                 Ptr{Float64}),
+                net.ptr, x, t, nx, ny, nz, npairs, Int32(batch), Int32(epochs), lr, Int32(seed), hist))
+    return hist
+end
 # versioned file of the weights and the Adam state; training resumes from a loaded file
 saveNet(net::CoarseNet, path::AbstractString) =
     check(ccall((:hz_net_save, libhelmgpu), Cint, (Ptr{Cvoid}, Cstring), net.ptr, path))

@@ -31,6 +31,20 @@ def num_params() -> int:
     return int(L.load().hz_net_num_params())
 
 
+def num_params_3d() -> int:
+    return int(L.load().hz_net3d_num_params())
+
+
+def layer_shapes_3d() -> list[tuple[int, int]]:
+    lib = L.load()
+    out = []
+    for k in range(6):
+        a, b = C.c_int32(), C.c_int32()
+        L.check(lib.hz_net3d_layer_shape(k, C.byref(a), C.byref(b)))
+        out.append((a.value, b.value))
+    return out
+
+
 def layer_shapes() -> list[tuple[int, int]]:
     lib = L.load()
     out = []
@@ -74,15 +88,20 @@ class CoarseNet:
         except Exception:
             pass
 
+    dim = 2
+
+    def _nparams(self) -> int:
+        return num_params()
+
     def get_weights(self) -> np.ndarray:
-        w = np.empty(num_params(), dtype=np.float32)
+        w = np.empty(self._nparams(), dtype=np.float32)
         L.check(L.load().hz_net_get_weights(self._h, w.ctypes.data))
         return w
 
     def set_weights(self, w) -> None:
         w = np.ascontiguousarray(w, dtype=np.float32)
-        if w.size != num_params():
-            raise ValueError(f"expected {num_params()} weights, got {w.size}")
+        if w.size != self._nparams():
+            raise ValueError(f"expected {self._nparams()} weights, got {w.size}")
         L.check(L.load().hz_net_set_weights(self._h, w.ctypes.data))
 
     def forward(self, x):
@@ -155,6 +174,60 @@ class CoarseNet:
         return hist
 
 
+class CoarseNet3D(CoarseNet):
+    """The 3D network (three grid levels, 8-16-32 channels, 3x3x3 convolutions) on
+    one CUDA device; arrays are (batch, nz, ny, nx, channels) with node counts 4k+1."""
+
+    dim = 3
+
+    def __init__(self, seed: int = 0, device: int | None = None):
+        device = current_device() if device is None else int(device)
+        self._h = C.c_void_p()
+        L.check(L.load().hz_net3d_create(int(seed), device, C.byref(self._h)))
+        self.device = device
+
+    def _nparams(self) -> int:
+        return num_params_3d()
+
+    def forward(self, x):
+        """y = net(x); x (batch, nz, ny, nx, 4) numpy float32 or CUDA tensor."""
+        B, nz, ny, nx, c = x.shape
+        if c != 4:
+            raise ValueError("x must have 4 channels")
+        if _is_device_array(x):
+            import torch
+            y = torch.empty((B, nz, ny, nx, 2), dtype=torch.float32, device=x.device)
+        else:
+            y = np.empty((B, nz, ny, nx, 2), dtype=np.float32)
+        px, mem = _ptr(x)
+        py, _ = _ptr(y)
+        L.check(L.load().hz_net3d_forward(self._h, px, py, nx, ny, nz, B, mem))
+        return y
+
+    def gradient(self, x, t):
+        """(loss, weight gradient as a flat float32 array) for one batch."""
+        B, nz, ny, nx, _ = x.shape
+        px, mem = _ptr(x)
+        pt, mem2 = _ptr(t)
+        if mem != mem2:
+            raise ValueError("x and t must both be on the host or both on the device")
+        g = np.empty(self._nparams(), dtype=np.float32)
+        loss = C.c_double()
+        L.check(L.load().hz_net3d_gradient(self._h, px, pt, nx, ny, nz, B, mem, C.byref(loss), g.ctypes.data))
+        return loss.value, g
+
+    def train(self, x, t, epochs: int = 10, batch: int = 8, lr: float = 2e-3, seed: int = 0) -> np.ndarray:
+        """Adam over the pairs (CUDA tensors) for epochs passes; returns the mean loss per epoch."""
+        if not (_is_device_array(x) and _is_device_array(t)):
+            raise ValueError("training pairs must be CUDA tensors")
+        P, nz, ny, nx, _ = x.shape
+        hist = np.zeros(int(epochs))
+        _device_inputs_ready()
+        L.check(L.load().hz_net3d_train(self._h, x.data_ptr(), t.data_ptr(), nx, ny, nz, P, int(batch), int(epochs),
+                                        float(lr), int(seed), hist.ctypes.data_as(C.POINTER(C.c_double))))
+        return hist
+
+
 def file_info(path) -> tuple[int, int]:
     """(parameter count, Adam step) of a saved network file; raises for a file
     that is not loadable (host only, no GPU)."""
@@ -163,15 +236,12 @@ def file_info(path) -> tuple[int, int]:
     return int(n.value), int(st.value)
 
 
-def level_grid(solver: ShiftedLaplacianMultigridSolver, level: int) -> tuple[int, int]:
-    """(nx, ny) node counts of a 2D multigrid level."""
-    nodes = _nodes(solver.helmParam.Mesh)
-    if len(nodes) != 2:
-        raise ValueError("the learned correction is 2D only")
-    nx, ny = int(nodes[0]), int(nodes[1])
+def level_grid(solver: ShiftedLaplacianMultigridSolver, level: int) -> tuple[int, ...]:
+    """Node counts (nx, ny) or (nx, ny, nz) of a multigrid level."""
+    nodes = [int(v) for v in _nodes(solver.helmParam.Mesh)]
     for _ in range(level):
-        nx, ny = (nx - 1) // 2 + 1, (ny - 1) // 2 + 1
-    return nx, ny
+        nodes = [(v - 1) // 2 + 1 for v in nodes]
+    return tuple(nodes)
 
 
 def collect_pairs(solver: ShiftedLaplacianMultigridSolver, B, level: int = 2, sweeps: int = 2,
@@ -179,9 +249,11 @@ def collect_pairs(solver: ShiftedLaplacianMultigridSolver, B, level: int = 2, sw
     """Training pairs from the FP64 solver (see hz_collect_pairs).
 
     B: (n, nrhs) complex right-hand sides on the host.  Returns a dict with
-    ``x``, ``t`` (CUDA tensors, layout above), ``plain_err`` (numpy: relative
-    error of one plain cycle on each pair), ``target_relres`` and ``X`` (the
-    solution of the solve that produced them)."""
+    ``x``, ``t`` (CUDA tensors, layout above; 3D: (pairs, nz, ny, nx, c)),
+    ``plain_err`` (numpy: relative error of the plain coarse correction on each
+    pair), ``target_relres`` and ``X`` (the solution of the solve that produced
+    them).  2D targets: band LU + (sweeps - 1) refinement steps; 3D targets:
+    `sweeps` restarted plain corrections."""
     import torch
     if solver.MG.precision != "fp64":
         raise ValueError("pairs come from the FP64 solver (precision='fp64')")
@@ -189,13 +261,13 @@ def collect_pairs(solver: ShiftedLaplacianMultigridSolver, B, level: int = 2, sw
     if Bc.ndim == 1:
         Bc = Bc.reshape(-1, 1)
     n, nrhs = Bc.shape
-    nx, ny = level_grid(solver, level)
+    grid = level_grid(solver, level)[::-1]  # (ny, nx) or (nz, ny, nx)
     if max_pairs is None:
         max_pairs = nrhs * solver.MG.maxOuterIter * max(1, solver.inner)
     h = _ensure_handle(solver)
     dev = torch.device("cuda", solver._device)
-    x = torch.empty((max_pairs, ny, nx, 4), dtype=torch.float32, device=dev)
-    t = torch.empty((max_pairs, ny, nx, 2), dtype=torch.float32, device=dev)
+    x = torch.empty((max_pairs, *grid, 4), dtype=torch.float32, device=dev)
+    t = torch.empty((max_pairs, *grid, 2), dtype=torch.float32, device=dev)
     pe = np.zeros(max_pairs)
     rr = C.c_double()
     cnt = C.c_int64()

@@ -278,8 +278,29 @@ int hz_net_set_profile(hz_net* net, int32_t on);
 int hz_net_kernel_times(hz_net* net, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                         int64_t* timed_launches, double* total_ms, double* alg_bytes, double* alg_flops);
 int hz_net_reset_kernel_times(hz_net* net);
+/* 3D variant (no counterpart in the reference either): a convolutional
+ * encoder-decoder over three grid levels with 8-16-32 channels and 3x3x3
+ * convolutions (six layers; BF16 weights and activations, FP32 accumulation on
+ * the tensor cores).  Input and output layouts as above on an nx x ny x nz grid
+ * (axis 1 fastest, node counts 4k+1); weights layer after layer, each
+ * [cout][27][cin] with tap 9 (dz + 1) + 3 (dy + 1) + (dx + 1).  The functions
+ * hz_net_get_weights, hz_net_set_weights, hz_net_save, hz_net_load,
+ * hz_net_set_profile, hz_net_kernel_times, hz_net_reset_kernel_times and
+ * hz_attach_net take either kind; hz_net_file_info reads either file format. */
+int hz_net3d_create(int32_t seed, int32_t device, hz_net** out);
+int64_t hz_net3d_num_params(void);
+int hz_net3d_layer_shape(int32_t layer, int32_t* cin, int32_t* cout);
+/* 2 or 3: the grid dimension of a network. */
+int hz_net_dim(const hz_net* net);
+int hz_net3d_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, int64_t nz, int32_t batch,
+                     int32_t mem);
+int hz_net3d_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int32_t batch,
+                      int32_t mem, double* loss, float* grad);
+int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int64_t npairs,
+                   int32_t batch, int32_t epochs, double lr, int32_t seed, double* loss_hist);
 /* Use the network for the coarse-grid correction of multigrid level `level`
- * (1 .. levels-1; 2D, FGMRES only: the network is a nonlinear preconditioner).
+ * (1 .. levels-1; a network of the problem's dimension; FGMRES only: the
+ * network is a nonlinear preconditioner).
  * A restart cycle that reduces some column's residual by less than stag_ratio
  * hands the rest of that solve to the plain cycle.  net = NULL detaches.  The
  * handle does not own the network; keep it alive while attached, and use one
@@ -290,8 +311,13 @@ int hz_learned_stats(const hz_handle* h, int64_t* net_calls, int32_t* fallbacks)
 /* Training pairs: solves H X = B (FP64 preconditioner, no network) like
  * hz_solve while recording the right-hand side r that each cycle hands to
  * `level` (at most max_pairs columns), then computes the target e = A^{-1} r on
- * that level with a banded LU of its operator (FP64) followed by sweeps - 1
- * steps of iterative refinement.
+ * that level: in 2D with a banded LU of its operator (FP64) followed by
+ * sweeps - 1 steps of iterative refinement; in 3D (where the band LU of a
+ * coarse level is out of reach) from the coarse-grid correction the plain
+ * solver applies on that level followed by sweeps - 1 restarted FP64 two-step
+ * FGMRES corrections e += K(r - A e) preconditioned by the level's cycle (which
+ * never raise the residual).  In 3D the grid is nx x ny x nz and plain_err
+ * compares that plain correction with the target.
  * x_out [max_pairs][N][4] and t_out [max_pairs][N][2] are DEVICE FP32 arrays in
  * the layout above; plain_err (host, may be NULL) gets ||e1 - e|| / ||e|| of one
  * plain cycle e1 per pair, target_relres (may be NULL) the largest

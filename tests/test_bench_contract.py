@@ -21,7 +21,7 @@ print(json.dumps({"product_modules": mods, "libhelmgpu_loaded": "libhelmgpu" in 
 """
 
 CONFIG_KEYS = {"workload", "nrhs", "levels", "tol", "krylov", "cycle", "coarse", "relax", "relax_from", "shift",
-               "seed", "learned", "l2", "precision", "outer_arithmetic", "cuda_graph", "autotune"}
+               "seed", "learned", "l2", "precision", "outer_arithmetic", "cuda_graph", "autotune", "net_level"}
 
 
 def _run(*extra):

@@ -80,6 +80,7 @@ C2CCALL = {
     "hz_handle*": {"Ptr{Cvoid}"},
     "const hz_handle*": {"Ptr{Cvoid}"},
     "hz_net*": {"Ptr{Cvoid}"},
+    "const hz_net*": {"Ptr{Cvoid}"},
     "hz_handle**": {"Ref{Ptr{Cvoid}}"},
     "hz_net**": {"Ref{Ptr{Cvoid}}"},
     "const hz_problem*": {"Ref{HzProblem}"},
