@@ -329,6 +329,11 @@ def sources_random3(P: dict, nrhs: int, seed: int, pad: int) -> np.ndarray:
     return B
 
 
+def learned_cycle(args) -> str:
+    """Cycle of the learned arms and of the solves that give their training pairs."""
+    return args.learned_cycle or args.cycle
+
+
 def train_network3d(args, wl, hz, lib):
     """Training pairs on the network's level from the FP64 solver on seeded
     training models (the first restart cycles of solves with random sources),
@@ -343,8 +348,8 @@ def train_network3d(args, wl, hz, lib):
         M = hz.getRegularMesh(sum(([0.0, c * h] for c, h in zip(P["cells"], P["h"])), []), list(P["cells"]))
         param = hz.HelmholtzParam(M, gam, P["m"], P["w"], True, True)
         MG = hz.getMGparam(complex, int, wl["levels"], 1, wl["train_outer"], wl["tol"],
-                           "Jac-GMRES" if args.relax == "jac-gmres" else "Jac", 0.8, 1, 1, args.cycle, "Julia",
-                           args.shift, 0.0, precision="fp64", relaxFrom=args.relax_from)
+                           "Jac-GMRES" if args.relax == "jac-gmres" else "Jac", 0.8, 1, 1, learned_cycle(args),
+                           "Julia", args.shift, 0.0, precision="fp64", relaxFrom=args.relax_from)
         S = hz.getShiftedLaplacianMultigridSolver(param, MG, args.shift, "GMRES", 10)
         B = sources_random3(P, wl["train_rhs"], seed=20_000 + s, pad=wl["pad"])
         d = hz.learned.collect_pairs(S, B, level=level, sweeps=wl["pair_sweeps"], max_pairs=wl["pairs_per_model"])
@@ -393,7 +398,7 @@ def run_ours(args, rank, ws, dist):
     n = B.shape[0]
     err_cols = list(range(min(nrhs, wl.get("err_cols", 1))))
 
-    def make_handle(precision, outer):
+    def make_handle(precision, outer, cycle):
         prob = L.hz_problem()
         prob.dim = P["dim"]
         for d in range(P["dim"]):
@@ -407,7 +412,7 @@ def run_ours(args, rank, ws, dist):
         o = L.hz_options()
         lib.hz_default_options(C.byref(o))
         o.levels, o.rel_tol, o.inner, o.max_outer = wl["levels"], wl["tol"], 10, args.max_outer
-        o.cycle = ord(args.cycle)
+        o.cycle = ord(cycle)
         o.coarse_op = L.HZ_COARSE_REDISCRETIZE if args.coarse == "rediscretize" else L.HZ_COARSE_GALERKIN
         o.relax_type = L.HZ_RELAX_JAC_GMRES if args.relax == "jac-gmres" else L.HZ_RELAX_JAC
         o.relax_from = args.relax_from
@@ -456,7 +461,8 @@ def run_ours(args, rank, ws, dist):
     for ai, name in enumerate(names):
         prec, outer, use_net = ARMS[name]
         head = ai == 0
-        hh = make_handle(prec, outer)
+        cyc = learned_cycle(args) if use_net else args.cycle
+        hh = make_handle(prec, outer, cyc)
         if use_net:
             L.check(lib.hz_attach_net(hh, net._h, wl["net_level"], args.stag_ratio), hh)
         warm = args.warmup if head else max(1, args.arm_warmup)
@@ -478,7 +484,7 @@ def run_ours(args, rank, ws, dist):
         calls, fbs = C.c_int64(0), C.c_int32(0)
         if use_net:
             lib.hz_learned_stats(hh, C.byref(calls), C.byref(fbs))
-        res = dict(precision=prec, outer_arithmetic=outer, learned=use_net, net_calls=int(calls.value),
+        res = dict(precision=prec, outer_arithmetic=outer, learned=use_net, cycle=cyc, net_calls=int(calls.value),
                    net_fallbacks=int(fbs.value), seconds=t, steps=steps, warmup=warm,
                    rhs_per_s=nrhs * ws * steps / t, ms_per_step=1000.0 * t / steps, max_relres=float(rr.max()),
                    converged_cols=int(np.sum(rr <= wl["tol"])), mean_iters=float(it.mean()), max_iters=int(it.max()),
@@ -607,6 +613,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the 3D oracle error")
     ap.add_argument("--no-learned", action="store_true",
                     help="3D 257^3 workload: skip the learned correction (no training, no learned arms)")
+    ap.add_argument("--learned-cycle", default=None, choices=["V", "K"],
+                    help="cycle of the learned arms and their training pairs (default: the workload's cycle)")
     ap.add_argument("--nrhs", type=int, default=0, help="override the workload's RHS count (small profiling cases)")
     ap.add_argument("--krylov", default="fgmres", choices=["fgmres", "bicgstab"])
     ap.add_argument("--no-graph", action="store_true", help="launch the cycles eagerly (no CUDA graphs)")
@@ -698,7 +706,7 @@ def main():
 
     def arm_summary(r, name):
         return dict(precision=r["precision"], outer_arithmetic=r["outer_arithmetic"], learned=r["learned"],
-                    rhs_per_s=r["rhs_per_s"], ms_per_step=r["ms_per_step"], steps=r["steps"], warmup=r["warmup"],
+                    cycle=r["cycle"], rhs_per_s=r["rhs_per_s"], ms_per_step=r["ms_per_step"], steps=r["steps"], warmup=r["warmup"],
                     mean_iters=r["mean_iters"], max_iters=r["max_iters"], max_relres=r["max_relres"],
                     converged_cols=r["converged_cols"], max_err_vs_oracle=errs.get(name),
                     net_calls=r["net_calls"], net_fallbacks=r["net_fallbacks"], clocks=r["clocks"])

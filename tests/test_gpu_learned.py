@@ -9,8 +9,9 @@
   "no correction" baseline on held-out pairs.
 * Inside FGMRES (outer FP64, stopping residual 1e-6) the learned form reaches
   the same stopping residual with error <= 1e-4 against the direct solution,
-  takes fewer iterations than the same cycle without any correction below the
-  network's level, and hands over to the plain cycle when it stagnates.
+  takes fewer iterations than the plain cycle (the same solver without the
+  network) on held-out models and than the same cycle without any correction
+  below the network's level, and hands over to the plain cycle when it stagnates.
 """
 import numpy as np
 import pytest
@@ -92,10 +93,13 @@ def _solver(hz, P, precision, levels=5, tol=1e-6, max_outer=60):
 
 @pytest.fixture(scope="module")
 def trained(hz):
-    """A network trained on pairs from three seeded layered+inclusion models (129x129 nodes, level 2 = 33x33)."""
+    """A network trained on pairs from twelve seeded layered+inclusion models
+    (129x129 nodes, level 2 = 33x33).  Trained on three models the network
+    still loses to the plain cycle on held-out models (194 against 162
+    iterations); on twelve it wins (118 against 162)."""
     import torch
     xs, ts, pes = [], [], []
-    for seed in (21, 22, 23):
+    for seed in range(21, 33):
         P = PB.layered((128, 128), seed=seed, pad=16, ellipsoid=True)
         S = _solver(hz, P, "fp64")
         nx = ny = 129
@@ -122,6 +126,31 @@ def test_training_lowers_loss(hz, trained):
     print(f"loss {hist[0]:.3f} -> {hist[-1]:.3f}; median pair error: network {np.median(err):.3f}, "
           f"one plain cycle {np.median(plain_err):.3f}")
     assert np.median(err) < 0.7, np.median(err)
+
+
+def test_learned_solve_gains_over_plain_cycle(hz, O, trained):
+    """On held-out models the network below level 2 takes fewer iterations than
+    the same solver without it (the plain V-cycle), with the fallback armed as in
+    production; the stopping residual and the error bound are those of the
+    mixed form."""
+    net = trained[0]
+    for seed in (101, 102, 103):
+        P = PB.layered((128, 128), seed=seed, pad=16, ellipsoid=True)
+        nx = ny = 129
+        B = _sources(nx * ny, nx, ny, P["M"].h, 4, seed, 16)
+        Xref = O.direct_solve(P["H"], B)
+        iters = {}
+        for name in ("plain", "learned"):
+            S = _solver(hz, P, "mixed")
+            if name == "learned":
+                hz.learned.attach(S, net, level=2, stag_ratio=0.95)
+            X, S = hz.solveLinearSystem(None, B, S)
+            assert S.last_relres.max() <= 1e-6
+            for c in range(B.shape[1]):
+                assert _rel(X[:, c], Xref[:, c]) <= 1e-4
+            iters[name] = int(S.last_iters.max())
+        print(f"held-out model {seed}: iterations (max over columns) {iters}")
+        assert iters["learned"] < iters["plain"], (seed, iters)
 
 
 def test_learned_solve_gains_over_no_correction(hz, O, trained):

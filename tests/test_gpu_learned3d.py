@@ -103,7 +103,7 @@ def _solver(hz, P, precision, cycle="V", levels=4, tol=1e-6, max_outer=60):
 
 @pytest.fixture(scope="module")
 def trained3(hz):
-    """A 3D network trained on pairs from seeded layered+ellipsoid models (33^3
+    """A 3D network trained on pairs from twelve seeded layered+ellipsoid models (33^3
     nodes, four levels, V-cycle with GMRES smoothing from level 1; the network
     replaces the correction below level 2 = 9^3).  With the K-cycle the plain
     correction there is already within a couple of iterations of an exact
@@ -111,7 +111,7 @@ def trained3(hz):
     correction below level 2 has something to gain (49 against 23)."""
     import torch
     xs, ts, pes = [], [], []
-    for seed in (31, 32, 33, 34, 35, 36):
+    for seed in range(31, 43):
         P = PB.layered((32, 32, 32), seed=seed, pad=4, ellipsoid=True)
         S = _solver(hz, P, "fp64")
         d = hz.learned.collect_pairs(S, _sources3(P, 4, seed, 4), level=2, sweeps=12, max_pairs=400)
