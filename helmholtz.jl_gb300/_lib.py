@@ -37,6 +37,8 @@ HZ_RELAX_JAC_GMRES = 1
 HZ_OP_H = 0
 HZ_OP_SH = 1
 HZ_NOALLOC_MAX_COLS = 4096
+HZ_NET_CONV_WARP_MMA = 0
+HZ_NET_CONV_TCGEN05 = 1
 
 
 class hz_problem(C.Structure):
@@ -131,6 +133,7 @@ SIGNATURES = {
     "hz_net3d_num_params": (C.c_int64, []),
     "hz_net3d_layer_shape": (C.c_int, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "hz_net_dim": (C.c_int, [_vp]),
+    "hz_net_set_conv_path": (C.c_int, [_vp, C.c_int32]),
     "hz_net3d_forward": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32]),
     "hz_net3d_gradient": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_int32, _dp,
                                     _vp]),

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp",
               "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
 SOURCES = ["hz_stencil.cu", "hz_krylov.cu", "hz_df64.cu", "hz_kcycle.cu", "hz_learn.cu", "hz_learn3d.cu",
-           "hz_solver.cu", "hz_host.cpp"]
+           "hz_conv_tc.cu", "hz_solver.cu", "hz_host.cpp"]
 
 
 def _nvcc() -> str:

@@ -33,6 +33,7 @@
 #include <numeric>
 #include <random>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "hz_launch.cuh"
@@ -613,6 +614,8 @@ CoarseNet::CoarseNet(unsigned seed) {
   dalloc(&g32_, off * 4);
   dalloc(&m_, off * 4);
   dalloc(&v_, off * 4);
+  dalloc(&tc_err_, sizeof(int));
+  cuda_ok(cudaMemset(tc_err_, 0, sizeof(int)), "tensor-core status");
   // He-normal initialisation (last layer scaled down), from a seeded host generator
   std::vector<float> w((size_t)num_params());
   std::mt19937 rng(seed);
@@ -627,6 +630,7 @@ CoarseNet::CoarseNet(unsigned seed) {
 
 CoarseNet::~CoarseNet() {
   release_acts();
+  dfree(tc_err_);
   dfree(w32_);
   dfree(wbf_);
   dfree(g32_);
@@ -848,11 +852,37 @@ float* CoarseNet::scale_staging(int B) {
   return scale_;
 }
 
+// One convolution: on the 5th-generation tensor cores (tcgen05) when that path
+// is selected and the channel counts suit it, else the warp-level MMA kernel.
+void CoarseNet::conv(Ctx& c, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi, int i_off,
+                     int Cout, const bf16* w, bf16* out, float* out32, int ldo, int o_off, int relu, const bf16* mask,
+                     int ldm, int m_off, int mask_lo) {
+  if (conv_path_ == 1 && conv_tc_supported(Cin, Cout)) {
+    const char* tc_name = std::strcmp(name, "net_conv_fwd") == 0 ? "net_conv_fwd_tc" : "net_conv_bwd_tc";
+    conv_tc_launch(c, tc_name, nx, ny, B, Cin, in, ldi, i_off, Cout, w, out, out32, ldo, o_off, relu, mask, ldm, m_off,
+                   mask_lo, tc_err_);
+    return;
+  }
+  conv_launch(c, name, nx, ny, B, Cin, in, ldi, i_off, Cout, w, out, out32, ldo, o_off, relu, mask, ldm, m_off,
+              mask_lo);
+}
+
+void CoarseNet::set_conv_path(int path) {
+  if (path != 0 && path != 1) throw std::runtime_error("coarse net: conv path must be 0 (warp MMA) or 1 (tcgen05)");
+  conv_path_ = path;
+}
+
+bool CoarseNet::tc_failed() {
+  int e = 0;
+  cuda_ok(cudaMemcpy(&e, tc_err_, sizeof(int), cudaMemcpyDeviceToHost), "tensor-core status");
+  return e != 0;
+}
+
 void CoarseNet::conv_fwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi, int i_off, bf16* out, int ldo,
                          int o_off, int relu, float* out32) {
   const auto& L = kSpec[l];
-  conv_launch(c, "net_conv_fwd", gx_[lev], gy_[lev], B, L.cinp, in, ldi, i_off, L.coutp, wbf_ + woff_[l], out, out32,
-              ldo, o_off, relu, nullptr, 0, 0, 0);
+  conv(c, "net_conv_fwd", gx_[lev], gy_[lev], B, L.cinp, in, ldi, i_off, L.coutp, wbf_ + woff_[l], out, out32, ldo,
+       o_off, relu, nullptr, 0, 0, 0);
 }
 
 void CoarseNet::forward(Ctx& c, const float* x4, int nx, int ny, int B, bool train) {
@@ -902,8 +932,8 @@ void CoarseNet::conv_bwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi,
   const int tot = L.cinp * 9 * K;
   HZ_LAUNCH(c, "net_wflip", (double)tot * 4.0, k_wflip, (unsigned)((tot + 255) / 256), 256, 0, L.coutp, L.cinp, K,
             wbf_ + woff_[l], wt_);
-  conv_launch(c, "net_conv_bwd", nx, ny, B, K, dout, ldd, d_off, L.cinp, wt_, din, nullptr, ldn, n_off, 0, mask, ldm,
-              i_off, mask_lo);
+  conv(c, "net_conv_bwd", nx, ny, B, K, dout, ldd, d_off, L.cinp, wt_, din, nullptr, ldn, n_off, 0, mask, ldm, i_off,
+       mask_lo);
 }
 
 double CoarseNet::backward(Ctx& c, const float* t, int nx, int ny, int B) {
@@ -936,6 +966,7 @@ double CoarseNet::backward(Ctx& c, const float* t, int nx, int ny, int B) {
   cuda_ok(cudaMemcpyAsync(&l, loss_, 8, cudaMemcpyDeviceToHost, c.stream), "loss");
   cuda_ok(cudaStreamSynchronize(c.stream), "sync");
   c.resolve();
+  if (conv_path_ == 1 && tc_failed()) throw std::runtime_error("coarse net: tensor-core convolution timed out");
   return l;
 }
 

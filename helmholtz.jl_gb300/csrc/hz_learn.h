@@ -56,7 +56,17 @@ class CoarseNet {
 
   Ctx ctx;  // own stream and launch table (training, standalone inference)
 
+  // convolution kernels: 0 = warp-level MMA (mma.sync), 1 = 5th-generation
+  // tensor cores (tcgen05.mma, TMEM accumulator) where the channel counts suit it
+  void set_conv_path(int path);
+  int conv_path() const { return conv_path_; }
+  // true when a tensor-core convolution gave up waiting (device flag; synchronous read)
+  bool tc_failed();
+
  private:
+  void conv(Ctx& c, const char* name, int nx, int ny, int B, int Cin, const __nv_bfloat16* in, int ldi, int i_off,
+            int Cout, const __nv_bfloat16* w, __nv_bfloat16* out, float* out32, int ldo, int o_off, int relu,
+            const __nv_bfloat16* mask, int ldm, int m_off, int mask_lo);
   void ensure(int nx, int ny, int B, bool grads);
   void release_acts();
   void conv_fwd(Ctx& c, int l, int lev, int B, const __nv_bfloat16* in, int ldi, int i_off, __nv_bfloat16* out,
@@ -91,7 +101,17 @@ class CoarseNet {
   float* bt_ = nullptr;
   int* perm_ = nullptr;
   long long bcap_ = 0;
+  int conv_path_ = 0;
+  int* tc_err_ = nullptr;
 };
+
+// 3x3 convolution on the 5th-generation tensor cores (hz_conv_tc.cu): Cin a
+// multiple of 16, Cout a multiple of 16 in [16, 256]; layouts as for the
+// warp-level kernel; *err is set when a wait timed out.
+bool conv_tc_supported(int Cin, int Cout);
+void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, const __nv_bfloat16* in, int ldi,
+                    int i_off, int Cout, const __nv_bfloat16* w, __nv_bfloat16* out, float* out32, int ldo, int o_off,
+                    int relu, const __nv_bfloat16* mask, int ldm, int m_off, int mask_lo, int* err);
 
 // 3D convolutional encoder-decoder of the same kind (three grid levels, 8-16-32
 // channels, 3x3x3 convolutions; the layers and their order are in hz_learn3d.cu):

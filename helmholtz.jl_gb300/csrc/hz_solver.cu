@@ -2115,6 +2115,8 @@ void net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, 
      "copy y");
   ck(cudaStreamSynchronize(cx.stream), "sync");
   cx.resolve();
+  if (net->net && net->net->conv_path() == HZ_NET_CONV_TCGEN05 && net->net->tc_failed())
+    fail(HZ_ERR_CUDA, "tensor-core convolution timed out");
 }
 
 void net_gradient(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int32_t batch,
@@ -2255,6 +2257,20 @@ int hz_net_file_info(const char* path, int64_t* nparams, int64_t* adam_step) {
   if (nparams) *nparams = n;
   if (adam_step) *adam_step = st;
   return HZ_OK;
+}
+
+int hz_net_set_conv_path(hz_net* net, int32_t path) {
+  if (!net) return HZ_ERR_ARG;
+  return guarded(nullptr, [&] {
+    if (path != HZ_NET_CONV_WARP_MMA && path != HZ_NET_CONV_TCGEN05)
+      fail(HZ_ERR_ARG, "conv path must be HZ_NET_CONV_WARP_MMA or HZ_NET_CONV_TCGEN05");
+    if (net->net3 && path != HZ_NET_CONV_WARP_MMA) fail(HZ_ERR_ARG, "the 3D network has the warp-level MMA path only");
+    ck(cudaSetDevice(net->dev), "cudaSetDevice");
+    if (net->net) {
+      cudaStreamSynchronize(net->net->ctx.stream);
+      net->net->set_conv_path(path);
+    }
+  });
 }
 
 int hz_net_set_profile(hz_net* net, int32_t on) {

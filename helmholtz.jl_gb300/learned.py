@@ -139,6 +139,12 @@ class CoarseNet:
         """Weights and Adam state from a file written by save (format, version and shapes checked)."""
         L.check(L.load().hz_net_load(self._h, str(path).encode()))
 
+    def set_conv_path(self, path: str) -> None:
+        """Convolution kernels: "mma" (warp-level mma.sync) or "tcgen05" (5th-generation
+        tensor cores with the accumulator in tensor memory; 2D network only)."""
+        code = {"mma": L.HZ_NET_CONV_WARP_MMA, "tcgen05": L.HZ_NET_CONV_TCGEN05}[path]
+        L.check(L.load().hz_net_set_conv_path(self._h, code))
+
     def set_profile(self, on: bool) -> None:
         """Time every kernel launch of the network's own stream with CUDA events."""
         L.check(L.load().hz_net_set_profile(self._h, int(bool(on))))

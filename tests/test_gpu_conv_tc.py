@@ -1,0 +1,69 @@
+"""GPU parity of the 2D network's convolutions on the 5th-generation tensor
+cores (tcgen05.mma with the accumulator in tensor memory) against the CPU
+oracle (oracle/coarse_net.py, BF16 rounding emulated) and against the
+warp-level MMA path: forward output to relative L2 error <= 1e-2, loss to
+<= 1e-3, every layer's weight gradient to <= 3e-2 (the tolerances of the
+network's other parity tests), on grids whose tiles are partial at the edges."""
+import numpy as np
+import pytest
+
+import coarse_net as CN
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+
+def _x(seed, B, ny, nx):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(B, ny, nx, 4)).astype(np.float32)
+    x[..., 2] = rng.uniform(0.5, 6.0, size=(B, ny, nx))
+    x[..., 3] = rng.uniform(0.01, 0.9, size=(B, ny, nx))
+    t = rng.normal(size=(B, ny, nx, 2)).astype(np.float32)
+    return x, t
+
+
+def _launches(net, name):
+    return sum(r["launches"] for r in net.kernel_times() if r["name"] == name)
+
+
+@pytest.mark.parametrize("ny,nx", [(17, 33), (41, 25)])
+def test_tcgen05_forward_matches_oracle_and_warp_mma(hz, ny, nx):
+    net = hz.learned.CoarseNet(seed=11)
+    w = net.get_weights()
+    x, _ = _x(1, 3, ny, nx)
+    y_mma = net.forward(x)
+    net.set_conv_path("tcgen05")
+    net.reset_kernel_times()
+    y_tc = net.forward(x)
+    assert _launches(net, "net_conv_fwd_tc") == 7  # every layer but the 8-channel output layer
+    yo, _ = CN.forward(w, x.astype(np.float64), emulate=True)
+    for b in range(x.shape[0]):
+        assert _rel(y_tc[b], yo[b]) <= 1e-2, (b, _rel(y_tc[b], yo[b]))
+        assert _rel(y_tc[b], y_mma[b]) <= 1e-2, (b, _rel(y_tc[b], y_mma[b]))
+
+
+def test_tcgen05_gradient_matches_oracle(hz):
+    net = hz.learned.CoarseNet(seed=5)
+    net.set_conv_path("tcgen05")
+    w = net.get_weights()
+    x, t = _x(2, 2, 25, 33)
+    net.reset_kernel_times()
+    loss, g = net.gradient(x, t)
+    assert _launches(net, "net_conv_bwd_tc") == 7  # data gradients of layers 1..7
+    yo, cache = CN.forward(w, x.astype(np.float64), emulate=True)
+    lo, go = CN.backward(cache, t.astype(np.float64))
+    assert abs(loss - lo) <= 1e-3 * lo
+    offs = np.cumsum([0] + [9 * a * b for a, b in CN.LAYERS])
+    for k in range(8):
+        a, b = g[offs[k]:offs[k + 1]], go[offs[k]:offs[k + 1]]
+        assert _rel(a, b) <= 3e-2, (k, _rel(a, b))
+
+
+def test_tcgen05_path_selection(hz):
+    net3 = hz.learned.CoarseNet3D(seed=1)
+    with pytest.raises(hz._lib.HelmgpuError):
+        net3.set_conv_path("tcgen05")
+    net3.set_conv_path("mma")
