@@ -71,8 +71,8 @@ WORKLOADS = {
                cells=(256, 256, 256), h=0.010, nrhs=32, levels=5, pad=16, ellipsoid=True, tol=1e-6, err_cols=1,
                cycle="K", relax="jac-gmres", relax_from=1, shift=0.3,
                # 3D learned correction below level 2 (65^3): pairs from seeded training models
-               learned3d=True, net_level=2, train_models=6, train_rhs=4, pairs_per_model=160, train_outer=2,
-               pair_sweeps=12, train_epochs=30, train_batch=8),
+               learned3d=True, net_level=2, train_models=6, train_rhs=8, pairs_per_model=320, train_outer=2,
+               pair_sweeps=30, train_epochs=30, train_batch=8),
 }
 DEFAULT_WORKLOAD = "c5"
 

@@ -758,6 +758,18 @@ void learned_correction(hz_handle* h, Hierarchy& H, int l, const cplx<T>* b, cpl
 template <typename T, typename TB>
 void mg_cycle(hz_handle* h, Hierarchy& H, int l, const cplx<TB>* b, cplx<T>* out, const int* cols, int nc);
 
+// The preconditioner of a K-cycle step on level k: the level's own cycle, or
+// the network when it is attached to level k (it then stands for everything
+// below level k - 1 that the cycle would do: smoothing on level k and the
+// recursion to the coarsest LU).
+template <typename T>
+void kcycle_precondition(hz_handle* h, Hierarchy& H, int k, const cplx<T>* v, cplx<T>* z, const int* cols, int nc) {
+  if (h->net_active && k == h->net_level)
+    learned_correction<T>(h, H, k, v, z, cols, nc);
+  else
+    mg_cycle<T, T>(h, H, k, v, z, cols, nc);
+}
+
 // out = e_k for the active columns of b_k by the K-cycle: two FGMRES steps on
 // level k's operator, right-preconditioned by level k's own cycle (zero
 // initial guess; Multigrid.jl cycleType 'K').
@@ -777,12 +789,12 @@ void kcycle_correction(hz_handle* h, Hierarchy& H, int k, const cplx<T>* b, cplx
   const cplx<T>* none = nullptr;
   launch_kc_sums<T>(c, N, ld, cols, nc, 0, 1, none, none, b, part, ks, 0);  // beta^2
   launch_kc_scale<T>(c, N, ld, cols, nc, ks, 0, b, V0);
-  mg_cycle<T, T>(h, H, k, V0, Z0, cols, nc);
+  kcycle_precondition<T>(h, H, k, V0, Z0, cols, nc);
   lev_op<T, T>(h, H, k, MODE_APPLY, Z0, none, W, cols, nc);
   launch_kc_sums<T>(c, N, ld, cols, nc, 1, 0, V0, none, W, part, ks, 1);  // h00
   launch_kc_update<T>(c, N, ld, cols, nc, 1, 1, ks, V0, none, W, part, 2);  // W -= h00 V0, h10^2
   launch_kc_scale<T>(c, N, ld, cols, nc, ks, 2, W, V1);
-  mg_cycle<T, T>(h, H, k, V1, Z1, cols, nc);
+  kcycle_precondition<T>(h, H, k, V1, Z1, cols, nc);
   lev_op<T, T>(h, H, k, MODE_APPLY, Z1, none, W, cols, nc);
   launch_kc_sums<T>(c, N, ld, cols, nc, 2, 0, V0, V1, W, part, ks, 3);  // h01, h11
   launch_kc_update<T>(c, N, ld, cols, nc, 2, 3, ks, V0, V1, W, part, 5);  // h21^2
@@ -849,7 +861,9 @@ template <typename T>
 void coarse_correction(hz_handle* h, Hierarchy& H, int l, const int* cols, int nc) {
   Level& C = *H.lv[l + 1];
   const int last = (int)H.lv.size() - 1;
-  if (h->net_active && l + 1 == h->net_level)
+  // K-cycle: the network preconditions the two FGMRES steps on its level
+  // (kcycle_precondition); V and W cycles: it replaces the level's cycle
+  if (h->net_active && l + 1 == h->net_level && !(h->opt.cycle == 'K' && l + 1 < last))
     learned_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
   else if (h->opt.cycle == 'K' && l + 1 < last)
     kcycle_correction<T>(h, H, l + 1, C.b.as<cplx<T>>(), C.x.as<cplx<T>>(), cols, nc);
@@ -2334,12 +2348,11 @@ int hz_learned_stats(const hz_handle* h, int64_t* net_calls, int32_t* fallbacks)
 namespace {
 // 3D training targets for the right-hand sides captured on `level`: a band LU of
 // a 3D coarse level is out of reach (65^3 nodes, bandwidth 4225), so the target
-// e = A^{-1} r starts from the coarse-grid correction the plain solver applies
-// on that level (what the network replaces: two FGMRES steps preconditioned by
-// the level's cycle for the K-cycle, one cycle otherwise) and takes sweeps - 1
-// restarted two-step FGMRES corrections e += K(r - A e) preconditioned by the
-// level's cycle, in FP64.  Each minimises the residual over its space, so the
-// residual never grows, whatever the cycle.
+// e = A^{-1} r starts from one cycle on that level (what the network stands
+// for: the level's cycle in V and W cycles, the preconditioner of the level's
+// two FGMRES steps in the K-cycle) and takes sweeps - 1 restarted two-step
+// FGMRES corrections e += K(r - A e) preconditioned by the level's cycle, in
+// FP64.  Each minimises the residual over its space, so the residual never grows.
 void collect_targets_iterative(hz_handle* h, Hierarchy& H, int level, int sweeps, long long cnt, float* x_out,
                                float* t_out, double* plain_err, double* target_relres) {
   const Grid g = level_grid(h, level);
@@ -2347,7 +2360,6 @@ void collect_targets_iterative(hz_handle* h, Hierarchy& H, int level, int sweeps
   const int R = h->rcap;
   const int last = (int)H.lv.size() - 1;
   if (level >= last) fail(HZ_ERR_ARG, "pairs need a level above the coarsest");
-  const bool kstep = h->opt.cycle == 'K';
   Level& Lv = *H.lv[level];
   if (!Lv.kv.p) {  // the two-step corrections' vectors (allocated by the K-cycle itself otherwise)
     Lv.kv.alloc((size_t)5 * R * Lv.ld * sizeof(double2));
@@ -2367,12 +2379,7 @@ void collect_targets_iterative(hz_handle* h, Hierarchy& H, int level, int sweeps
   ck(cudaMemcpy(idc.p, seq.data(), R * sizeof(int), cudaMemcpyHostToDevice), "upload cols");
   const int* dc = idc.as<int>();
   const float2* feat = net_features(h, level);
-  auto plain = [&](const double2* b, double2* out, int k) {
-    if (kstep)
-      kcycle_correction<double>(h, H, level, b, out, dc, k);
-    else
-      mg_cycle<double, double>(h, H, level, b, out, dc, k);
-  };
+  auto plain = [&](const double2* b, double2* out, int k) { mg_cycle<double, double>(h, H, level, b, out, dc, k); };
   std::vector<double> hn((size_t)R * 6);
   double worst = 0.0;
   for (long long i0 = 0; i0 < cnt; i0 += R) {

@@ -308,7 +308,9 @@ int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int6
 int hz_net_set_conv_path(hz_net* net, int32_t path);
 /* Use the network for the coarse-grid correction of multigrid level `level`
  * (1 .. levels-1; a network of the problem's dimension; FGMRES only: the
- * network is a nonlinear preconditioner).
+ * network is a nonlinear preconditioner).  With the K-cycle the network
+ * preconditions the two FGMRES steps on its level in place of that level's
+ * cycle; with the V and W cycles it replaces the level's cycle.
  * A restart cycle that reduces some column's residual by less than stag_ratio
  * hands the rest of that solve to the plain cycle.  net = NULL detaches.  The
  * handle does not own the network; keep it alive while attached, and use one
@@ -321,11 +323,11 @@ int hz_learned_stats(const hz_handle* h, int64_t* net_calls, int32_t* fallbacks)
  * `level` (at most max_pairs columns), then computes the target e = A^{-1} r on
  * that level: in 2D with a banded LU of its operator (FP64) followed by
  * sweeps - 1 steps of iterative refinement; in 3D (where the band LU of a
- * coarse level is out of reach) from the coarse-grid correction the plain
- * solver applies on that level followed by sweeps - 1 restarted FP64 two-step
+ * coarse level is out of reach) from one cycle on that level followed by
+ * sweeps - 1 restarted FP64 two-step
  * FGMRES corrections e += K(r - A e) preconditioned by the level's cycle (which
  * never raise the residual).  In 3D the grid is nx x ny x nz and plain_err
- * compares that plain correction with the target.
+ * compares one cycle on that level (what the network stands for) with the target.
  * x_out [max_pairs][N][4] and t_out [max_pairs][N][2] are DEVICE FP32 arrays in
  * the layout above; plain_err (host, may be NULL) gets ||e1 - e|| / ||e|| of one
  * plain cycle e1 per pair, target_relres (may be NULL) the largest
