@@ -78,12 +78,17 @@ DEFAULT_WORKLOAD = "c5"
 
 
 def workload(args) -> dict:
-    """The chosen workload with the command line's overrides (RHS count, level count)."""
+    """The chosen workload with the command line's overrides (RHS count, level
+    count, the learned correction's level and pairs per training model)."""
     wl = dict(WORKLOADS[args.workload])
     if args.nrhs > 0:
         wl["nrhs"] = args.nrhs
     if args.levels > 0:
         wl["levels"] = args.levels
+    if getattr(args, "net_level", 0) > 0 and "net_level" in wl:
+        wl["net_level"] = args.net_level
+    if getattr(args, "pairs_per_model", None) and wl.get("learned3d"):
+        wl["pairs_per_model"] = args.pairs_per_model
     return wl
 
 
@@ -635,7 +640,8 @@ def main():
                     help="learned workload: outer arithmetic of its mixed arms")
     ap.add_argument("--train-models", type=int, default=48, help="learned workload: seeded training models")
     ap.add_argument("--train-rhs", type=int, default=4, help="learned workload: random sources per training model")
-    ap.add_argument("--pairs-per-model", type=int, default=200)
+    ap.add_argument("--pairs-per-model", type=int, default=None,
+                    help="learned workloads: training pairs per seeded model (default: the workload's)")
     ap.add_argument("--train-epochs", type=int, default=20)
     ap.add_argument("--net-level", type=int, default=0, help="learned workload: multigrid level of the network "
                     "(0: the workload's)")
@@ -851,7 +857,7 @@ def run_learned(args, rank, ws, dist):
         P = make_problem(wl, seed=10_000 + 97 * rank + s)
         S = solver(P, "fp64")
         B = random_sources(P, args.train_rhs, seed=20_000 + s, pad=wl["pad"])
-        d = hz.learned.collect_pairs(S, B, level=level, sweeps=2, max_pairs=args.pairs_per_model)
+        d = hz.learned.collect_pairs(S, B, level=level, sweeps=2, max_pairs=args.pairs_per_model or 200)
         xs.append(d["x"].clone())
         ts.append(d["t"].clone())
         pes.append(d["plain_err"])
