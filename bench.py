@@ -281,19 +281,19 @@ def kernel_table(lib, h):
     return rows
 
 
-def traffic_ratio_from_profiles(kernel: str, workload: str):
-    """DRAM bytes / algorithmic bytes of `kernel` from the committed ncu
-    summary (a small case of the same workload; traffic scales with the
-    columns processed), or None."""
+def profile_entry(kernel: str, workload: str) -> dict:
+    """The committed ncu summary of `kernel` on a small case of the workload's
+    path (profiles/traffic.json): DRAM / algorithmic bytes (traffic scales with
+    the columns processed) and, for the FP64 kernels, the FP64 pipe's share of
+    its peak; {} when there is none."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
-        return None
+        return {}
     try:
-        d = json.loads(p.read_text())
-        e = d.get(workload, {}).get(kernel)
-        return float(e["dram_over_algorithmic"]) if e else None
-    except (ValueError, OSError, KeyError, TypeError):
-        return None
+        e = json.loads(p.read_text()).get(workload, {}).get(kernel)
+        return dict(e) if e else {}
+    except (ValueError, OSError, TypeError):
+        return {}
 
 
 # ---------------------------------------------------------------------------
@@ -672,13 +672,19 @@ def main():
     roofline = None
     if dom:
         achieved = dom["bytes"] / (dom["ms"] / 1000.0) / 1e9
-        ratio = traffic_ratio_from_profiles(dom["name"], args.workload) if args.nrhs == 0 else None
+        prof = profile_entry(dom["name"], args.workload) if args.nrhs == 0 else {}
+        ratio = prof.get("dram_over_algorithmic")
         tr = None if ratio is None else ratio * dom["bytes"] / dom["launches"]
         roofline = dict(bound="hbm", kernel=dom["name"], achieved=achieved, peak=peak, unit="GB/s",
                         frac=achieved / peak, peak_source=f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                         traffic=tr, avg_launch_ms=dom["ms"] / dom["timed"], share=dom["ms"] / tot_ms,
                         source="CUDA events around every launch on the handle's stream, over one eager solve "
                                "right after the timed ones")
+        if "fp64_pipe_pct_of_peak" in prof:
+            # native-FP64 kernels: GB300's FP64 pipe, not HBM, is the limit
+            roofline["fp64_pipe_pct_of_peak_ncu"] = prof["fp64_pipe_pct_of_peak"]
+            roofline["note"] = ("FP64 arithmetic: bound by the FP64 pipe (ncu, small case of the same path), "
+                                "not by HBM; see profiles/fgmres_fp64_kernels_3d129_kcycle_8rhs.md")
     # whole-solve roofline: the algorithmic bytes of every launched kernel of a solve over
     # the unprofiled time of a solve
     solve_bytes = sum(k["bytes"] for k in head["kernels"])
