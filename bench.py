@@ -70,8 +70,9 @@ WORKLOADS = {
     "c5": dict(name="3D 257^3 layered+ellipsoid, 32 surface sources, 5 levels, FGMRES(10) tol 1e-6",
                cells=(256, 256, 256), h=0.010, nrhs=32, levels=5, pad=16, ellipsoid=True, tol=1e-6, err_cols=1,
                cycle="K", relax="jac-gmres", relax_from=1, shift=0.3,
-               # 3D learned correction below level 2 (65^3): pairs from seeded training models
-               learned3d=True, net_level=2, train_models=6, train_rhs=8, pairs_per_model=320, train_outer=2,
+               # 3D learned correction: the network preconditions the K-cycle steps on level 3 (33^3) in
+               # place of the level-3 cycle and the coarsest band LU; pairs from seeded training models
+               learned3d=True, net_level=3, train_models=6, train_rhs=8, pairs_per_model=640, train_outer=2,
                pair_sweeps=30, train_epochs=30, train_batch=8),
 }
 DEFAULT_WORKLOAD = "c5"
@@ -380,9 +381,9 @@ def train_network3d(args, wl, hz, lib):
                 loss_last=float(hist[-1]), collect_s=collect_s, train_s=train_s,
                 target_relres_max=worst, pair_error_median_network=float(np.median(err)),
                 pair_error_median_plain_correction=float(np.median(pe)),
-                pairs="level-2 right-hand sides of the first %d restart cycles of FP64 solves of %d random sources "
-                      "per training model; targets from %d restarted plain corrections on that level"
-                      % (wl["train_outer"], wl["train_rhs"], wl["pair_sweeps"]))
+                pairs="level-%d right-hand sides of the first %d restart cycles of FP64 solves of %d random sources "
+                      "per training model; targets from %d restarted corrections on that level"
+                      % (level, wl["train_outer"], wl["train_rhs"], wl["pair_sweeps"]))
     del x, t
     torch.cuda.empty_cache()
     return net, info
