@@ -1,5 +1,6 @@
 // 3x3 convolution of the 2D learned-correction network on the 5th-generation
-// tensor cores (tcgen05.mma, accumulator in tensor memory).
+// tensor cores (tcgen05.mma, accumulator in tensor memory), operands staged by
+// the tensor memory accelerator (cp.async.bulk.tensor).
 //
 // Implicit GEMM: D[node][co] = sum_t sum_ci in[node + off_t][ci] * w[co][t][ci],
 // M = 128 nodes per tile (8 along x by 16 along y), N = Cout (16..256, a
@@ -16,20 +17,34 @@
 //      are SBO = 10 rows = 160 bytes apart; the two 8-channel halves of a
 //      16-channel K step are LBO = one plane = 2880 bytes apart.  Tap (dx, dy)
 //      only moves the start address, by ((dy + 1) * 10 + dx + 1) rows, so the
-//      nine taps read one staged tile.  Halo nodes outside the grid are staged
-//      as zeros: the zero padding of the convolution.
-//   B: all the layer's weights, staged once per CTA: for tap t and 16-channel
-//      K step c, two planes (8-channel halves) of Cout rows; SBO = 8 rows =
-//      128 bytes (the next 8 output channels), LBO = one plane.
-// One thread issues the 9 x Cin/16 MMAs of a tile (M=128, N=Cout, K=16 each,
-// BF16 x BF16 -> FP32) and commits them to an mbarrier; the four warps then
-// read their 32 accumulator rows (tensor-memory lanes) with tcgen05.ld and
-// apply ReLU / the mask and store.  CTAs are persistent over the tiles so the
-// weights are staged once.  Every wait is bounded: on a timeout the kernel sets
-// *err, skips the rest of its tiles and still frees its tensor memory.
+//      nine taps read one staged tile.
+//   B: all the layer's weights, staged once per CTA: for tap t and 8-channel
+//      group p, one plane of Cout rows (row co = w[co][t][8p .. 8p + 8));
+//      SBO = 8 rows = 128 bytes (the next 8 output channels), LBO = one plane.
+// The weights reach shared memory as one image in exactly the layout of B
+// (k_tc_wimage writes it once per weight update, or per backward convolution
+// for the flipped weights), copied by the TMA unit's bulk engine
+// (cp.async.bulk, 1-D, 32 KiB per copy).  The halo tile is one TMA tensor
+// load: the activation tensor [B][N][ldi] is described to the TMA unit as the
+// 5-D tensor (8 channels, x, y, plane, batch) with the plane dimension (stride
+// 16 bytes) ordered after y, so that one box of (8, 10, 18, Cin / 8, 1) lands
+// plane after plane exactly as A above; halo nodes outside the grid are filled
+// with zeros by the TMA unit, which is the zero padding of the convolution.
+//
+// Warp-specialised persistent CTAs: a producer thread keeps up to four halo
+// buffers in flight, an MMA thread issues the 9 x Cin / 16 MMAs of a tile into
+// one of two tensor-memory accumulators as soon as its halo has landed and the
+// accumulator is free, and four epilogue warps read the other accumulator out
+// (tcgen05.ld, ReLU / mask, BF16 or FP32 stores); the roles hand buffers to one
+// another through mbarriers only, so the loads, MMAs and epilogues of
+// consecutive tiles overlap.  Every wait is bounded: on a timeout the kernel
+// sets *err and a shared abort flag, the roles leave their loops, wait (again
+// bounded) for their copies and MMAs in flight, and the tensor memory is freed.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -47,13 +62,10 @@ constexpr int kTcHX = kTcTX + 2, kTcHY = kTcTY + 2;  // halo tile
 constexpr int kTcRows = kTcHX * kTcHY;               // 180 halo nodes
 constexpr int kTcPlane = kTcRows * 16;               // bytes of one 8-channel plane of the halo tile
 constexpr int kTcM = 128;
-constexpr int kTcHeader = 128;                       // mbarrier + tensor-memory address
+constexpr int kTcHeader = 128;                       // mbarriers + tensor-memory address
+constexpr int kTcAlign = 128;                        // TMA destinations start on 128-byte boundaries
 constexpr long long kTcSpinLimit = 1LL << 22;        // bounded mbarrier waits
-// Shared memory after the operands, so that a reading of the descriptors'
-// byte offsets other than the one this kernel assumes (LBO along K, SBO along
-// M / N) would still stay inside the allocation: the halo tile comes first,
-// then the weights, then this guard band.
-constexpr size_t kTcGuard = 40 * 1024;
+constexpr size_t kTcSmemMax = 227 * 1024;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -73,7 +85,6 @@ __host__ __device__ constexpr unsigned idesc_bf16(int M, int N) {
 
 __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
 // true once the phase with this parity has completed; false after the spin limit
@@ -90,9 +101,36 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
   return false;
 }
 
+// arrive on the barrier and add the bytes the copies of this phase will deliver
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// 1-D bulk copy global -> shared on the TMA unit: 16-byte aligned, size a multiple of 16
+__device__ __forceinline__ void bulk_load(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(src)), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void tma_load_5d(unsigned dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            int c4, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+      : "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void tc_mma(unsigned d_tmem, unsigned long long adesc, unsigned long long bdesc,
                                        unsigned idesc, unsigned accumulate) {
@@ -119,165 +157,353 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, float (&v)[16]) {
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+__device__ __forceinline__ unsigned pack_bf16x2(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const unsigned*>(&h);
+}
+
+struct TileCoord {
+  int b, x0, y0;
+};
+
+__device__ __forceinline__ TileCoord tile_coord(long long tile, int tiles_x, int tiles_y) {
+  const long long per = (long long)tiles_x * tiles_y;
+  const int tr = (int)(tile % per);
+  return {(int)(tile / per), (tr % tiles_x) * kTcTX, (tr / tiles_x) * kTcTY};
+}
+
 }  // namespace
 
-__global__ void __launch_bounds__(128, 1) k_conv_tc(int nx, int ny, int B, int Cin, int Cout,
-                                                    const bf16* __restrict__ in, int ldi, int i_off,
-                                                    const bf16* __restrict__ w, bf16* __restrict__ out,
-                                                    float* __restrict__ out32, int ldo, int o_off, int relu,
-                                                    const bf16* __restrict__ mask, int ldm, int m_off, int mask_lo,
-                                                    unsigned tmem_cols, int* __restrict__ err) {
-  extern __shared__ __align__(128) unsigned char tc_smem[];
-  unsigned long long* bar_p = reinterpret_cast<unsigned long long*>(tc_smem);
-  unsigned* tmem_slot = reinterpret_cast<unsigned*>(tc_smem + 8);
-  const int NC = Cin / 16;                       // 16-channel K steps
-  const int wplane = Cout * 16;                  // bytes of one weight plane
-  unsigned char* sA = tc_smem + kTcHeader;       // 2 * NC halo planes
-  unsigned char* sB = sA + 2 * NC * kTcPlane;    // 9 * NC * 2 weight planes
-  const unsigned bar = smem_u32(bar_p);
+// One row of the weight image per thread: row (t * Cin / 8 + p) * Cout + co holds
+// W[co][t][8p .. 8p + 8) of the convolution's weights W [Cout][9][Cin], where
+//   flip = 0: W = w;
+//   flip = 1: W[co][t][ci] = ci < wcout ? w[ci][8 - t][co] : 0 for w [wcout][9][wcin]
+//             (wcin = Cout): the transposed, flipped weights of the data gradient.
+__global__ void k_tc_wimage(int Cin, int Cout, const bf16* __restrict__ w, int flip, int wcin, int wcout,
+                            bf16* __restrict__ img) {
+  const int NP = Cin / 8;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 9 * NP * Cout) return;
+  const int co = idx % Cout, p = (idx / Cout) % NP, t = idx / (Cout * NP);
+  alignas(16) bf16 v[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int ci = 8 * p + e;
+    if (!flip)
+      v[e] = w[((long long)co * 9 + t) * Cin + ci];
+    else
+      v[e] = ci < wcout ? w[((long long)ci * 9 + (8 - t)) * wcin + co] : __float2bfloat16_rn(0.f);
+  }
+  reinterpret_cast<uint4*>(img)[idx] = *reinterpret_cast<const uint4*>(v);
+}
+
+// Shared memory (from a 128-byte aligned base): header (mbarriers and the
+// tensor-memory address), weights (9 * Cin / 8 planes of Cout * 16 bytes), then
+// nbuf halo buffers of Cin / 8 planes each.
+// Warp roles (192 threads): warps 0-3 epilogue (warp w reads tensor-memory lanes
+// 32 w .. 32 w + 31, tile rows of the same numbers), warp 4 lane 0 TMA
+// producer, warp 5 lane 0 MMA issuer.  Barriers:
+//   wbar        weights landed (TMA bytes)
+//   full[s]     halo buffer s landed (TMA bytes)         producer -> MMA
+//   empty[s]    halo buffer s read by its MMAs (commit)  MMA -> producer
+//   accf[a]     accumulator a complete (commit)          MMA -> epilogue
+//   acce[a]     accumulator a read out (4 warp arrivals) epilogue -> MMA
+// The k-th use of a stage waits its "full" barrier with parity k & 1 and, from
+// the second use on, its "empty" barrier with parity (k - 1) & 1.
+constexpr int kTcMaxBuf = 4;
+constexpr int kTcThreads = 192;
+
+__global__ void __launch_bounds__(kTcThreads, 2)
+    k_conv_tc(const __grid_constant__ CUtensorMap tin, int i_plane, int nx, int ny, int B, int Cin, int Cout,
+              int nbuf, const bf16* __restrict__ wimg, bf16* __restrict__ out, float* __restrict__ out32, int ldo,
+              int o_off, int relu, const bf16* __restrict__ mask, int ldm, int m_off, int mask_lo, unsigned acc_cols,
+              int* __restrict__ err) {
+  extern __shared__ unsigned char tc_raw[];
+  unsigned char* smem = tc_raw + ((kTcAlign - (smem_u32(tc_raw) & (kTcAlign - 1))) & (kTcAlign - 1));
+  const unsigned base = smem_u32(smem);
+  const unsigned wbar = base;
+  const unsigned full0 = base + 8, empty0 = full0 + 8 * kTcMaxBuf;  // [s] at + 8 s
+  const unsigned accf0 = empty0 + 8 * kTcMaxBuf, acce0 = accf0 + 16;  // [a] at + 8 a
+  unsigned* tmem_slot = reinterpret_cast<unsigned*>(smem + 112);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 116);
+  const int NP = Cin / 8;                          // 8-channel planes (2 per 16-channel K step)
+  const unsigned wplane = (unsigned)Cout * 16;     // bytes of one weight plane
+  const unsigned wbytes = 9u * NP * wplane;
+  const unsigned bBase = base + kTcHeader;
+  const unsigned aBase = bBase + wbytes;           // 128-byte aligned: wplane is a multiple of 256
+  const unsigned tileBytes = (unsigned)NP * kTcPlane;
+  const unsigned abuf = (tileBytes + kTcAlign - 1) / kTcAlign * kTcAlign;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long N = (long long)nx * ny;
   const int tiles_x = (nx + kTcTX - 1) / kTcTX, tiles_y = (ny + kTcTY - 1) / kTcTY;
   const long long tiles = (long long)tiles_x * tiles_y * B;
+  const int n = tiles > blockIdx.x ? (int)((tiles - blockIdx.x + gridDim.x - 1) / gridDim.x) : 0;
 
-  if (tid == 0) mbar_init(bar, 1);
+  if (tid == 0) {
+    mbar_init(wbar, 1);
+    for (int s = 0; s < kTcMaxBuf; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(accf0 + 8 * a, 1);
+      mbar_init(acce0 + 8 * a, 4);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_async_smem();
+  }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(tmem_cols)
+                 "r"(2 * acc_cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  // weights: plane ((t * NC + c) * 2 + h), row co = w[co][t][16 c + 8 h .. +8)
-  const int wunits = 9 * NC * 2 * Cout;
-  for (int u = tid; u < wunits; u += blockDim.x) {
-    const int h = u % 2, c = (u / 2) % NC, co = (u / (2 * NC)) % Cout, t = u / (2 * NC * Cout);
-    const uint4 v = *reinterpret_cast<const uint4*>(w + ((long long)co * 9 + t) * Cin + 16 * c + 8 * h);
-    *reinterpret_cast<uint4*>(sB + ((t * NC + c) * 2 + h) * wplane + co * 16) = v;
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const unsigned tmem = *tmem_slot;
-  const unsigned idesc = idesc_bf16(kTcM, Cout);
-  const unsigned aBase = smem_u32(sA), bBase = smem_u32(sB);
-  const int aunits = 2 * NC * kTcRows;
-  unsigned phase = 0;
-  bool ok = true;
-  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-    const int b = (int)(tile / ((long long)tiles_x * tiles_y));
-    const int tr = (int)(tile % ((long long)tiles_x * tiles_y));
-    const int x0 = (tr % tiles_x) * kTcTX, y0 = (tr / tiles_x) * kTcTY;
-    const bf16* inb = in + (long long)b * N * ldi + i_off;
-    // halo tile: unit u = (row r, plane p), planes fastest so a warp reads whole node rows
-    for (int u = tid; u < aunits; u += blockDim.x) {
-      const int p = u % (2 * NC), r = u / (2 * NC);
-      const int x = x0 + r % kTcHX - 1, y = y0 + r / kTcHX - 1;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (x >= 0 && x < nx && y >= 0 && y < ny)
-        v = *reinterpret_cast<const uint4*>(inb + ((long long)y * nx + x) * ldi + 8 * p);
-      *reinterpret_cast<uint4*>(sA + p * kTcPlane + r * 16) = v;
+  auto give_up = [&]() {
+    *abort_flag = 1;
+    atomicExch(err, 1);
+  };
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // producer: weights once, then the halo of every tile
+      mbar_expect_tx(wbar, wbytes);
+      for (unsigned o = 0; o < wbytes; o += 32768u)
+        bulk_load(bBase + o, reinterpret_cast<const unsigned char*>(wimg) + o, min(32768u, wbytes - o), wbar);
+      int j = 0;
+      for (; j < n && !*abort_flag; ++j) {
+        const int s = j % nbuf, k = j / nbuf;
+        if (k >= 1 && !mbar_wait(empty0 + 8 * s, (unsigned)(k - 1) & 1u)) {
+          give_up();
+          break;
+        }
+        const TileCoord tc = tile_coord(blockIdx.x + (long long)j * gridDim.x, tiles_x, tiles_y);
+        mbar_expect_tx(full0 + 8 * s, tileBytes);
+        tma_load_5d(aBase + (unsigned)s * abuf, &tin, 0, tc.x0 - 1, tc.y0 - 1, i_plane, tc.b, full0 + 8 * s);
+      }
+      if (*abort_flag) {
+        // bounded waits for the copies still in flight: the weights and the last nbuf halo loads
+        mbar_wait(wbar, 0);
+        for (int q = max(0, j - nbuf); q < j; ++q) mbar_wait(full0 + 8 * (q % nbuf), (unsigned)(q / nbuf) & 1u);
+      }
     }
-    fence_async_smem();  // the staged tile is read by the tensor cores (async proxy)
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // MMA issuer: M = 128 tile rows, N = Cout, K = 16 per instruction, 9 * Cin / 16 instructions per tile
+      const unsigned idesc = idesc_bf16(kTcM, Cout);
+      int committed = -1;
+      if (!mbar_wait(wbar, 0)) give_up();
+      for (int j = 0; j < n && !*abort_flag; ++j) {
+        const int s = j % nbuf, a = j & 1;
+        if (!mbar_wait(full0 + 8 * s, (unsigned)(j / nbuf) & 1u) ||
+            (j >= 2 && !mbar_wait(acce0 + 8 * a, (unsigned)((j >> 1) - 1) & 1u))) {
+          give_up();
+          break;
+        }
+        tc_fence_after();
+        const unsigned acc = tmem + (unsigned)a * acc_cols;
+        const unsigned long long a0 = sdesc(aBase + (unsigned)s * abuf, kTcPlane, kTcHX * 16);
+        const unsigned long long b0 = sdesc(bBase, wplane, 128);
+        for (int t = 0; t < 9; ++t) {
+          const unsigned tap = (unsigned)(((t / 3) * kTcHX + t % 3) * 16);  // halo row offset of tap t, bytes
+          for (int c = 0; c < NP / 2; ++c) {
+            const unsigned aoff = (2u * c * kTcPlane + tap) >> 4, boff = ((unsigned)(t * NP + 2 * c) * wplane) >> 4;
+            tc_mma(acc, a0 + aoff, b0 + boff, idesc, (t | c) != 0);
+          }
+        }
+        tc_commit(empty0 + 8 * s);  // halo buffer s free once these MMAs have read it
+        tc_commit(accf0 + 8 * a);   // accumulator a ready for the epilogue
+        committed = j;
+      }
+      if (*abort_flag && committed >= 0)
+        mbar_wait(accf0 + 8 * (committed & 1), (unsigned)(committed >> 1) & 1u);
+    }
+  } else {
+    // epilogue warps 0-3: this thread's accumulator row is tile row warp * 32 + lane
+    for (int j = 0; j < n; ++j) {
+      const int a = j & 1;
+      const bool done = __all_sync(0xffffffffu, mbar_wait(accf0 + 8 * a, (unsigned)(j >> 1) & 1u));
+      if (!done) {
+        if (lane == 0) give_up();
+        break;
+      }
       tc_fence_after();
-      for (int t = 0; t < 9; ++t) {
-        const int dx = t % 3, dy = t / 3;  // offsets + 1
-        for (int c = 0; c < NC; ++c) {
-          const unsigned a = aBase + (2 * c) * kTcPlane + (dy * kTcHX + dx) * 16;
-          const unsigned bb = bBase + ((t * NC + c) * 2) * wplane;
-          tc_mma(tmem, sdesc(a, kTcPlane, kTcHX * 16), sdesc(bb, wplane, 128), idesc, (t | c) != 0);
+      const TileCoord tc = tile_coord(blockIdx.x + (long long)j * gridDim.x, tiles_x, tiles_y);
+      const int row = warp * 32 + lane;
+      const int x = tc.x0 + row % kTcTX, y = tc.y0 + row / kTcTX;
+      const bool in_grid = x < nx && y < ny;
+      const long long orow = (long long)tc.b * N + (long long)y * nx + x;
+      const unsigned acc = tmem + (unsigned)a * acc_cols + ((unsigned)(warp * 32) << 16);
+      for (int cb = 0; cb < Cout; cb += 16) {
+        float v[16];
+        tc_ld16(acc + (unsigned)cb, v);
+        if (!in_grid) continue;
+        if (relu) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.f);
+        }
+        if (mask && cb >= mask_lo) {
+          const uint4* mp = reinterpret_cast<const uint4*>(mask + orow * ldm + m_off + cb);
+          const uint4 m2[2] = {mp[0], mp[1]};
+          const bf16* mh = reinterpret_cast<const bf16*>(m2);
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if (!(__bfloat162float(mh[k]) > 0.f)) v[k] = 0.f;
+        }
+        if (out32) {
+          float4* op = reinterpret_cast<float4*>(out32 + orow * ldo + o_off + cb);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) op[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+          uint4* op = reinterpret_cast<uint4*>(out + orow * ldo + o_off + cb);
+          op[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                             pack_bf16x2(v[6], v[7]));
+          op[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
+                             pack_bf16x2(v[14], v[15]));
         }
       }
-      tc_commit(bar);
+      // accumulator a read out: one arrival per warp
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce0 + 8 * a);
+      if (*abort_flag) break;
     }
-    __syncwarp();
-    // every thread waits; the block agrees on the outcome before anyone leaves the loop
-    const bool done = mbar_wait(bar, phase);
-    if (!__syncthreads_and(done)) {
-      ok = false;
-      if (tid == 0) {
-        atomicExch(err, 1);
-        mbar_wait(bar, phase);  // one more bounded wait for MMAs still in flight before the memory is freed
-      }
-      break;
-    }
-    phase ^= 1u;
-    tc_fence_after();
-    // epilogue: this thread's accumulator row is tile row warp * 32 + lane
-    const int row = warp * 32 + lane;
-    const int x = x0 + row % kTcTX, y = y0 + row / kTcTX;
-    const bool in_grid = x < nx && y < ny;
-    const long long orow = (long long)b * N + (long long)y * nx + x;
-    for (int cb = 0; cb < Cout; cb += 16) {
-      float v[16];
-      tc_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)cb, v);
-      if (!in_grid) continue;
-#pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        const int co = cb + k;
-        float s = v[k];
-        if (relu) s = fmaxf(s, 0.f);
-        if (mask && co >= mask_lo && !(__bfloat162float(mask[orow * ldm + m_off + co]) > 0.f)) s = 0.f;
-        if (out32)
-          out32[orow * ldo + o_off + co] = s;
-        else
-          out[orow * ldo + o_off + co] = __float2bfloat16_rn(s);
-      }
-    }
-    tc_fence_before();
-    __syncthreads();  // accumulator read and halo tile consumed before the next tile reuses them
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * acc_cols) : "memory");
 }
 
-static size_t conv_tc_operands(int Cin, int Cout) {
-  return (size_t)kTcHeader + (size_t)9 * (Cin / 16) * 2 * Cout * 16 + (size_t)2 * (Cin / 16) * kTcPlane;
+namespace {
+
+size_t tc_weights(int Cin, int Cout) { return (size_t)9 * (Cin / 8) * Cout * 16; }
+size_t tc_halo(int Cin) { return ((size_t)(Cin / 8) * kTcPlane + kTcAlign - 1) / kTcAlign * kTcAlign; }
+size_t tc_smem(int Cin, int Cout, int nbuf) {
+  return (size_t)kTcAlign + kTcHeader + tc_weights(Cin, Cout) + (size_t)nbuf * tc_halo(Cin);
+}
+unsigned tc_cols(int Cout) {
+  unsigned cols = 32;
+  while ((int)cols < Cout) cols <<= 1;
+  return cols;
 }
 
-static constexpr size_t kTcSmemMax = 227 * 1024;
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-size_t conv_tc_smem(int Cin, int Cout) {
-  return std::min(kTcSmemMax, conv_tc_operands(Cin, Cout) + kTcGuard);
+// the driver's tensor-map encoder, looked up once through the runtime
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  if (!fn) throw std::runtime_error("conv_tc: cuTensorMapEncodeTiled is not available");
+  return fn;
 }
+
+void encode(CUtensorMap* map, const void* ptr, int rank, const cuuint64_t* dims, const cuuint64_t* strides,
+            const cuuint32_t* box, const char* what) {
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  const CUresult r = encode_tiled()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void*>(ptr),
+                                    dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::runtime_error(std::string("conv_tc: tensor map of the ") + what + " rejected");
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
 
 bool conv_tc_supported(int Cin, int Cout) {
-  return Cin % 16 == 0 && Cin >= 16 && Cout % 16 == 0 && Cout >= 16 && Cout <= 256 &&
-         conv_tc_operands(Cin, Cout) <= kTcSmemMax;
+  return Cin % 16 == 0 && Cin >= 16 && Cin <= 256 && Cout % 16 == 0 && Cout >= 16 && Cout <= 256 &&
+         tc_smem(Cin, Cout, 1) <= kTcSmemMax;
+}
+
+void conv_tc_weight_image(Ctx& ctx, const char* name, int Cin, int Cout, const bf16* w, int flip, int wcin,
+                          int wcout, bf16* img) {
+  if (!conv_tc_supported(Cin, Cout)) throw std::runtime_error("conv_tc: unsupported channel counts");
+  if (flip && wcin != Cout) throw std::runtime_error("conv_tc: flipped weights of another shape");
+  if (!aligned16(img)) throw std::runtime_error("conv_tc: weight image not aligned to 16 bytes");
+  const int rows = 9 * (Cin / 8) * Cout;
+  HZ_LAUNCH(ctx, name, (double)rows * 32.0, k_tc_wimage, (unsigned)((rows + 255) / 256), 256, 0, Cin, Cout, w, flip,
+            wcin, wcout, img);
 }
 
 void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi, int i_off,
-                    int Cout, const bf16* w, bf16* out, float* out32, int ldo, int o_off, int relu, const bf16* mask,
+                    int Cout, const bf16* wimg, bf16* out, float* out32, int ldo, int o_off, int relu, const bf16* mask,
                     int ldm, int m_off, int mask_lo, int* err) {
   if (!conv_tc_supported(Cin, Cout)) throw std::runtime_error("conv_tc: unsupported channel counts");
-  if ((ldi % 8) || (i_off % 8)) throw std::runtime_error("conv_tc: channel layout not aligned");
-  const size_t smem = conv_tc_smem(Cin, Cout);
-  static size_t set_bytes[kMaxDevices] = {};
+  if (ldi % 8 || i_off % 8 || i_off + Cin > ldi || !aligned16(in) || !aligned16(wimg))
+    throw std::runtime_error("conv_tc: input or weight layout not aligned to 16 bytes");
+  if (out32 ? (ldo % 4 || o_off % 4 || !aligned16(out32)) : (ldo % 8 || o_off % 8 || !aligned16(out)))
+    throw std::runtime_error("conv_tc: output layout not aligned to 16 bytes");
+  if (mask && (mask_lo % 16 || ldm % 8 || m_off % 8 || !aligned16(mask)))
+    throw std::runtime_error("conv_tc: mask layout not aligned to 16 bytes");
+  if (o_off + Cout > ldo || (mask && m_off + Cout > ldm))
+    throw std::runtime_error("conv_tc: channel offset beyond the row");
+  if (nx < 1 || ny < 1 || B < 1) throw std::runtime_error("conv_tc: empty grid");
+
+  static std::mutex mu;
+  static bool attr_set[kMaxDevices] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("conv_tc: device ordinal out of range");
-  if (set_bytes[dev] < smem) {
-    const cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      throw std::runtime_error(std::string("conv_tc: shared memory attribute: ") + cudaGetErrorString(e));
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!attr_set[dev]) {
+      // the largest shared-memory carveout, so that as many CTAs stay resident as the occupancy query reports
+      cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemMax);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw std::runtime_error(std::string("conv_tc: shared memory attribute: ") + cudaGetErrorString(e));
+      }
+      attr_set[dev] = true;
     }
-    set_bytes[dev] = smem;
   }
-  unsigned cols = 32;
-  while ((int)cols < Cout) cols <<= 1;
+  // activations [B][ny][nx][ldi] as (8 channels, x, y, plane, batch), plane after y
+  alignas(64) CUtensorMap tin = {};
+  {
+    const cuuint64_t dims[5] = {8, (cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)(ldi / 8), (cuuint64_t)B};
+    const cuuint64_t strides[4] = {(cuuint64_t)ldi * 2, (cuuint64_t)nx * ldi * 2, 16, (cuuint64_t)nx * ny * ldi * 2};
+    const cuuint32_t box[5] = {8, kTcHX, kTcHY, (cuuint32_t)(Cin / 8), 1};
+    encode(&tin, in, 5, dims, strides, box, "activations");
+  }
+  // halo buffers: as many as fit (up to four); CTAs per SM as shared and tensor
+  // memory (512 columns per SM) allow
+  const unsigned cols = tc_cols(Cout);
+  int nbuf = kTcMaxBuf;
+  while (nbuf > 1 && tc_smem(Cin, Cout, nbuf) > kTcSmemMax) --nbuf;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc, kTcThreads, tc_smem(Cin, Cout, nbuf)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  per_sm = std::max(1, std::min(per_sm, (int)(512 / (2 * cols))));
+  const size_t smem = tc_smem(Cin, Cout, nbuf);
   const long long N = (long long)nx * ny;
   const long long tiles = (long long)((nx + kTcTX - 1) / kTcTX) * ((ny + kTcTY - 1) / kTcTY) * B;
-  const int grid = (int)std::max<long long>(1, std::min<long long>(tiles, kSMs));
+  const int grid = (int)std::max<long long>(1, std::min<long long>(tiles, (long long)kSMs * per_sm));
   const double bytes = (double)B * N * (Cin * 2.0 + Cout * (out32 ? 4.0 : 2.0)) + 9.0 * Cin * Cout * 2.0;
   ctx.add_flops(name, 2.0 * 9.0 * Cin * Cout * (double)N * B);
-  HZ_LAUNCH(ctx, name, bytes, k_conv_tc, grid, 128, smem, nx, ny, B, Cin, Cout, in, ldi, i_off, w, out, out32, ldo,
-            o_off, relu, mask, ldm, m_off, mask_lo, cols, err);
+  HZ_LAUNCH(ctx, name, bytes, k_conv_tc, grid, kTcThreads, smem, tin, i_off / 8, nx, ny, B, Cin, Cout, nbuf, wimg,
+            out, out32, ldo, o_off, relu, mask, ldm, m_off, mask_lo, cols, err);
 }
 
 }  // namespace hz

@@ -631,6 +631,7 @@ CoarseNet::CoarseNet(unsigned seed) {
 CoarseNet::~CoarseNet() {
   release_acts();
   dfree(tc_err_);
+  dfree(wimg_);
   dfree(w32_);
   dfree(wbf_);
   dfree(g32_);
@@ -663,6 +664,7 @@ void CoarseNet::set_weights(const float* host) {
   step_ = 0;
   k_f2bf<<<256, 256, 0, ctx.stream>>>(wtotal_, w32_, wbf_);
   cuda_ok(cudaGetLastError(), "weights to bf16");
+  refresh_images(ctx);
   cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
 }
 
@@ -853,11 +855,21 @@ float* CoarseNet::scale_staging(int B) {
 }
 
 // One convolution: on the 5th-generation tensor cores (tcgen05) when that path
-// is selected and the channel counts suit it, else the warp-level MMA kernel.
+// is selected and the channel counts suit it (w is then the layer's weight
+// image), else the warp-level MMA kernel.  At 16 input and 16 output channels
+// the warp-level kernel stays: there each tcgen05.mma (N = 16) re-reads the
+// 128-row activation operand from shared memory for a sixteenth of the work of
+// a full-width one, and the warp-level kernel was the faster of the two on a
+// 129 x 129 x 32 batch (44.8 against 55.2 us; the layers with 32 or more
+// channels on either side ran 1.1-2.3x faster on tcgen05).
+bool CoarseNet::use_tc(int Cin, int Cout) const {
+  return conv_path_ != 0 && conv_tc_supported(Cin, Cout) && (Cin > 16 || Cout > 16);
+}
+
 void CoarseNet::conv(Ctx& c, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi, int i_off,
                      int Cout, const bf16* w, bf16* out, float* out32, int ldo, int o_off, int relu, const bf16* mask,
                      int ldm, int m_off, int mask_lo) {
-  if (conv_path_ == 1 && conv_tc_supported(Cin, Cout)) {
+  if (use_tc(Cin, Cout)) {
     const char* tc_name = std::strcmp(name, "net_conv_fwd") == 0 ? "net_conv_fwd_tc" : "net_conv_bwd_tc";
     conv_tc_launch(c, tc_name, nx, ny, B, Cin, in, ldi, i_off, Cout, w, out, out32, ldo, o_off, relu, mask, ldm, m_off,
                    mask_lo, tc_err_);
@@ -867,9 +879,23 @@ void CoarseNet::conv(Ctx& c, const char* name, int nx, int ny, int B, int Cin, c
               mask_lo);
 }
 
+// Weight images of the forward layers on the tensor-core path, rewritten on c's
+// stream whenever the BF16 weights change.
+void CoarseNet::refresh_images(Ctx& c) {
+  if (conv_path_ == 0) return;
+  if (!wimg_) dalloc(&wimg_, wtotal_ * 2);
+  for (int l = 0; l < kLayers; ++l) {
+    const auto& L = kSpec[l];
+    if (use_tc(L.cinp, L.coutp))
+      conv_tc_weight_image(c, "net_wimage", L.cinp, L.coutp, wbf_ + woff_[l], 0, 0, 0, wimg_ + woff_[l]);
+  }
+}
+
 void CoarseNet::set_conv_path(int path) {
   if (path != 0 && path != 1) throw std::runtime_error("coarse net: conv path must be 0 (warp MMA) or 1 (tcgen05)");
   conv_path_ = path;
+  refresh_images(ctx);
+  cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
 }
 
 bool CoarseNet::tc_failed() {
@@ -881,8 +907,9 @@ bool CoarseNet::tc_failed() {
 void CoarseNet::conv_fwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi, int i_off, bf16* out, int ldo,
                          int o_off, int relu, float* out32) {
   const auto& L = kSpec[l];
-  conv(c, "net_conv_fwd", gx_[lev], gy_[lev], B, L.cinp, in, ldi, i_off, L.coutp, wbf_ + woff_[l], out, out32, ldo,
-       o_off, relu, nullptr, 0, 0, 0);
+  const bf16* w = (use_tc(L.cinp, L.coutp) ? wimg_ : wbf_) + woff_[l];
+  conv(c, "net_conv_fwd", gx_[lev], gy_[lev], B, L.cinp, in, ldi, i_off, L.coutp, w, out, out32, ldo, o_off, relu,
+       nullptr, 0, 0, 0);
 }
 
 void CoarseNet::forward(Ctx& c, const float* x4, int nx, int ny, int B, bool train) {
@@ -930,8 +957,12 @@ void CoarseNet::conv_bwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi,
   if (!din) return;
   const int K = round16(L.coutp);
   const int tot = L.cinp * 9 * K;
-  HZ_LAUNCH(c, "net_wflip", (double)tot * 4.0, k_wflip, (unsigned)((tot + 255) / 256), 256, 0, L.coutp, L.cinp, K,
-            wbf_ + woff_[l], wt_);
+  if (use_tc(K, L.cinp)) {
+    conv_tc_weight_image(c, "net_wflip", K, L.cinp, wbf_ + woff_[l], 1, L.cinp, L.coutp, wt_);
+  } else {
+    HZ_LAUNCH(c, "net_wflip", (double)tot * 4.0, k_wflip, (unsigned)((tot + 255) / 256), 256, 0, L.coutp, L.cinp, K,
+              wbf_ + woff_[l], wt_);
+  }
   conv(c, "net_conv_bwd", nx, ny, B, K, dout, ldd, d_off, L.cinp, wt_, din, nullptr, ldn, n_off, 0, mask, ldm, i_off,
        mask_lo);
 }
@@ -966,7 +997,7 @@ double CoarseNet::backward(Ctx& c, const float* t, int nx, int ny, int B) {
   cuda_ok(cudaMemcpyAsync(&l, loss_, 8, cudaMemcpyDeviceToHost, c.stream), "loss");
   cuda_ok(cudaStreamSynchronize(c.stream), "sync");
   c.resolve();
-  if (conv_path_ == 1 && tc_failed()) throw std::runtime_error("coarse net: tensor-core convolution timed out");
+  if (conv_path_ != 0 && tc_failed()) throw std::runtime_error("coarse net: tensor-core convolution timed out");
   return l;
 }
 
@@ -976,6 +1007,7 @@ void CoarseNet::adam(Ctx& c, double lr) {
   const float c1 = 1.f - std::pow(b1, (float)step_), c2 = 1.f - std::pow(b2, (float)step_);
   HZ_LAUNCH(c, "net_adam", (double)wtotal_ * 22.0, k_adam, 304, 256, 0, wtotal_, w32_, g32_, m_, v_, wbf_, (float)lr,
             b1, b2, 1e-8f, c1, c2);
+  refresh_images(c);
 }
 
 void CoarseNet::train(Ctx& c, const float* x, const float* t, int nx, int ny, long long nsamples, int batch,

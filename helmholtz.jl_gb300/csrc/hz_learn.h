@@ -56,8 +56,9 @@ class CoarseNet {
 
   Ctx ctx;  // own stream and launch table (training, standalone inference)
 
-  // convolution kernels: 0 = warp-level MMA (mma.sync), 1 = 5th-generation
-  // tensor cores (tcgen05.mma, TMEM accumulator) where the channel counts suit it
+  // convolution kernels: 0 = warp-level MMA (mma.sync); 1 = 5th-generation
+  // tensor cores (tcgen05.mma, TMEM accumulator, operands staged by TMA) where
+  // the channel counts suit it
   void set_conv_path(int path);
   int conv_path() const { return conv_path_; }
   // true when a tensor-core convolution gave up waiting (device flag; synchronous read)
@@ -103,15 +104,24 @@ class CoarseNet {
   long long bcap_ = 0;
   int conv_path_ = 0;
   int* tc_err_ = nullptr;
+  __nv_bfloat16* wimg_ = nullptr;  // tensor-core weight images of the forward layers (at woff_)
+  bool use_tc(int Cin, int Cout) const;
+  void refresh_images(Ctx& c);
 };
 
 // 3x3 convolution on the 5th-generation tensor cores (hz_conv_tc.cu): Cin a
-// multiple of 16, Cout a multiple of 16 in [16, 256]; layouts as for the
-// warp-level kernel; *err is set when a wait timed out.
+// multiple of 16 in [16, 256], Cout a multiple of 16 in [16, 256]; layouts as
+// for the warp-level kernel except the weights, which come as the image that
+// conv_tc_weight_image writes; *err is set when a wait timed out.
 bool conv_tc_supported(int Cin, int Cout);
 void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, const __nv_bfloat16* in, int ldi,
-                    int i_off, int Cout, const __nv_bfloat16* w, __nv_bfloat16* out, float* out32, int ldo, int o_off,
-                    int relu, const __nv_bfloat16* mask, int ldm, int m_off, int mask_lo, int* err);
+                    int i_off, int Cout, const __nv_bfloat16* wimg, __nv_bfloat16* out, float* out32, int ldo,
+                    int o_off, int relu, const __nv_bfloat16* mask, int ldm, int m_off, int mask_lo, int* err);
+// Weight image of a convolution with Cin inputs and Cout outputs (9 * Cin * Cout
+// BF16 values): flip = 0 from w [Cout][9][Cin]; flip = 1 the data-gradient
+// weights of a layer w [wcout][9][wcin] (wcin = Cout; inputs >= wcout are zero).
+void conv_tc_weight_image(Ctx& ctx, const char* name, int Cin, int Cout, const __nv_bfloat16* w, int flip, int wcin,
+                          int wcout, __nv_bfloat16* img);
 
 // 3D convolutional encoder-decoder of the same kind (three grid levels, 8-16-32
 // channels, 3x3x3 convolutions; the layers and their order are in hz_learn3d.cu):

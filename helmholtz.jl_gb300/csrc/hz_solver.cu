@@ -2129,7 +2129,7 @@ void net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, 
      "copy y");
   ck(cudaStreamSynchronize(cx.stream), "sync");
   cx.resolve();
-  if (net->net && net->net->conv_path() == HZ_NET_CONV_TCGEN05 && net->net->tc_failed())
+  if (net->net && net->net->conv_path() != HZ_NET_CONV_WARP_MMA && net->net->tc_failed())
     fail(HZ_ERR_CUDA, "tensor-core convolution timed out");
 }
 

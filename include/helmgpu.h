@@ -300,8 +300,9 @@ int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int6
                    int32_t batch, int32_t epochs, double lr, int32_t seed, double* loss_hist);
 /* Convolution kernels of a 2D network: HZ_NET_CONV_WARP_MMA (warp-level
  * mma.sync, every layer) or HZ_NET_CONV_TCGEN05 (5th-generation tensor cores,
- * tcgen05.mma with the accumulator in tensor memory, for the layers whose
- * channel counts are multiples of 16; the 8-channel output layer keeps the
+ * tcgen05.mma with the accumulator in tensor memory and the operands staged by
+ * the TMA unit, for the layers whose channel counts are multiples of 16 with
+ * more than 16 on one side; the 16 -> 16 and 8-channel layers keep the
  * warp-level kernel).  The 3D network accepts HZ_NET_CONV_WARP_MMA only. */
 #define HZ_NET_CONV_WARP_MMA 0
 #define HZ_NET_CONV_TCGEN05 1

@@ -1,9 +1,10 @@
 """GPU parity of the 2D network's convolutions on the 5th-generation tensor
-cores (tcgen05.mma with the accumulator in tensor memory) against the CPU
-oracle (oracle/coarse_net.py, BF16 rounding emulated) and against the
-warp-level MMA path: forward output to relative L2 error <= 1e-2, loss to
-<= 1e-3, every layer's weight gradient to <= 3e-2 (the tolerances of the
-network's other parity tests), on grids whose tiles are partial at the edges."""
+cores (tcgen05.mma with the accumulator in tensor memory, operands staged by
+the TMA unit) against the CPU oracle (oracle/coarse_net.py,
+BF16 rounding emulated) and against the warp-level MMA path: forward output to
+relative L2 error <= 1e-2, loss to <= 1e-3, every layer's weight gradient to
+<= 3e-2 (the tolerances of the network's other parity tests), on grids whose
+tiles are partial at the edges; weight images follow Adam steps."""
 import numpy as np
 import pytest
 
@@ -29,30 +30,36 @@ def _launches(net, name):
     return sum(r["launches"] for r in net.kernel_times() if r["name"] == name)
 
 
+PATHS = ["tcgen05"]
+
+
+@pytest.mark.parametrize("path", PATHS)
 @pytest.mark.parametrize("ny,nx", [(17, 33), (41, 25)])
-def test_tcgen05_forward_matches_oracle_and_warp_mma(hz, ny, nx):
+def test_tcgen05_forward_matches_oracle_and_warp_mma(hz, ny, nx, path):
     net = hz.learned.CoarseNet(seed=11)
     w = net.get_weights()
     x, _ = _x(1, 3, ny, nx)
     y_mma = net.forward(x)
-    net.set_conv_path("tcgen05")
+    net.set_conv_path(path)
     net.reset_kernel_times()
     y_tc = net.forward(x)
-    assert _launches(net, "net_conv_fwd_tc") == 7  # every layer but the 8-channel output layer
+    # every layer but the 16 -> 16 input layer and the 8-channel output layer
+    assert _launches(net, "net_conv_fwd_tc") == 6
     yo, _ = CN.forward(w, x.astype(np.float64), emulate=True)
     for b in range(x.shape[0]):
         assert _rel(y_tc[b], yo[b]) <= 1e-2, (b, _rel(y_tc[b], yo[b]))
         assert _rel(y_tc[b], y_mma[b]) <= 1e-2, (b, _rel(y_tc[b], y_mma[b]))
 
 
-def test_tcgen05_gradient_matches_oracle(hz):
+@pytest.mark.parametrize("path", PATHS)
+def test_tcgen05_gradient_matches_oracle(hz, path):
     net = hz.learned.CoarseNet(seed=5)
-    net.set_conv_path("tcgen05")
+    net.set_conv_path(path)
     w = net.get_weights()
     x, t = _x(2, 2, 25, 33)
     net.reset_kernel_times()
     loss, g = net.gradient(x, t)
-    assert _launches(net, "net_conv_bwd_tc") == 7  # data gradients of layers 1..7
+    assert _launches(net, "net_conv_bwd_tc") == 6  # data gradients of layers 1..6 (layer 7's is 16 -> 16)
     yo, cache = CN.forward(w, x.astype(np.float64), emulate=True)
     lo, go = CN.backward(cache, t.astype(np.float64))
     assert abs(loss - lo) <= 1e-3 * lo
@@ -64,6 +71,29 @@ def test_tcgen05_gradient_matches_oracle(hz):
 
 def test_tcgen05_path_selection(hz):
     net3 = hz.learned.CoarseNet3D(seed=1)
-    with pytest.raises(hz._lib.HelmgpuError):
-        net3.set_conv_path("tcgen05")
+    for path in PATHS:
+        with pytest.raises(hz._lib.HelmgpuError):
+            net3.set_conv_path(path)
     net3.set_conv_path("mma")
+
+
+def test_tcgen05_weight_images_follow_training(hz):
+    """Adam steps and set_weights on the tensor-core path rewrite the weight
+    images: afterwards both paths give the same forward output for the same
+    weights."""
+    import torch
+    x, t = _x(3, 8, 17, 17)
+    net = hz.learned.CoarseNet(seed=2)
+    net.set_conv_path("tcgen05")
+    hist = net.train(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda(), epochs=3, batch=4, lr=1e-3, seed=1)
+    assert np.all(np.isfinite(hist))
+    y_tc = net.forward(x)
+    net.set_conv_path("mma")
+    y_mma = net.forward(x)
+    assert _rel(y_tc, y_mma) <= 1e-2, _rel(y_tc, y_mma)
+    w = net.get_weights()
+    net.set_weights(1.5 * w)
+    y_mma = net.forward(x)
+    for path in PATHS:
+        net.set_conv_path(path)
+        assert _rel(net.forward(x), y_mma) <= 1e-2, path
