@@ -484,18 +484,34 @@ void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, 
     const cuuint32_t box[5] = {8, kTcHX, kTcHY, (cuuint32_t)(Cin / 8), 1};
     encode(&tin, in, 5, dims, strides, box, "activations");
   }
-  // halo buffers: as many as fit (up to four); CTAs per SM as shared and tensor
-  // memory (512 columns per SM) allow
+  // halo buffers: as many as fit (up to four).  CTAs per SM from the kernel's
+  // footprint against the SM's shared memory, registers, threads and tensor
+  // memory (512 columns); the runtime's occupancy query reports one CTA per SM
+  // for this kernel at every shared-memory size, so it is not used.
   const unsigned cols = tc_cols(Cout);
   int nbuf = kTcMaxBuf;
   while (nbuf > 1 && tc_smem(Cin, Cout, nbuf) > kTcSmemMax) --nbuf;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv_tc, kTcThreads, tc_smem(Cin, Cout, nbuf)) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    per_sm = 1;
+  static int sm_smem[kMaxDevices] = {}, sm_regs[kMaxDevices] = {}, blk_resv[kMaxDevices] = {}, k_regs[kMaxDevices] = {};
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!sm_smem[dev]) {
+      cudaFuncAttributes fa{};
+      if (cudaDeviceGetAttribute(&sm_smem[dev], cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sm_regs[dev], cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&blk_resv[dev], cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+          cudaFuncGetAttributes(&fa, k_conv_tc) != cudaSuccess) {
+        cudaGetLastError();
+        sm_smem[dev] = 0;
+        throw std::runtime_error("conv_tc: device or kernel attributes unavailable");
+      }
+      k_regs[dev] = fa.numRegs;
+    }
   }
-  per_sm = std::max(1, std::min(per_sm, (int)(512 / (2 * cols))));
+  const long long warp_regs = ((long long)k_regs[dev] * 32 + 255) / 256 * 256;  // allocated per warp in 256s
+  int per_sm = (int)std::min<long long>(
+      {(long long)sm_smem[dev] / ((long long)tc_smem(Cin, Cout, nbuf) + blk_resv[dev]),
+       (long long)sm_regs[dev] / (warp_regs * (kTcThreads / 32)), 2048 / kTcThreads, 512 / (2 * (long long)cols)});
+  per_sm = std::max(1, per_sm);
   const size_t smem = tc_smem(Cin, Cout, nbuf);
   const long long N = (long long)nx * ny;
   const long long tiles = (long long)((nx + kTcTX - 1) / kTcTX) * ((ny + kTcTY - 1) / kTcTY) * B;

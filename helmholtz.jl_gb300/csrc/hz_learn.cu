@@ -856,15 +856,8 @@ float* CoarseNet::scale_staging(int B) {
 
 // One convolution: on the 5th-generation tensor cores (tcgen05) when that path
 // is selected and the channel counts suit it (w is then the layer's weight
-// image), else the warp-level MMA kernel.  At 16 input and 16 output channels
-// the warp-level kernel stays: there each tcgen05.mma (N = 16) re-reads the
-// 128-row activation operand from shared memory for a sixteenth of the work of
-// a full-width one, and the warp-level kernel was the faster of the two on a
-// 129 x 129 x 32 batch (44.8 against 55.2 us; the layers with 32 or more
-// channels on either side ran 1.1-2.3x faster on tcgen05).
-bool CoarseNet::use_tc(int Cin, int Cout) const {
-  return conv_path_ != 0 && conv_tc_supported(Cin, Cout) && (Cin > 16 || Cout > 16);
-}
+// image), else the warp-level MMA kernel.
+bool CoarseNet::use_tc(int Cin, int Cout) const { return conv_path_ != 0 && conv_tc_supported(Cin, Cout); }
 
 void CoarseNet::conv(Ctx& c, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi, int i_off,
                      int Cout, const bf16* w, bf16* out, float* out32, int ldo, int o_off, int relu, const bf16* mask,

@@ -56,9 +56,9 @@ class CoarseNet {
 
   Ctx ctx;  // own stream and launch table (training, standalone inference)
 
-  // convolution kernels: 0 = warp-level MMA (mma.sync); 1 = 5th-generation
-  // tensor cores (tcgen05.mma, TMEM accumulator, operands staged by TMA) where
-  // the channel counts suit it
+  // convolution kernels: 0 = warp-level MMA (mma.sync); 1 (the default) =
+  // 5th-generation tensor cores (tcgen05.mma, TMEM accumulator, operands staged
+  // by TMA) where the channel counts suit it
   void set_conv_path(int path);
   int conv_path() const { return conv_path_; }
   // true when a tensor-core convolution gave up waiting (device flag; synchronous read)
@@ -102,7 +102,7 @@ class CoarseNet {
   float* bt_ = nullptr;
   int* perm_ = nullptr;
   long long bcap_ = 0;
-  int conv_path_ = 0;
+  int conv_path_ = 1;  // tcgen05 by default
   int* tc_err_ = nullptr;
   __nv_bfloat16* wimg_ = nullptr;  // tensor-core weight images of the forward layers (at woff_)
   bool use_tc(int Cin, int Cout) const;

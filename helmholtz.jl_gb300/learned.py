@@ -142,7 +142,7 @@ class CoarseNet:
     def set_conv_path(self, path: str) -> None:
         """Convolution kernels: "mma" (warp-level mma.sync) or "tcgen05" (5th-generation
         tensor cores with the accumulator in tensor memory and the operands staged
-        by the TMA unit; 2D network only)."""
+        by the TMA unit; the default of a 2D network; the 3D network has "mma" only)."""
         code = {"mma": L.HZ_NET_CONV_WARP_MMA, "tcgen05": L.HZ_NET_CONV_TCGEN05}[path]
         L.check(L.load().hz_net_set_conv_path(self._h, code))
 

@@ -299,11 +299,11 @@ int hz_net3d_gradient(hz_net* net, const float* x, const float* t, int64_t nx, i
 int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int64_t npairs,
                    int32_t batch, int32_t epochs, double lr, int32_t seed, double* loss_hist);
 /* Convolution kernels of a 2D network: HZ_NET_CONV_WARP_MMA (warp-level
- * mma.sync, every layer) or HZ_NET_CONV_TCGEN05 (5th-generation tensor cores,
+ * mma.sync, every layer) or HZ_NET_CONV_TCGEN05 (the default: 5th-generation tensor cores,
  * tcgen05.mma with the accumulator in tensor memory and the operands staged by
- * the TMA unit, for the layers whose channel counts are multiples of 16 with
- * more than 16 on one side; the 16 -> 16 and 8-channel layers keep the
- * warp-level kernel).  The 3D network accepts HZ_NET_CONV_WARP_MMA only. */
+ * the TMA unit, for the layers whose channel counts are multiples of 16; the
+ * 8-channel output layer keeps the warp-level kernel).  The 3D network accepts
+ * HZ_NET_CONV_WARP_MMA only. */
 #define HZ_NET_CONV_WARP_MMA 0
 #define HZ_NET_CONV_TCGEN05 1
 int hz_net_set_conv_path(hz_net* net, int32_t path);

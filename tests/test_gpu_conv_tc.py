@@ -39,12 +39,12 @@ def test_tcgen05_forward_matches_oracle_and_warp_mma(hz, ny, nx, path):
     net = hz.learned.CoarseNet(seed=11)
     w = net.get_weights()
     x, _ = _x(1, 3, ny, nx)
+    net.set_conv_path("mma")
     y_mma = net.forward(x)
     net.set_conv_path(path)
     net.reset_kernel_times()
     y_tc = net.forward(x)
-    # every layer but the 16 -> 16 input layer and the 8-channel output layer
-    assert _launches(net, "net_conv_fwd_tc") == 6
+    assert _launches(net, "net_conv_fwd_tc") == 7  # every layer but the 8-channel output layer
     yo, _ = CN.forward(w, x.astype(np.float64), emulate=True)
     for b in range(x.shape[0]):
         assert _rel(y_tc[b], yo[b]) <= 1e-2, (b, _rel(y_tc[b], yo[b]))
@@ -59,7 +59,7 @@ def test_tcgen05_gradient_matches_oracle(hz, path):
     x, t = _x(2, 2, 25, 33)
     net.reset_kernel_times()
     loss, g = net.gradient(x, t)
-    assert _launches(net, "net_conv_bwd_tc") == 6  # data gradients of layers 1..6 (layer 7's is 16 -> 16)
+    assert _launches(net, "net_conv_bwd_tc") == 7  # data gradients of layers 1..7
     yo, cache = CN.forward(w, x.astype(np.float64), emulate=True)
     lo, go = CN.backward(cache, t.astype(np.float64))
     assert abs(loss - lo) <= 1e-3 * lo
@@ -70,6 +70,11 @@ def test_tcgen05_gradient_matches_oracle(hz, path):
 
 
 def test_tcgen05_path_selection(hz):
+    net = hz.learned.CoarseNet(seed=1)
+    x, _ = _x(4, 1, 17, 17)
+    net.reset_kernel_times()
+    net.forward(x)  # the tensor-core path is the default of a 2D network
+    assert _launches(net, "net_conv_fwd_tc") == 7
     net3 = hz.learned.CoarseNet3D(seed=1)
     for path in PATHS:
         with pytest.raises(hz._lib.HelmgpuError):
