@@ -39,6 +39,7 @@ HZ_OP_SH = 1
 HZ_NOALLOC_MAX_COLS = 4096
 HZ_NET_CONV_WARP_MMA = 0
 HZ_NET_CONV_TCGEN05 = 1
+HZ_NET_CONV_AUTO = 2
 
 
 class hz_problem(C.Structure):

@@ -162,8 +162,9 @@ __device__ __forceinline__ unsigned pack_bf16x2(float a, float b) {
   return *reinterpret_cast<const unsigned*>(&h);
 }
 
+// a tile: 8 x 16 nodes of plane zb = b * nz + z (z = 0 and zb = b on a 2D grid)
 struct TileCoord {
-  int b, x0, y0;
+  int zb, x0, y0;
 };
 
 __device__ __forceinline__ TileCoord tile_coord(long long tile, int tiles_x, int tiles_y) {
@@ -175,31 +176,35 @@ __device__ __forceinline__ TileCoord tile_coord(long long tile, int tiles_x, int
 }  // namespace
 
 // One row of the weight image per thread: row (t * Cin / 8 + p) * Cout + co holds
-// W[co][t][8p .. 8p + 8) of the convolution's weights W [Cout][9][Cin], where
-//   flip = 0: W = w;
-//   flip = 1: W[co][t][ci] = ci < wcout ? w[ci][8 - t][co] : 0 for w [wcout][9][wcin]
+// W[co][t][8p .. 8p + 8) of the convolution's weights W [Cout][taps][Cin], where
+//   flip = 0: W[co][t][ci] = co < wcout ? w[co][t][ci] : 0 for w [wcout][taps][Cin];
+//   flip = 1: W[co][t][ci] = ci < wcout ? w[ci][taps - 1 - t][co] : 0 for w [wcout][taps][wcin]
 //             (wcin = Cout): the transposed, flipped weights of the data gradient.
-__global__ void k_tc_wimage(int Cin, int Cout, const bf16* __restrict__ w, int flip, int wcin, int wcout,
+__global__ void k_tc_wimage(int taps, int Cin, int Cout, const bf16* __restrict__ w, int flip, int wcin, int wcout,
                             bf16* __restrict__ img) {
   const int NP = Cin / 8;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= 9 * NP * Cout) return;
+  if (idx >= taps * NP * Cout) return;
   const int co = idx % Cout, p = (idx / Cout) % NP, t = idx / (Cout * NP);
   alignas(16) bf16 v[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int ci = 8 * p + e;
     if (!flip)
-      v[e] = w[((long long)co * 9 + t) * Cin + ci];
+      v[e] = co < wcout ? w[((long long)co * taps + t) * Cin + ci] : __float2bfloat16_rn(0.f);
     else
-      v[e] = ci < wcout ? w[((long long)ci * 9 + (8 - t)) * wcin + co] : __float2bfloat16_rn(0.f);
+      v[e] = ci < wcout ? w[((long long)ci * taps + (taps - 1 - t)) * wcin + co] : __float2bfloat16_rn(0.f);
   }
   reinterpret_cast<uint4*>(img)[idx] = *reinterpret_cast<const uint4*>(v);
 }
 
 // Shared memory (from a 128-byte aligned base): header (mbarriers and the
-// tensor-memory address), weights (9 * Cin / 8 planes of Cout * 16 bytes), then
-// nbuf halo buffers of Cin / 8 planes each.
+// tensor-memory address), weights (taps * Cin / 8 planes of Cout * 16 bytes),
+// then nbuf halo buffers of nzp z-planes (1 in 2D, 3 in 3D) of Cin / 8 planes
+// each.  taps = 9 (2D) or 27 (3D, tap t = 9 (dz + 1) + 3 (dy + 1) + dx + 1); a
+// 3D halo loads its three z-planes as three TMA boxes, a plane outside the grid
+// from coordinate -1 (all zero fill).  Cst <= Cout output channels are stored
+// (Cout is the MMA's N, a multiple of 16; Cst a multiple of 8).
 // Warp roles (192 threads): warps 0-3 epilogue (warp w reads tensor-memory lanes
 // 32 w .. 32 w + 31, tile rows of the same numbers), warp 4 lane 0 TMA
 // producer, warp 5 lane 0 MMA issuer.  Barriers:
@@ -214,10 +219,11 @@ constexpr int kTcMaxBuf = 4;
 constexpr int kTcThreads = 192;
 
 __global__ void __launch_bounds__(kTcThreads, 2)
-    k_conv_tc(const __grid_constant__ CUtensorMap tin, int i_plane, int nx, int ny, int B, int Cin, int Cout,
-              int nbuf, const bf16* __restrict__ wimg, bf16* __restrict__ out, float* __restrict__ out32, int ldo,
-              int o_off, int relu, const bf16* __restrict__ mask, int ldm, int m_off, int mask_lo, unsigned acc_cols,
-              int* __restrict__ err) {
+    k_conv_tc(const __grid_constant__ CUtensorMap tin, int i_plane, int nx, int ny, int nz, int B, int tiles_x,
+              int tiles_y, int taps, int Cin, int Cout, int Cst, int nbuf, const bf16* __restrict__ wimg,
+              bf16* __restrict__ out,
+              float* __restrict__ out32, int ldo, int o_off, int relu, const bf16* __restrict__ mask, int ldm,
+              int m_off, int mask_lo, unsigned acc_cols, int* __restrict__ err) {
   extern __shared__ unsigned char tc_raw[];
   unsigned char* smem = tc_raw + ((kTcAlign - (smem_u32(tc_raw) & (kTcAlign - 1))) & (kTcAlign - 1));
   const unsigned base = smem_u32(smem);
@@ -228,15 +234,16 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 116);
   const int NP = Cin / 8;                          // 8-channel planes (2 per 16-channel K step)
   const unsigned wplane = (unsigned)Cout * 16;     // bytes of one weight plane
-  const unsigned wbytes = 9u * NP * wplane;
+  const unsigned wbytes = (unsigned)taps * NP * wplane;
   const unsigned bBase = base + kTcHeader;
   const unsigned aBase = bBase + wbytes;           // 128-byte aligned: wplane is a multiple of 256
-  const unsigned tileBytes = (unsigned)NP * kTcPlane;
+  const int nzp = taps == 27 ? 3 : 1;              // z-planes of a halo tile
+  const unsigned zBytes = (unsigned)NP * kTcPlane;  // one z-plane: a multiple of 128 (NP is even)
+  const unsigned tileBytes = (unsigned)nzp * zBytes;
   const unsigned abuf = (tileBytes + kTcAlign - 1) / kTcAlign * kTcAlign;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long N = (long long)nx * ny;
-  const int tiles_x = (nx + kTcTX - 1) / kTcTX, tiles_y = (ny + kTcTY - 1) / kTcTY;
-  const long long tiles = (long long)tiles_x * tiles_y * B;
+  const long long Nxy = (long long)nx * ny;
+  const long long tiles = (long long)tiles_x * tiles_y * nz * B;
   const int n = tiles > blockIdx.x ? (int)((tiles - blockIdx.x + gridDim.x - 1) / gridDim.x) : 0;
 
   if (tid == 0) {
@@ -283,7 +290,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         }
         const TileCoord tc = tile_coord(blockIdx.x + (long long)j * gridDim.x, tiles_x, tiles_y);
         mbar_expect_tx(full0 + 8 * s, tileBytes);
-        tma_load_5d(aBase + (unsigned)s * abuf, &tin, 0, tc.x0 - 1, tc.y0 - 1, i_plane, tc.b, full0 + 8 * s);
+        const int z = tc.zb % nz;
+        for (int q = 0; q < nzp; ++q) {
+          const int dz = nzp == 3 ? q - 1 : 0;
+          const int zc = (z + dz >= 0 && z + dz < nz) ? tc.zb + dz : -1;  // -1: a plane of zeros
+          tma_load_5d(aBase + (unsigned)s * abuf + (unsigned)q * zBytes, &tin, 0, tc.x0 - 1, tc.y0 - 1, i_plane, zc,
+                      full0 + 8 * s);
+        }
       }
       if (*abort_flag) {
         // bounded waits for the copies still in flight: the weights and the last nbuf halo loads
@@ -308,8 +321,9 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         const unsigned acc = tmem + (unsigned)a * acc_cols;
         const unsigned long long a0 = sdesc(aBase + (unsigned)s * abuf, kTcPlane, kTcHX * 16);
         const unsigned long long b0 = sdesc(bBase, wplane, 128);
-        for (int t = 0; t < 9; ++t) {
-          const unsigned tap = (unsigned)(((t / 3) * kTcHX + t % 3) * 16);  // halo row offset of tap t, bytes
+        for (int t = 0; t < taps; ++t) {
+          // z-plane and halo row offset of tap t, bytes
+          const unsigned tap = (unsigned)(t / 9) * zBytes + (unsigned)((((t / 3) % 3) * kTcHX + t % 3) * 16);
           for (int c = 0; c < NP / 2; ++c) {
             const unsigned aoff = (2u * c * kTcPlane + tap) >> 4, boff = ((unsigned)(t * NP + 2 * c) * wplane) >> 4;
             tc_mma(acc, a0 + aoff, b0 + boff, idesc, (t | c) != 0);
@@ -336,19 +350,20 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       const int row = warp * 32 + lane;
       const int x = tc.x0 + row % kTcTX, y = tc.y0 + row / kTcTX;
       const bool in_grid = x < nx && y < ny;
-      const long long orow = (long long)tc.b * N + (long long)y * nx + x;
+      const long long orow = (long long)tc.zb * Nxy + (long long)y * nx + x;
       const unsigned acc = tmem + (unsigned)a * acc_cols + ((unsigned)(warp * 32) << 16);
       for (int cb = 0; cb < Cout; cb += 16) {
         float v[16];
         tc_ld16(acc + (unsigned)cb, v);
-        if (!in_grid) continue;
+        if (!in_grid || cb >= Cst) continue;
+        const bool half = cb + 16 > Cst;  // 8 channels stored from this chunk
         if (relu) {
 #pragma unroll
           for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.f);
         }
         if (mask && cb >= mask_lo) {
           const uint4* mp = reinterpret_cast<const uint4*>(mask + orow * ldm + m_off + cb);
-          const uint4 m2[2] = {mp[0], mp[1]};
+          const uint4 m2[2] = {mp[0], half ? make_uint4(0u, 0u, 0u, 0u) : mp[1]};
           const bf16* mh = reinterpret_cast<const bf16*>(m2);
 #pragma unroll
           for (int k = 0; k < 16; ++k)
@@ -357,13 +372,15 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         if (out32) {
           float4* op = reinterpret_cast<float4*>(out32 + orow * ldo + o_off + cb);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) op[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+          for (int q = 0; q < 4; ++q)
+            if (q < 2 || !half) op[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
         } else {
           uint4* op = reinterpret_cast<uint4*>(out + orow * ldo + o_off + cb);
           op[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
                              pack_bf16x2(v[6], v[7]));
-          op[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
-                             pack_bf16x2(v[14], v[15]));
+          if (!half)
+            op[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
+                               pack_bf16x2(v[14], v[15]));
         }
       }
       // accumulator a read out: one arrival per warp
@@ -382,10 +399,12 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 
 namespace {
 
-size_t tc_weights(int Cin, int Cout) { return (size_t)9 * (Cin / 8) * Cout * 16; }
-size_t tc_halo(int Cin) { return ((size_t)(Cin / 8) * kTcPlane + kTcAlign - 1) / kTcAlign * kTcAlign; }
-size_t tc_smem(int Cin, int Cout, int nbuf) {
-  return (size_t)kTcAlign + kTcHeader + tc_weights(Cin, Cout) + (size_t)nbuf * tc_halo(Cin);
+size_t tc_weights(int taps, int Cin, int Cout) { return (size_t)taps * (Cin / 8) * Cout * 16; }
+size_t tc_halo(int taps, int Cin) {
+  return ((size_t)(taps == 27 ? 3 : 1) * (Cin / 8) * kTcPlane + kTcAlign - 1) / kTcAlign * kTcAlign;
+}
+size_t tc_smem(int taps, int Cin, int Cout, int nbuf) {
+  return (size_t)kTcAlign + kTcHeader + tc_weights(taps, Cin, Cout) + (size_t)nbuf * tc_halo(taps, Cin);
 }
 unsigned tc_cols(int Cout) {
   unsigned cols = 32;
@@ -427,34 +446,37 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 }  // namespace
 
-bool conv_tc_supported(int Cin, int Cout) {
-  return Cin % 16 == 0 && Cin >= 16 && Cin <= 256 && Cout % 16 == 0 && Cout >= 16 && Cout <= 256 &&
-         tc_smem(Cin, Cout, 1) <= kTcSmemMax;
+bool conv_tc_supported(int taps, int Cin, int Cout) {
+  return (taps == 9 || taps == 27) && Cin % 16 == 0 && Cin >= 16 && Cin <= 256 && Cout % 16 == 0 && Cout >= 16 &&
+         Cout <= 256 && tc_smem(taps, Cin, Cout, 1) <= kTcSmemMax;
 }
 
-void conv_tc_weight_image(Ctx& ctx, const char* name, int Cin, int Cout, const bf16* w, int flip, int wcin,
+void conv_tc_weight_image(Ctx& ctx, const char* name, int taps, int Cin, int Cout, const bf16* w, int flip, int wcin,
                           int wcout, bf16* img) {
-  if (!conv_tc_supported(Cin, Cout)) throw std::runtime_error("conv_tc: unsupported channel counts");
-  if (flip && wcin != Cout) throw std::runtime_error("conv_tc: flipped weights of another shape");
+  if (!conv_tc_supported(taps, Cin, Cout)) throw std::runtime_error("conv_tc: unsupported channel counts");
+  if (flip ? (wcin != Cout || wcout > Cin) : wcout > Cout)
+    throw std::runtime_error("conv_tc: weights of another shape");
   if (!aligned16(img)) throw std::runtime_error("conv_tc: weight image not aligned to 16 bytes");
-  const int rows = 9 * (Cin / 8) * Cout;
-  HZ_LAUNCH(ctx, name, (double)rows * 32.0, k_tc_wimage, (unsigned)((rows + 255) / 256), 256, 0, Cin, Cout, w, flip,
-            wcin, wcout, img);
+  const int rows = taps * (Cin / 8) * Cout;
+  HZ_LAUNCH(ctx, name, (double)rows * 32.0, k_tc_wimage, (unsigned)((rows + 255) / 256), 256, 0, taps, Cin, Cout, w,
+            flip, wcin, wcout, img);
 }
 
-void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi, int i_off,
-                    int Cout, const bf16* wimg, bf16* out, float* out32, int ldo, int o_off, int relu, const bf16* mask,
-                    int ldm, int m_off, int mask_lo, int* err) {
-  if (!conv_tc_supported(Cin, Cout)) throw std::runtime_error("conv_tc: unsupported channel counts");
-  if (ldi % 8 || i_off % 8 || i_off + Cin > ldi || !aligned16(in) || !aligned16(wimg))
+void conv_tc_launch(Ctx& ctx, const char* name, const ConvTc& a, int* err) {
+  const int taps = a.nz > 1 ? 27 : 9;
+  const int Cin = a.Cin, Cout = a.Cout;
+  if (a.taps3d != (taps == 27)) throw std::runtime_error("conv_tc: a 3D convolution needs a grid with nz > 1");
+  if (!conv_tc_supported(taps, Cin, Cout)) throw std::runtime_error("conv_tc: unsupported channel counts");
+  if (a.Cst < 8 || a.Cst > Cout || a.Cst % 8) throw std::runtime_error("conv_tc: stored channels out of range");
+  if (a.ldi % 8 || a.i_off % 8 || a.i_off + Cin > a.ldi || !aligned16(a.in) || !aligned16(a.wimg))
     throw std::runtime_error("conv_tc: input or weight layout not aligned to 16 bytes");
-  if (out32 ? (ldo % 4 || o_off % 4 || !aligned16(out32)) : (ldo % 8 || o_off % 8 || !aligned16(out)))
+  if (a.out32 ? (a.ldo % 4 || a.o_off % 4 || !aligned16(a.out32)) : (a.ldo % 8 || a.o_off % 8 || !aligned16(a.out)))
     throw std::runtime_error("conv_tc: output layout not aligned to 16 bytes");
-  if (mask && (mask_lo % 16 || ldm % 8 || m_off % 8 || !aligned16(mask)))
+  if (a.mask && (a.mask_lo % 16 || a.ldm % 8 || a.m_off % 8 || !aligned16(a.mask)))
     throw std::runtime_error("conv_tc: mask layout not aligned to 16 bytes");
-  if (o_off + Cout > ldo || (mask && m_off + Cout > ldm))
+  if (a.o_off + a.Cst > a.ldo || (a.mask && a.m_off + a.Cst > a.ldm))
     throw std::runtime_error("conv_tc: channel offset beyond the row");
-  if (nx < 1 || ny < 1 || B < 1) throw std::runtime_error("conv_tc: empty grid");
+  if (a.nx < 1 || a.ny < 1 || a.nz < 1 || a.B < 1) throw std::runtime_error("conv_tc: empty grid");
 
   static std::mutex mu;
   static bool attr_set[kMaxDevices] = {};
@@ -464,7 +486,7 @@ void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, 
   {
     std::lock_guard<std::mutex> lk(mu);
     if (!attr_set[dev]) {
-      // the largest shared-memory carveout, so that as many CTAs stay resident as the occupancy query reports
+      // the largest shared-memory carveout, so that the CTAs counted below stay resident
       cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemMax);
       if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -476,13 +498,15 @@ void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, 
       attr_set[dev] = true;
     }
   }
-  // activations [B][ny][nx][ldi] as (8 channels, x, y, plane, batch), plane after y
+  // activations [B][nz][ny][nx][ldi] as (8 channels, x, y, plane, z + nz * batch), plane after y
   alignas(64) CUtensorMap tin = {};
   {
-    const cuuint64_t dims[5] = {8, (cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)(ldi / 8), (cuuint64_t)B};
-    const cuuint64_t strides[4] = {(cuuint64_t)ldi * 2, (cuuint64_t)nx * ldi * 2, 16, (cuuint64_t)nx * ny * ldi * 2};
+    const cuuint64_t dims[5] = {8, (cuuint64_t)a.nx, (cuuint64_t)a.ny, (cuuint64_t)(a.ldi / 8),
+                                (cuuint64_t)a.nz * a.B};
+    const cuuint64_t strides[4] = {(cuuint64_t)a.ldi * 2, (cuuint64_t)a.nx * a.ldi * 2, 16,
+                                   (cuuint64_t)a.nx * a.ny * a.ldi * 2};
     const cuuint32_t box[5] = {8, kTcHX, kTcHY, (cuuint32_t)(Cin / 8), 1};
-    encode(&tin, in, 5, dims, strides, box, "activations");
+    encode(&tin, a.in, 5, dims, strides, box, "activations");
   }
   // halo buffers: as many as fit (up to four).  CTAs per SM from the kernel's
   // footprint against the SM's shared memory, registers, threads and tensor
@@ -490,7 +514,8 @@ void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, 
   // for this kernel at every shared-memory size, so it is not used.
   const unsigned cols = tc_cols(Cout);
   int nbuf = kTcMaxBuf;
-  while (nbuf > 1 && tc_smem(Cin, Cout, nbuf) > kTcSmemMax) --nbuf;
+  while (nbuf > 1 && tc_smem(taps, Cin, Cout, nbuf) > kTcSmemMax) --nbuf;
+  const size_t smem = tc_smem(taps, Cin, Cout, nbuf);
   static int sm_smem[kMaxDevices] = {}, sm_regs[kMaxDevices] = {}, blk_resv[kMaxDevices] = {}, k_regs[kMaxDevices] = {};
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -508,18 +533,20 @@ void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, 
     }
   }
   const long long warp_regs = ((long long)k_regs[dev] * 32 + 255) / 256 * 256;  // allocated per warp in 256s
-  int per_sm = (int)std::min<long long>(
-      {(long long)sm_smem[dev] / ((long long)tc_smem(Cin, Cout, nbuf) + blk_resv[dev]),
-       (long long)sm_regs[dev] / (warp_regs * (kTcThreads / 32)), 2048 / kTcThreads, 512 / (2 * (long long)cols)});
+  int per_sm = (int)std::min<long long>({(long long)sm_smem[dev] / ((long long)smem + blk_resv[dev]),
+                                         (long long)sm_regs[dev] / (warp_regs * (kTcThreads / 32)),
+                                         2048 / kTcThreads, 512 / (2 * (long long)cols)});
   per_sm = std::max(1, per_sm);
-  const size_t smem = tc_smem(Cin, Cout, nbuf);
-  const long long N = (long long)nx * ny;
-  const long long tiles = (long long)((nx + kTcTX - 1) / kTcTX) * ((ny + kTcTY - 1) / kTcTY) * B;
-  const int grid = (int)std::max<long long>(1, std::min<long long>(tiles, (long long)kSMs * per_sm));
-  const double bytes = (double)B * N * (Cin * 2.0 + Cout * (out32 ? 4.0 : 2.0)) + 9.0 * Cin * Cout * 2.0;
-  ctx.add_flops(name, 2.0 * 9.0 * Cin * Cout * (double)N * B);
-  HZ_LAUNCH(ctx, name, bytes, k_conv_tc, grid, kTcThreads, smem, tin, i_off / 8, nx, ny, B, Cin, Cout, nbuf, wimg,
-            out, out32, ldo, o_off, relu, mask, ldm, m_off, mask_lo, cols, err);
+  // tiles of 8 x 16 nodes per plane; partial tiles at the grid's edges (TMA zero fill, stores masked)
+  const int tiles_x = (a.nx + kTcTX - 1) / kTcTX, tiles_y = (a.ny + kTcTY - 1) / kTcTY;
+  const long long tiles = (long long)tiles_x * tiles_y * a.nz * a.B;
+  const long long N = (long long)a.nx * a.ny * a.nz;
+  const int grid = (int)std::min<long long>(tiles, (long long)kSMs * per_sm);
+  ctx.add_flops(name, 2.0 * taps * Cin * a.Cst * (double)N * a.B);
+  HZ_LAUNCH(ctx, name, (double)N * a.B * (Cin * 2.0 + a.Cst * (a.out32 ? 4.0 : 2.0)) + (double)taps * Cin * Cout * 2.0,
+            k_conv_tc, grid, kTcThreads, smem, tin, a.i_off / 8, a.nx, a.ny, a.nz, a.B, tiles_x, tiles_y, taps, Cin,
+            Cout, a.Cst, nbuf, a.wimg, a.out, a.out32, a.ldo, a.o_off, a.relu, a.mask, a.ldm, a.m_off, a.mask_lo, cols,
+            err);
 }
 
 }  // namespace hz

@@ -857,15 +857,16 @@ float* CoarseNet::scale_staging(int B) {
 // One convolution: on the 5th-generation tensor cores (tcgen05) when that path
 // is selected and the channel counts suit it (w is then the layer's weight
 // image), else the warp-level MMA kernel.
-bool CoarseNet::use_tc(int Cin, int Cout) const { return conv_path_ != 0 && conv_tc_supported(Cin, Cout); }
+bool CoarseNet::use_tc(int Cin, int Cout) const { return conv_path_ != 0 && conv_tc_supported(9, Cin, Cout); }
 
 void CoarseNet::conv(Ctx& c, const char* name, int nx, int ny, int B, int Cin, const bf16* in, int ldi, int i_off,
                      int Cout, const bf16* w, bf16* out, float* out32, int ldo, int o_off, int relu, const bf16* mask,
                      int ldm, int m_off, int mask_lo) {
   if (use_tc(Cin, Cout)) {
     const char* tc_name = std::strcmp(name, "net_conv_fwd") == 0 ? "net_conv_fwd_tc" : "net_conv_bwd_tc";
-    conv_tc_launch(c, tc_name, nx, ny, B, Cin, in, ldi, i_off, Cout, w, out, out32, ldo, o_off, relu, mask, ldm, m_off,
-                   mask_lo, tc_err_);
+    const ConvTc a{nx, ny, 1, B, false, Cin, in, ldi, i_off, Cout, Cout, w, out, out32, ldo, o_off, relu, mask, ldm,
+                   m_off, mask_lo};
+    conv_tc_launch(c, tc_name, a, tc_err_);
     return;
   }
   conv_launch(c, name, nx, ny, B, Cin, in, ldi, i_off, Cout, w, out, out32, ldo, o_off, relu, mask, ldm, m_off,
@@ -880,12 +881,13 @@ void CoarseNet::refresh_images(Ctx& c) {
   for (int l = 0; l < kLayers; ++l) {
     const auto& L = kSpec[l];
     if (use_tc(L.cinp, L.coutp))
-      conv_tc_weight_image(c, "net_wimage", L.cinp, L.coutp, wbf_ + woff_[l], 0, 0, 0, wimg_ + woff_[l]);
+      conv_tc_weight_image(c, "net_wimage", 9, L.cinp, L.coutp, wbf_ + woff_[l], 0, 0, L.coutp, wimg_ + woff_[l]);
   }
 }
 
 void CoarseNet::set_conv_path(int path) {
-  if (path != 0 && path != 1) throw std::runtime_error("coarse net: conv path must be 0 (warp MMA) or 1 (tcgen05)");
+  if (path < 0 || path > 2)
+    throw std::runtime_error("coarse net: conv path must be 0 (warp MMA), 1 (tcgen05) or 2 (per layer)");
   conv_path_ = path;
   refresh_images(ctx);
   cuda_ok(cudaStreamSynchronize(ctx.stream), "sync");
@@ -951,7 +953,7 @@ void CoarseNet::conv_bwd(Ctx& c, int l, int lev, int B, const bf16* in, int ldi,
   const int K = round16(L.coutp);
   const int tot = L.cinp * 9 * K;
   if (use_tc(K, L.cinp)) {
-    conv_tc_weight_image(c, "net_wflip", K, L.cinp, wbf_ + woff_[l], 1, L.cinp, L.coutp, wt_);
+    conv_tc_weight_image(c, "net_wflip", 9, K, L.cinp, wbf_ + woff_[l], 1, L.cinp, L.coutp, wt_);
   } else {
     HZ_LAUNCH(c, "net_wflip", (double)tot * 4.0, k_wflip, (unsigned)((tot + 255) / 256), 256, 0, L.coutp, L.cinp, K,
               wbf_ + woff_[l], wt_);

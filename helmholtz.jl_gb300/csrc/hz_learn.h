@@ -56,9 +56,10 @@ class CoarseNet {
 
   Ctx ctx;  // own stream and launch table (training, standalone inference)
 
-  // convolution kernels: 0 = warp-level MMA (mma.sync); 1 (the default) =
-  // 5th-generation tensor cores (tcgen05.mma, TMEM accumulator, operands staged
-  // by TMA) where the channel counts suit it
+  // convolution kernels: 0 = warp-level MMA (mma.sync); 1 = 5th-generation
+  // tensor cores (tcgen05.mma, TMEM accumulator, operands staged by TMA) where
+  // the channel counts suit it; 2 (the default) = per layer the faster of the
+  // two: the tensor cores for every such layer of this network
   void set_conv_path(int path);
   int conv_path() const { return conv_path_; }
   // true when a tensor-core convolution gave up waiting (device flag; synchronous read)
@@ -102,26 +103,41 @@ class CoarseNet {
   float* bt_ = nullptr;
   int* perm_ = nullptr;
   long long bcap_ = 0;
-  int conv_path_ = 1;  // tcgen05 by default
+  int conv_path_ = 2;  // per layer the faster path (here: the tensor cores)
   int* tc_err_ = nullptr;
   __nv_bfloat16* wimg_ = nullptr;  // tensor-core weight images of the forward layers (at woff_)
   bool use_tc(int Cin, int Cout) const;
   void refresh_images(Ctx& c);
 };
 
-// 3x3 convolution on the 5th-generation tensor cores (hz_conv_tc.cu): Cin a
-// multiple of 16 in [16, 256], Cout a multiple of 16 in [16, 256]; layouts as
-// for the warp-level kernel except the weights, which come as the image that
-// conv_tc_weight_image writes; *err is set when a wait timed out.
-bool conv_tc_supported(int Cin, int Cout);
-void conv_tc_launch(Ctx& ctx, const char* name, int nx, int ny, int B, int Cin, const __nv_bfloat16* in, int ldi,
-                    int i_off, int Cout, const __nv_bfloat16* wimg, __nv_bfloat16* out, float* out32, int ldo,
-                    int o_off, int relu, const __nv_bfloat16* mask, int ldm, int m_off, int mask_lo, int* err);
-// Weight image of a convolution with Cin inputs and Cout outputs (9 * Cin * Cout
-// BF16 values): flip = 0 from w [Cout][9][Cin]; flip = 1 the data-gradient
-// weights of a layer w [wcout][9][wcin] (wcin = Cout; inputs >= wcout are zero).
-void conv_tc_weight_image(Ctx& ctx, const char* name, int Cin, int Cout, const __nv_bfloat16* w, int flip, int wcin,
-                          int wcout, __nv_bfloat16* img);
+// 3x3 (2D, 9 taps) or 3x3x3 (3D, 27 taps) convolution on the 5th-generation
+// tensor cores (hz_conv_tc.cu): Cin a multiple of 16 in [16, 256], Cout (the MMA
+// width) a multiple of 16 in [16, 256] of which the first Cst (a multiple of 8)
+// are stored; layouts as for the warp-level kernels except the weights, which
+// come as the image that conv_tc_weight_image writes; *err is set when a wait
+// timed out.
+struct ConvTc {
+  int nx, ny, nz, B;  // nz = 1: a 2D grid
+  bool taps3d;        // 27 taps (needs nz > 1) or 9
+  int Cin;
+  const __nv_bfloat16* in;
+  int ldi, i_off;
+  int Cout, Cst;
+  const __nv_bfloat16* wimg;
+  __nv_bfloat16* out;
+  float* out32;
+  int ldo, o_off, relu;
+  const __nv_bfloat16* mask;
+  int ldm, m_off, mask_lo;
+};
+bool conv_tc_supported(int taps, int Cin, int Cout);
+void conv_tc_launch(Ctx& ctx, const char* name, const ConvTc& a, int* err);
+// Weight image of a convolution with taps taps, Cin inputs and Cout outputs
+// (taps * Cin * Cout BF16 values): flip = 0 from w [wcout][taps][Cin] (outputs
+// >= wcout are zero); flip = 1 the data-gradient weights of a layer
+// w [wcout][taps][wcin] (wcin = Cout; inputs >= wcout are zero).
+void conv_tc_weight_image(Ctx& ctx, const char* name, int taps, int Cin, int Cout, const __nv_bfloat16* w, int flip,
+                          int wcin, int wcout, __nv_bfloat16* img);
 
 // 3D convolutional encoder-decoder of the same kind (three grid levels, 8-16-32
 // channels, 3x3x3 convolutions; the layers and their order are in hz_learn3d.cu):
@@ -159,9 +175,19 @@ class CoarseNet3 {
 
   Ctx ctx;
 
+  // convolution kernels, as for the 2D network: 0 = warp-level MMA; 1 =
+  // 5th-generation tensor cores for every layer; 2 (the default) = per layer
+  // the faster of the two, by the waste of the tensor-core tiles on the
+  // layer's grid (tc_waste in hz_learn3d.cu)
+  void set_conv_path(int path);
+  int conv_path() const { return conv_path_; }
+  bool tc_failed();
+
  private:
   void ensure(int nx, int ny, int nz, int B, bool grads);
   void release_acts();
+  bool use_tc(int Cin, int Cout, int lev) const;
+  void refresh_images(Ctx& c);
   void conv_fwd(Ctx& c, int l, int B, const __nv_bfloat16* in, int ldi, int i_off, __nv_bfloat16* out, int ldo,
                 int o_off, int relu, float* out32);
   void conv_bwd(Ctx& c, int l, int B, const __nv_bfloat16* in, int ldi, const __nv_bfloat16* dout, int ldd,
@@ -191,6 +217,11 @@ class CoarseNet3 {
   float* bt_ = nullptr;
   int* perm_ = nullptr;
   long long bcap_ = 0;
+  int conv_path_ = 2;  // per layer the faster path
+  int* tc_err_ = nullptr;
+  __nv_bfloat16* wimg_ = nullptr;  // tensor-core weight images of the forward layers (at imgoff_)
+  long long imgoff_[kLayers] = {};
+  long long imgtotal_ = 0;
 };
 
 // Kernels the 2D and 3D networks share (hz_learn.cu): input assembly into

@@ -554,6 +554,12 @@ CoarseNet3::CoarseNet3(unsigned seed) {
     off += (long long)kSpec3[l].coutp * kTaps3 * kSpec3[l].cinp;
   }
   wtotal_ = off;
+  for (int l = 0; l < kLayers; ++l) {
+    imgoff_[l] = imgtotal_;
+    imgtotal_ += (long long)round16(kSpec3[l].coutp) * kTaps3 * kSpec3[l].cinp;
+  }
+  dalloc3(&tc_err_, sizeof(int));
+  cuda_ok3(cudaMemset(tc_err_, 0, sizeof(int)), "tensor-core status");
   dalloc3(&w32_, off * 4);
   dalloc3(&wbf_, off * 2);
   dalloc3(&g32_, off * 4);
@@ -573,6 +579,8 @@ CoarseNet3::CoarseNet3(unsigned seed) {
 
 CoarseNet3::~CoarseNet3() {
   release_acts();
+  dfree3(tc_err_);
+  dfree3(wimg_);
   dfree3(w32_);
   dfree3(wbf_);
   dfree3(g32_);
@@ -622,6 +630,7 @@ void CoarseNet3::set_weights(const float* host) {
   step_ = 0;
   k_f2bf<<<256, 256, 0, ctx.stream>>>(wtotal_, w32_, wbf_);
   cuda_ok3(cudaGetLastError(), "weights to bf16");
+  refresh_images(ctx);
   cuda_ok3(cudaStreamSynchronize(ctx.stream), "sync");
 }
 
@@ -795,11 +804,64 @@ float* CoarseNet3::scale_staging(int B) {
   return scale_;
 }
 
+// The tensor-core path: N = Cout rounded up to 16 (the 8-channel layers compute
+// 8 zero channels more and store 8), the weights as images (hz_conv_tc.cu), tiles
+// of 8 x 16 nodes per z-plane.  tc_waste: the MMA work over the useful work on a
+// grid level (partial tiles times the padding of N).  On the 2^k + 1-node grids
+// of this network it is 2.7-4.4 on the 17^3 and 33^3 levels of the forward
+// (measured on a 33^3 x 32 batch: 200, 505 and 201 us on tcgen05 against 192,
+// 334 and 190 us with the warp-level kernel on the three 33^3 layers, 47 and
+// 135 against 45 and 105 us on the two 17^3 layers) and 1.4-2.7 on 65^3; the
+// default path takes the tensor cores where the waste is at most 2.5.
+static double tc_waste(const int* gd, int Cout) {
+  const double tx = (gd[0] + 7) / 8 * 8.0, ty = (gd[1] + 15) / 16 * 16.0;
+  return tx * ty / ((double)gd[0] * gd[1]) * round16(Cout) / (double)Cout;
+}
+
+bool CoarseNet3::use_tc(int Cin, int Cout, int lev) const {
+  if (conv_path_ == 0 || !conv_tc_supported(kTaps3, Cin, round16(Cout))) return false;
+  return conv_path_ == 1 || lev < 0 || tc_waste(g_[lev], Cout) <= 2.5;
+}
+
+// Weight images of the forward layers, rewritten on c's stream whenever the BF16
+// weights change.
+void CoarseNet3::refresh_images(Ctx& c) {
+  if (conv_path_ == 0) return;
+  if (!wimg_) dalloc3(&wimg_, imgtotal_ * 2);
+  for (int l = 0; l < kLayers; ++l) {
+    const auto& L = kSpec3[l];
+    if (use_tc(L.cinp, L.coutp, -1))  // every layer the path may run on the tensor cores
+      conv_tc_weight_image(c, "net3_wimage", kTaps3, L.cinp, round16(L.coutp), wbf_ + woff_[l], 0, 0, L.coutp,
+                           wimg_ + imgoff_[l]);
+  }
+}
+
+void CoarseNet3::set_conv_path(int path) {
+  if (path < 0 || path > 2)
+    throw std::runtime_error("coarse net 3D: conv path must be 0 (warp MMA), 1 (tcgen05) or 2 (per layer)");
+  conv_path_ = path;
+  refresh_images(ctx);
+  cuda_ok3(cudaStreamSynchronize(ctx.stream), "sync");
+}
+
+bool CoarseNet3::tc_failed() {
+  int e = 0;
+  cuda_ok3(cudaMemcpy(&e, tc_err_, sizeof(int), cudaMemcpyDeviceToHost), "tensor-core status");
+  return e != 0;
+}
+
 void CoarseNet3::conv_fwd(Ctx& c, int l, int B, const bf16* in, int ldi, int i_off, bf16* out, int ldo, int o_off,
                           int relu, float* out32) {
   const auto& L = kSpec3[l];
-  conv3_launch(c, "net3_conv_fwd", g_[L.lev], B, L.cinp, in, ldi, i_off, L.coutp, wbf_ + woff_[l], out, out32, ldo,
-               o_off, relu, nullptr, 0, 0, 0);
+  const int* gd = g_[L.lev];
+  if (use_tc(L.cinp, L.coutp, L.lev)) {
+    const ConvTc a{gd[0], gd[1], gd[2], B, true, L.cinp, in, ldi, i_off, round16(L.coutp), L.coutp,
+                   wimg_ + imgoff_[l], out, out32, ldo, o_off, relu, nullptr, 0, 0, 0};
+    conv_tc_launch(c, "net3_conv_fwd_tc", a, tc_err_);
+    return;
+  }
+  conv3_launch(c, "net3_conv_fwd", gd, B, L.cinp, in, ldi, i_off, L.coutp, wbf_ + woff_[l], out, out32, ldo, o_off,
+               relu, nullptr, 0, 0, 0);
 }
 
 void CoarseNet3::forward(Ctx& c, const float* x4, int nx, int ny, int nz, int B, bool train) {
@@ -845,6 +907,13 @@ void CoarseNet3::conv_bwd(Ctx& c, int l, int B, const bf16* in, int ldi, const b
   if (!din) return;
   const int K = round16(L.coutp);
   const int tot = L.cinp * kTaps3 * K;
+  if (use_tc(K, L.cinp, L.lev)) {
+    conv_tc_weight_image(c, "net3_wflip", kTaps3, K, L.cinp, wbf_ + woff_[l], 1, L.cinp, L.coutp, wt_);
+    const ConvTc a{gd[0], gd[1], gd[2], B, true, K, dout, ldd, d_off, L.cinp, L.cinp, wt_, din, nullptr, ldn, n_off,
+                   0, mask, ldm, 0, mask_lo};
+    conv_tc_launch(c, "net3_conv_bwd_tc", a, tc_err_);
+    return;
+  }
   HZ_LAUNCH(c, "net3_wflip", (double)tot * 4.0, k_wflip3, (unsigned)((tot + 255) / 256), 256, 0, L.coutp, L.cinp, K,
             wbf_ + woff_[l], wt_);
   conv3_launch(c, "net3_conv_bwd", gd, B, K, dout, ldd, d_off, L.cinp, wt_, din, nullptr, ldn, n_off, 0, mask, ldm,
@@ -878,6 +947,7 @@ double CoarseNet3::backward(Ctx& c, const float* t, int nx, int ny, int nz, int 
   cuda_ok3(cudaMemcpyAsync(&l, loss_, 8, cudaMemcpyDeviceToHost, c.stream), "loss");
   cuda_ok3(cudaStreamSynchronize(c.stream), "sync");
   c.resolve();
+  if (conv_path_ != 0 && tc_failed()) throw std::runtime_error("coarse net 3D: tensor-core convolution timed out");
   return l;
 }
 
@@ -887,6 +957,7 @@ void CoarseNet3::adam(Ctx& c, double lr) {
   const float c1 = 1.f - std::pow(b1, (float)step_), c2 = 1.f - std::pow(b2, (float)step_);
   HZ_LAUNCH(c, "net3_adam", (double)wtotal_ * 22.0, k_adam, 304, 256, 0, wtotal_, w32_, g32_, m_, v_, wbf_, (float)lr,
             b1, b2, 1e-8f, c1, c2);
+  refresh_images(c);
 }
 
 void CoarseNet3::train(Ctx& c, const float* x, const float* t, int nx, int ny, int nz, long long nsamples, int batch,

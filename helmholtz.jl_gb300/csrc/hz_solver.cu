@@ -1793,6 +1793,10 @@ int hz_solve(hz_handle* h, const double* B, double* X, int64_t n, int32_t nrhs, 
     int outer = (h->opt.krylov == HZ_KRYLOV_BICGSTAB) ? bicgstab(h, transpose, nrhs) : fgmres(h, transpose, nrhs);
     copy_out(h, h->Xd.as<double2>(), X, n, nrhs, mem);
     sync(h);
+    // a tensor-core convolution of the attached network that gave up waiting makes the solve invalid
+    if ((h->net && h->net->conv_path() != HZ_NET_CONV_WARP_MMA && h->net->tc_failed()) ||
+        (h->net3 && h->net3->conv_path() != HZ_NET_CONV_WARP_MMA && h->net3->tc_failed()))
+      fail(HZ_ERR_CUDA, "tensor-core convolution of the network timed out");
     auto t2 = clk::now();
     h->solve_time += secs(t1, t2);
     int nconv = 0, maxit = 0;
@@ -2129,7 +2133,8 @@ void net_forward(hz_net* net, const float* x, float* y, int64_t nx, int64_t ny, 
      "copy y");
   ck(cudaStreamSynchronize(cx.stream), "sync");
   cx.resolve();
-  if (net->net && net->net->conv_path() != HZ_NET_CONV_WARP_MMA && net->net->tc_failed())
+  if ((net->net && net->net->conv_path() != HZ_NET_CONV_WARP_MMA && net->net->tc_failed()) ||
+      (net->net3 && net->net3->conv_path() != HZ_NET_CONV_WARP_MMA && net->net3->tc_failed()))
     fail(HZ_ERR_CUDA, "tensor-core convolution timed out");
 }
 
@@ -2276,13 +2281,15 @@ int hz_net_file_info(const char* path, int64_t* nparams, int64_t* adam_step) {
 int hz_net_set_conv_path(hz_net* net, int32_t path) {
   if (!net) return HZ_ERR_ARG;
   return guarded(nullptr, [&] {
-    if (path != HZ_NET_CONV_WARP_MMA && path != HZ_NET_CONV_TCGEN05)
-      fail(HZ_ERR_ARG, "conv path must be HZ_NET_CONV_WARP_MMA or HZ_NET_CONV_TCGEN05");
-    if (net->net3 && path != HZ_NET_CONV_WARP_MMA) fail(HZ_ERR_ARG, "the 3D network has the warp-level MMA path only");
+    if (path != HZ_NET_CONV_WARP_MMA && path != HZ_NET_CONV_TCGEN05 && path != HZ_NET_CONV_AUTO)
+      fail(HZ_ERR_ARG, "conv path must be HZ_NET_CONV_WARP_MMA, HZ_NET_CONV_TCGEN05 or HZ_NET_CONV_AUTO");
     ck(cudaSetDevice(net->dev), "cudaSetDevice");
     if (net->net) {
       cudaStreamSynchronize(net->net->ctx.stream);
       net->net->set_conv_path(path);
+    } else if (net->net3) {
+      cudaStreamSynchronize(net->net3->ctx.stream);
+      net->net3->set_conv_path(path);
     }
   });
 }

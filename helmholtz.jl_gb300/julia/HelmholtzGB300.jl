@@ -374,7 +374,7 @@ function CoarseNet3D(seed::Integer = 0, device::Integer = 0)
     return net
 end
 netDim(net::CoarseNet) = Int(ccall((:hz_net_dim, libhelmgpu), Cint, (Ptr{Cvoid},), net.ptr))
-# convolution kernels of a 2D network: 0 warp-level MMA, 1 tcgen05 tensor cores (the default)
+# convolution kernels of a network: 0 warp-level MMA, 1 tcgen05 tensor cores, 2 per layer the faster (the default)
 setNetConvPath!(net::CoarseNet, path::Integer) =
     check(ccall((:hz_net_set_conv_path, libhelmgpu), Cint, (Ptr{Cvoid}, Int32), net.ptr, Int32(path)))
 function netWeights3D(net::CoarseNet)

@@ -140,10 +140,11 @@ class CoarseNet:
         L.check(L.load().hz_net_load(self._h, str(path).encode()))
 
     def set_conv_path(self, path: str) -> None:
-        """Convolution kernels: "mma" (warp-level mma.sync) or "tcgen05" (5th-generation
+        """Convolution kernels: "mma" (warp-level mma.sync), "tcgen05" (5th-generation
         tensor cores with the accumulator in tensor memory and the operands staged
-        by the TMA unit; the default of a 2D network; the 3D network has "mma" only)."""
-        code = {"mma": L.HZ_NET_CONV_WARP_MMA, "tcgen05": L.HZ_NET_CONV_TCGEN05}[path]
+        by the TMA unit, every layer they support) or "auto" (the default: per layer
+        the faster of the two)."""
+        code = {"mma": L.HZ_NET_CONV_WARP_MMA, "tcgen05": L.HZ_NET_CONV_TCGEN05, "auto": L.HZ_NET_CONV_AUTO}[path]
         L.check(L.load().hz_net_set_conv_path(self._h, code))
 
     def set_profile(self, on: bool) -> None:

@@ -298,14 +298,18 @@ int hz_net3d_gradient(hz_net* net, const float* x, const float* t, int64_t nx, i
                       int32_t mem, double* loss, float* grad);
 int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int64_t ny, int64_t nz, int64_t npairs,
                    int32_t batch, int32_t epochs, double lr, int32_t seed, double* loss_hist);
-/* Convolution kernels of a 2D network: HZ_NET_CONV_WARP_MMA (warp-level
- * mma.sync, every layer) or HZ_NET_CONV_TCGEN05 (the default: 5th-generation tensor cores,
- * tcgen05.mma with the accumulator in tensor memory and the operands staged by
- * the TMA unit, for the layers whose channel counts are multiples of 16; the
- * 8-channel output layer keeps the warp-level kernel).  The 3D network accepts
- * HZ_NET_CONV_WARP_MMA only. */
+/* Convolution kernels of a network: HZ_NET_CONV_WARP_MMA (warp-level mma.sync,
+ * every layer), HZ_NET_CONV_TCGEN05 (5th-generation tensor cores, tcgen05.mma
+ * with the accumulator in tensor memory and the operands staged by the TMA
+ * unit; 2D: the layers whose channel counts are multiples of 16, the 8-channel
+ * output layer keeps the warp-level kernel; 3D: every layer, the 8-channel
+ * layers computing 16 output channels and storing 8) or HZ_NET_CONV_AUTO (the
+ * default: per layer the faster of the two; the 2D network's tensor-core
+ * layers all, the 3D network's where its 8 x 16-node tiles waste at most 2.5x
+ * the work on that layer's grid). */
 #define HZ_NET_CONV_WARP_MMA 0
 #define HZ_NET_CONV_TCGEN05 1
+#define HZ_NET_CONV_AUTO 2
 int hz_net_set_conv_path(hz_net* net, int32_t path);
 /* Use the network for the coarse-grid correction of multigrid level `level`
  * (1 .. levels-1; a network of the problem's dimension; FGMRES only: the

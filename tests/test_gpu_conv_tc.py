@@ -1,4 +1,4 @@
-"""GPU parity of the 2D network's convolutions on the 5th-generation tensor
+"""GPU parity of the networks' convolutions on the 5th-generation tensor
 cores (tcgen05.mma with the accumulator in tensor memory, operands staged by
 the TMA unit) against the CPU oracle (oracle/coarse_net.py,
 BF16 rounding emulated) and against the warp-level MMA path: forward output to
@@ -45,6 +45,7 @@ def test_tcgen05_forward_matches_oracle_and_warp_mma(hz, ny, nx, path):
     net.reset_kernel_times()
     y_tc = net.forward(x)
     assert _launches(net, "net_conv_fwd_tc") == 7  # every layer but the 8-channel output layer
+    assert _launches(net, "net_conv_fwd") == 1
     yo, _ = CN.forward(w, x.astype(np.float64), emulate=True)
     for b in range(x.shape[0]):
         assert _rel(y_tc[b], yo[b]) <= 1e-2, (b, _rel(y_tc[b], yo[b]))
@@ -60,6 +61,7 @@ def test_tcgen05_gradient_matches_oracle(hz, path):
     net.reset_kernel_times()
     loss, g = net.gradient(x, t)
     assert _launches(net, "net_conv_bwd_tc") == 7  # data gradients of layers 1..7
+    assert _launches(net, "net_conv_bwd") == 0
     yo, cache = CN.forward(w, x.astype(np.float64), emulate=True)
     lo, go = CN.backward(cache, t.astype(np.float64))
     assert abs(loss - lo) <= 1e-3 * lo
@@ -73,13 +75,57 @@ def test_tcgen05_path_selection(hz):
     net = hz.learned.CoarseNet(seed=1)
     x, _ = _x(4, 1, 17, 17)
     net.reset_kernel_times()
-    net.forward(x)  # the tensor-core path is the default of a 2D network
-    assert _launches(net, "net_conv_fwd_tc") == 7
-    net3 = hz.learned.CoarseNet3D(seed=1)
-    for path in PATHS:
-        with pytest.raises(hz._lib.HelmgpuError):
-            net3.set_conv_path(path)
-    net3.set_conv_path("mma")
+    net.forward(x)  # the default path: the tensor cores for every 2D layer they support
+    assert _launches(net, "net_conv_fwd_tc") == 7 and _launches(net, "net_conv_fwd") == 1
+    with pytest.raises(KeyError):
+        net.set_conv_path("wmma")
+
+
+def _x3(seed, B, nz, ny, nx):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(B, nz, ny, nx, 4)).astype(np.float32)
+    x[..., 2] = rng.uniform(0.5, 6.0, size=(B, nz, ny, nx))
+    x[..., 3] = rng.uniform(0.01, 0.9, size=(B, nz, ny, nx))
+    t = rng.normal(size=(B, nz, ny, nx, 2)).astype(np.float32)
+    return x, t
+
+
+@pytest.mark.parametrize("nz,ny,nx", [(9, 33, 17), (13, 21, 9)])
+def test_tcgen05_3d_forward_matches_oracle_and_warp_mma(hz, nz, ny, nx):
+    """3x3x3 convolutions: three z-planes per halo tile (the planes outside the grid
+    zero-filled by the TMA unit), the 8-channel layers computed 16 wide."""
+    import coarse_net3d as CN3
+    net = hz.learned.CoarseNet3D(seed=11)
+    w = net.get_weights()
+    x, _ = _x3(1, 2, nz, ny, nx)
+    net.set_conv_path("mma")
+    y_mma = net.forward(x)
+    net.set_conv_path("tcgen05")
+    net.reset_kernel_times()
+    y_tc = net.forward(x)
+    assert _launches(net, "net3_conv_fwd_tc") == 6 and _launches(net, "net3_conv_fwd") == 0  # every layer
+    yo, _ = CN3.forward(w, x.astype(np.float64), emulate=True)
+    for b in range(x.shape[0]):
+        assert _rel(y_tc[b], yo[b]) <= 1e-2, (b, _rel(y_tc[b], yo[b]))
+        assert _rel(y_tc[b], y_mma[b]) <= 1e-2, (b, _rel(y_tc[b], y_mma[b]))
+
+
+def test_tcgen05_3d_gradient_matches_oracle(hz):
+    import coarse_net3d as CN3
+    net = hz.learned.CoarseNet3D(seed=5)
+    net.set_conv_path("tcgen05")
+    w = net.get_weights()
+    x, t = _x3(2, 2, 9, 33, 17)
+    net.reset_kernel_times()
+    loss, g = net.gradient(x, t)
+    assert _launches(net, "net3_conv_bwd_tc") == 5 and _launches(net, "net3_conv_bwd") == 0  # layers 1..5
+    yo, cache = CN3.forward(w, x.astype(np.float64), emulate=True)
+    lo, go = CN3.backward(cache, t.astype(np.float64))
+    assert abs(loss - lo) <= 1e-3 * lo
+    offs = np.cumsum([0] + [27 * a * b for a, b in CN3.LAYERS])
+    for k in range(len(CN3.LAYERS)):
+        a, b = g[offs[k]:offs[k + 1]], go[offs[k]:offs[k + 1]]
+        assert _rel(a, b) <= 3e-2, (k, _rel(a, b))
 
 
 def test_tcgen05_weight_images_follow_training(hz):
@@ -102,3 +148,18 @@ def test_tcgen05_weight_images_follow_training(hz):
     for path in PATHS:
         net.set_conv_path(path)
         assert _rel(net.forward(x), y_mma) <= 1e-2, path
+
+
+def test_auto_path_3d_picks_per_layer(hz):
+    """The default path runs a 3D layer on the tensor cores where the 8 x 16-node
+    tiles waste at most 2.5x the work on its grid: on a 65^3-node batch the
+    16- and 32-channel layers of the two finer levels, the rest warp-level."""
+    net = hz.learned.CoarseNet3D(seed=3)
+    x, _ = _x3(6, 1, 65, 65, 65)
+    net.reset_kernel_times()
+    y_auto = net.forward(x)
+    tc, mma = _launches(net, "net3_conv_fwd_tc"), _launches(net, "net3_conv_fwd")
+    assert tc >= 1 and mma >= 1 and tc + mma == 6, (tc, mma)
+    net.set_conv_path("mma")
+    y_mma = net.forward(x)
+    assert _rel(y_auto, y_mma) <= 1e-2
