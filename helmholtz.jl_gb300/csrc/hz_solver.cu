@@ -2360,15 +2360,16 @@ namespace {
 // two FGMRES steps in the K-cycle) and takes sweeps - 1 restarted two-step
 // FGMRES corrections e += K(r - A e) preconditioned by the level's cycle, in
 // FP64.  Each minimises the residual over its space, so the residual never grows.
+// On the coarsest level the cycle is the band LU: its solve is the target.
 void collect_targets_iterative(hz_handle* h, Hierarchy& H, int level, int sweeps, long long cnt, float* x_out,
                                float* t_out, double* plain_err, double* target_relres) {
   const Grid g = level_grid(h, level);
   const long long N = g.N;
   const int R = h->rcap;
   const int last = (int)H.lv.size() - 1;
-  if (level >= last) fail(HZ_ERR_ARG, "pairs need a level above the coarsest");
+  if (level >= last) sweeps = 1;
   Level& Lv = *H.lv[level];
-  if (!Lv.kv.p) {  // the two-step corrections' vectors (allocated by the K-cycle itself otherwise)
+  if (sweeps > 1 && !Lv.kv.p) {  // the two-step corrections' vectors (allocated by the K-cycle itself otherwise)
     Lv.kv.alloc((size_t)5 * R * Lv.ld * sizeof(double2));
     Lv.ks.alloc((size_t)R * 8 * 16);
     Lv.kp.alloc((size_t)R * 3 * kcycle_nblk(Lv.g.N) * 16);

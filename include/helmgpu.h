@@ -331,7 +331,8 @@ int hz_learned_stats(const hz_handle* h, int64_t* net_calls, int32_t* fallbacks)
  * coarse level is out of reach) from one cycle on that level followed by
  * sweeps - 1 restarted FP64 two-step
  * FGMRES corrections e += K(r - A e) preconditioned by the level's cycle (which
- * never raise the residual).  In 3D the grid is nx x ny x nz and plain_err
+ * never raise the residual); on the coarsest level the cycle is the band LU and
+ * its solve is the target.  In 3D the grid is nx x ny x nz and plain_err
  * compares one cycle on that level (what the network stands for) with the target.
  * x_out [max_pairs][N][4] and t_out [max_pairs][N][2] are DEVICE FP32 arrays in
  * the layout above; plain_err (host, may be NULL) gets ||e1 - e|| / ||e|| of one

@@ -157,3 +157,14 @@ def test_learned_3d_solve_beats_plain_cycle(hz, O, trained3):
             assert calls > 0
     print(f"3D held-out iterations: {iters}")
     assert iters["learned"] < iters["plain"], iters
+
+
+def test_pairs_on_the_coarsest_level(hz):
+    """On the coarsest level the cycle is the band LU: its solve is the target
+    (residual at rounding level) and one plain cycle equals it."""
+    P = PB.layered((32, 32, 32), seed=5, pad=4, ellipsoid=True)
+    S = _solver(hz, P, "fp64", levels=4)  # 33^3, 17^3, 9^3, 5^3
+    d = hz.learned.collect_pairs(S, _sources3(P, 2, 5, 4), level=3, sweeps=5, max_pairs=16)
+    assert d["x"].shape[1:] == (5, 5, 5, 4)
+    assert d["target_relres"] < 1e-10, d["target_relres"]
+    assert np.max(d["plain_err"]) < 1e-12
