@@ -1,10 +1,11 @@
-// 3x3 convolution of the 2D learned-correction network on the 5th-generation
-// tensor cores (tcgen05.mma, accumulator in tensor memory), operands staged by
-// the tensor memory accelerator (cp.async.bulk.tensor).
+// 3x3 (2D) and 3x3x3 (3D) convolutions of the learned-correction networks on the
+// 5th-generation tensor cores (tcgen05.mma, accumulator in tensor memory),
+// operands staged by the tensor memory accelerator (cp.async.bulk.tensor).
 //
 // Implicit GEMM: D[node][co] = sum_t sum_ci in[node + off_t][ci] * w[co][t][ci],
-// M = 128 nodes per tile (8 along x by 16 along y), N = Cout (16..256, a
-// multiple of 16), K = 9 taps x Cin (Cin a multiple of 16).
+// M = 128 nodes per tile (8 along x by 16 along y of one z-plane), N = Cout
+// (16..256, a multiple of 16; the first Cst <= Cout channels are stored), K =
+// taps x Cin (9 or 27 taps, Cin a multiple of 16).
 //
 // Shared memory holds the operands in the canonical K-major layout without
 // swizzle: a "core matrix" is 8 rows of 16 bytes (8 BF16 channels) stored
@@ -17,22 +18,26 @@
 //      are SBO = 10 rows = 160 bytes apart; the two 8-channel halves of a
 //      16-channel K step are LBO = one plane = 2880 bytes apart.  Tap (dx, dy)
 //      only moves the start address, by ((dy + 1) * 10 + dx + 1) rows, so the
-//      nine taps read one staged tile.
+//      nine taps read one staged tile.  In 3D the halo tile holds three such
+//      z-planes (z - 1, z, z + 1) one after the other and tap dz moves the
+//      start address by whole z-planes.
 //   B: all the layer's weights, staged once per CTA: for tap t and 8-channel
 //      group p, one plane of Cout rows (row co = w[co][t][8p .. 8p + 8));
 //      SBO = 8 rows = 128 bytes (the next 8 output channels), LBO = one plane.
 // The weights reach shared memory as one image in exactly the layout of B
 // (k_tc_wimage writes it once per weight update, or per backward convolution
 // for the flipped weights), copied by the TMA unit's bulk engine
-// (cp.async.bulk, 1-D, 32 KiB per copy).  The halo tile is one TMA tensor
-// load: the activation tensor [B][N][ldi] is described to the TMA unit as the
-// 5-D tensor (8 channels, x, y, plane, batch) with the plane dimension (stride
-// 16 bytes) ordered after y, so that one box of (8, 10, 18, Cin / 8, 1) lands
-// plane after plane exactly as A above; halo nodes outside the grid are filled
-// with zeros by the TMA unit, which is the zero padding of the convolution.
+// (cp.async.bulk, 1-D, 32 KiB per copy).  A z-plane of the halo tile is one TMA
+// tensor load: the activation tensor [B][N][ldi] is described to the TMA unit
+// as the 5-D tensor (8 channels, x, y, plane, z + nz * batch) with the plane
+// dimension (stride 16 bytes) ordered after y, so that one box of
+// (8, 10, 18, Cin / 8, 1) lands plane after plane exactly as A above; halo nodes
+// outside the grid are filled with zeros by the TMA unit, which is the zero
+// padding of the convolution (a z-plane outside the grid is loaded from
+// coordinate -1: all zeros).
 //
 // Warp-specialised persistent CTAs: a producer thread keeps up to four halo
-// buffers in flight, an MMA thread issues the 9 x Cin / 16 MMAs of a tile into
+// buffers in flight, an MMA thread issues the taps x Cin / 16 MMAs of a tile into
 // one of two tensor-memory accumulators as soon as its halo has landed and the
 // accumulator is free, and four epilogue warps read the other accumulator out
 // (tcgen05.ld, ReLU / mask, BF16 or FP32 stores); the roles hand buffers to one
