@@ -224,11 +224,11 @@ constexpr int kTcMaxBuf = 4;
 constexpr int kTcThreads = 192;
 
 __global__ void __launch_bounds__(kTcThreads, 2)
-    k_conv_tc(const __grid_constant__ CUtensorMap tin, int i_plane, int nx, int ny, int nz, int B, int tiles_x,
-              int tiles_y, int taps, int Cin, int Cout, int Cst, int nbuf, const bf16* __restrict__ wimg,
-              bf16* __restrict__ out,
-              float* __restrict__ out32, int ldo, int o_off, int relu, const bf16* __restrict__ mask, int ldm,
-              int m_off, int mask_lo, unsigned acc_cols, int* __restrict__ err) {
+    k_conv_tc(const __grid_constant__ CUtensorMap tin, int i_off, int nx, int ny, int nz, int B, int zl, int y0z,
+              int tiles_x, int tiles_l, int taps, int Cin, int Cout, int Cst, int nbuf, const bf16* __restrict__ wimg,
+              bf16* __restrict__ out, float* __restrict__ out32, int ldo, int o_off, int relu,
+              const bf16* __restrict__ mask, int ldm, int m_off, int mask_lo, unsigned acc_cols,
+              int* __restrict__ err) {
   extern __shared__ unsigned char tc_raw[];
   unsigned char* smem = tc_raw + ((kTcAlign - (smem_u32(tc_raw) & (kTcAlign - 1))) & (kTcAlign - 1));
   const unsigned base = smem_u32(smem);
@@ -242,13 +242,17 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const unsigned wbytes = (unsigned)taps * NP * wplane;
   const unsigned bBase = base + kTcHeader;
   const unsigned aBase = bBase + wbytes;           // 128-byte aligned: wplane is a multiple of 256
-  const int nzp = taps == 27 ? 3 : 1;              // z-planes of a halo tile
-  const unsigned zBytes = (unsigned)NP * kTcPlane;  // one z-plane: a multiple of 128 (NP is even)
-  const unsigned tileBytes = (unsigned)nzp * zBytes;
-  const unsigned abuf = (tileBytes + kTcAlign - 1) / kTcAlign * kTcAlign;
+  const int nzp = taps == 27 ? 3 : 1;              // z-planes (y-planes with z-lines) of a halo tile
+  // one 8-channel plane of a halo plane: 2880 bytes written by one box (y-lines), or
+  // 2944 (128-byte aligned destinations of the per-plane boxes of the z-lines)
+  const unsigned pitch = zl ? (unsigned)(kTcPlane + 64) : (unsigned)kTcPlane;
+  const unsigned zBytes = (unsigned)NP * pitch;     // a multiple of 128 (NP is even)
+  const unsigned tileBytes = (unsigned)nzp * NP * kTcPlane;
+  const unsigned abuf = (nzp * zBytes + kTcAlign - 1) / kTcAlign * kTcAlign;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long Nxy = (long long)nx * ny;
-  const long long tiles = (long long)tiles_x * tiles_y * nz * B;
+  const int nyz = ny - y0z;                          // y-rows of the z-line tiles
+  const long long tiles = (long long)tiles_x * tiles_l * (zl ? (long long)nyz * B : (long long)nz * B);
   const int n = tiles > blockIdx.x ? (int)((tiles - blockIdx.x + gridDim.x - 1) / gridDim.x) : 0;
 
   if (tid == 0) {
@@ -293,14 +297,25 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           give_up();
           break;
         }
-        const TileCoord tc = tile_coord(blockIdx.x + (long long)j * gridDim.x, tiles_x, tiles_y);
+        const TileCoord tc = tile_coord(blockIdx.x + (long long)j * gridDim.x, tiles_x, tiles_l);
         mbar_expect_tx(full0 + 8 * s, tileBytes);
-        const int z = tc.zb % nz;
-        for (int q = 0; q < nzp; ++q) {
-          const int dz = nzp == 3 ? q - 1 : 0;
-          const int zc = (z + dz >= 0 && z + dz < nz) ? tc.zb + dz : -1;  // -1: a plane of zeros
-          tma_load_5d(aBase + (unsigned)s * abuf + (unsigned)q * zBytes, &tin, 0, tc.x0 - 1, tc.y0 - 1, i_plane, zc,
-                      full0 + 8 * s);
+        if (!zl) {
+          // y-lines: one box per z-plane over (8 channels, x, y, plane, z + nz * batch)
+          const int z = tc.zb % nz;
+          for (int q = 0; q < nzp; ++q) {
+            const int dz = nzp == 3 ? q - 1 : 0;
+            const int zc = (z + dz >= 0 && z + dz < nz) ? tc.zb + dz : -1;  // -1: a plane of zeros
+            tma_load_5d(aBase + (unsigned)s * abuf + (unsigned)q * zBytes, &tin, 0, tc.x0 - 1, tc.y0 - 1, i_off / 8,
+                        zc, full0 + 8 * s);
+          }
+        } else {
+          // z-lines: one box per y-plane and 8-channel plane over (channels, x, z, y, batch);
+          // a y outside the grid reads zeros
+          const int y = y0z + tc.zb % nyz, b = tc.zb / nyz;
+          for (int q = 0; q < nzp; ++q)
+            for (int p = 0; p < NP; ++p)
+              tma_load_5d(aBase + (unsigned)s * abuf + (unsigned)q * zBytes + (unsigned)p * pitch, &tin, i_off + 8 * p,
+                          tc.x0 - 1, tc.y0 - 1, y + q - 1, b, full0 + 8 * s);
         }
       }
       if (*abort_flag) {
@@ -324,13 +339,16 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         }
         tc_fence_after();
         const unsigned acc = tmem + (unsigned)a * acc_cols;
-        const unsigned long long a0 = sdesc(aBase + (unsigned)s * abuf, kTcPlane, kTcHX * 16);
+        const unsigned long long a0 = sdesc(aBase + (unsigned)s * abuf, pitch, kTcHX * 16);
         const unsigned long long b0 = sdesc(bBase, wplane, 128);
         for (int t = 0; t < taps; ++t) {
-          // z-plane and halo row offset of tap t, bytes
-          const unsigned tap = (unsigned)(t / 9) * zBytes + (unsigned)((((t / 3) % 3) * kTcHX + t % 3) * 16);
+          // halo plane and row offset of tap t, bytes: the planes run along z and the
+          // lines along y, or (z-lines) the planes along y and the lines along z
+          const int tz = t / 9, ty = (t / 3) % 3;
+          const unsigned tap =
+              (unsigned)(zl ? ty : tz) * zBytes + (unsigned)(((zl ? tz : ty) * kTcHX + t % 3) * 16);
           for (int c = 0; c < NP / 2; ++c) {
-            const unsigned aoff = (2u * c * kTcPlane + tap) >> 4, boff = ((unsigned)(t * NP + 2 * c) * wplane) >> 4;
+            const unsigned aoff = (2u * c * pitch + tap) >> 4, boff = ((unsigned)(t * NP + 2 * c) * wplane) >> 4;
             tc_mma(acc, a0 + aoff, b0 + boff, idesc, (t | c) != 0);
           }
         }
@@ -351,11 +369,19 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         break;
       }
       tc_fence_after();
-      const TileCoord tc = tile_coord(blockIdx.x + (long long)j * gridDim.x, tiles_x, tiles_y);
+      const TileCoord tc = tile_coord(blockIdx.x + (long long)j * gridDim.x, tiles_x, tiles_l);
       const int row = warp * 32 + lane;
-      const int x = tc.x0 + row % kTcTX, y = tc.y0 + row / kTcTX;
-      const bool in_grid = x < nx && y < ny;
-      const long long orow = (long long)tc.zb * Nxy + (long long)y * nx + x;
+      const int x = tc.x0 + row % kTcTX, l = tc.y0 + row / kTcTX;  // l: y, or z with z-lines
+      bool in_grid;
+      long long orow;
+      if (!zl) {
+        in_grid = x < nx && l < ny;
+        orow = (long long)tc.zb * Nxy + (long long)l * nx + x;
+      } else {
+        const int y = y0z + tc.zb % nyz, b = tc.zb / nyz;
+        in_grid = x < nx && l < nz;
+        orow = ((long long)b * nz + l) * Nxy + (long long)y * nx + x;
+      }
       const unsigned acc = tmem + (unsigned)a * acc_cols + ((unsigned)(warp * 32) << 16);
       for (int cb = 0; cb < Cout; cb += 16) {
         float v[16];
@@ -405,8 +431,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 namespace {
 
 size_t tc_weights(int taps, int Cin, int Cout) { return (size_t)taps * (Cin / 8) * Cout * 16; }
+// a halo buffer: 3D tiles use the z-lines' plane pitch (2944 bytes) in either mode
 size_t tc_halo(int taps, int Cin) {
-  return ((size_t)(taps == 27 ? 3 : 1) * (Cin / 8) * kTcPlane + kTcAlign - 1) / kTcAlign * kTcAlign;
+  return taps == 27 ? (size_t)3 * (Cin / 8) * (kTcPlane + 64)
+                    : ((size_t)(Cin / 8) * kTcPlane + kTcAlign - 1) / kTcAlign * kTcAlign;
 }
 size_t tc_smem(int taps, int Cin, int Cout, int nbuf) {
   return (size_t)kTcAlign + kTcHeader + tc_weights(taps, Cin, Cout) + (size_t)nbuf * tc_halo(taps, Cin);
@@ -503,7 +531,7 @@ void conv_tc_launch(Ctx& ctx, const char* name, const ConvTc& a, int* err) {
       attr_set[dev] = true;
     }
   }
-  // activations [B][nz][ny][nx][ldi] as (8 channels, x, y, plane, z + nz * batch), plane after y
+  // y-line tiles: activations [B][nz][ny][nx][ldi] as (8 channels, x, y, plane, z + nz * batch), plane after y
   alignas(64) CUtensorMap tin = {};
   {
     const cuuint64_t dims[5] = {8, (cuuint64_t)a.nx, (cuuint64_t)a.ny, (cuuint64_t)(a.ldi / 8),
@@ -513,14 +541,26 @@ void conv_tc_launch(Ctx& ctx, const char* name, const ConvTc& a, int* err) {
     const cuuint32_t box[5] = {8, kTcHX, kTcHY, (cuuint32_t)(Cin / 8), 1};
     encode(&tin, a.in, 5, dims, strides, box, "activations");
   }
-  // halo buffers: as many as fit (up to four).  CTAs per SM from the kernel's
-  // footprint against the SM's shared memory, registers, threads and tensor
-  // memory (512 columns); the runtime's occupancy query reports one CTA per SM
-  // for this kernel at every shared-memory size, so it is not used.
+  // 3D: full y-tiles on y-lines, the remaining y-rows of each plane (ny % 16 of
+  // them, one on the 2^k + 1-node grids) on z-line tiles, 16 lines along z, over
+  // the activations as (channels, x, z, y, batch)
+  const int y0z = taps == 27 ? a.ny / kTcTY * kTcTY : a.ny;
+  alignas(64) CUtensorMap tinz = {};
+  if (y0z < a.ny) {
+    const cuuint64_t dims[5] = {(cuuint64_t)a.ldi, (cuuint64_t)a.nx, (cuuint64_t)a.nz, (cuuint64_t)a.ny,
+                                (cuuint64_t)a.B};
+    const cuuint64_t strides[4] = {(cuuint64_t)a.ldi * 2, (cuuint64_t)a.nx * a.ny * a.ldi * 2,
+                                   (cuuint64_t)a.nx * a.ldi * 2, (cuuint64_t)a.nx * a.ny * a.nz * a.ldi * 2};
+    const cuuint32_t box[5] = {8, kTcHX, kTcHY, 1, 1};
+    encode(&tinz, a.in, 5, dims, strides, box, "activations (z-lines)");
+  }
+  // Halo buffers and CTAs per SM.  CTAs per SM come from the kernel's footprint
+  // against the SM's shared memory, registers, threads and tensor memory (512
+  // columns); the runtime's occupancy query reports one CTA per SM for this
+  // kernel at every shared-memory size, so it is not used.  Buffers: the most
+  // CTAs per SM with at least two buffers each, then the most buffers (up to
+  // four) at that count; one buffer only when two do not fit.
   const unsigned cols = tc_cols(Cout);
-  int nbuf = kTcMaxBuf;
-  while (nbuf > 1 && tc_smem(taps, Cin, Cout, nbuf) > kTcSmemMax) --nbuf;
-  const size_t smem = tc_smem(taps, Cin, Cout, nbuf);
   static int sm_smem[kMaxDevices] = {}, sm_regs[kMaxDevices] = {}, blk_resv[kMaxDevices] = {}, k_regs[kMaxDevices] = {};
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -538,20 +578,43 @@ void conv_tc_launch(Ctx& ctx, const char* name, const ConvTc& a, int* err) {
     }
   }
   const long long warp_regs = ((long long)k_regs[dev] * 32 + 255) / 256 * 256;  // allocated per warp in 256s
-  int per_sm = (int)std::min<long long>({(long long)sm_smem[dev] / ((long long)smem + blk_resv[dev]),
-                                         (long long)sm_regs[dev] / (warp_regs * (kTcThreads / 32)),
-                                         2048 / kTcThreads, 512 / (2 * (long long)cols)});
-  per_sm = std::max(1, per_sm);
+  auto ctas_per_sm = [&](int nb) {
+    return (int)std::max<long long>(
+        1, std::min<long long>({(long long)sm_smem[dev] / ((long long)tc_smem(taps, Cin, Cout, nb) + blk_resv[dev]),
+                                (long long)sm_regs[dev] / (warp_regs * (kTcThreads / 32)), 2048 / kTcThreads,
+                                512 / (2 * (long long)cols)}));
+  };
+  int nbuf = 1, per_sm = ctas_per_sm(1);
+  for (int nb = 2; nb <= kTcMaxBuf && tc_smem(taps, Cin, Cout, nb) <= kTcSmemMax; ++nb) {
+    const int k = ctas_per_sm(nb);
+    if (nb == 2 || k >= per_sm) {
+      nbuf = nb;
+      per_sm = k;
+    }
+  }
+  const size_t smem = tc_smem(taps, Cin, Cout, nbuf);
   // tiles of 8 x 16 nodes per plane; partial tiles at the grid's edges (TMA zero fill, stores masked)
-  const int tiles_x = (a.nx + kTcTX - 1) / kTcTX, tiles_y = (a.ny + kTcTY - 1) / kTcTY;
-  const long long tiles = (long long)tiles_x * tiles_y * a.nz * a.B;
+  const int tiles_x = (a.nx + kTcTX - 1) / kTcTX;
   const long long N = (long long)a.nx * a.ny * a.nz;
-  const int grid = (int)std::min<long long>(tiles, (long long)kSMs * per_sm);
+  const double bytes = (double)N * a.B * (Cin * 2.0 + a.Cst * (a.out32 ? 4.0 : 2.0)) + (double)taps * Cin * Cout * 2.0;
   ctx.add_flops(name, 2.0 * taps * Cin * a.Cst * (double)N * a.B);
-  HZ_LAUNCH(ctx, name, (double)N * a.B * (Cin * 2.0 + a.Cst * (a.out32 ? 4.0 : 2.0)) + (double)taps * Cin * Cout * 2.0,
-            k_conv_tc, grid, kTcThreads, smem, tin, a.i_off / 8, a.nx, a.ny, a.nz, a.B, tiles_x, tiles_y, taps, Cin,
-            Cout, a.Cst, nbuf, a.wimg, a.out, a.out32, a.ldo, a.o_off, a.relu, a.mask, a.ldm, a.m_off, a.mask_lo, cols,
-            err);
+  if (y0z > 0) {
+    const int tiles_y = (y0z + kTcTY - 1) / kTcTY;
+    const long long tiles = (long long)tiles_x * tiles_y * a.nz * a.B;
+    const int grid = (int)std::min<long long>(tiles, (long long)kSMs * per_sm);
+    HZ_LAUNCH(ctx, name, bytes * y0z / a.ny, k_conv_tc, grid, kTcThreads, smem, tin, a.i_off, a.nx, a.ny, a.nz, a.B,
+              0, 0, tiles_x, tiles_y, taps, Cin, Cout, a.Cst, nbuf, a.wimg, a.out, a.out32, a.ldo, a.o_off, a.relu,
+              a.mask, a.ldm, a.m_off, a.mask_lo, cols, err);
+  }
+  if (y0z < a.ny) {
+    const int tiles_z = (a.nz + kTcTY - 1) / kTcTY;
+    const long long tiles = (long long)tiles_x * tiles_z * (a.ny - y0z) * a.B;
+    const int grid = (int)std::min<long long>(tiles, (long long)kSMs * per_sm);
+    const std::string zn = std::string(name) + "_zlines";
+    HZ_LAUNCH(ctx, zn.c_str(), bytes * (a.ny - y0z) / a.ny, k_conv_tc, grid, kTcThreads, smem, tinz, a.i_off, a.nx,
+              a.ny, a.nz, a.B, 1, y0z, tiles_x, tiles_z, taps, Cin, Cout, a.Cst, nbuf, a.wimg, a.out, a.out32, a.ldo,
+              a.o_off, a.relu, a.mask, a.ldm, a.m_off, a.mask_lo, cols, err);
+  }
 }
 
 }  // namespace hz

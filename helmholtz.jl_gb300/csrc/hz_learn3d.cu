@@ -806,16 +806,16 @@ float* CoarseNet3::scale_staging(int B) {
 
 // The tensor-core path: N = Cout rounded up to 16 (the 8-channel layers compute
 // 8 zero channels more and store 8), the weights as images (hz_conv_tc.cu), tiles
-// of 8 x 16 nodes per z-plane.  tc_waste: the MMA work over the useful work on a
-// grid level (partial tiles times the padding of N).  On the 2^k + 1-node grids
-// of this network it is 2.7-4.4 on the 17^3 and 33^3 levels of the forward
-// (measured on a 33^3 x 32 batch: 200, 505 and 201 us on tcgen05 against 192,
-// 334 and 190 us with the warp-level kernel on the three 33^3 layers, 47 and
-// 135 against 45 and 105 us on the two 17^3 layers) and 1.4-2.7 on 65^3; the
-// default path takes the tensor cores where the waste is at most 2.5.
+// of 8 x 16 nodes per z-plane and z-line tiles for the last y-rows of a plane.
+// tc_waste: the MMA work over the useful work on a grid level (partial tiles
+// times the padding of N); the default path takes the tensor cores where it is
+// at most 2.5 (the measurements behind the bound are in the design notes).
 static double tc_waste(const int* gd, int Cout) {
-  const double tx = (gd[0] + 7) / 8 * 8.0, ty = (gd[1] + 15) / 16 * 16.0;
-  return tx * ty / ((double)gd[0] * gd[1]) * round16(Cout) / (double)Cout;
+  const int nx = gd[0], ny = gd[1], nz = gd[2];
+  const double wx = (nx + 7) / 8 * 8.0 / nx;
+  const int y0z = ny / 16 * 16;
+  const double wyz = (y0z + (ny - y0z) * ((nz + 15) / 16 * 16.0 / nz)) / ny;
+  return wx * wyz * round16(Cout) / (double)Cout;
 }
 
 bool CoarseNet3::use_tc(int Cin, int Cout, int lev) const {
