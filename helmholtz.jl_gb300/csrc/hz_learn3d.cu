@@ -809,7 +809,9 @@ float* CoarseNet3::scale_staging(int B) {
 // of 8 x 16 nodes per z-plane and z-line tiles for the last y-rows of a plane.
 // tc_waste: the MMA work over the useful work on a grid level (partial tiles
 // times the padding of N); the default path takes the tensor cores where it is
-// at most 2.5 (the measurements behind the bound are in the design notes).
+// at most 3.5.  On a 33^3 x 32 batch every layer ran faster on the tensor cores
+// (waste 1.5-3.2: 96, 30, 14, 93, 205 and 96 us against 192, 45, 16, 105, 335
+// and 191 us warp-level); a 5^3 level (waste 5.1) stays warp-level.
 static double tc_waste(const int* gd, int Cout) {
   const int nx = gd[0], ny = gd[1], nz = gd[2];
   const double wx = (nx + 7) / 8 * 8.0 / nx;
@@ -820,7 +822,7 @@ static double tc_waste(const int* gd, int Cout) {
 
 bool CoarseNet3::use_tc(int Cin, int Cout, int lev) const {
   if (conv_path_ == 0 || !conv_tc_supported(kTaps3, Cin, round16(Cout))) return false;
-  return conv_path_ == 1 || lev < 0 || tc_waste(g_[lev], Cout) <= 2.5;
+  return conv_path_ == 1 || lev < 0 || tc_waste(g_[lev], Cout) <= 3.5;
 }
 
 // Weight images of the forward layers, rewritten on c's stream whenever the BF16

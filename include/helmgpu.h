@@ -305,8 +305,8 @@ int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int6
  * output layer keeps the warp-level kernel; 3D: every layer, the 8-channel
  * layers computing 16 output channels and storing 8) or HZ_NET_CONV_AUTO (the
  * default: per layer the faster of the two; the 2D network's tensor-core
- * layers all, the 3D network's where its 8 x 16-node tiles waste at most 2.5x
- * the work on that layer's grid). */
+ * layers all, the 3D network's where its tiles waste at most 3.5x the work on
+ * that layer's grid). */
 #define HZ_NET_CONV_WARP_MMA 0
 #define HZ_NET_CONV_TCGEN05 1
 #define HZ_NET_CONV_AUTO 2

@@ -156,10 +156,10 @@ def test_tcgen05_weight_images_follow_training(hz):
 
 def test_auto_path_3d_picks_per_layer(hz):
     """The default path runs a 3D layer on the tensor cores where its tiles waste at
-    most 2.5x the work on its grid: on a 33^3-node batch every layer but the one on
-    the 9^3 level, which stays warp-level."""
+    most 3.5x the work on its grid: on a 17^3-node batch every layer but the one on
+    the 5^3 level, which stays warp-level."""
     net = hz.learned.CoarseNet3D(seed=3)
-    x, _ = _x3(6, 2, 33, 33, 33)
+    x, _ = _x3(6, 4, 17, 17, 17)
     net.reset_kernel_times()
     y_auto = net.forward(x)
     tc = _launches(net, "net3_conv_fwd_tc") + _launches(net, "net3_conv_fwd_tc_zlines")
