@@ -256,3 +256,24 @@ def test_3d_sommerfeld_and_mass_match_oracle(hz, O):
         p = hz.HelmholtzParam(M3, g["gamma3"], m3, w3, neu, somm)
         np.testing.assert_allclose(hz.helmholtz_mass(p), O.helmholtz_mass(Mo, m3, w3, g["gamma3"], neu, somm),
                                    rtol=1e-14, atol=0)
+
+
+def _header_constants():
+    text = (ROOT / "include" / "helmgpu.h").read_text()
+    return {k: int(v) for k, v in re.findall(r"^#define (HZ_[A-Z0-9_]+)\s+\(?(-?\d+)\)?", text, flags=re.M)}
+
+
+def test_binding_constants_match_header(hz):
+    """Every HZ_* value the Python and Julia bindings define is the header's."""
+    consts = _header_constants()
+    assert {"HZ_NET_CONV_WARP_MMA", "HZ_NET_CONV_TCGEN05", "HZ_NET_CONV_AUTO", "HZ_ERR_NO_DEVICE"} <= set(consts)
+    lib = hz._lib
+    py = {k: getattr(lib, k) for k in dir(lib) if re.fullmatch(r"HZ_[A-Z0-9_]+", k)}
+    assert py, "the Python binding defines no HZ_* constants"
+    for k, v in py.items():
+        assert k in consts and consts[k] == v, (k, v, consts.get(k))
+    shim = (ROOT / "helmholtz.jl_gb300" / "julia" / "HelmholtzGB300.jl").read_text()
+    jl = dict(re.findall(r"^const (HZ_[A-Z0-9_]+) = Int32\((-?\d+)\)", shim, flags=re.M))
+    assert jl, "the Julia shim defines no HZ_* constants"
+    for k, v in jl.items():
+        assert k in consts and consts[k] == int(v), (k, v, consts.get(k))
