@@ -93,6 +93,9 @@ const HZ_COARSE_GALERKIN = Int32(0)
 const HZ_COARSE_REDISCRETIZE = Int32(1)
 const HZ_RELAX_JAC = Int32(0)
 const HZ_RELAX_JAC_GMRES = Int32(1)
+const HZ_NET_CONV_WARP_MMA = Int32(0)
+const HZ_NET_CONV_TCGEN05 = Int32(1)
+const HZ_NET_CONV_AUTO = Int32(2)
 
 lasterror(h::Ptr{Cvoid}) = unsafe_string(ccall((:hz_last_error, libhelmgpu), Cstring, (Ptr{Cvoid},), h))
 function check(st::Integer, h::Ptr{Cvoid} = C_NULL)
@@ -374,7 +377,8 @@ function CoarseNet3D(seed::Integer = 0, device::Integer = 0)
     return net
 end
 netDim(net::CoarseNet) = Int(ccall((:hz_net_dim, libhelmgpu), Cint, (Ptr{Cvoid},), net.ptr))
-# convolution kernels of a network: 0 warp-level MMA, 1 tcgen05 tensor cores, 2 per layer the faster (the default)
+# convolution kernels of a network: HZ_NET_CONV_WARP_MMA, HZ_NET_CONV_TCGEN05 or
+# HZ_NET_CONV_AUTO (the default: per layer the faster)
 setNetConvPath!(net::CoarseNet, path::Integer) =
     check(ccall((:hz_net_set_conv_path, libhelmgpu), Cint, (Ptr{Cvoid}, Int32), net.ptr, Int32(path)))
 function netWeights3D(net::CoarseNet)
