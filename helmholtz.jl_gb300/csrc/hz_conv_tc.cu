@@ -617,4 +617,210 @@ void conv_tc_launch(Ctx& ctx, const char* name, const ConvTc& a, int* err) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient on the tensor cores:
+//   dW[co][t][ci] += sum_n dout[n][co] * in[n + off_t][ci]
+// a GEMM per tap with M = 128 rows (co, zero rows beyond Cout), N = Cin and
+// K = the nodes, in slices of 64 nodes.  A CTA owns one tap (blockIdx.z) and a
+// range of nodes (blockIdx.y).  Both operands take the K-major layout without
+// swizzle of the convolution kernel (core matrix = 8 rows x 8 nodes of 16 bytes):
+// each thread loads an 8-node x 8-channel block (8 rows of 16 bytes from
+// global memory; zeros where the tap leaves the grid or the range ends),
+// transposes it in registers (byte permutes) and stores its 8 channel rows as
+// one core matrix.  Two staging buffers: the block stages slice s + 1 while the
+// tensor cores run the four MMAs (K = 16 nodes each) of slice s.  The FP32
+// accumulator (128 lanes x Cin columns of tensor memory) is added to dW with one
+// atomic per weight at the end.  Every wait is bounded (err, as above).  The
+// staging (a transpose of every node row, per tap) bounds it: measured slower
+// than the warp-level kernels, which the default path keeps.
+constexpr int kWgNodes = 64;  // nodes per slice (K)
+
+__device__ __forceinline__ unsigned prmt(unsigned a, unsigned b, unsigned sel) {
+  unsigned r;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+  return r;
+}
+
+// out[r] holds channel r of the 8 nodes of v (node 2i in the low half of word i)
+__device__ __forceinline__ void transpose8x8(const uint4 (&v)[8], uint4 (&out)[8]) {
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const unsigned sel = (r & 1) ? 0x7632u : 0x5410u;
+    unsigned w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const uint4& a = v[2 * i];
+      const uint4& b = v[2 * i + 1];
+      const int q = r >> 1;
+      const unsigned wa = q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : a.w;
+      const unsigned wb = q == 0 ? b.x : q == 1 ? b.y : q == 2 ? b.z : b.w;
+      w[i] = prmt(wa, wb, sel);
+    }
+    out[r] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_wgrad_tc(int nx, int ny, int nz, long long nodes, int taps, int Cin,
+                                                  const bf16* __restrict__ in, int ldi, int Cout,
+                                                  const bf16* __restrict__ dout, int ldd, int d_off,
+                                                  float* __restrict__ dw, long long kc, unsigned acc_cols,
+                                                  int* __restrict__ err) {
+  extern __shared__ unsigned char wg_raw[];
+  unsigned char* smem = wg_raw + ((kTcAlign - (smem_u32(wg_raw) & (kTcAlign - 1))) & (kTcAlign - 1));
+  const unsigned base = smem_u32(smem);
+  const unsigned mbar0 = base;  // mma[b] at + 8 b
+  unsigned* tmem_slot = reinterpret_cast<unsigned*>(smem + 16);
+  const int GA = Cout / 8, GB = Cin / 8;           // 8-channel groups of the two operands
+  const unsigned aBytes = 16u * 8u * 128u;         // M = 128 rows x 64 nodes
+  const unsigned bBytes = (unsigned)GB * 8u * 128u;
+  const unsigned buf0 = base + kTcHeader;           // buffer b: A at buf0 + b (aBytes + bBytes), then B
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int t = blockIdx.z;
+  const int dz = taps == 27 ? t / 9 - 1 : 0, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+  const long long off = dx + (long long)dy * nx + (long long)dz * nx * ny;
+  const long long n0 = (long long)blockIdx.y * kc;
+  const long long n1 = min(nodes, n0 + kc);
+  const int ns = n1 > n0 ? (int)((n1 - n0 + kWgNodes - 1) / kWgNodes) : 0;
+
+  if (tid == 0) {
+    mbar_init(mbar0, 1);
+    mbar_init(mbar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // the rows of A beyond Cout stay zero: clear both buffers once
+  for (unsigned o = tid * 16u; o < 2u * (aBytes + bBytes); o += 128u * 16u)
+    *reinterpret_cast<uint4*>(smem + kTcHeader + o) = make_uint4(0u, 0u, 0u, 0u);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(acc_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *tmem_slot;
+  const unsigned idesc = idesc_bf16(kTcM, Cin);
+  const long long Nxy = (long long)nx * ny;
+  bool ok = true;
+  int issued = 0;  // slices whose MMAs thread 0 committed
+  for (int s = 0; s < ns && ok; ++s) {
+    const int b = s & 1;
+    // buffer b was last read by the MMAs of slice s - 2
+    if (s >= 2) ok = mbar_wait(mbar0 + 8 * b, (unsigned)((s - 2) >> 1) & 1u);
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    const unsigned aB = buf0 + (unsigned)b * (aBytes + bBytes), bB = aB + aBytes;
+    const long long ns0 = n0 + (long long)s * kWgNodes;
+    for (int task = tid; task < 8 * (GA + GB); task += blockDim.x) {
+      const int kg = task % 8, gi = task / 8;
+      const bool isA = gi < GA;
+      const int g = isA ? gi : gi - GA;
+      uint4 v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const long long n = ns0 + kg * 8 + j;
+        v[j] = make_uint4(0u, 0u, 0u, 0u);
+        if (n < n1) {
+          if (isA) {
+            v[j] = *reinterpret_cast<const uint4*>(dout + n * ldd + d_off + 8 * g);
+          } else {
+            const int x = (int)(n % nx), y = (int)((n / nx) % ny), z = (int)((n / Nxy) % nz);
+            if (x + dx >= 0 && x + dx < nx && y + dy >= 0 && y + dy < ny && z + dz >= 0 && z + dz < nz)
+              v[j] = *reinterpret_cast<const uint4*>(in + (n + off) * ldi + 8 * g);
+          }
+        }
+      }
+      uint4 w[8];
+      transpose8x8(v, w);
+      unsigned char* dst = smem + ((isA ? aB : bB) - base) + (unsigned)(kg * (isA ? 16 : GB) + g) * 128u;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) *reinterpret_cast<uint4*>(dst + r * 16) = w[r];
+    }
+    fence_async_smem();  // the staged slice is read by the tensor cores (async proxy)
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const unsigned long long a0 = sdesc(aB, 16u * 128u, 128u);        // LBO: next 8 nodes, SBO: next 8 rows
+      const unsigned long long b0 = sdesc(bB, (unsigned)GB * 128u, 128u);
+#pragma unroll
+      for (int q = 0; q < kWgNodes / 16; ++q)
+        tc_mma(tmem, a0 + ((2u * q * 16u * 128u) >> 4), b0 + ((2u * q * GB * 128u) >> 4), idesc, (s | q) != 0);
+      tc_commit(mbar0 + 8 * b);
+      ++issued;
+    }
+  }
+  // the last slice's MMAs (the commit tracks all earlier ones too)
+  bool done = true;
+  if (ok && ns > 0) done = mbar_wait(mbar0 + 8 * ((ns - 1) & 1), (unsigned)((ns - 1) >> 1) & 1u);
+  done = __syncthreads_and(done && ok);
+  if (!done) {
+    if (tid == 0) {
+      atomicExch(err, 1);
+      if (issued > 0) mbar_wait(mbar0 + 8 * ((issued - 1) & 1), (unsigned)((issued - 1) >> 1) & 1u);
+    }
+  } else if (ns > 0) {
+    tc_fence_after();
+    // epilogue: this thread's accumulator row is co = warp * 32 + lane
+    const int co = warp * 32 + lane;
+    for (int cb = 0; cb < Cin; cb += 16) {
+      float v[16];
+      tc_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)cb, v);
+      if (co < Cout) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) atomicAdd(&dw[((long long)co * taps + t) * Cin + cb + k], v[k]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(acc_cols) : "memory");
+}
+
+bool wgrad_tc_supported(int taps, int Cin, int Cout) {
+  return (taps == 9 || taps == 27) && Cin % 16 == 0 && Cin >= 16 && Cin <= 128 && Cout % 8 == 0 && Cout >= 8 &&
+         Cout <= 128;
+}
+
+void wgrad_tc_launch(Ctx& ctx, const char* name, const WgradTc& a, int* err) {
+  const int taps = a.nz > 1 ? 27 : 9;
+  if (!wgrad_tc_supported(taps, a.Cin, a.Cout)) throw std::runtime_error("wgrad_tc: unsupported channel counts");
+  if (a.ldi % 8 || a.ldd % 8 || a.d_off % 8 || a.d_off + a.Cout > a.ldd || a.Cin > a.ldi || !aligned16(a.in) ||
+      !aligned16(a.dout))
+    throw std::runtime_error("wgrad_tc: layout not aligned to 16 bytes");
+  if (a.nodes < 1 || a.nodes % ((long long)a.nx * a.ny * a.nz)) throw std::runtime_error("wgrad_tc: node count");
+  const size_t smem = (size_t)kTcAlign + kTcHeader + 2 * ((size_t)16 * 8 * 128 + (size_t)(a.Cin / 8) * 8 * 128);
+  {
+    static std::mutex mu;
+    static bool attr_set[kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices) throw std::runtime_error("wgrad_tc: device ordinal out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!attr_set[dev]) {
+      if (cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemMax) !=
+          cudaSuccess) {
+        cudaGetLastError();
+        throw std::runtime_error("wgrad_tc: shared memory attribute");
+      }
+      attr_set[dev] = true;
+    }
+  }
+  const unsigned cols = tc_cols(a.Cin);
+  // 64 slices of 64 nodes per CTA, fewer when that leaves too few CTAs to fill the GPU
+  long long kc = 64LL * kWgNodes;
+  while (kc > kWgNodes && ((a.nodes + kc - 1) / kc) * taps < 4LL * kSMs) kc /= 2;
+  const long long chunks = (a.nodes + kc - 1) / kc;
+  if (chunks > 65535) throw std::runtime_error("wgrad_tc: too many nodes");
+  ctx.add_flops(name, 2.0 * taps * a.Cin * a.Cout * (double)a.nodes);
+  HZ_LAUNCH(ctx, name, (double)a.nodes * (a.Cin + a.Cout) * 2.0 * taps, k_wgrad_tc, dim3(1u, (unsigned)chunks, taps),
+            128, smem, a.nx, a.ny, a.nz, a.nodes, taps, a.Cin, a.in, a.ldi, a.Cout, a.dout, a.ldd, a.d_off, a.dw, kc,
+            cols, err);
+}
+
 }  // namespace hz

@@ -132,6 +132,24 @@ struct ConvTc {
 };
 bool conv_tc_supported(int taps, int Cin, int Cout);
 void conv_tc_launch(Ctx& ctx, const char* name, const ConvTc& a, int* err);
+// Weight gradient on the 5th-generation tensor cores (hz_conv_tc.cu):
+// dw [Cout][taps][Cin] (FP32) += sum over the nodes of dout[n][co] * in[n + off_t][ci],
+// taps = 27 when nz > 1 else 9; Cin a multiple of 16 in [16, 128], Cout a
+// multiple of 8 in [8, 128]; nodes = B * nx * ny * nz rows; *err is set when a
+// wait timed out.
+struct WgradTc {
+  int nx, ny, nz;
+  long long nodes;
+  int Cin;
+  const __nv_bfloat16* in;
+  int ldi;
+  int Cout;
+  const __nv_bfloat16* dout;
+  int ldd, d_off;
+  float* dw;
+};
+bool wgrad_tc_supported(int taps, int Cin, int Cout);
+void wgrad_tc_launch(Ctx& ctx, const char* name, const WgradTc& a, int* err);
 // Weight image of a convolution with taps taps, Cin inputs and Cout outputs
 // (taps * Cin * Cout BF16 values): flip = 0 from w [wcout][taps][Cin] (outputs
 // >= wcout are zero); flip = 1 the data-gradient weights of a layer

@@ -52,16 +52,19 @@ def test_tcgen05_forward_matches_oracle_and_warp_mma(hz, ny, nx, path):
         assert _rel(y_tc[b], y_mma[b]) <= 1e-2, (b, _rel(y_tc[b], y_mma[b]))
 
 
-@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("path", PATHS + ["mma"])
 def test_tcgen05_gradient_matches_oracle(hz, path):
+    """Loss and weight gradients (weight gradient on tcgen05 with the tensor-core
+    path, warp-level with "mma") against the oracle."""
     net = hz.learned.CoarseNet(seed=5)
     net.set_conv_path(path)
     w = net.get_weights()
     x, t = _x(2, 2, 25, 33)
     net.reset_kernel_times()
     loss, g = net.gradient(x, t)
-    assert _launches(net, "net_conv_bwd_tc") == 7  # data gradients of layers 1..7
-    assert _launches(net, "net_conv_bwd") == 0
+    tc = path != "mma"
+    assert _launches(net, "net_conv_bwd_tc") == (7 if tc else 0)  # data gradients of layers 1..7
+    assert _launches(net, "net_wgrad_tc") == (8 if tc else 0) and _launches(net, "net_wgrad") == (0 if tc else 8)
     yo, cache = CN.forward(w, x.astype(np.float64), emulate=True)
     lo, go = CN.backward(cache, t.astype(np.float64))
     assert abs(loss - lo) <= 1e-3 * lo
@@ -113,16 +116,21 @@ def test_tcgen05_3d_forward_matches_oracle_and_warp_mma(hz, nz, ny, nx):
         assert _rel(y_tc[b], y_mma[b]) <= 1e-2, (b, _rel(y_tc[b], y_mma[b]))
 
 
-def test_tcgen05_3d_gradient_matches_oracle(hz):
+@pytest.mark.parametrize("path", ["tcgen05", "mma"])
+def test_tcgen05_3d_gradient_matches_oracle(hz, path):
     import coarse_net3d as CN3
     net = hz.learned.CoarseNet3D(seed=5)
-    net.set_conv_path("tcgen05")
+    net.set_conv_path(path)
     w = net.get_weights()
     x, t = _x3(2, 2, 9, 33, 17)
     net.reset_kernel_times()
     loss, g = net.gradient(x, t)
-    assert _launches(net, "net3_conv_bwd") == 0  # data gradients of layers 1..5 on the tensor cores
-    assert _launches(net, "net3_conv_bwd_tc") + _launches(net, "net3_conv_bwd_tc_zlines") >= 5
+    if path == "tcgen05":  # data and weight gradients on the tensor cores
+        assert _launches(net, "net3_conv_bwd") == 0 and _launches(net, "net3_wgrad") == 0
+        assert _launches(net, "net3_conv_bwd_tc") + _launches(net, "net3_conv_bwd_tc_zlines") >= 5
+        assert _launches(net, "net3_wgrad_tc") == 6
+    else:
+        assert _launches(net, "net3_wgrad") == 6 and _launches(net, "net3_wgrad_tc") == 0
     yo, cache = CN3.forward(w, x.astype(np.float64), emulate=True)
     lo, go = CN3.backward(cache, t.astype(np.float64))
     assert abs(loss - lo) <= 1e-3 * lo
