@@ -303,10 +303,11 @@ int hz_net3d_train(hz_net* net, const float* x, const float* t, int64_t nx, int6
  * with the accumulator in tensor memory and the operands staged by the TMA
  * unit; 2D: the layers whose channel counts are multiples of 16, the 8-channel
  * output layer keeps the warp-level kernel; 3D: every layer, the 8-channel
- * layers computing 16 output channels and storing 8) or HZ_NET_CONV_AUTO (the
- * default: per layer the faster of the two; the 2D network's tensor-core
- * layers all, the 3D network's where its tiles waste at most 3.5x the work on
- * that layer's grid). */
+ * layers computing 16 output channels and storing 8; the weight gradients
+ * too) or HZ_NET_CONV_AUTO (the default: per layer the faster of the two; the
+ * 2D network's tensor-core layers all, the 3D network's where its tiles waste
+ * at most 3.5x the work on that layer's grid; the weight gradients on the
+ * warp-level kernels, which measured faster). */
 #define HZ_NET_CONV_WARP_MMA 0
 #define HZ_NET_CONV_TCGEN05 1
 #define HZ_NET_CONV_AUTO 2
