@@ -272,3 +272,26 @@ def test_emulated_fp64_outer_matches_native(hz, O, case):
             assert np.linalg.norm(Href @ X[:, c] - B[:, c]) / np.linalg.norm(B[:, c]) <= 1e-6 * 1.0001
         its[arith] = S.last_iters.astype(int)
     assert np.all(np.abs(its["emulated"] - its["fp64"]) <= 2), its
+
+
+@pytest.fixture(scope="module")
+def full_2d(O):
+    """configs[1] at its full size: 1025 x 513 nodes (cells of 10 m), a seeded layered
+    model with an absorbing layer of 32 cells; four random right-hand sides and their
+    direct solution (SciPy SuperLU of the oracle's operator)."""
+    P = PB.layered((1024, 512), seed=7, pad=32, lengths=[10.24, 5.12])
+    B = PB.rhs(P["m"].size, 4, seed=5)
+    return P, B, O.direct_solve(P["H"], B)
+
+
+@pytest.mark.parametrize("precision,tol,bound", [("fp64", 1e-8, 1e-6), ("mixed", 1e-6, 1e-4)])
+def test_full_size_2d_against_direct_solve(hz, full_2d, precision, tol, bound):
+    """Five Galerkin levels, the K-cycle with damped Jacobi, FGMRES(10): every column to
+    the tolerance and within the specification's error bound of the direct solve."""
+    P, B, Xref = full_2d
+    S = _solver(hz, P, 5, tol, precision, cycle="K")
+    X, S = hz.solveLinearSystem(None, B, S)
+    assert S.last_relres.max() <= tol
+    for c in range(B.shape[1]):
+        assert _rel(X[:, c], Xref[:, c]) <= bound, (c, _rel(X[:, c], Xref[:, c]))
+        assert np.linalg.norm(P["H"] @ X[:, c] - B[:, c]) / np.linalg.norm(B[:, c]) <= tol * 1.0001
