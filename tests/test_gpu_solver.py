@@ -295,3 +295,43 @@ def test_full_size_2d_against_direct_solve(hz, full_2d, precision, tol, bound):
     for c in range(B.shape[1]):
         assert _rel(X[:, c], Xref[:, c]) <= bound, (c, _rel(X[:, c], Xref[:, c]))
         assert np.linalg.norm(P["H"] @ X[:, c] - B[:, c]) / np.linalg.norm(B[:, c]) <= tol * 1.0001
+
+
+@pytest.fixture(scope="module")
+def full_3d(O, cpu_slmg):
+    """configs[2] at its full size: 129^3 nodes (cells of 10 m), a seeded layered model
+    with an ellipsoidal body, an absorbing layer of 12 cells and 16 point sources on a
+    4 x 4 grid of the surface (depth index 1).  The FP64 reference for column 0 is the C
+    oracle's plain FP64 solve (the same 4-level V(1,1) cycle) continued to relative
+    residual 1e-9; its iteration count to 1e-6 is kept for the FP64 form."""
+    P = PB.layered((128, 128, 128), seed=11, pad=12, ellipsoid=True, lengths=[1.28] * 3)
+    nn = P["M"].n + 1
+    B = np.zeros((P["m"].size, 16), dtype=np.complex128, order="F")
+    grid = np.linspace(0.2 * nn[0], 0.8 * nn[0], 4).astype(np.int64)
+    amp = 1.0 / float(np.linalg.norm(P["M"].h)) ** 2
+    for c in range(16):
+        B[int(grid[c % 4]) + nn[0] * (int(grid[c // 4]) + nn[1] * 1), c] = amp
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    cpu = cpu_slmg.CpuSLMG(P["H"], SH, P["M"], 4)
+    r6 = cpu.solve(B[:, :1], tol=1e-6, max_outer=80)
+    r9 = cpu.solve(B[:, :1], tol=1e-9, max_outer=80, X0=r6.X)
+    assert r9.relres[0] <= 1e-9
+    return P, B, int(r6.iters[0]), r9.X[:, 0]
+
+
+def test_full_size_3d_against_oracle(hz, full_3d):
+    """The mixed form on all 16 columns and the plain FP64 form on two, four Galerkin
+    levels, V(1,1) damped Jacobi, FGMRES(10) to 1e-6: every column to the tolerance, the
+    error of column 0 within the specification's bound of the oracle's solution, and the
+    FP64 form's iterations within 2 % (at least 2) of the oracle's."""
+    P, B, it_ref, xref = full_3d
+    H = P["H"]
+    for precision, cols in (("mixed", 16), ("fp64", 2)):
+        S = _solver(hz, P, 4, 1e-6, precision, max_outer=80)
+        X, S = hz.solveLinearSystem(None, np.asfortranarray(B[:, :cols]), S)
+        assert S.last_relres.max() <= 1e-6, precision
+        for c in range(cols):
+            assert np.linalg.norm(H @ X[:, c] - B[:, c]) / np.linalg.norm(B[:, c]) <= 1e-6 * 1.0001, (precision, c)
+        assert _rel(X[:, 0], xref) <= 1e-4, (precision, _rel(X[:, 0], xref))
+        if precision == "fp64":
+            assert abs(int(S.last_iters[0]) - it_ref) <= max(2, 0.02 * it_ref), (S.last_iters, it_ref)
