@@ -418,3 +418,145 @@ def test_jac_gmres_rescues_deep_galerkin_3d(O, cpu_slmg):
     assert jg.relres[0] <= 1e-6 and jg.iters[0] <= 60, (jg.iters, jg.relres)
     jc = S.solve(B, tol=1e-6, max_outer=15, cycle="K", relax="Jac-GMRES", gmres_from=1)
     assert jc.relres[0] <= 1e-6 and jc.iters[0] <= 1.1 * jg.iters[0], (jc.iters, jg.iters)
+
+
+# ---------------------------------------------------------------------------
+# The multigrid and Krylov internals (Multigrid.jl and KrylovMethods.jl, absent
+# from the reference tree) pinned against formulations independent of the
+# oracle's code: SciPy's GMRES and BiCGSTAB, and the algebraic error
+# propagation operator of a multigrid cycle.
+# ---------------------------------------------------------------------------
+def _pin_problem(O, dims=(32, 32), levels=3, pad=4):
+    P = PB.layered(dims, seed=3, pad=pad, ellipsoid=len(dims) == 3)
+    SH = (P["H"] + O.GetHelmholtzShiftOP(P["m"], P["w"], 0.5)).tocsr()
+    return P, SH, O.build_hierarchy(SH, P["M"], levels)
+
+
+def _gmres_scipy(A, prec, b, restart, maxiter, tol):
+    """SciPy's restarted GMRES (modified Gram-Schmidt, LAPACK Givens rotations) on
+    the right-preconditioned operator A M from a zero guess; returns x = M u, the
+    inner iterations taken and SciPy's exit code."""
+    import scipy.sparse.linalg as spla
+    n = A.shape[0]
+    AM = spla.LinearOperator((n, n), matvec=lambda u: A @ prec(u.reshape(n, 1))[:, 0], dtype=np.complex128)
+    hist = []
+    u, info = spla.gmres(AM, b, rtol=tol, atol=0.0, restart=restart, maxiter=maxiter, callback=hist.append,
+                         callback_type="pr_norm")
+    return prec(u.reshape(n, 1))[:, 0], len(hist), info
+
+
+@pytest.mark.parametrize("cycle,sweeps,tol", [("V", 1, 1e-6), ("V", 1, 1e-10), ("W", 2, 1e-8)])
+def test_fgmres_matches_scipy_gmres_on_the_preconditioned_operator(O, cycle, sweeps, tol):
+    """With a linear preconditioner M (a V or W cycle from a zero guess), FGMRES(10)
+    right-preconditioned by M takes the iterates x_k = M u_k of GMRES(10) on H M:
+    SciPy's GMRES must stop after as many iterations, across restarts, at the same
+    solution to rounding."""
+    P, SH, hier = _pin_problem(O)
+    H = P["H"]
+    prec = lambda V: O.mg_cycle(hier, 0, V, 0.8, sweeps, sweeps, cycle)
+    b = PB.rhs(H.shape[0], 1, seed=4)[:, 0]
+    res = O.fgmres(lambda X: H @ X, prec, b[:, None], 10, tol, 50)
+    x, its, info = _gmres_scipy(H, prec, b, 10, 50, tol)
+    assert info == 0 and res.converged[0]
+    assert res.outer >= 2  # the comparison spans restarts
+    assert its == res.iters[0]
+    assert np.linalg.norm(x - res.X[:, 0]) <= 1e-12 * np.linalg.norm(res.X[:, 0])
+
+
+@pytest.mark.parametrize("k", [1, 3, 8])
+def test_bicgstab_matches_scipy_bicgstab_iterates(O, k):
+    """The oracle's right-preconditioned BiCGSTAB (the Krylov method of
+    solveBiCGSTAB_MG) and SciPy's BiCGSTAB, both van der Vorst's recurrences with
+    the preconditioner applied to p and s, agree after every number of iterations."""
+    import scipy.sparse.linalg as spla
+    P, SH, hier = _pin_problem(O)
+    H = P["H"]
+    n = H.shape[0]
+    prec = lambda V: O.mg_cycle(hier, 0, V, 0.8, 1, 1, "V")
+    b = PB.rhs(n, 1, seed=6)[:, 0]
+    r = O.bicgstab(lambda X: H @ X, prec, b[:, None], 1e-30, k)
+    M = spla.LinearOperator((n, n), matvec=lambda v: prec(v.reshape(n, 1))[:, 0], dtype=np.complex128)
+    x, _ = spla.bicgstab(H, b, rtol=1e-30, atol=0.0, maxiter=k, M=M)
+    assert r.iters[0] == k
+    assert np.linalg.norm(x - r.X[:, 0]) <= 1e-12 * np.linalg.norm(r.X[:, 0])
+
+
+def _interp_1d(c):
+    """Nodal linear interpolation from c coarse cells to 2c fine cells, from its
+    stencil: 1 at the coincident nodes, 1/2 from both neighbours in between."""
+    P = np.zeros((2 * c + 1, c + 1))
+    for i in range(c + 1):
+        P[2 * i, i] = 1.0
+    for i in range(c):
+        P[2 * i + 1, i] = P[2 * i + 1, i + 1] = 0.5
+    return P
+
+
+@pytest.mark.parametrize("dims,cycle,sweeps", [((16, 16), "V", 1), ((16, 16), "W", 2), ((16, 8), "W", 1),
+                                               ((8, 8, 8), "V", 1)])
+def test_cycle_is_its_error_propagation_operator(O, dims, cycle, sweeps):
+    """A V or W cycle from a zero guess is the linear map B_l = (I - E_l) A_l^-1,
+    E_l = S^s (I - P_l B_{l+1} R_l A_l)^c S^s with damped Jacobi S = I - w D^-1 A_l,
+    c = 1 (V) or 2 (W; above the coarsest level the exact correction is a projection,
+    so squaring it changes nothing there), B = A^-1 on the coarsest level.  P_l is
+    the Kronecker product (axis 1 fastest) of the 1D interpolation built here,
+    R_l = P_l^T / 2^d and A_{l+1} = R_l A_l P_l.  The oracle's hierarchy must hold
+    these matrices and its cycle applied to the identity must be B_0."""
+    levels = 3
+    P, SH, hier = _pin_problem(O, dims, levels, pad=2)
+    d, w, c = len(dims), 0.8, 2 if cycle == "W" else 1
+    A, Ps, Rs = [SH.toarray()], [], []
+    cells = list(dims)
+    for _ in range(levels - 1):
+        Pl = _interp_1d(cells[0] // 2)
+        for ck in cells[1:]:
+            Pl = np.kron(_interp_1d(ck // 2), Pl)
+        Ps.append(Pl)
+        Rs.append(Pl.T / 2.0**d)
+        A.append(Rs[-1] @ A[-1] @ Pl)
+        cells = [ck // 2 for ck in cells]
+    for lev in range(levels):
+        Ao = hier.levels[lev].A.toarray()
+        assert np.linalg.norm(Ao - A[lev]) <= 1e-13 * np.linalg.norm(A[lev])
+    B = np.linalg.inv(A[-1])
+    for lev in range(levels - 2, -1, -1):
+        I = np.eye(A[lev].shape[0])
+        S = np.linalg.matrix_power(I - w * A[lev] / np.diag(A[lev])[:, None], sweeps)
+        E = S @ np.linalg.matrix_power(I - Ps[lev] @ B @ Rs[lev] @ A[lev], c) @ S
+        B = (I - E) @ np.linalg.inv(A[lev])
+    Bo = O.mg_cycle(hier, 0, np.eye(A[0].shape[0], dtype=np.complex128), w, sweeps, sweeps, cycle)
+    assert np.linalg.norm(Bo - B) <= 1e-12 * np.linalg.norm(B)
+
+
+def test_kcycle_correction_is_two_gmres_steps(O):
+    """The K-cycle's coarse correction on a level (Multigrid.jl cycleType 'K') is two
+    FGMRES steps from a zero guess right-preconditioned by the level's cycle; with
+    the exact solve below, that cycle is linear and the correction equals one
+    GMRES(2) cycle of SciPy's on A_l M_l."""
+    P, SH, hier = _pin_problem(O)
+    A1 = hier.levels[1].A
+    b = PB.rhs(A1.shape[0], 2, seed=8)
+    out = O.kcycle(hier, 1, b, 0.8, 1, 1)
+    prec = lambda V: O.mg_cycle(hier, 1, V, 0.8, 1, 1, "K")
+    for c in range(2):
+        x, its, _ = _gmres_scipy(A1, prec, b[:, c], 2, 1, 1e-30)
+        assert its == 2
+        assert np.linalg.norm(x - out[:, c]) <= 1e-12 * np.linalg.norm(out[:, c])
+
+
+@pytest.mark.parametrize("steps", [1, 2, 3])
+def test_jac_gmres_smoother_is_gmres_on_the_correction(O, steps):
+    """relaxType "Jac-GMRES" from an iterate x0: x0 plus `steps` GMRES steps on the
+    correction A e = b - A x0, right-preconditioned by one damped-Jacobi sweep
+    (M = w D^-1); SciPy's GMRES(steps) on A M for that residual gives the same x."""
+    P, SH, hier = _pin_problem(O)
+    L0 = hier.levels[0]
+    A0 = L0.A
+    b = PB.rhs(A0.shape[0], 2, seed=9)
+    x0 = 0.1 * PB.rhs(A0.shape[0], 2, seed=10)
+    xr = O.gmres_relax(L0, x0.copy(), b, 0.8, steps)
+    prec = lambda V: 0.8 * L0.dinv[:, None] * V
+    for c in range(2):
+        e, its, _ = _gmres_scipy(A0, prec, b[:, c] - A0 @ x0[:, c], steps, 1, 1e-30)
+        assert its == steps
+        assert np.linalg.norm(x0[:, c] + e - xr[:, c]) <= 1e-12 * np.linalg.norm(xr[:, c])
