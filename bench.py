@@ -267,6 +267,13 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+# GB300's FP64 rate: no measured figure exists for it, so the nominal one is used
+FP64_PEAK_TFLOPS = 1.25
+# the kernels of the outer Krylov method that compute in FP64 (the library counts
+# their flops only when they do: the emulated form's kernels of these names count none)
+FP64_KERNELS = ("krylov_dots", "krylov_update", "update_x", "outer_apply", "outer_resid")
+
+
 def kernel_table(lib, h):
     n = lib.hz_kernel_times(h, -1, None, 0, None, None, None, None)
     rows = []
@@ -276,10 +283,42 @@ def kernel_table(lib, h):
         lt = C.c_int64()
         ms = C.c_double()
         by = C.c_double()
+        fl = C.c_double()
         lib.hz_kernel_times(h, i, name, 64, C.byref(la), C.byref(lt), C.byref(ms), C.byref(by))
+        lib.hz_kernel_flops(h, i, C.byref(fl))
         rows.append(dict(name=name.value.decode(), launches=la.value, timed=lt.value, ms=ms.value,
-                         bytes=by.value))
+                         bytes=by.value, flops=fl.value))
     return rows
+
+
+def fp64_rate(k: dict):
+    """FP64 TFLOP/s of a kernel-table row and its fraction of the nominal FP64
+    peak, or None for a row that is not a native-FP64 kernel or was not timed."""
+    if k["name"] not in FP64_KERNELS or not k.get("flops") or not k["ms"] > 0:
+        return None
+    t = k["flops"] / (k["ms"] / 1e3) / 1e12
+    return dict(achieved=t, peak=FP64_PEAK_TFLOPS, unit="TFLOP/s", frac=t / FP64_PEAK_TFLOPS,
+                peak_source="nominal GB300 FP64 rate (no measured FP64 peak)")
+
+
+def kernel_rows(kt, peak: float, tot_ms: float, top: int = 24) -> list:
+    """The bench line's per-kernel table: HBM rate and fraction of the measured
+    copy bandwidth for every row, the tensor or FP64 rate where the library
+    counts the kernel's flops."""
+    out = []
+    for k in sorted(kt, key=lambda k: -k["ms"])[:top]:
+        r = dict(name=k["name"], launches=k["launches"], ms=round(k["ms"], 3),
+                 gbs=(k["bytes"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None,
+                 frac=(k["bytes"] / (k["ms"] / 1e3) / 1e9 / peak) if k["ms"] > 0 else None,
+                 share=k["ms"] / tot_ms)
+        f64 = fp64_rate(k)
+        if f64 is not None:
+            r["fp64_tflops"] = f64["achieved"]
+            r["fp64_frac"] = f64["frac"]
+        elif k.get("flops") and k["ms"] > 0:
+            r["tflops"] = k["flops"] / (k["ms"] / 1e3) / 1e12
+        out.append(r)
+    return out
 
 
 def profile_entry(kernel: str, workload: str) -> dict:
@@ -681,6 +720,10 @@ def main():
                         traffic=tr, avg_launch_ms=dom["ms"] / dom["timed"], share=dom["ms"] / tot_ms,
                         source="CUDA events around every launch on the handle's stream, over one eager solve "
                                "right after the timed ones")
+        f64 = fp64_rate(dom)
+        if f64 is not None:
+            # the same kernel against GB300's FP64 rate: its algorithmic FP64 flops over the same events
+            roofline["fp64"] = f64
         if "fp64_pipe_pct_of_peak" in prof:
             # native-FP64 kernels: GB300's FP64 pipe, not HBM, is the limit
             roofline["fp64_pipe_pct_of_peak_ncu"] = prof["fp64_pipe_pct_of_peak"]
@@ -754,11 +797,7 @@ def main():
                 emulated_over_plain=over_plain("mixed_emulated"),
                 learned_emulated_over_plain=over_plain("learned_emulated"),
                 training=train_info,
-                kernels=[dict(name=k["name"], launches=k["launches"], ms=round(k["ms"], 3),
-                              gbs=(k["bytes"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None,
-                              frac=(k["bytes"] / (k["ms"] / 1e3) / 1e9 / peak) if k["ms"] > 0 else None,
-                              share=k["ms"] / tot_ms)
-                         for k in sorted(kt, key=lambda k: -k["ms"])[:24]],
+                kernels=kernel_rows(kt, peak, tot_ms),
                 kernels_source="one eager solve (cycle kernels launched one by one) after the timed solves")
     print(json.dumps(line))
 

@@ -26,7 +26,7 @@ struct Ctx {
   std::vector<long long> timed;    // launches with an event pair (profiling on)
   std::vector<double> total_ms;    // event-timed milliseconds per kernel
   std::vector<double> alg_bytes;   // algorithmic bytes per kernel (all launches)
-  std::vector<double> alg_flops;   // algorithmic flops per kernel (tensor-core kernels; 0 elsewhere)
+  std::vector<double> alg_flops;   // algorithmic flops per kernel (tensor-core and native-FP64 outer kernels; 0 elsewhere)
   struct Pending {
     int id;
     cudaEvent_t a, b;

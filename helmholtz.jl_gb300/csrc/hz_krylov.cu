@@ -144,6 +144,8 @@ void launch_dots(Ctx& ctx, long long N, const double2* V, long long vstride, lon
   dim3 grid(nblk, ncols);
   // a masked pass is charged by the host once it knows which columns took it
   const double bytes = mask ? 0.0 : (double)N * ncols * (K + 1) * sizeof(double2);
+  // FP64 arithmetic: a complex multiply-add (8 flops) per vector and node, 4 for ||w||^2
+  if (!mask) ctx.add_flops("krylov_dots", (double)N * ncols * (8.0 * K + (want_norm ? 4.0 : 0.0)));
   switch (K) {
 #define HZ_DOTS_CASE(k)                                                                                     \
   case k:                                                                                                   \
@@ -164,6 +166,7 @@ void launch_update(Ctx& ctx, long long N, const double2* V, long long vstride, l
   if (ncols <= 0) return;
   dim3 grid(nblk, ncols);
   const double bytes = mask ? 0.0 : (double)N * ncols * (K + 2) * sizeof(double2);
+  if (!mask) ctx.add_flops("krylov_update", (double)N * ncols * (8.0 * K + (want_norm ? 4.0 : 0.0)));
   switch (K) {
 #define HZ_UPD_CASE(k)                                                                                           \
   case k:                                                                                                        \
@@ -377,6 +380,7 @@ void launch_update_x(Ctx& ctx, long long N, const cplx<TZ>* Z, long long zstride
   int nb = krylov_nblk(N, ncols);
   dim3 grid(nb, ncols);
   const double bytes = (double)N * (ncols * 2.0 * sizeof(double2) + zcols * sizeof(cplx<TZ>));
+  ctx.add_flops("update_x", 8.0 * N * zcols);  // FP64: a complex multiply-add per stored Z vector and node
   HZ_LAUNCH(ctx, "update_x", bytes, k_update_x<TZ>, grid, 256, 0, N, Z, zstride, ld, kcol, y, ystride, x, xld, cols);
 }
 

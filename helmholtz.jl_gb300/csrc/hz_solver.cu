@@ -184,6 +184,7 @@ struct hz_handle {
     long long seen = 0;      // applications with this key (captured on the second)
     long long launches = 0;  // kernels in the graph
     double bytes = 0.0;
+    double flops = 0.0;      // algorithmic flops of the captured kernels that count theirs
     std::vector<std::pair<int, long long>> counts;
   };
   std::map<std::tuple<int, int, int, int>, CycleGraph> graphs;
@@ -1167,6 +1168,7 @@ void cycle_graph(hz_handle* h, int adj, int j, int nl, int form, F&& body) {
     c.profile = false;
     const std::vector<long long> counts0 = c.counts;
     const std::vector<double> bytes0 = c.alg_bytes;
+    const std::vector<double> flops0 = c.alg_flops;
     const long long l0 = c.launches;
     cudaGraph_t g = nullptr;
     bool ok = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
@@ -1190,13 +1192,17 @@ void cycle_graph(hz_handle* h, int adj, int j, int nl, int form, F&& body) {
     c.launches = l0;
     cg.counts.clear();
     cg.bytes = 0.0;
+    cg.flops = 0.0;
     for (size_t i = 0; i < c.counts.size(); ++i) {
       const long long c0 = i < counts0.size() ? counts0[i] : 0;
       const double b0 = i < bytes0.size() ? bytes0[i] : 0.0;
+      const double f0 = i < flops0.size() ? flops0[i] : 0.0;
       if (c.counts[i] != c0) cg.counts.push_back({(int)i, c.counts[i] - c0});
       cg.bytes += c.alg_bytes[i] - b0;
+      cg.flops += c.alg_flops[i] - f0;
       c.counts[i] = c0;
       c.alg_bytes[i] = b0;
+      c.alg_flops[i] = f0;
     }
     if (!ok) {
       cudaGetLastError();
@@ -1211,6 +1217,7 @@ void cycle_graph(hz_handle* h, int adj, int j, int nl, int form, F&& body) {
   c.before(gid, &a);
   ck(cudaGraphLaunch(cg.exec, c.stream), "cudaGraphLaunch");
   c.after(gid, a, cg.bytes);
+  if (cg.flops != 0.0) c.alg_flops[gid] += cg.flops;
   c.launches += cg.launches - 1;  // after() counted the graph as one launch
   for (auto& pc : cg.counts) c.counts[pc.first] += pc.second;
 }
@@ -1347,6 +1354,10 @@ int fgmres(hz_handle* h, int adj, int nrhs) {
         for (int c : live) n2 += h->h_flag[c] ? 1 : 0;
         h->ctx.add_bytes("krylov_dots", (double)N * n2 * (K + 1) * 16.0);
         h->ctx.add_bytes("krylov_update", (double)N * n2 * (K + 2) * 16.0);
+        if (!df) {  // the second pass's FP64 arithmetic (no ||w||^2 in its dots)
+          h->ctx.add_flops("krylov_dots", (double)N * n2 * 8.0 * K);
+          h->ctx.add_flops("krylov_update", (double)N * n2 * (8.0 * K + 4.0));
+        }
         h->reorth += n2;
       }
       std::vector<int> still;

@@ -11,6 +11,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include <cooperative_groups.h>
 
@@ -206,6 +207,12 @@ void launch_fine(Ctx& ctx, int mode, const FineOp& op, const cplx<T>* diag, cons
   HZ_LAUNCH(ctx, NAME, fbytes, (k_fine<T, TX, TB, M, D>), grid, TPB, 0, o, diag, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
   const char* nm_apply = op.outer ? "outer_apply" : "fine_apply";
   const char* nm_resid = op.outer ? "outer_resid" : "fine_resid";
+  // FP64 arithmetic of the Krylov method's operator, per node and column: a multiply
+  // and an add per component of each real-coefficient neighbour, 8 flops for the
+  // complex diagonal, 2 for b - H x
+  if (op.outer && std::is_same<T, double>::value && mode != MODE_JACOBI)
+    ctx.add_flops(mode == MODE_APPLY ? nm_apply : nm_resid,
+                  (8.0 * (is3d ? 3 : 2) + 8.0 + (mode == MODE_RESID ? 2.0 : 0.0)) * (double)op.g.N * ncols);
   if (mode == MODE_APPLY) {
     if (is3d) HZ_FINE_CASE(MODE_APPLY, true, nm_apply);
     else HZ_FINE_CASE(MODE_APPLY, false, nm_apply);

@@ -214,8 +214,10 @@ int hz_reset_kernel_times(hz_handle* h);
  * process and, when the environment variable HELMGPU_TUNE_CACHE names a file,
  * persisted there.  Returns HZ_OK once tuned, HZ_NOT_CONVERGED before. */
 int hz_tune_info(const hz_handle* h, int32_t* fine_ctas, int32_t* rap_ctas);
-/* Algorithmic flops of entry idx of the launch table (the tensor-core kernels
- * of the learned correction; 0 for the memory-bound kernels). */
+/* Algorithmic flops of entry idx of the launch table: the tensor-core kernels of
+ * the learned correction (BF16) and the native-FP64 kernels of the outer Krylov
+ * method (krylov_dots, krylov_update, update_x, outer_apply, outer_resid: the
+ * complex arithmetic they do in FP64); 0 for the other, memory-bound kernels. */
 int hz_kernel_flops(hz_handle* h, int32_t idx, double* alg_flops);
 /* Replay the preconditioner applications from CUDA graphs (1) or launch them
  * eagerly (0) from the next application on (options.cuda_graph at create time);

@@ -73,3 +73,29 @@ def test_workload_defaults_fill_the_solver_options():
     bench.resolve_solver_args(b)
     assert (b.cycle, b.relax, b.shift) == ("W", "jac", 0.5)
     assert bench.DEFAULT_WORKLOAD == "c5"
+
+
+def test_kernel_rows_rate_the_fp64_and_tensor_kernels():
+    """The per-kernel table gives every row its HBM rate; the native-FP64 outer
+    kernels (flops counted by the library) also their FP64 rate against GB300's
+    nominal FP64 peak, the tensor-core kernels their TFLOP/s; rows without flops
+    (memory-bound kernels, the emulated form's kernels of the same names) neither."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    kt = [dict(name="krylov_dots", launches=10, timed=10, ms=1000.0, bytes=2.0e12, flops=1.0e12),
+          dict(name="net3_conv_fwd_tc", launches=4, timed=4, ms=10.0, bytes=1.0e9, flops=1.0e12),
+          dict(name="fine_jacobi", launches=5, timed=5, ms=100.0, bytes=5.0e11, flops=0.0),
+          dict(name="krylov_update", launches=5, timed=5, ms=500.0, bytes=3.0e12, flops=0.0)]
+    rows = {r["name"]: r for r in bench.kernel_rows(kt, 6000.0, 1610.0)}
+    assert [r["name"] for r in bench.kernel_rows(kt, 6000.0, 1610.0)] == \
+        ["krylov_dots", "krylov_update", "fine_jacobi", "net3_conv_fwd_tc"]
+    d = rows["krylov_dots"]
+    assert abs(d["gbs"] - 2000.0) < 1e-9 and abs(d["frac"] - 2000.0 / 6000.0) < 1e-12
+    assert abs(d["fp64_tflops"] - 1.0) < 1e-12 and abs(d["fp64_frac"] - 1.0 / bench.FP64_PEAK_TFLOPS) < 1e-12
+    assert "tflops" not in d
+    assert abs(rows["net3_conv_fwd_tc"]["tflops"] - 100.0) < 1e-9 and "fp64_frac" not in rows["net3_conv_fwd_tc"]
+    for name in ("fine_jacobi", "krylov_update"):
+        assert "tflops" not in rows[name] and "fp64_frac" not in rows[name]
+    f = bench.fp64_rate(kt[0])
+    assert f["unit"] == "TFLOP/s" and f["peak"] == bench.FP64_PEAK_TFLOPS and abs(f["frac"] - 0.8) < 1e-12
+    assert bench.fp64_rate(kt[1]) is None and bench.fp64_rate(dict(kt[0], ms=0.0)) is None
