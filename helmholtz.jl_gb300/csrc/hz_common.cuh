@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace hz {
 
@@ -64,25 +65,59 @@ template <typename T> __host__ __device__ __forceinline__ cplx<T> cscale(T s, cp
 }
 template <typename T> __host__ __device__ __forceinline__ cplx<T> cconj(cplx<T> a) { return mk<T>(a.x, -a.y); }
 
-// FP32 -> FP64 widening from the IEEE-754 bit layouts, exact: for a normal
-// number the 8-bit exponent is re-biased (127 -> 1023) and the 23-bit fraction
-// moves to the top of the 52-bit fraction, with integer operations only.
-// Returns false for zero, subnormal, infinite and NaN inputs (the caller uses
-// the hardware conversion for those).  GB300's FP64 pipe also executes the
-// hardware conversion, so FP64 kernels that widen FP32 data (H z with z from
-// the complex-FP32 cycle, x += Z y) use this to keep the conversions off it.
-__host__ __device__ __forceinline__ bool widen_f32_bits(uint32_t u, uint32_t& hi, uint32_t& lo) {
-  const uint32_t a = u & 0x7fffffffu;
-  if (a - 0x00800000u >= 0x7f000000u) return false;
-  hi = ((a >> 3) + 0x38000000u) | (u & 0x80000000u);
-  lo = u << 29;
-  return true;
+// FP32 -> FP64 widening from the IEEE-754 bit layouts, exact for every input,
+// with no FP64 operation.  GB300's FP64 pipe also executes the hardware
+// conversion, and the FP64 kernels that read FP32 data (H z with z from the
+// complex-FP32 cycle, x += Z y) are bound by that pipe, so no conversion of
+// theirs may land there, not even a predicated one for the rare inputs.  The
+// high and low words of the FP64 result:
+//  - normal: the 8-bit exponent is re-biased (127 -> 1023), the 23-bit fraction
+//    moves to the top of the 52-bit fraction;
+//  - subnormal: scaled by 2^24 in FP32 (exact, the product is normal), widened
+//    as a normal number, then 24 taken off the exponent;
+//  - a zero keeps its sign, an infinity stays infinite, a NaN keeps its payload
+//    (moved up with the fraction) and becomes quiet.
+__host__ __device__ __forceinline__ void widen_f32_hilo(uint32_t u, uint32_t& hi, uint32_t& lo) {
+  const uint32_t sg = u & 0x80000000u;
+  uint32_t a = u & 0x7fffffffu;
+  uint32_t bias = 0x38000000u;  // (1023 - 127) << 20
+  if (a - 0x00800000u >= 0x7f000000u) {  // exponent field 0 or 255
+    if (a >= 0x7f800000u) {
+      hi = sg | 0x7ff00000u | ((a & 0x007fffffu) >> 3) | (a > 0x7f800000u ? 0x00080000u : 0u);
+      lo = a << 29;
+      return;
+    }
+    if (a == 0u) {
+      hi = sg;
+      lo = 0u;
+      return;
+    }
+    float f, g;
+#ifdef __CUDA_ARCH__
+    f = __uint_as_float(a);
+    g = f * 16777216.0f;
+    a = __float_as_uint(g);
+#else
+    memcpy(&f, &a, 4);
+    g = f * 16777216.0f;
+    memcpy(&a, &g, 4);
+#endif
+    bias -= 24u << 20;
+  }
+  hi = sg | ((a >> 3) + bias);
+  lo = a << 29;
+}
+
+__host__ __device__ __forceinline__ uint64_t widen_f32_bits(uint32_t u) {
+  uint32_t hi, lo;
+  widen_f32_hilo(u, hi, lo);
+  return ((uint64_t)hi << 32) | lo;
 }
 
 #ifdef __CUDACC__
 __device__ __forceinline__ double widen_f32(float f) {
   uint32_t hi, lo;
-  if (!widen_f32_bits(__float_as_uint(f), hi, lo)) return (double)f;
+  widen_f32_hilo(__float_as_uint(f), hi, lo);
   return __hiloint2double((int)hi, (int)lo);
 }
 #endif
