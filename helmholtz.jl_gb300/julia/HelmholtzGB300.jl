@@ -21,7 +21,9 @@ using Multigrid: MGparam
 
 export HelmholtzParam, ShiftedLaplacianMultigridSolver, getShiftedLaplacianMultigridSolver, solveLinearSystem,
        solveLinearSystem!, copySolver, clear!, getMaximalFrequency, getABL, getSommerfeldBC,
-       getAcousticPointSource, getHelmholtzFun, HzApply,
+       getAcousticPointSource, getHelmholtzFun, HzApply, applyNoAlloc!,
+       helmgpuVersion, columnStats, setCudaGraph!, setProfile!, kernelTimes, resetKernelTimes!, tuneInfo,
+       learnedStats,
        CoarseNet, netWeights, setNetWeights!, netForward, netGradient, netTrain!, collectPairs!, attachNet!,
        saveNet, loadNet!
 
@@ -299,6 +301,76 @@ function (f::HzApply)(x::AbstractVecOrMat)
     return y
 end
 getHelmholtzFun(s::ShiftedLaplacianMultigridSolver, transpose::Integer = 0) = HzApply(s, Int32(transpose))
+
+# Y = H X on DEVICE arrays (e.g. CUDA.jl CuArray pointers, n x nrhs complex FP64)
+# without any GPU memory allocation; the caller's writes of X must be complete
+# (synchronised) before the call.
+function applyNoAlloc!(s::ShiftedLaplacianMultigridSolver, X::Ptr{ComplexF64}, Y::Ptr{ComplexF64}, n::Integer,
+                       nrhs::Integer, transpose::Integer = 0)
+    h = ensure_handle!(s)
+    check(ccall((:hz_apply_noalloc, libhelmgpu), Cint,
+                (Ptr{Cvoid}, Int32, Int32, Ptr{ComplexF64}, Ptr{ComplexF64}, Int64, Int32),
+                h, HZ_OP_H, Int32(transpose), X, Y, Int64(n), Int32(nrhs)), h)
+    return Y
+end
+
+# ---- diagnostics (no counterpart in the reference) --------------------------------
+helmgpuVersion() = Int(ccall((:hz_version, libhelmgpu), Int32, ()))
+
+# per-column relative residuals and iteration counts of the last solve of s
+function columnStats(s::ShiftedLaplacianMultigridSolver, nrhs::Integer)
+    s.handle == C_NULL && throw(ArgumentError("the solver has not solved yet"))
+    rr = zeros(Float64, nrhs)
+    it = zeros(Int32, nrhs)
+    check(ccall((:hz_column_stats, libhelmgpu), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Int32}, Int32),
+                s.handle, rr, it, Int32(nrhs)), s.handle)
+    return rr, it
+end
+
+# replay the preconditioner's cycles from CUDA graphs (true, the default) or launch them one by one
+setCudaGraph!(s::ShiftedLaplacianMultigridSolver, on::Bool) =
+    check(ccall((:hz_set_cuda_graph, libhelmgpu), Cint, (Ptr{Cvoid}, Int32), ensure_handle!(s), Int32(on)),
+          s.handle)
+# per-launch CUDA-event timing of the kernels (for kernelTimes)
+setProfile!(s::ShiftedLaplacianMultigridSolver, on::Bool) =
+    check(ccall((:hz_set_profile, libhelmgpu), Cint, (Ptr{Cvoid}, Int32), ensure_handle!(s), Int32(on)), s.handle)
+
+# the handle's launch table: (name, launches, timed launches, total ms, algorithmic bytes, algorithmic flops)
+function kernelTimes(s::ShiftedLaplacianMultigridSolver)
+    h = ensure_handle!(s)
+    n = ccall((:hz_kernel_times, libhelmgpu), Cint,
+              (Ptr{Cvoid}, Int32, Ptr{UInt8}, Int32, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}),
+              h, Int32(-1), C_NULL, Int32(0), C_NULL, C_NULL, C_NULL, C_NULL)
+    check(n, h)
+    rows = Vector{NamedTuple}()
+    for i in 0:n-1
+        name = zeros(UInt8, 64)
+        la, lt, ms, by, fl = Ref{Int64}(0), Ref{Int64}(0), Ref{Float64}(0.0), Ref{Float64}(0.0), Ref{Float64}(0.0)
+        check(ccall((:hz_kernel_times, libhelmgpu), Cint,
+                    (Ptr{Cvoid}, Int32, Ptr{UInt8}, Int32, Ref{Int64}, Ref{Int64}, Ref{Float64}, Ref{Float64}),
+                    h, Int32(i), name, Int32(64), la, lt, ms, by), h)
+        check(ccall((:hz_kernel_flops, libhelmgpu), Cint, (Ptr{Cvoid}, Int32, Ref{Float64}), h, Int32(i), fl), h)
+        push!(rows, (name = unsafe_string(pointer(name)), launches = la[], timed = lt[], ms = ms[],
+                     bytes = by[], flops = fl[]))
+    end
+    return rows
+end
+resetKernelTimes!(s::ShiftedLaplacianMultigridSolver) =
+    check(ccall((:hz_reset_kernel_times, libhelmgpu), Cint, (Ptr{Cvoid},), ensure_handle!(s)), s.handle)
+# launch shapes the autotuner chose (CTAs per launch of the fine and the Galerkin stencils)
+function tuneInfo(s::ShiftedLaplacianMultigridSolver)
+    f, r = Ref{Int32}(0), Ref{Int32}(0)
+    st = check(ccall((:hz_tune_info, libhelmgpu), Cint, (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}), ensure_handle!(s), f, r),
+               s.handle)
+    return st == 0 ? (fine = Int(f[]), rap = Int(r[])) : nothing
+end
+# network applications and fallbacks to the plain cycle in the solves of s
+function learnedStats(s::ShiftedLaplacianMultigridSolver)
+    c, f = Ref{Int64}(0), Ref{Int32}(0)
+    s.handle == C_NULL && return (calls = 0, fallbacks = 0)
+    check(ccall((:hz_learned_stats, libhelmgpu), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int32}), s.handle, c, f), s.handle)
+    return (calls = Int(c[]), fallbacks = Int(f[]))
+end
 
 # ---- learned coarse-grid correction (no counterpart in the reference) ------------
 # Arrays are Julia column-major (4, nx, ny, batch) for inputs and (2, nx, ny, batch)
