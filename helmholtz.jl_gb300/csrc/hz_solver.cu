@@ -1951,11 +1951,17 @@ int hz_copy(const hz_handle* h, hz_handle** out) {
 
 void* hz_stream(hz_handle* h) { return h ? (void*)h->ctx.stream : nullptr; }
 
+// make the table's device current and fold its finished launches' events in;
+// a device error (a failed launch before) is reported, not swallowed
+static void ctx_settle(Ctx& c, int dev) {
+  ck(cudaSetDevice(dev), "cudaSetDevice");
+  if (c.stream) ck(cudaStreamSynchronize(c.stream), "synchronize the launch table's stream");
+  c.resolve();
+}
+
 static int ctx_times(Ctx& c, int dev, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                      int64_t* timed_launches, double* total_ms, double* alg_bytes, double* alg_flops) {
-  cudaSetDevice(dev);
-  if (c.stream) cudaStreamSynchronize(c.stream);
-  c.resolve();
+  ctx_settle(c, dev);
   const int n = (int)c.names.size();
   if (idx < 0 || idx >= n) return n;
   if (name && name_len > 0) {
@@ -1971,9 +1977,7 @@ static int ctx_times(Ctx& c, int dev, int32_t idx, char* name, int32_t name_len,
 }
 
 static void ctx_reset(Ctx& c, int dev) {
-  cudaSetDevice(dev);
-  if (c.stream) cudaStreamSynchronize(c.stream);
-  c.resolve();
+  ctx_settle(c, dev);
   std::fill(c.counts.begin(), c.counts.end(), 0);
   std::fill(c.timed.begin(), c.timed.end(), 0);
   std::fill(c.total_ms.begin(), c.total_ms.end(), 0.0);
@@ -1984,12 +1988,20 @@ static void ctx_reset(Ctx& c, int dev) {
 int hz_kernel_times(hz_handle* h, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                     int64_t* timed_launches, double* total_ms, double* alg_bytes) {
   if (!h) return HZ_ERR_ARG;
-  return ctx_times(h->ctx, h->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes, nullptr);
+  int n = 0;
+  const int st = guarded(h, [&] {
+    n = ctx_times(h->ctx, h->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes, nullptr);
+  });
+  return st < 0 ? st : n;
 }
 
 int hz_kernel_flops(hz_handle* h, int32_t idx, double* alg_flops) {
   if (!h) return HZ_ERR_ARG;
-  return ctx_times(h->ctx, h->dev, idx, nullptr, 0, nullptr, nullptr, nullptr, nullptr, alg_flops);
+  int n = 0;
+  const int st = guarded(h, [&] {
+    n = ctx_times(h->ctx, h->dev, idx, nullptr, 0, nullptr, nullptr, nullptr, nullptr, alg_flops);
+  });
+  return st < 0 ? st : n;
 }
 
 int hz_tune_info(const hz_handle* h, int32_t* fine_ctas, int32_t* rap_ctas) {
@@ -2001,8 +2013,7 @@ int hz_tune_info(const hz_handle* h, int32_t* fine_ctas, int32_t* rap_ctas) {
 
 int hz_reset_kernel_times(hz_handle* h) {
   if (!h) return HZ_ERR_ARG;
-  ctx_reset(h->ctx, h->dev);
-  return HZ_OK;
+  return guarded(h, [&] { ctx_reset(h->ctx, h->dev); });
 }
 
 int hz_set_cuda_graph(hz_handle* h, int32_t on) {
@@ -2013,11 +2024,10 @@ int hz_set_cuda_graph(hz_handle* h, int32_t on) {
 
 int hz_set_profile(hz_handle* h, int32_t on) {
   if (!h) return HZ_ERR_ARG;
-  cudaSetDevice(h->dev);
-  if (h->ctx.stream) cudaStreamSynchronize(h->ctx.stream);
-  h->ctx.resolve();
-  h->ctx.profile = on != 0;
-  return HZ_OK;
+  return guarded(h, [&] {
+    ctx_settle(h->ctx, h->dev);
+    h->ctx.profile = on != 0;
+  });
 }
 
 // ---- learned coarse-grid correction -------------------------------------------
@@ -2307,25 +2317,26 @@ int hz_net_set_conv_path(hz_net* net, int32_t path) {
 
 int hz_net_set_profile(hz_net* net, int32_t on) {
   if (!net) return HZ_ERR_ARG;
-  cudaSetDevice(net->dev);
-  Ctx& c = net->ctx();
-  cudaStreamSynchronize(c.stream);
-  c.resolve();
-  c.profile = on != 0;
-  return HZ_OK;
+  return guarded(nullptr, [&] {
+    ctx_settle(net->ctx(), net->dev);
+    net->ctx().profile = on != 0;
+  });
 }
 
 int hz_net_kernel_times(hz_net* net, int32_t idx, char* name, int32_t name_len, int64_t* launches,
                         int64_t* timed_launches, double* total_ms, double* alg_bytes, double* alg_flops) {
   if (!net) return HZ_ERR_ARG;
-  return ctx_times(net->ctx(), net->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes,
-                   alg_flops);
+  int n = 0;
+  const int st = guarded(nullptr, [&] {
+    n = ctx_times(net->ctx(), net->dev, idx, name, name_len, launches, timed_launches, total_ms, alg_bytes,
+                  alg_flops);
+  });
+  return st < 0 ? st : n;
 }
 
 int hz_net_reset_kernel_times(hz_net* net) {
   if (!net) return HZ_ERR_ARG;
-  ctx_reset(net->ctx(), net->dev);
-  return HZ_OK;
+  return guarded(nullptr, [&] { ctx_reset(net->ctx(), net->dev); });
 }
 
 int hz_attach_net(hz_handle* h, hz_net* net, int32_t level, double stag_ratio) {
