@@ -2305,13 +2305,11 @@ int hz_net_set_conv_path(hz_net* net, int32_t path) {
     if (path != HZ_NET_CONV_WARP_MMA && path != HZ_NET_CONV_TCGEN05 && path != HZ_NET_CONV_AUTO)
       fail(HZ_ERR_ARG, "conv path must be HZ_NET_CONV_WARP_MMA, HZ_NET_CONV_TCGEN05 or HZ_NET_CONV_AUTO");
     ck(cudaSetDevice(net->dev), "cudaSetDevice");
-    if (net->net) {
-      cudaStreamSynchronize(net->net->ctx.stream);
+    ck(cudaStreamSynchronize(net->ctx().stream), "synchronize the network's stream");
+    if (net->net)
       net->net->set_conv_path(path);
-    } else if (net->net3) {
-      cudaStreamSynchronize(net->net3->ctx.stream);
+    else if (net->net3)
       net->net3->set_conv_path(path);
-    }
   });
 }
 
