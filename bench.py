@@ -291,6 +291,18 @@ def kernel_table(lib, h):
     return rows
 
 
+def device_gb_in_use():
+    """GB in use on the current CUDA device: every allocation on it, the library's
+    own cudaMalloc buffers included (torch's allocator does not see those); None
+    where the query fails."""
+    try:
+        import torch
+        free, total = torch.cuda.mem_get_info()
+        return (total - free) / 1e9
+    except Exception:
+        return None
+
+
 def fp64_rate(k: dict):
     """FP64 TFLOP/s of a kernel-table row and its fraction of the nominal FP64
     peak, or None for a row that is not a native-FP64 kernel or was not timed."""
@@ -534,7 +546,7 @@ def run_ours(args, rank, ws, dist):
                    rhs_per_s=nrhs * ws * steps / t, ms_per_step=1000.0 * t / steps, max_relres=float(rr.max()),
                    converged_cols=int(np.sum(rr <= wl["tol"])), mean_iters=float(it.mean()), max_iters=int(it.max()),
                    outer=int(st.outer), launches_per_step=launches, clocks=clocks.summary(),
-                   setup_warm_s=setup_and_warm, code=int(code),
+                   setup_warm_s=setup_and_warm, code=int(code), device_gb=device_gb_in_use(),
                    x_err_cols=Xd[err_cols].cpu().numpy())
         if head:
             # per-kernel CUDA events on the handle's stream over one solve right after the timed
@@ -765,7 +777,8 @@ def main():
                     cycle=r["cycle"], rhs_per_s=r["rhs_per_s"], ms_per_step=r["ms_per_step"], steps=r["steps"], warmup=r["warmup"],
                     mean_iters=r["mean_iters"], max_iters=r["max_iters"], max_relres=r["max_relres"],
                     converged_cols=r["converged_cols"], max_err_vs_oracle=errs.get(name),
-                    net_calls=r["net_calls"], net_fallbacks=r["net_fallbacks"], clocks=r["clocks"])
+                    net_calls=r["net_calls"], net_fallbacks=r["net_fallbacks"], clocks=r["clocks"],
+                    device_gb_in_use=r.get("device_gb"))
 
     def over_plain(name):
         r = results.get(name)
@@ -788,6 +801,7 @@ def main():
                 max_relres=head["max_relres"], check_relres_max=head.get("check_relres_max"),
                 converged_cols=head["converged_cols"], mean_iters=head["mean_iters"],
                 max_err_vs_oracle=errs.get(names[0]), err_oracle=err_info,
+                device_gb_in_use=head.get("device_gb"),
                 arms={nm: arm_summary(r, nm) for nm, r in results.items()},
                 plain_fp64=None if plain is None else arm_summary(plain, "fp64"),
                 headline_over_plain=over_plain(names[0]),
