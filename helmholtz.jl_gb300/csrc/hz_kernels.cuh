@@ -43,6 +43,9 @@ struct Ctx {
   // fine-level and the Galerkin stencils (0: the default rule), which set how
   // many right-hand sides a block loops over
   int tune_fine = 0, tune_rap = 0;
+  // 3D Galerkin stencils of the complex-FP32 cycle on staged tiles (k_rap_tile)
+  // instead of k_rap: opt-in (HELMGPU_RAP_TILED=1) until timed on a GB300
+  bool rap_tiled = false;
   void release();
 };
 

@@ -1744,6 +1744,10 @@ int hz_create(const hz_problem* prob, const hz_options* opt, hz_handle** out) {
     ck(cudaStreamCreateWithFlags(&h->ctx.stream, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming), "ordering event");
     h->ctx.profile = opt->profile != 0;
+    {
+      const char* rt = std::getenv("HELMGPU_RAP_TILED");
+      h->ctx.rap_tiled = rt && std::strcmp(rt, "1") == 0;
+    }
     auto t0 = clk::now();
     init_fine(h.get());
     h->setup_time += secs(t0, clk::now());

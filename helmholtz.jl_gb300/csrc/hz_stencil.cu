@@ -16,6 +16,7 @@
 #include <cooperative_groups.h>
 
 #include "hz_launch.cuh"
+#include "hz_rap_tile.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -289,6 +290,46 @@ __global__ void __launch_bounds__(128) k_rap(Grid g, const cplx<T>* __restrict__
   }
 }
 
+// The 3D Galerkin stencil of the complex-FP32 cycle on staged tiles (the steps
+// and the layout are in hz_rap_tile.cuh); the same outputs, bit for bit, as k_rap.
+template <typename TB, int MODE>
+__global__ void __launch_bounds__(kRtThreads) k_rap_tile(Grid g, const float2* __restrict__ coef, long long cld,
+                                                         const float2* __restrict__ dinv,
+                                                         const float2* __restrict__ x, const cplx<TB>* __restrict__ b,
+                                                         float2* __restrict__ y, long long ld,
+                                                         const int* __restrict__ cols, int ncols, float w) {
+  __shared__ float2 sm[kRtSmemElems];
+  const RapTileCta t = rap_tile_cta(g, blockIdx.x, blockIdx.y, blockIdx.z, ncols);
+  const int tid = threadIdx.x;
+  rap_tile_load<float>(t, tid, t.z0 - 1, x, ld, cols, sm);
+  rap_tile_load<float>(t, tid, t.z0, x, ld, cols, sm);
+  for (int z = t.z0; z < t.z1; ++z) {
+    // plane z + 1 takes the slot of plane z - 2, free since the barrier closing the last step
+    rap_tile_load<float>(t, tid, z + 1, x, ld, cols, sm);
+    __syncthreads();
+    rap_tile_node<float, TB, MODE>(t, tid, z, coef, cld, dinv, b, y, ld, cols, sm, w);
+    __syncthreads();
+  }
+}
+
+template <typename TB>
+void launch_rap_tile(Ctx& ctx, int mode, const Grid& g, const float2* coef, long long cld, const float2* dinv,
+                     const float2* x, const cplx<TB>* b, float2* y, long long ld, const int* cols, int ncols, double w,
+                     double bytes) {
+  int bx, by, bz;
+  rap_tile_grid(g, ncols, bx, by, bz);
+  const dim3 grid((unsigned)bx, (unsigned)by, (unsigned)bz);
+  if (mode == MODE_APPLY)
+    HZ_LAUNCH(ctx, "rap_tile_apply", bytes, (k_rap_tile<TB, MODE_APPLY>), grid, kRtThreads, 0, g, coef, cld, dinv, x,
+              b, y, ld, cols, ncols, (float)w);
+  else if (mode == MODE_RESID)
+    HZ_LAUNCH(ctx, "rap_tile_resid", bytes, (k_rap_tile<TB, MODE_RESID>), grid, kRtThreads, 0, g, coef, cld, dinv, x,
+              b, y, ld, cols, ncols, (float)w);
+  else
+    HZ_LAUNCH(ctx, "rap_tile_jacobi", bytes, (k_rap_tile<TB, MODE_JACOBI>), grid, kRtThreads, 0, g, coef, cld, dinv,
+              x, b, y, ld, cols, ncols, (float)w);
+}
+
 template <typename T, typename TB>
 void launch_rap(Ctx& ctx, int mode, const Grid& g, const cplx<T>* coef, long long cld, const cplx<T>* dinv,
                 const cplx<T>* x, const cplx<TB>* b, cplx<T>* y, long long ld, const int* cols, int ncols, double w) {
@@ -303,6 +344,12 @@ void launch_rap(Ctx& ctx, int mode, const Grid& g, const cplx<T>* coef, long lon
   double rbytes = (double)g.N * ncols * 2 * sizeof(cplx<T>) + (double)g.N * ns * sizeof(cplx<T>);
   if (mode != MODE_APPLY) rbytes += (double)g.N * ncols * sizeof(cplx<TB>);
   if (mode == MODE_JACOBI) rbytes += (double)g.N * sizeof(cplx<T>);
+  if constexpr (std::is_same<T, float>::value) {
+    if (is3d && ctx.rap_tiled) {
+      launch_rap_tile<TB>(ctx, mode, g, coef, cld, dinv, x, b, y, ld, cols, ncols, w, rbytes);
+      return;
+    }
+  }
 #define HZ_RAP_CASE(M, D, NAME) \
   HZ_LAUNCH(ctx, NAME, rbytes, (k_rap<T, TB, M, D>), grid, TPB, 0, g, coef, cld, dinv, x, b, y, ld, cols, ncols, cpb, (T)w)
   if (mode == MODE_APPLY) {
