@@ -144,7 +144,10 @@ void hz_default_options(hz_options* opt);
  * assembly of GetHelmholtzOperator (src/GetHelmholtz.jl:33-50) and
  * GetHelmholtzShiftOP (src/GetHelmholtz.jl:81-83), which the library keeps
  * matrix-free on the device.  The multigrid hierarchy is built lazily by the
- * first hz_solve, as MGsetup is (src/ShiftedLaplacianMultigridSolver.jl:50-66). */
+ * first hz_solve, as MGsetup is (src/ShiftedLaplacianMultigridSolver.jl:50-66).
+ * With the environment variable HELMGPU_RAP_TILED=1 at this call, the handle's
+ * 3D Galerkin stencils in the complex-FP32 cycle use the staged-tile kernel
+ * (same results; an experimental launch shape, off by default). */
 int hz_create(const hz_problem* prob, const hz_options* opt, hz_handle** out);
 
 /* Release everything the handle owns. */
